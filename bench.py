@@ -1,0 +1,368 @@
+#!/usr/bin/env python
+"""Throughput of the kagome VMC hot path on GB300: accepted moves per second.
+
+Workload (the headline configuration): 6x6 doubled kagome cells (N=216,
+n_up = n_down = 108), pi-flux parton orbitals, the reference's acceptance
+rule, 2048 independent walkers from seeded random starts.  One step = every
+walker makes `--proposals` exchange proposals (local energy every 108
+proposals), with W refreshed in FP64 every `--refresh` accepted moves
+(mixed form) or every 108 proposals (plain FP64 form).  The walkers' FP32 W
+state (2048 x 186.6 KB = 382 MB) is larger than L2, so no flush is needed.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Prints one JSON line (rank 0).  The reference arm times the reference
+algorithm's CPU restatement (complex double, one chain per host thread).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "kagomedsl.jl_gb300"))
+
+CELLS = (6, 6)          # doubled cells -> DoubleKagome(1.0, 12, 6)
+N_SITES = 216
+METRIC = "accepted moves/sec at N=216, mixed-prec batched vs plain FP64, at |dE/N|<=1e-4"
+UNIT = "accepted_moves/s"
+
+
+def args_():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=8)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--walkers", type=int, default=2048)
+    p.add_argument("--proposals", type=int, default=2048, help="proposals per walker per step")
+    p.add_argument("--refresh", type=int, default=256, help="mixed form: accepted moves between FP64 refreshes")
+    p.add_argument("--seed", type=int, default=2024)
+    p.add_argument("--skip-plain", action="store_true")
+    p.add_argument("--skip-cpu", action="store_true")
+    return p.parse_args()
+
+
+def dist_env():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+def model():
+    import kagomevmc as kv
+
+    lat = kv.DoubleKagome(1.0, 2 * CELLS[0], CELLS[1], (True, True), (False, True))
+    return kv.Hamiltonian.build(N_SITES // 2, N_SITES // 2, lat)
+
+
+# ---------------------------------------------------------------------------
+# CPU restatement (oracle port): the cpu_baseline and the reference arm
+# ---------------------------------------------------------------------------
+
+def cpu_port_run(ham, chains, proposals, seed, threads):
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import kagome_oracle as o
+    import oracle_c
+
+    bonds = ham.nn
+    m = oracle_c.OracleModel(ham.U_up, ham.U_down, bonds, "cplx")
+    starts = [o.seeded_start(seed, w, ham.U_up, ham.U_down)[:2] for w in range(chains)]
+    n = N_SITES // 2
+    sec, ch = oracle_c.run_chains(m, starts, seed, proposals, n, n, 0, threads)
+    acc = sum(c.c.accepted for c in ch)
+    return acc, sec
+
+
+def cpu_threads():
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
+
+
+def reference_arm(a):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    ham = model()
+    threads = cpu_threads()
+    proposals = 1080  # ten reference refresh intervals per chain per step
+    vals = []
+    for s in range(a.warmup + a.steps):
+        acc, sec = cpu_port_run(ham, threads, proposals, a.seed + 7919 * s, threads)
+        if s >= a.warmup:
+            vals.append((acc, sec))
+    acc = sum(v[0] for v in vals)
+    sec = sum(v[1] for v in vals)
+    value = acc / sec
+    sample = f"{threads} chains x {proposals} proposals per step, N=216, complex double, refresh and E_L every 108 proposals"
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": a.gpus, "steps": a.steps,
+            "warmup": a.warmup, "ms_per_step": 1e3 * sec / a.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "c128", "data": "synthetic (seeded random starts)",
+            "config": {"workload": "kagome VMC, 6x6 doubled cells (N=216), reference acceptance rule",
+                       "walkers": threads, "proposals_per_walker_per_step": proposals},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------------
+# GPU arm
+# ---------------------------------------------------------------------------
+
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        rows = []
+        for line in open(self.path):
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) >= 9:
+                rows.append(parts)
+        os.unlink(self.path)
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = max(float(r[2]) for r in rows if r[2].replace(".", "").isdigit())
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": reasons,
+                "samples": len(rows)}
+
+
+def measure_peaks(device):
+    """FP64 and FP32 (no TF32) GEMM throughput of this GPU, measured in-run
+    with cuBLAS through torch (the denominators for FP64/FP32-pipe kernels)."""
+    out = {}
+    try:
+        import torch
+
+        torch.backends.cuda.matmul.allow_tf32 = False
+        dev = torch.device("cuda", device)
+        for name, dt, n in (("fp64_tflops", torch.float64, 4096), ("fp32_tflops", torch.float32, 8192)):
+            a = torch.randn(n, n, device=dev, dtype=dt)
+            b = torch.randn(n, n, device=dev, dtype=dt)
+            best = math.inf
+            for _ in range(4):
+                s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                torch.cuda.synchronize(dev)
+                s.record()
+                torch.matmul(a, b)
+                e.record()
+                torch.cuda.synchronize(dev)
+                best = min(best, s.elapsed_time(e))
+            out[name] = 2 * n ** 3 / (best * 1e-3) / 1e12
+            del a, b
+        torch.cuda.empty_cache()
+    except Exception as exc:  # torch missing: peaks stay unknown
+        out["error"] = str(exc)
+    return out
+
+
+def run_steps(eng, steps, proposals):
+    tot = {"accepted": 0, "proposals": 0, "launches": 0, "refreshes": 0, "measurements": 0, "sum_energy": 0.0,
+           "max_drift": 0.0, "bad_walkers": 0}
+    for _ in range(steps):
+        st = eng.sweep(proposals)
+        for k in ("accepted", "proposals", "launches", "refreshes", "measurements", "sum_energy", "bad_walkers"):
+            tot[k] += st[k]
+        tot["max_drift"] = max(tot["max_drift"], st["max_drift"])
+    return tot
+
+
+def energy_gate(ham, kv, walkers, proposals, refresh, seed):
+    """Both forms on identical walkers and proposal streams: |dE/N| over walkers whose chains agree."""
+    import numpy as np
+
+    res = {}
+    for prec in ("plain", "mixed"):
+        eng = kv.Engine(ham, walkers, precision=prec, seed=seed, refresh_interval=(refresh if prec == "mixed" else 0))
+        eng.init()
+        st = eng.sweep(proposals)
+        ws = eng.walker_stats()
+        res[prec] = (ws["sum_e"], ws["n_meas"], eng.get_state()[0], st["max_drift"])
+        eng.close()
+    (ep, np_, kp, _), (em, nm, km, drift) = res["plain"], res["mixed"]
+    same = np.array([np.array_equal(kp[w], km[w]) for w in range(walkers)])
+    dE = abs(ep[same].sum() / np_[same].sum() - em[same].sum() / nm[same].sum()) / N_SITES
+    return {"dE_per_site": float(dE), "walkers": walkers, "proposals_per_walker": proposals,
+            "identical_chains": int(same.sum()), "max_w_drift_at_refresh": float(drift), "pass": bool(dE <= 1e-4)}
+
+
+def gpu_arm(a):
+    import numpy as np
+
+    import kagomevmc as kv
+
+    rank, world, local = dist_env()
+    torch = None
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+
+    ham = model()
+    n = N_SITES // 2
+    peaks = measure_peaks(local) if rank == 0 else {}
+    eng = kv.Engine(ham, a.walkers, precision="mixed", seed=a.seed + 104729 * rank, refresh_interval=a.refresh,
+                    device=local)
+    eng.init()
+    run_steps(eng, a.warmup, a.proposals)
+    eng.enable_timing(True)
+    clocks = ClockSampler(local)
+    barrier()
+    clocks.start()
+    eng.region_start()
+    tot = run_steps(eng, a.steps, a.proposals)
+    ms = eng.region_stop()
+    clk = clocks.stop()
+    barrier()
+    sweep_ms, sweep_n = eng.kernel_time(0)
+    ref_ms, ref_n = eng.kernel_time(1)
+    eng.enable_timing(False)
+    accepted = tot["accepted"]
+    if world > 1:
+        t = torch.tensor([ms, float(accepted)], dtype=torch.float64, device="cuda")
+        mx = t.clone()
+        torch.distributed.all_reduce(mx, op=torch.distributed.ReduceOp.MAX)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.SUM)
+        ms, accepted = float(mx[0]), float(t[1])
+    value = accepted / (ms * 1e-3)
+
+    # end to end through the public API with host buffers: the walkers'
+    # configurations and stream counters go host -> device, the step runs,
+    # configurations, counters and per-walker statistics come back.
+    ku, kd, ct = eng.get_state()
+    e2e_steps = min(a.steps, 4)
+    e2e_acc = 0
+    eng.region_start()
+    for _ in range(e2e_steps):
+        eng.set_state(ku, kd, ct)
+        st = eng.sweep(a.proposals)
+        ku, kd, ct = eng.get_state()
+        ws = eng.walker_stats()
+        e2e_acc += st["accepted"]
+    e2e_ms = eng.region_stop()
+    Wk = a.walkers
+    h2d = ku.nbytes + kd.nbytes + ct.nbytes
+    d2h = ku.nbytes + kd.nbytes + ct.nbytes + sum(v.nbytes for v in ws.values())
+    e2e = {"value": e2e_acc / (e2e_ms * 1e-3), "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+           "d2h_bytes_per_step": int(d2h), "steps": e2e_steps,
+           "path": "kvmc_set_state (H2D + FP64 rebuild) -> kvmc_sweep -> kvmc_get_state + kvmc_walker_stats (D2H)"}
+    eng.close()
+    if rank != 0:
+        if world > 1:
+            torch.distributed.destroy_process_group()
+        return
+
+    # plain FP64 form on the same walkers (the spec denominator)
+    plain = None
+    if not a.skip_plain:
+        pe = kv.Engine(ham, a.walkers, precision="plain", seed=a.seed, device=local)
+        pe.init()
+        run_steps(pe, 1, 2 * n)
+        pe.region_start()
+        ptot = run_steps(pe, 2, 4 * n)
+        pms = pe.region_stop()
+        pe.close()
+        plain = {"value": ptot["accepted"] / (pms * 1e-3), "unit": UNIT, "ms": pms,
+                 "proposals_per_walker": 8 * n, "accepted": ptot["accepted"]}
+    gate = energy_gate(ham, kv, 256, 4 * a.proposals, a.refresh, a.seed + 1)
+
+    # roofline of the dominant kernel
+    refreshes = tot["refreshes"]
+    f_refresh = 2 * ((2.0 / 3.0) * n ** 3 + 2.0 * (N_SITES - n) * n ** 2)   # FP64 flop per walker refresh
+    f_move = 2.0 * N_SITES * N_SITES                                        # FP32 flop per accepted move
+    kern = {
+        "sweep_mixed": {"ms": sweep_ms, "launches": sweep_n, "flop": tot["accepted"] * f_move,
+                        "unit_work": "2*N^2 FP32 flop per accepted move (both spins' rank-1 update)"},
+        "refresh_fp64": {"ms": ref_ms, "launches": ref_n, "flop": refreshes * f_refresh,
+                         "unit_work": "2*((2/3)n^3 + 2(N-n)n^2) FP64 flop per walker refresh"},
+    }
+    for k in kern.values():
+        k["achieved_tflops"] = k["flop"] / (k["ms"] * 1e-3) / 1e12 if k["ms"] > 0 else None
+    dom = max(kern, key=lambda k: kern[k]["ms"])
+    peak_key = "fp64_tflops" if dom == "refresh_fp64" else "fp32_tflops"
+    peak = peaks.get(peak_key)
+    traffic = None
+    tfile = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(tfile):
+        traffic = json.load(open(tfile)).get(dom)
+    ach = kern[dom]["achieved_tflops"]
+    roof = {"bound": "fp64" if dom == "refresh_fp64" else "fp32", "kernel": dom,
+            "achieved": ach, "peak": peak, "unit": "TFLOP/s",
+            "frac": (ach / peak) if (ach and peak) else None, "traffic": traffic,
+            "peak_source": f"cuBLAS {peak_key[:4].upper()} GEMM via torch.matmul, measured in this run",
+            "per_launch_flop": kern[dom]["flop"] / max(kern[dom]["launches"], 1),
+            "kernels": kern}
+
+    cpu = None
+    if not a.skip_cpu:
+        threads = cpu_threads()
+        acc, sec = cpu_port_run(ham, threads, 2160, a.seed, threads)
+        cpu = {"value": acc / sec, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": f"{threads} chains x 2160 proposals, N=216, complex double (oracle port), "
+                         f"refresh and E_L every 108 proposals, {sec:.1f} s wall"}
+
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
+            "ms_per_step": ms / a.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32 (W, ratios, rank-1) + f64 (refresh, energy sums)", "data": "synthetic (seeded random starts)",
+            "config": {"workload": "kagome VMC, 6x6 doubled cells (N=216), pi-flux partons, reference acceptance rule",
+                       "walkers_per_gpu": a.walkers, "proposals_per_walker_per_step": a.proposals,
+                       "refresh_every_accepted": a.refresh, "measure_every_proposals": n,
+                       "parallelism": f"replicas x{world}", "l2": "inputs larger than L2 (W state 382 MB per GPU)"},
+            "proposals_per_step": tot["proposals"] / a.steps * world, "acceptance": tot["accepted"] / tot["proposals"],
+            "gpu_launches": tot["launches"], "e2e": e2e, "roofline": roof, "cpu_baseline": cpu,
+            "plain_fp64": plain, "speedup_vs_plain_fp64": (value / plain["value"]) if plain else None,
+            "energy_gate": gate, "clocks": clk, "peaks_measured": peaks}
+    print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    a = args_()
+    if a.impl == "reference":
+        reference_arm(a)
+    else:
+        gpu_arm(a)
+
+
+if __name__ == "__main__":
+    main()

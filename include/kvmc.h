@@ -1,0 +1,222 @@
+/*
+ * kvmc.h -- C ABI of libkvmc, the GB300 (sm_103a) variational Monte Carlo
+ * engine for Gutzwiller-projected parton states of the kagome Heisenberg
+ * model.  It drops in for the hot path of KagomeDSL.jl: the Monte Carlo
+ * driver callbacks (init!, sweep!, measure!, checkpoint I/O) and the
+ * lattice / hopping-matrix constructors.
+ *
+ * Conventions
+ *  - Every function returns int status: KVMC_OK (0) or a kvmc_status code;
+ *    kvmc_last_error() gives the message.  No function aborts the process.
+ *  - Site indices are 0-based.  Configuration vectors ("kappa") keep the
+ *    reference's values: 0 = site empty for that spin, 1..n = orbital label
+ *    (src/MonteCarlo.jl:92-135), so a Julia Vector{Int} passes through after
+ *    conversion to Int32 only.
+ *  - Orbital matrices U are column-major (Julia layout), n_sites x n.
+ *  - A handle owns all device memory it uses; calls on one handle are
+ *    synchronous with respect to the host and a handle is not thread-safe.
+ *  - Per-walker arrays are walker-major: [n_walkers][n_sites].
+ */
+#ifndef KVMC_H
+#define KVMC_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(__GNUC__)
+#define KVMC_API __attribute__((visibility("default")))
+#else
+#define KVMC_API
+#endif
+
+#define KVMC_ABI_VERSION 1
+
+enum kvmc_status {
+    KVMC_OK = 0,
+    KVMC_ERR_ARGUMENT = 1,  /* ArgumentError / AssertionError / DimensionMismatch */
+    KVMC_ERR_BOUNDS = 2,    /* BoundsError */
+    KVMC_ERR_SINGULAR = 3,  /* singular tilde_U (SingularException, singular init) */
+    KVMC_ERR_CUDA = 4,      /* CUDA runtime failure */
+    KVMC_ERR_NUMERIC = 5,   /* non-finite ratio or W detected by a kernel */
+    KVMC_ERR_NO_DEVICE = 6, /* no usable sm_103 device */
+    KVMC_ERR_UNSUPPORTED = 7
+};
+
+enum kvmc_precision {
+    KVMC_PLAIN_FP64 = 0, /* reference algorithm: FP64 W, rank-1 per accepted move,
+                            refresh every refresh_interval proposals */
+    KVMC_MIXED_FP32 = 1  /* FP32 W resident in shared memory, FP64 refresh every
+                            refresh_interval accepted moves, FP64 energy sums */
+};
+
+enum kvmc_accept {
+    KVMC_ACCEPT_REFERENCE = 0, /* src/MonteCarlo.jl:544-591: stationary law |psi|^2/Z_mu */
+    KVMC_ACCEPT_METROPOLIS = 1 /* uniform bond + min(1,|ratio|^2): stationary law |psi|^2 */
+};
+
+/* ---- lattice and hopping matrix (host FP64) ---------------------------- */
+
+typedef struct {
+    int32_t n1, n2;     /* DoubleKagome repetitions, n1 even (src/Lattice.jl:68-92) */
+    int32_t pbc[2];     /* periodic along a1, a2 */
+    int32_t antipbc[2]; /* antiperiodic along a1, a2 (requires pbc) */
+    double t;           /* triangle side parameter, 1.0 in the reference */
+} kvmc_lattice_desc;
+
+/* One hopping table entry.  In-cell tables (src/Hamiltonian.jl:219-235) use
+ * label1, label2 only; inter-cell tables (src/Hamiltonian.jl:250-261) also
+ * use the cell offset (dx, dy).  Labels are 1..6 as in the reference. */
+typedef struct {
+    int32_t label1, label2, dx, dy;
+    double amplitude;
+} kvmc_link;
+
+/* Number of sites n1*n2*3 (src/Lattice.jl:97).  Replaces ns(lat). */
+KVMC_API int kvmc_lattice_sites(const kvmc_lattice_desc *lat, int32_t *n_sites);
+
+/* Spinon hopping matrix H = -(T + T^dagger) with Peierls phase and
+ * (anti)periodic images.  Replaces Hmat (src/Hamiltonian.jl:308-354) with
+ * get_boundary_shifts / apply_boundary_conditions! (:99-207).
+ * link_in / link_inter may be NULL for the reference's pi-flux tables.
+ * H receives 2*N*N doubles: column-major, (re, im) interleaved. */
+KVMC_API int kvmc_hopping_matrix(const kvmc_lattice_desc *lat,
+                        const kvmc_link *link_in, int32_t n_link_in,
+                        const kvmc_link *link_inter, int32_t n_link_inter,
+                        double B, double *H);
+
+/* Bond list: upper-triangular nonzeros of H in column-major order, 0-based
+ * (i < j).  Replaces get_nn (src/Hamiltonian.jl:447-451).  Pass bonds=NULL to
+ * query the count. */
+KVMC_API int kvmc_bonds_from_hopping(int32_t n_sites, const double *H, int32_t *n_bonds,
+                            int32_t *bonds);
+
+/* ---- batched Monte Carlo state ----------------------------------------- */
+
+typedef struct {
+    int32_t n_sites;
+    int32_t n_up, n_down;  /* n_up + n_down == n_sites (one spinon per site) */
+    int32_t n_bonds;
+    const int32_t *bonds;  /* [n_bonds][2], 0-based, as kvmc_bonds_from_hopping */
+    const double *U_up;    /* column-major n_sites x n_up (real orbitals) */
+    const double *U_down;  /* column-major n_sites x n_down */
+} kvmc_model_desc;
+
+typedef struct {
+    int32_t n_walkers;
+    int32_t precision;        /* enum kvmc_precision */
+    int32_t accept_rule;      /* enum kvmc_accept */
+    int32_t refresh_interval; /* plain: proposals, mixed: accepted moves; 0 = default
+                                 (plain: min(n_up,n_down) as src/MonteCarlo.jl:594-595) */
+    int32_t measure_interval; /* proposals between local-energy samples; 0 = min(n_up,n_down)
+                                 (src/MonteCarlo.jl:628-634) */
+    int32_t delay_k;          /* reserved: delayed-update depth, 0 or 1 = rank-1 */
+    int32_t device;           /* CUDA device ordinal */
+    uint64_t seed;            /* Philox4x32-10 key for proposals and seeded starts */
+} kvmc_batch_desc;
+
+typedef struct kvmc_handle kvmc_handle;
+
+/* Replaces MC(params) (src/MonteCarlo.jl:165-185, :209-234): uploads the
+ * orbitals and bonds and allocates every walker's state on the device. */
+KVMC_API int kvmc_create(const kvmc_model_desc *model, const kvmc_batch_desc *batch,
+                kvmc_handle **out);
+KVMC_API int kvmc_destroy(kvmc_handle *h);
+
+/* Message of the last failure on h (or of the last failed kvmc_create when
+ * h is NULL). */
+KVMC_API int kvmc_last_error(const kvmc_handle *h, char *buf, size_t len);
+
+/* Replaces Carlo.init! (src/MonteCarlo.jl:435-441) and
+ * find_initial_configuration! (:382-410).  With kappa_up == NULL every
+ * walker draws a seeded uniformly random configuration, redrawn until
+ * tilde_U is regular for both spins (min|pivot|/max|pivot| of its partially
+ * pivoted LU above 1e-8); otherwise the given configurations
+ * ([n_walkers][n_sites]) are validated and used.  Builds W in FP64 either
+ * way.  attempts (may be NULL) receives the draws each walker needed.
+ * Returns KVMC_ERR_SINGULAR if a given configuration is singular. */
+KVMC_API int kvmc_init(kvmc_handle *h, const int32_t *kappa_up, const int32_t *kappa_down,
+              int32_t *attempts);
+
+typedef struct {
+    int64_t proposals;    /* proposals made by all walkers in the call */
+    int64_t accepted;     /* accepted moves of all walkers in the call */
+    int64_t measurements; /* local-energy samples taken in the call */
+    double sum_energy;    /* sum of those samples (FP64) */
+    double sum_energy2;   /* sum of their squares */
+    int64_t refreshes;    /* walker W refreshes performed (FP64 LU + solves) */
+    double max_drift;     /* mixed: max |W_fp32 - W_fp64 fresh| seen at a refresh */
+    int32_t bad_walkers;  /* walkers whose status word is nonzero */
+    int32_t launches;     /* kernels launched by the call */
+} kvmc_sweep_stats;
+
+/* Replaces Carlo.sweep! (src/MonteCarlo.jl:538-607) plus the cadenced
+ * Carlo.measure! (:628-634): every walker makes exactly
+ * proposals_per_walker exchange proposals, refreshing W and sampling the
+ * local energy at the configured intervals.  stats may be NULL. */
+KVMC_API int kvmc_sweep(kvmc_handle *h, int64_t proposals_per_walker, kvmc_sweep_stats *stats);
+
+/* Local energy of every walker's current state (getOL,
+ * src/Hamiltonian.jl:762-778), FP64 result: local_energy[n_walkers]. */
+KVMC_API int kvmc_measure(kvmc_handle *h, double *local_energy);
+
+/* Determinant ratios W_up[K_up, l_up] * W_down[K_down, l_down] for given
+ * moves, read from the device W (src/MonteCarlo.jl:576-580).
+ * moves: [n_walkers][n_moves][4] = {K_up, l_up, K_down, l_down}, sites
+ * 0-based, labels 1-based; ratios: [n_walkers][n_moves]. */
+KVMC_API int kvmc_eval_ratios(kvmc_handle *h, int32_t n_moves, const int32_t *moves,
+                     double *ratios);
+
+/* Applies one exchange per walker through the device update path
+ * (update_configurations!, src/MonteCarlo.jl:497-511 with update_W!,
+ * :279-292).  moves: [n_walkers][5] = {flag, i, site, l_up, l_down};
+ * flag 1 or 2 as in the reference, 0 = leave the walker unchanged; sites
+ * 0-based, labels 1-based. */
+KVMC_API int kvmc_apply_moves(kvmc_handle *h, const int32_t *moves);
+
+/* Rebuilds every walker's W from its configuration in FP64
+ * (reevaluateW!, src/MonteCarlo.jl:55-66). */
+KVMC_API int kvmc_refresh(kvmc_handle *h);
+
+/* Checkpoint state (write_checkpoint / read_checkpoint!,
+ * src/MonteCarlo.jl:715-755): configurations plus the per-walker proposal
+ * counter (the position in the Philox stream).  set_state rebuilds W.
+ * Any pointer may be NULL to skip that field (set_state: counters NULL
+ * keeps the current counters). */
+KVMC_API int kvmc_get_state(kvmc_handle *h, int32_t *kappa_up, int32_t *kappa_down,
+                   int64_t *counters);
+KVMC_API int kvmc_set_state(kvmc_handle *h, const int32_t *kappa_up, const int32_t *kappa_down,
+                   const int64_t *counters);
+
+/* Copies W to the host as FP64, row-major [n_walkers][n_sites][n]. */
+KVMC_API int kvmc_get_w(kvmc_handle *h, double *W_up, double *W_down);
+
+/* Per-walker accumulators since creation or the last kvmc_reset_stats:
+ * sums of E_L and E_L^2, sample counts, accepted moves, proposals, status
+ * words.  Any pointer may be NULL. */
+KVMC_API int kvmc_walker_stats(kvmc_handle *h, double *sum_e, double *sum_e2, int64_t *n_meas,
+                      int64_t *accepted, int64_t *proposals, int32_t *status);
+KVMC_API int kvmc_reset_stats(kvmc_handle *h);
+
+/* Device-side timing of the kernels launched by kvmc_sweep, measured with
+ * CUDA events on the handle's stream (enable before the calls to time).
+ * kind: 0 = sweep kernel, 1 = refresh kernel.  Totals since enabling. */
+KVMC_API int kvmc_enable_timing(kvmc_handle *h, int32_t on);
+KVMC_API int kvmc_kernel_time(kvmc_handle *h, int32_t kind, double *total_ms, int64_t *launches);
+
+/* Device time of everything the handle enqueues between a call with
+ * start=1 and a call with start=0 (CUDA events on the handle's stream);
+ * the second call waits for the stream and returns the milliseconds. */
+KVMC_API int kvmc_region_timer(kvmc_handle *h, int32_t start, double *ms);
+
+/* Library version / build facts: abi version, compiled arch (e.g. 1030). */
+KVMC_API int kvmc_version(int32_t *abi, int32_t *arch);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* KVMC_H */

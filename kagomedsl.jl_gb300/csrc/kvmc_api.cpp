@@ -1,0 +1,849 @@
+// Host side of libkvmc: the C ABI declared in include/kvmc.h.
+//
+// Handle lifecycle, argument validation with the reference's error classes,
+// the FP64 hopping-matrix builder, and the launch loop that drives the CUDA
+// kernels of kvmc_kernels.cu on one stream per handle.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <complex>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <string>
+#include <tuple>
+#include <vector>
+
+#include "kvmc.h"
+#include "kvmc_internal.h"
+
+using kvmc::DevBatch;
+using kvmc::DevModel;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail_global(int code, const char *fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    g_last_error = buf;
+    return code;
+}
+
+}  // namespace
+
+struct kvmc_handle {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    kvmc_model_desc model{};
+    kvmc_batch_desc batch{};
+    int n_sites = 0, n_up = 0, n_dn = 0, ld_up = 0, ld_dn = 0, n_bonds = 0, n_walkers = 0;
+    bool mixed = false;
+    bool smem_w = false;
+    int refresh_every = 0;
+    int measure_every = 0;
+    std::string err;
+
+    DevModel dm{};
+    DevBatch db{};
+    // owned device buffers (freed in destroy)
+    std::vector<void *> allocs;
+    int *d_active = nullptr;
+    int *d_attempt = nullptr;
+    int *d_redo = nullptr;
+    void *d_scratch = nullptr;
+    size_t scratch_bytes = 0;
+
+    // timing: per-launch event pairs recorded without host syncs, read after
+    // the call's final synchronisation
+    bool timing = false;
+    std::vector<cudaEvent_t> ev_pool;
+    std::vector<std::pair<int, int>> ev_used;  // (kind, first event index)
+    cudaEvent_t region[2] = {nullptr, nullptr};
+    double t_ms[2] = {0, 0};
+    long long t_launch[2] = {0, 0};
+
+    int fail(int code, const char *fmt, ...) {
+        char buf[512];
+        va_list ap;
+        va_start(ap, fmt);
+        vsnprintf(buf, sizeof buf, fmt, ap);
+        va_end(ap);
+        err = buf;
+        g_last_error = buf;
+        return code;
+    }
+    int cuda(cudaError_t e, const char *what) {
+        if (e == cudaSuccess) return KVMC_OK;
+        return fail(KVMC_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+    }
+    template <typename T>
+    int alloc(T **p, size_t count) {
+        void *q = nullptr;
+        cudaError_t e = cudaMalloc(&q, count * sizeof(T) > 0 ? count * sizeof(T) : 16);
+        if (e != cudaSuccess) return cuda(e, "cudaMalloc");
+        allocs.push_back(q);
+        *p = static_cast<T *>(q);
+        return KVMC_OK;
+    }
+    int scratch(size_t bytes, void **p) {
+        if (bytes > scratch_bytes) {
+            if (d_scratch) cudaFree(d_scratch);
+            d_scratch = nullptr;
+            cudaError_t e = cudaMalloc(&d_scratch, bytes);
+            if (e != cudaSuccess) { scratch_bytes = 0; return cuda(e, "cudaMalloc(scratch)"); }
+            scratch_bytes = bytes;
+        }
+        *p = d_scratch;
+        return KVMC_OK;
+    }
+};
+
+#define KV_TRY(expr)                 \
+    do {                             \
+        int _rc = (expr);            \
+        if (_rc != KVMC_OK) return _rc; \
+    } while (0)
+
+namespace {
+
+int set_device(kvmc_handle *h) { return h->cuda(cudaSetDevice(h->device), "cudaSetDevice"); }
+
+// kappa validation: every site holds exactly one spinon, labels are a
+// permutation of 1..n per spin (src/Hamiltonian.jl:548-564, src/MonteCarlo.jl:92-115).
+int validate_kappa(kvmc_handle *h, const int32_t *ku, const int32_t *kd, int walker) {
+    const int N = h->n_sites;
+    std::vector<char> seen_u(h->n_up + 1, 0), seen_d(h->n_dn + 1, 0);
+    for (int s = 0; s < N; ++s) {
+        const int a = ku[s], b = kd[s];
+        if (a < 0 || a > h->n_up || b < 0 || b > h->n_dn)
+            return h->fail(KVMC_ERR_BOUNDS, "walker %d site %d: label out of range (kappa_up=%d kappa_down=%d)", walker, s, a, b);
+        if ((a != 0) == (b != 0))
+            return h->fail(KVMC_ERR_ARGUMENT, "walker %d site %d is %s", walker, s, a != 0 ? "doubly occupied" : "unoccupied");
+        if (a != 0) {
+            if (seen_u[a]) return h->fail(KVMC_ERR_ARGUMENT, "walker %d: up label %d repeated", walker, a);
+            seen_u[a] = 1;
+        } else {
+            if (seen_d[b]) return h->fail(KVMC_ERR_ARGUMENT, "walker %d: down label %d repeated", walker, b);
+            seen_d[b] = 1;
+        }
+    }
+    return KVMC_OK;
+}
+
+int upload_kappa(kvmc_handle *h, const int32_t *ku, const int32_t *kd) {
+    const size_t tot = (size_t)h->n_walkers * h->n_sites;
+    for (int w = 0; w < h->n_walkers; ++w)
+        KV_TRY(validate_kappa(h, ku + (size_t)w * h->n_sites, kd + (size_t)w * h->n_sites, w));
+    std::vector<short> a(tot), b(tot);
+    for (size_t e = 0; e < tot; ++e) { a[e] = (short)ku[e]; b[e] = (short)kd[e]; }
+    KV_TRY(h->cuda(cudaMemcpyAsync(h->db.kappa_up, a.data(), tot * 2, cudaMemcpyHostToDevice, h->stream), "upload kappa"));
+    KV_TRY(h->cuda(cudaMemcpyAsync(h->db.kappa_dn, b.data(), tot * 2, cudaMemcpyHostToDevice, h->stream), "upload kappa"));
+    return h->cuda(cudaStreamSynchronize(h->stream), "upload kappa");
+}
+
+int full_refresh(kvmc_handle *h, bool track_drift) {
+    KV_TRY(h->cuda(cudaMemsetAsync(h->db.drift, 0, sizeof(float) * h->n_walkers, h->stream), "memset"));
+    KV_TRY(h->cuda(kvmc::launch_refresh(h->dm, h->db, h->mixed, 0, track_drift ? 1 : 0, h->stream), "refresh launch"));
+    KV_TRY(h->cuda(cudaMemsetAsync(h->db.since, 0, sizeof(int) * h->n_walkers, h->stream), "memset"));
+    return h->cuda(cudaStreamSynchronize(h->stream), "refresh");
+}
+
+int check_status(kvmc_handle *h, int *bad) {
+    std::vector<int> st(h->n_walkers);
+    KV_TRY(h->cuda(cudaMemcpy(st.data(), h->db.status, sizeof(int) * h->n_walkers, cudaMemcpyDeviceToHost), "status"));
+    int nb = 0, first = -1, code = 0;
+    for (int w = 0; w < h->n_walkers; ++w)
+        if (st[w]) { ++nb; if (first < 0) { first = w; code = st[w]; } }
+    if (bad) *bad = nb;
+    if (nb) {
+        if (code & kvmc::kStatusSingular)
+            return h->fail(KVMC_ERR_SINGULAR, "%d walker(s) have a singular tilde_U (first: walker %d)", nb, first);
+        return h->fail(KVMC_ERR_NUMERIC, "%d walker(s) produced a non-finite ratio (first: walker %d)", nb, first);
+    }
+    return KVMC_OK;
+}
+
+struct Vec2 { double x, y; };
+
+}  // namespace
+
+// ===========================================================================
+// Lattice and hopping matrix (host FP64)
+// ===========================================================================
+
+extern "C" int kvmc_lattice_sites(const kvmc_lattice_desc *lat, int32_t *n_sites) {
+    if (!lat || !n_sites) return fail_global(KVMC_ERR_ARGUMENT, "null argument");
+    if (lat->n1 % 2 != 0) return fail_global(KVMC_ERR_ARGUMENT, "n1 must be even in DoubleKagome");
+    if (lat->n1 <= 0 || lat->n2 <= 0) return fail_global(KVMC_ERR_ARGUMENT, "n1, n2 must be positive");
+    *n_sites = lat->n1 * lat->n2 * 3;
+    return KVMC_OK;
+}
+
+namespace {
+
+// Default tables: src/Hamiltonian.jl:219-235 and :250-261.
+const kvmc_link kPiLinkIn[] = {
+    {1, 2, 0, 0, 1}, {1, 3, 0, 0, 1}, {2, 3, 0, 0, 1}, {2, 4, 0, 0, -1}, {4, 6, 0, 0, 1},
+    {4, 5, 0, 0, 1}, {5, 6, 0, 0, 1}, {2, 1, 0, 0, 1}, {3, 1, 0, 0, 1}, {3, 2, 0, 0, 1},
+    {4, 2, 0, 0, -1}, {6, 4, 0, 0, 1}, {5, 4, 0, 0, 1}, {6, 5, 0, 0, 1}};
+const kvmc_link kPiLinkInter[] = {
+    {3, 5, -1, 1, -1}, {3, 1, 0, 1, -1}, {6, 2, 0, 1, -1}, {6, 4, 0, 1, 1}, {5, 1, 1, 0, 1},
+    {1, 5, -1, 0, 1}, {1, 3, 0, -1, -1}, {2, 6, 0, -1, -1}, {4, 6, 0, -1, 1}, {5, 3, 1, -1, -1}};
+
+struct LatticeGeom {
+    int n1h, n2;
+    Vec2 a1, a2, r[6];
+    bool pbc1, pbc2, anti1, anti2;
+    // src/Hamiltonian.jl:28-38 (s 1-based)
+    Vec2 uc(int s) const {
+        const int u = (s - 1) / 6;
+        const double k1 = (double)(u % n1h), k2 = (double)(u / n1h);
+        return {k1 * a1.x + k2 * a2.x, k1 * a1.y + k2 * a2.y};
+    }
+    // src/Hamiltonian.jl:279-283
+    Vec2 site(int s) const {
+        const Vec2 u = uc(s);
+        const Vec2 d = r[(s - 1) % 6];
+        return {u.x + d.x, u.y + d.y};
+    }
+};
+
+LatticeGeom make_geom(const kvmc_lattice_desc *lat) {
+    // src/Lattice.jl:68-92
+    LatticeGeom g;
+    const double t = lat->t, a = 2 * t;
+    g.n1h = lat->n1 / 2;
+    g.n2 = lat->n2;
+    g.a1 = {2 * a, 0.0};
+    g.a2 = {0.5 * a, 0.5 * std::sqrt(3.0) * a};
+    g.r[0] = {0.0, 0.0};
+    g.r[1] = {0.25 * g.a1.x, 0.25 * g.a1.y};
+    g.r[2] = {0.5 * g.a2.x, 0.5 * g.a2.y};
+    g.r[3] = {0.5 * g.a1.x, 0.5 * g.a1.y};
+    g.r[4] = {0.75 * g.a1.x, 0.75 * g.a1.y};
+    g.r[5] = {2.5 * t, 0.5 * std::sqrt(3.0) * t};
+    g.pbc1 = lat->pbc[0] != 0;
+    g.pbc2 = lat->pbc[1] != 0;
+    g.anti1 = lat->antipbc[0] != 0;
+    g.anti2 = lat->antipbc[1] != 0;
+    return g;
+}
+
+std::complex<double> peierls(double B, Vec2 r1, Vec2 r2) {
+    // src/Hamiltonian.jl:201-202, :325-326
+    const double phase = (B / 2) * (r1.x + r2.x) * (r2.y - r1.y);
+    return {std::cos(phase), std::sin(phase)};
+}
+
+}  // namespace
+
+extern "C" int kvmc_hopping_matrix(const kvmc_lattice_desc *lat, const kvmc_link *link_in, int32_t n_link_in,
+                                   const kvmc_link *link_inter, int32_t n_link_inter, double B, double *H) {
+    int32_t N = 0;
+    int rc = kvmc_lattice_sites(lat, &N);
+    if (rc) return rc;
+    if (!H) return fail_global(KVMC_ERR_ARGUMENT, "null H");
+    for (int d = 0; d < 2; ++d)
+        if (lat->antipbc[d] && !lat->pbc[d])
+            return fail_global(KVMC_ERR_ARGUMENT,
+                               "Invalid boundary conditions in %s direction: Cannot have antiperiodic boundary "
+                               "conditions without periodic boundary conditions",
+                               d == 0 ? "first" : "second");
+    if (!link_in) { link_in = kPiLinkIn; n_link_in = (int32_t)(sizeof kPiLinkIn / sizeof kPiLinkIn[0]); }
+    if (!link_inter) { link_inter = kPiLinkInter; n_link_inter = (int32_t)(sizeof kPiLinkInter / sizeof kPiLinkInter[0]); }
+    std::map<std::pair<int, int>, double> lin;
+    std::map<std::tuple<int, int, int, int>, double> linter;
+    for (int e = 0; e < n_link_in; ++e) {
+        const auto &k = link_in[e];
+        if (k.label1 < 1 || k.label1 > 6 || k.label2 < 1 || k.label2 > 6)
+            return fail_global(KVMC_ERR_ARGUMENT, "link_in entry %d: labels must be 1..6", e);
+        if (!lin.emplace(std::make_pair(k.label1, k.label2), k.amplitude).second)
+            return fail_global(KVMC_ERR_ARGUMENT, "link_in entry %d repeats a key", e);
+    }
+    for (int e = 0; e < n_link_inter; ++e) {
+        const auto &k = link_inter[e];
+        if (k.label1 < 1 || k.label1 > 6 || k.label2 < 1 || k.label2 > 6)
+            return fail_global(KVMC_ERR_ARGUMENT, "link_inter entry %d: labels must be 1..6", e);
+        if (!linter.emplace(std::make_tuple(k.label1, k.label2, k.dx, k.dy), k.amplitude).second)
+            return fail_global(KVMC_ERR_ARGUMENT, "link_inter entry %d repeats a key", e);
+    }
+    const LatticeGeom g = make_geom(lat);
+    const int ncell = lat->n1 * lat->n2 / 2;
+    std::vector<std::complex<double>> T((size_t)N * N);
+    auto at = [&](int s1, int s2) -> std::complex<double> & { return T[(size_t)(s1 - 1) + (size_t)(s2 - 1) * N]; };
+    // in-cell (src/Hamiltonian.jl:316-330)
+    for (int c = 1; c <= ncell; ++c)
+        for (int s1 = (c - 1) * 6 + 1; s1 <= c * 6; ++s1)
+            for (int s2 = s1 + 1; s2 <= c * 6; ++s2) {
+                auto it = lin.find({(s1 - 1) % 6 + 1, (s2 - 1) % 6 + 1});
+                if (it != lin.end()) at(s1, s2) = it->second * peierls(B, g.site(s1), g.site(s2));
+            }
+    // inter-cell (src/Hamiltonian.jl:333-343 with :99-153, :177-207)
+    const double det = g.a1.x * g.a2.y - g.a1.y * g.a2.x;
+    struct Shift { int dx, dy; double sign; };
+    std::vector<Shift> shifts;
+    for (int c1 = 1; c1 <= ncell; ++c1)
+        for (int c2 = 1; c2 <= ncell; ++c2) {
+            if (c1 == c2) continue;
+            for (int s1 = (c1 - 1) * 6 + 1; s1 <= c1 * 6; ++s1)
+                for (int s2 = (c2 - 1) * 6 + 1; s2 <= c2 * 6; ++s2) {
+                    if (s1 >= s2) continue;
+                    const int l1 = (s1 - 1) % 6 + 1, l2 = (s2 - 1) % 6 + 1;
+                    const Vec2 u1 = g.uc(s1), u2 = g.uc(s2);
+                    const double ddx = u2.x - u1.x, ddy = u2.y - u1.y;
+                    const int dx = (int)std::nearbyint((g.a2.y * ddx - g.a2.x * ddy) / det);
+                    const int dy = (int)std::nearbyint((-g.a1.y * ddx + g.a1.x * ddy) / det);
+                    shifts.clear();
+                    shifts.push_back({dx, dy, 1.0});
+                    if (g.pbc1 || g.pbc2) {
+                        const int sx[3] = {-g.n1h, 0, g.n1h}, sy[3] = {-g.n2, 0, g.n2};
+                        for (int ix = 0; ix < 3; ++ix) {
+                            if (!g.pbc1 && ix != 1) continue;
+                            for (int iy = 0; iy < 3; ++iy) {
+                                if (!g.pbc2 && iy != 1) continue;
+                                if (ix == 1 && iy == 1) continue;
+                                double sign = 1.0;
+                                if (g.anti1 && sx[ix] != 0) sign *= -1.0;
+                                if (g.anti2 && sy[iy] != 0) sign *= -1.0;
+                                const Shift cand{dx + sx[ix], dy + sy[iy], sign};
+                                bool dup = false;
+                                for (const auto &q : shifts)
+                                    if (q.dx == cand.dx && q.dy == cand.dy && q.sign == cand.sign) { dup = true; break; }
+                                if (!dup) shifts.push_back(cand);
+                            }
+                        }
+                    }
+                    const Vec2 r1 = g.site(s1);
+                    const Vec2 s2c = g.site(s2);
+                    const Vec2 dr2 = {s2c.x - u2.x, s2c.y - u2.y};
+                    for (const auto &q : shifts) {
+                        auto it = linter.find(std::make_tuple(l1, l2, q.dx, q.dy));
+                        if (it == linter.end()) continue;
+                        Vec2 ruc2 = {u1.x + q.dx * g.a1.x, u1.y + q.dx * g.a1.y};
+                        ruc2 = {ruc2.x + q.dy * g.a2.x, ruc2.y + q.dy * g.a2.y};
+                        const Vec2 r2 = {ruc2.x + dr2.x, ruc2.y + dr2.y};
+                        at(s1, s2) += (q.sign * it->second) * peierls(B, r1, r2);
+                    }
+                }
+        }
+    // H = -(T + T^dagger), column-major interleaved
+    for (int j = 0; j < N; ++j)
+        for (int i = 0; i < N; ++i) {
+            const std::complex<double> v = -(T[(size_t)i + (size_t)j * N] + std::conj(T[(size_t)j + (size_t)i * N]));
+            H[2 * ((size_t)i + (size_t)j * N)] = v.real();
+            H[2 * ((size_t)i + (size_t)j * N) + 1] = v.imag();
+        }
+    return KVMC_OK;
+}
+
+extern "C" int kvmc_bonds_from_hopping(int32_t n_sites, const double *H, int32_t *n_bonds, int32_t *bonds) {
+    if (!H || !n_bonds || n_sites <= 0) return fail_global(KVMC_ERR_ARGUMENT, "bad argument");
+    int32_t c = 0;
+    for (int j = 0; j < n_sites; ++j)
+        for (int i = 0; i <= j; ++i) {
+            const size_t e = 2 * ((size_t)i + (size_t)j * n_sites);
+            if (H[e] != 0.0 || H[e + 1] != 0.0) {
+                if (bonds) { bonds[2 * c] = i; bonds[2 * c + 1] = j; }
+                ++c;
+            }
+        }
+    *n_bonds = c;
+    return KVMC_OK;
+}
+
+// ===========================================================================
+// Handle
+// ===========================================================================
+
+extern "C" int kvmc_version(int32_t *abi, int32_t *arch) {
+    if (abi) *abi = KVMC_ABI_VERSION;
+    if (arch) *arch = 1030;
+    return KVMC_OK;
+}
+
+extern "C" int kvmc_last_error(const kvmc_handle *h, char *buf, size_t len) {
+    if (!buf || len == 0) return KVMC_ERR_ARGUMENT;
+    const std::string &s = h ? h->err : g_last_error;
+    snprintf(buf, len, "%s", s.c_str());
+    return KVMC_OK;
+}
+
+extern "C" int kvmc_destroy(kvmc_handle *h) {
+    if (!h) return KVMC_OK;
+    cudaSetDevice(h->device);
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    for (void *p : h->allocs) cudaFree(p);
+    if (h->d_scratch) cudaFree(h->d_scratch);
+    for (auto &e : h->ev_pool) cudaEventDestroy(e);
+    for (auto &e : h->region)
+        if (e) cudaEventDestroy(e);
+    if (h->stream) cudaStreamDestroy(h->stream);
+    delete h;
+    return KVMC_OK;
+}
+
+extern "C" int kvmc_create(const kvmc_model_desc *model, const kvmc_batch_desc *batch, kvmc_handle **out) {
+    if (!model || !batch || !out) return fail_global(KVMC_ERR_ARGUMENT, "null argument");
+    *out = nullptr;
+    const int N = model->n_sites, nu = model->n_up, nd = model->n_down, nb = model->n_bonds;
+    if (N <= 0 || N > 30000) return fail_global(KVMC_ERR_ARGUMENT, "n_sites must be in 1..30000");
+    if (nu <= 0 || nd <= 0 || nu + nd != N)
+        return fail_global(KVMC_ERR_ARGUMENT, "n_up + n_down must equal n_sites with both positive (got %d + %d vs %d)", nu, nd, N);
+    if (nb <= 0 || !model->bonds) return fail_global(KVMC_ERR_ARGUMENT, "empty bond list");
+    if (!model->U_up || !model->U_down) return fail_global(KVMC_ERR_ARGUMENT, "null orbitals");
+    for (int e = 0; e < nb; ++e) {
+        const int i = model->bonds[2 * e], j = model->bonds[2 * e + 1];
+        if (i < 0 || j < 0 || i >= N || j >= N) return fail_global(KVMC_ERR_BOUNDS, "bond %d (%d,%d) out of range", e, i, j);
+        if (i == j) return fail_global(KVMC_ERR_ARGUMENT, "bond %d joins site %d to itself", e, i);
+    }
+    if (batch->n_walkers <= 0) return fail_global(KVMC_ERR_ARGUMENT, "n_walkers must be positive");
+    if (batch->precision != KVMC_PLAIN_FP64 && batch->precision != KVMC_MIXED_FP32)
+        return fail_global(KVMC_ERR_ARGUMENT, "unknown precision %d", batch->precision);
+    if (batch->accept_rule != KVMC_ACCEPT_REFERENCE && batch->accept_rule != KVMC_ACCEPT_METROPOLIS)
+        return fail_global(KVMC_ERR_ARGUMENT, "unknown accept rule %d", batch->accept_rule);
+    if (batch->refresh_interval < 0 || batch->measure_interval < 0)
+        return fail_global(KVMC_ERR_ARGUMENT, "intervals must be >= 0");
+    if (std::max(nu, nd) > 160)
+        return fail_global(KVMC_ERR_UNSUPPORTED, "more than 160 orbitals per spin is not supported by this build");
+
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        cudaGetLastError();
+        return fail_global(KVMC_ERR_NO_DEVICE, "no CUDA device");
+    }
+    if (batch->device < 0 || batch->device >= ndev) return fail_global(KVMC_ERR_NO_DEVICE, "device %d not present", batch->device);
+    cudaDeviceProp prop{};
+    cudaGetDeviceProperties(&prop, batch->device);
+    if (prop.major * 10 + prop.minor != 103)
+        return fail_global(KVMC_ERR_NO_DEVICE, "device %d is sm_%d%d; this library is built for sm_103a", batch->device, prop.major, prop.minor);
+
+    kvmc_handle *h = new kvmc_handle();
+    h->device = batch->device;
+    h->model = *model;
+    h->batch = *batch;
+    h->n_sites = N; h->n_up = nu; h->n_dn = nd; h->n_bonds = nb; h->n_walkers = batch->n_walkers;
+    h->ld_up = (nu + 3) / 4 * 4;
+    h->ld_dn = (nd + 3) / 4 * 4;
+    h->mixed = batch->precision == KVMC_MIXED_FP32;
+    const int nocc = std::min(nu, nd);
+    h->measure_every = batch->measure_interval > 0 ? batch->measure_interval : nocc;
+    if (h->mixed) h->refresh_every = batch->refresh_interval > 0 ? batch->refresh_interval : 128;
+    else h->refresh_every = batch->refresh_interval > 0 ? batch->refresh_interval : nocc;
+
+    auto bail = [&](int rc) { g_last_error = h->err; kvmc_destroy(h); return rc; };
+    if (int rc = set_device(h)) return bail(rc);
+    if (int rc = h->cuda(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking), "stream")) return bail(rc);
+
+    DevModel &m = h->dm;
+    m.n_sites = N; m.n_up = nu; m.n_dn = nd; m.ld_up = h->ld_up; m.ld_dn = h->ld_dn; m.n_bonds = nb;
+    // orbitals row-major
+    std::vector<double> Uu((size_t)N * nu), Ud((size_t)N * nd);
+    for (int r = 0; r < N; ++r) {
+        for (int c = 0; c < nu; ++c) Uu[(size_t)r * nu + c] = model->U_up[(size_t)r + (size_t)c * N];
+        for (int c = 0; c < nd; ++c) Ud[(size_t)r * nd + c] = model->U_down[(size_t)r + (size_t)c * N];
+    }
+    // bonds and adjacency
+    std::vector<short2> bonds(nb);
+    std::vector<int> deg(N + 1, 0);
+    for (int e = 0; e < nb; ++e) {
+        bonds[e] = make_short2((short)model->bonds[2 * e], (short)model->bonds[2 * e + 1]);
+        deg[model->bonds[2 * e]]++;
+        deg[model->bonds[2 * e + 1]]++;
+    }
+    std::vector<int> off(N + 1, 0);
+    for (int s = 0; s < N; ++s) off[s + 1] = off[s] + deg[s];
+    std::vector<short> nbr(2 * (size_t)nb);
+    std::vector<int> fill(off.begin(), off.end() - 1);
+    for (int e = 0; e < nb; ++e) {
+        const int i = model->bonds[2 * e], j = model->bonds[2 * e + 1];
+        nbr[fill[i]++] = (short)j;
+        nbr[fill[j]++] = (short)i;
+    }
+    double *dUu, *dUd;
+    short2 *dB;
+    int *dOff;
+    short *dNbr;
+    int rc = KVMC_OK;
+    if ((rc = h->alloc(&dUu, Uu.size())) || (rc = h->alloc(&dUd, Ud.size())) || (rc = h->alloc(&dB, nb)) ||
+        (rc = h->alloc(&dOff, N + 1)) || (rc = h->alloc(&dNbr, nbr.size())))
+        return bail(rc);
+    cudaMemcpy(dUu, Uu.data(), Uu.size() * 8, cudaMemcpyHostToDevice);
+    cudaMemcpy(dUd, Ud.data(), Ud.size() * 8, cudaMemcpyHostToDevice);
+    cudaMemcpy(dB, bonds.data(), nb * sizeof(short2), cudaMemcpyHostToDevice);
+    cudaMemcpy(dOff, off.data(), (N + 1) * sizeof(int), cudaMemcpyHostToDevice);
+    cudaMemcpy(dNbr, nbr.data(), nbr.size() * sizeof(short), cudaMemcpyHostToDevice);
+    m.U_up = dUu; m.U_dn = dUd; m.bonds = dB; m.nbr_off = dOff; m.nbr = dNbr;
+
+    DevBatch &b = h->db;
+    const int Wk = h->n_walkers;
+    b.n_walkers = Wk;
+    const size_t wblock = (size_t)N * (h->ld_up + h->ld_dn);
+    b.W64 = nullptr;
+    b.W32 = nullptr;
+    if (h->mixed) rc = h->alloc(&b.W32, wblock * Wk);
+    else rc = h->alloc(&b.W64, wblock * Wk);
+    if (rc) return bail(rc);
+    if ((rc = h->alloc(&b.kappa_up, (size_t)Wk * N)) || (rc = h->alloc(&b.kappa_dn, (size_t)Wk * N)) ||
+        (rc = h->alloc(&b.t, Wk)) || (rc = h->alloc(&b.t_end, Wk)) || (rc = h->alloc(&b.since, Wk)) ||
+        (rc = h->alloc(&b.sum_e, Wk)) || (rc = h->alloc(&b.sum_e2, Wk)) || (rc = h->alloc(&b.n_meas, Wk)) ||
+        (rc = h->alloc(&b.accepted, Wk)) || (rc = h->alloc(&b.proposals, Wk)) || (rc = h->alloc(&b.status, Wk)) ||
+        (rc = h->alloc(&b.logdet, 4 * (size_t)Wk)) || (rc = h->alloc(&b.drift, Wk)) ||
+        (rc = h->alloc(&b.energy_out, Wk)) || (rc = h->alloc(&b.refresh_count, 1)) || (rc = h->alloc(&h->d_active, 1)) ||
+        (rc = h->alloc(&h->d_attempt, Wk)) || (rc = h->alloc(&h->d_redo, Wk)))
+        return bail(rc);
+    if (h->mixed) cudaMemset(b.W32, 0, wblock * Wk * sizeof(float));
+    else cudaMemset(b.W64, 0, wblock * Wk * sizeof(double));
+    cudaMemset(b.kappa_up, 0, (size_t)Wk * N * 2);
+    cudaMemset(b.kappa_dn, 0, (size_t)Wk * N * 2);
+    cudaMemset(b.t, 0, Wk * 8);
+    cudaMemset(b.t_end, 0, Wk * 8);
+    cudaMemset(b.since, 0, Wk * 4);
+    cudaMemset(b.status, 0, Wk * 4);
+    cudaMemset(b.drift, 0, Wk * 4);
+    cudaMemset(b.refresh_count, 0, 8);
+    if (int e = kvmc_reset_stats(h)) return bail(e);
+    // shared-memory capacity decides whether the FP32 W can be staged on chip
+    const int optin = kvmc::max_smem_optin(h->device);
+    if ((size_t)optin < kvmc::refresh_smem(m))
+        return bail(h->fail(KVMC_ERR_UNSUPPORTED, "refresh needs %zu B shared memory, device offers %d", kvmc::refresh_smem(m), optin));
+    h->smem_w = h->mixed && kvmc::mixed_sweep_smem(m) <= (size_t)optin;
+    for (auto &e : h->region)
+        if ((rc = h->cuda(cudaEventCreate(&e), "event"))) return bail(rc);
+    if ((rc = h->cuda(cudaDeviceSynchronize(), "create"))) return bail(rc);
+    *out = h;
+    return KVMC_OK;
+}
+
+extern "C" int kvmc_reset_stats(kvmc_handle *h) {
+    if (!h) return fail_global(KVMC_ERR_ARGUMENT, "null handle");
+    KV_TRY(set_device(h));
+    const size_t Wk = h->n_walkers;
+    auto &b = h->db;
+    cudaMemsetAsync(b.sum_e, 0, Wk * 8, h->stream);
+    cudaMemsetAsync(b.sum_e2, 0, Wk * 8, h->stream);
+    cudaMemsetAsync(b.n_meas, 0, Wk * 8, h->stream);
+    cudaMemsetAsync(b.accepted, 0, Wk * 8, h->stream);
+    cudaMemsetAsync(b.proposals, 0, Wk * 8, h->stream);
+    return h->cuda(cudaStreamSynchronize(h->stream), "reset stats");
+}
+
+extern "C" int kvmc_init(kvmc_handle *h, const int32_t *kappa_up, const int32_t *kappa_down, int32_t *attempts) {
+    if (!h) return fail_global(KVMC_ERR_ARGUMENT, "null handle");
+    KV_TRY(set_device(h));
+    const int Wk = h->n_walkers;
+    KV_TRY(h->cuda(cudaMemsetAsync(h->db.t, 0, Wk * 8, h->stream), "memset"));
+    KV_TRY(h->cuda(cudaMemsetAsync(h->db.status, 0, Wk * 4, h->stream), "memset"));
+    if (kappa_up || kappa_down) {
+        if (!kappa_up || !kappa_down) return h->fail(KVMC_ERR_ARGUMENT, "give both kappa_up and kappa_down, or neither");
+        KV_TRY(upload_kappa(h, kappa_up, kappa_down));
+        KV_TRY(full_refresh(h, false));
+        if (attempts) for (int w = 0; w < Wk; ++w) attempts[w] = 0;
+        return check_status(h, nullptr);
+    }
+    // seeded random starts, redrawn while tilde_U is singular for either spin:
+    // min|pivot| / max|pivot| of its partially pivoted LU at most 1e-8
+    std::vector<int> att(Wk, 0), redo(Wk, 1);
+    std::vector<double> ld(4 * (size_t)Wk);
+    const double min_log_ratio = std::log(1e-8);
+    const int max_attempts = 256;
+    for (int round = 0; round < max_attempts; ++round) {
+        KV_TRY(h->cuda(cudaMemcpyAsync(h->d_attempt, att.data(), Wk * 4, cudaMemcpyHostToDevice, h->stream), "upload"));
+        KV_TRY(h->cuda(cudaMemcpyAsync(h->d_redo, redo.data(), Wk * 4, cudaMemcpyHostToDevice, h->stream), "upload"));
+        KV_TRY(h->cuda(kvmc::launch_init_random(h->dm, h->db, h->batch.seed, h->d_attempt, h->d_redo, h->stream), "init launch"));
+        KV_TRY(full_refresh(h, false));
+        KV_TRY(h->cuda(cudaMemcpy(ld.data(), h->db.logdet, ld.size() * 8, cudaMemcpyDeviceToHost), "logdet"));
+        int left = 0;
+        for (int w = 0; w < Wk; ++w) {
+            if (!redo[w]) continue;
+            const bool ok = ld[4 * w + 2] > min_log_ratio && ld[4 * w + 3] > min_log_ratio;
+            if (ok) redo[w] = 0;
+            else { ++att[w]; ++left; }
+        }
+        if (!left) break;
+        if (round == max_attempts - 1)
+            return h->fail(KVMC_ERR_SINGULAR, "%d walker(s) found no non-singular start in %d draws", left, max_attempts);
+    }
+    KV_TRY(h->cuda(cudaMemsetAsync(h->db.status, 0, Wk * 4, h->stream), "memset"));
+    KV_TRY(full_refresh(h, false));
+    if (attempts) for (int w = 0; w < Wk; ++w) attempts[w] = att[w] + 1;
+    return check_status(h, nullptr);
+}
+
+extern "C" int kvmc_enable_timing(kvmc_handle *h, int32_t on) {
+    if (!h) return fail_global(KVMC_ERR_ARGUMENT, "null handle");
+    h->timing = on != 0;
+    h->t_ms[0] = h->t_ms[1] = 0;
+    h->t_launch[0] = h->t_launch[1] = 0;
+    return KVMC_OK;
+}
+
+extern "C" int kvmc_region_timer(kvmc_handle *h, int32_t start, double *ms) {
+    if (!h) return fail_global(KVMC_ERR_ARGUMENT, "null handle");
+    KV_TRY(set_device(h));
+    if (start) return h->cuda(cudaEventRecord(h->region[0], h->stream), "event");
+    KV_TRY(h->cuda(cudaEventRecord(h->region[1], h->stream), "event"));
+    KV_TRY(h->cuda(cudaEventSynchronize(h->region[1]), "event"));
+    float t = 0.f;
+    KV_TRY(h->cuda(cudaEventElapsedTime(&t, h->region[0], h->region[1]), "event time"));
+    if (ms) *ms = t;
+    return KVMC_OK;
+}
+
+extern "C" int kvmc_kernel_time(kvmc_handle *h, int32_t kind, double *total_ms, int64_t *launches) {
+    if (!h || kind < 0 || kind > 1) return fail_global(KVMC_ERR_ARGUMENT, "bad argument");
+    if (total_ms) *total_ms = h->t_ms[kind];
+    if (launches) *launches = h->t_launch[kind];
+    return KVMC_OK;
+}
+
+namespace {
+
+// One launch with optional event timing (kind 0 sweep, 1 refresh).  The
+// events are only read by collect_timing() after the stream is synchronised.
+template <typename F>
+int timed(kvmc_handle *h, int kind, F &&launch, const char *what) {
+    int first = -1;
+    if (h->timing) {
+        first = 0;
+        for (const auto &u : h->ev_used) first = std::max(first, u.second + 2);
+        while ((int)h->ev_pool.size() < first + 2) {
+            cudaEvent_t e;
+            KV_TRY(h->cuda(cudaEventCreate(&e), "event"));
+            h->ev_pool.push_back(e);
+        }
+        KV_TRY(h->cuda(cudaEventRecord(h->ev_pool[first], h->stream), "event"));
+    }
+    KV_TRY(h->cuda(launch(), what));
+    if (h->timing) {
+        KV_TRY(h->cuda(cudaEventRecord(h->ev_pool[first + 1], h->stream), "event"));
+        h->ev_used.push_back({kind, first});
+    }
+    return KVMC_OK;
+}
+
+int collect_timing(kvmc_handle *h) {
+    for (const auto &u : h->ev_used) {
+        float ms = 0.f;
+        KV_TRY(h->cuda(cudaEventElapsedTime(&ms, h->ev_pool[u.second], h->ev_pool[u.second + 1]), "event time"));
+        h->t_ms[u.first] += ms;
+        h->t_launch[u.first] += 1;
+    }
+    h->ev_used.clear();
+    return KVMC_OK;
+}
+
+struct Snapshot {
+    std::vector<double> se, se2;
+    std::vector<long long> nm, acc, prop;
+};
+
+int snapshot(kvmc_handle *h, Snapshot &s) {
+    const size_t Wk = h->n_walkers;
+    s.se.resize(Wk); s.se2.resize(Wk); s.nm.resize(Wk); s.acc.resize(Wk); s.prop.resize(Wk);
+    auto &b = h->db;
+    KV_TRY(h->cuda(cudaMemcpyAsync(s.se.data(), b.sum_e, Wk * 8, cudaMemcpyDeviceToHost, h->stream), "stats"));
+    KV_TRY(h->cuda(cudaMemcpyAsync(s.se2.data(), b.sum_e2, Wk * 8, cudaMemcpyDeviceToHost, h->stream), "stats"));
+    KV_TRY(h->cuda(cudaMemcpyAsync(s.nm.data(), b.n_meas, Wk * 8, cudaMemcpyDeviceToHost, h->stream), "stats"));
+    KV_TRY(h->cuda(cudaMemcpyAsync(s.acc.data(), b.accepted, Wk * 8, cudaMemcpyDeviceToHost, h->stream), "stats"));
+    KV_TRY(h->cuda(cudaMemcpyAsync(s.prop.data(), b.proposals, Wk * 8, cudaMemcpyDeviceToHost, h->stream), "stats"));
+    return h->cuda(cudaStreamSynchronize(h->stream), "stats");
+}
+
+}  // namespace
+
+extern "C" int kvmc_sweep(kvmc_handle *h, int64_t proposals_per_walker, kvmc_sweep_stats *stats) {
+    if (!h) return fail_global(KVMC_ERR_ARGUMENT, "null handle");
+    if (proposals_per_walker < 0) return h->fail(KVMC_ERR_ARGUMENT, "proposals_per_walker must be >= 0");
+    KV_TRY(set_device(h));
+    Snapshot before;
+    unsigned long long ref0 = 0, ref1 = 0;
+    if (stats) {
+        KV_TRY(snapshot(h, before));
+        std::memset(stats, 0, sizeof *stats);
+        KV_TRY(h->cuda(cudaMemcpy(&ref0, h->db.refresh_count, 8, cudaMemcpyDeviceToHost), "refresh count"));
+    }
+    if (proposals_per_walker == 0) return KVMC_OK;
+    kvmc::SweepParams p{};
+    p.seed = h->batch.seed;
+    p.accept_rule = h->batch.accept_rule;
+    p.refresh_every = h->refresh_every;
+    p.measure_every = h->measure_every;
+    KV_TRY(h->cuda(kvmc::launch_set_tend(h->db, proposals_per_walker, h->stream), "set t_end"));
+    KV_TRY(h->cuda(cudaMemsetAsync(h->db.drift, 0, sizeof(float) * h->n_walkers, h->stream), "memset"));
+    int launches = 1;
+    // Between host checks the loop issues a group of (sweep, refresh) pairs;
+    // walkers that are done return at once.
+    const int group = h->mixed ? 4 : 8;
+    for (int iter = 0;; iter += group) {
+        for (int g = 0; g < group; ++g) {
+            KV_TRY(h->cuda(cudaMemsetAsync(h->d_active, 0, sizeof(int), h->stream), "memset"));
+            KV_TRY(timed(h, 0, [&] { return kvmc::launch_sweep(h->dm, h->db, p, h->mixed, h->smem_w, h->d_active, h->stream); },
+                         "sweep launch"));
+            KV_TRY(timed(h, 1, [&] { return kvmc::launch_refresh(h->dm, h->db, h->mixed, 1, h->mixed ? 1 : 0, h->stream); },
+                         "refresh launch"));
+            launches += 2;
+        }
+        int active = 0;
+        KV_TRY(h->cuda(cudaMemcpyAsync(&active, h->d_active, sizeof(int), cudaMemcpyDeviceToHost, h->stream), "active"));
+        KV_TRY(h->cuda(cudaStreamSynchronize(h->stream), "sweep"));
+        KV_TRY(collect_timing(h));
+        if (active == 0) break;
+        if (iter > 100000000) return h->fail(KVMC_ERR_NUMERIC, "sweep made no progress");
+    }
+    int bad = 0;
+    KV_TRY(check_status(h, &bad));
+    if (stats) {
+        Snapshot after;
+        KV_TRY(snapshot(h, after));
+        for (int w = 0; w < h->n_walkers; ++w) {
+            stats->proposals += after.prop[w] - before.prop[w];
+            stats->accepted += after.acc[w] - before.acc[w];
+            stats->measurements += after.nm[w] - before.nm[w];
+            stats->sum_energy += after.se[w] - before.se[w];
+            stats->sum_energy2 += after.se2[w] - before.se2[w];
+        }
+        std::vector<float> dr(h->n_walkers);
+        KV_TRY(h->cuda(cudaMemcpy(dr.data(), h->db.drift, dr.size() * 4, cudaMemcpyDeviceToHost), "drift"));
+        double md = 0;
+        for (float d : dr) md = std::max(md, (double)d);
+        stats->max_drift = md;
+        stats->bad_walkers = bad;
+        stats->launches = launches;
+        KV_TRY(h->cuda(cudaMemcpy(&ref1, h->db.refresh_count, 8, cudaMemcpyDeviceToHost), "refresh count"));
+        stats->refreshes = (int64_t)(ref1 - ref0);
+    }
+    return KVMC_OK;
+}
+
+extern "C" int kvmc_measure(kvmc_handle *h, double *local_energy) {
+    if (!h || !local_energy) return fail_global(KVMC_ERR_ARGUMENT, "null argument");
+    KV_TRY(set_device(h));
+    KV_TRY(h->cuda(kvmc::launch_measure(h->dm, h->db, h->mixed, h->stream), "measure launch"));
+    KV_TRY(h->cuda(cudaMemcpyAsync(local_energy, h->db.energy_out, sizeof(double) * h->n_walkers,
+                                   cudaMemcpyDeviceToHost, h->stream), "measure"));
+    return h->cuda(cudaStreamSynchronize(h->stream), "measure");
+}
+
+extern "C" int kvmc_eval_ratios(kvmc_handle *h, int32_t n_moves, const int32_t *moves, double *ratios) {
+    if (!h || !moves || !ratios || n_moves <= 0) return fail_global(KVMC_ERR_ARGUMENT, "bad argument");
+    KV_TRY(set_device(h));
+    const size_t cnt = (size_t)h->n_walkers * n_moves;
+    for (size_t k = 0; k < cnt; ++k) {
+        const int32_t *mv = moves + 4 * k;
+        if (mv[0] < 0 || mv[0] >= h->n_sites || mv[2] < 0 || mv[2] >= h->n_sites || mv[1] < 1 || mv[1] > h->n_up ||
+            mv[3] < 1 || mv[3] > h->n_dn)
+            return h->fail(KVMC_ERR_BOUNDS, "move %zu out of range", k);
+    }
+    void *scr = nullptr;
+    KV_TRY(h->scratch(cnt * 4 * sizeof(int) + cnt * sizeof(double) + 256, &scr));
+    int *d_moves = static_cast<int *>(scr);
+    double *d_out = reinterpret_cast<double *>(static_cast<char *>(scr) + ((cnt * 16 + 255) / 256) * 256);
+    KV_TRY(h->cuda(cudaMemcpyAsync(d_moves, moves, cnt * 16, cudaMemcpyHostToDevice, h->stream), "upload"));
+    KV_TRY(h->cuda(kvmc::launch_eval_ratios(h->dm, h->db, h->mixed, n_moves, d_moves, d_out, h->stream), "ratio launch"));
+    KV_TRY(h->cuda(cudaMemcpyAsync(ratios, d_out, cnt * 8, cudaMemcpyDeviceToHost, h->stream), "ratios"));
+    return h->cuda(cudaStreamSynchronize(h->stream), "ratios");
+}
+
+extern "C" int kvmc_apply_moves(kvmc_handle *h, const int32_t *moves) {
+    if (!h || !moves) return fail_global(KVMC_ERR_ARGUMENT, "bad argument");
+    KV_TRY(set_device(h));
+    for (int w = 0; w < h->n_walkers; ++w) {
+        const int32_t *mv = moves + 5 * (size_t)w;
+        if (mv[0] == 0) continue;
+        if (mv[0] != 1 && mv[0] != 2) return h->fail(KVMC_ERR_ARGUMENT, "walker %d: flag must be 0, 1 or 2", w);
+        if (mv[1] < 0 || mv[1] >= h->n_sites || mv[2] < 0 || mv[2] >= h->n_sites || mv[3] < 1 || mv[3] > h->n_up ||
+            mv[4] < 1 || mv[4] > h->n_dn)
+            return h->fail(KVMC_ERR_BOUNDS, "walker %d: move out of range", w);
+    }
+    void *scr = nullptr;
+    KV_TRY(h->scratch((size_t)h->n_walkers * 5 * sizeof(int), &scr));
+    KV_TRY(h->cuda(cudaMemcpyAsync(scr, moves, (size_t)h->n_walkers * 5 * sizeof(int), cudaMemcpyHostToDevice, h->stream), "upload"));
+    KV_TRY(h->cuda(kvmc::launch_apply_moves(h->dm, h->db, h->mixed, static_cast<int *>(scr), h->stream), "move launch"));
+    return h->cuda(cudaStreamSynchronize(h->stream), "apply moves");
+}
+
+extern "C" int kvmc_refresh(kvmc_handle *h) {
+    if (!h) return fail_global(KVMC_ERR_ARGUMENT, "null handle");
+    KV_TRY(set_device(h));
+    KV_TRY(h->cuda(cudaMemsetAsync(h->db.status, 0, h->n_walkers * 4, h->stream), "memset"));
+    KV_TRY(full_refresh(h, h->mixed));
+    return check_status(h, nullptr);
+}
+
+extern "C" int kvmc_get_state(kvmc_handle *h, int32_t *kappa_up, int32_t *kappa_down, int64_t *counters) {
+    if (!h) return fail_global(KVMC_ERR_ARGUMENT, "null handle");
+    KV_TRY(set_device(h));
+    const size_t tot = (size_t)h->n_walkers * h->n_sites;
+    std::vector<short> a(tot), b(tot);
+    KV_TRY(h->cuda(cudaMemcpy(a.data(), h->db.kappa_up, tot * 2, cudaMemcpyDeviceToHost), "kappa"));
+    KV_TRY(h->cuda(cudaMemcpy(b.data(), h->db.kappa_dn, tot * 2, cudaMemcpyDeviceToHost), "kappa"));
+    if (kappa_up) for (size_t e = 0; e < tot; ++e) kappa_up[e] = a[e];
+    if (kappa_down) for (size_t e = 0; e < tot; ++e) kappa_down[e] = b[e];
+    if (counters)
+        KV_TRY(h->cuda(cudaMemcpy(counters, h->db.t, h->n_walkers * 8, cudaMemcpyDeviceToHost), "counters"));
+    return KVMC_OK;
+}
+
+extern "C" int kvmc_set_state(kvmc_handle *h, const int32_t *kappa_up, const int32_t *kappa_down, const int64_t *counters) {
+    if (!h || !kappa_up || !kappa_down) return fail_global(KVMC_ERR_ARGUMENT, "null argument");
+    KV_TRY(set_device(h));
+    if (counters)
+        for (int w = 0; w < h->n_walkers; ++w)
+            if (counters[w] < 0) return h->fail(KVMC_ERR_ARGUMENT, "negative counter for walker %d", w);
+    KV_TRY(upload_kappa(h, kappa_up, kappa_down));
+    if (counters)
+        KV_TRY(h->cuda(cudaMemcpy(h->db.t, counters, h->n_walkers * 8, cudaMemcpyHostToDevice), "counters"));
+    KV_TRY(h->cuda(cudaMemsetAsync(h->db.status, 0, h->n_walkers * 4, h->stream), "memset"));
+    KV_TRY(full_refresh(h, false));
+    return check_status(h, nullptr);
+}
+
+extern "C" int kvmc_get_w(kvmc_handle *h, double *W_up, double *W_down) {
+    if (!h) return fail_global(KVMC_ERR_ARGUMENT, "null handle");
+    KV_TRY(set_device(h));
+    const int N = h->n_sites;
+    const size_t wblock = (size_t)N * (h->ld_up + h->ld_dn);
+    const size_t tot = wblock * h->n_walkers;
+    std::vector<double> buf(tot);
+    if (h->mixed) {
+        std::vector<float> f(tot);
+        KV_TRY(h->cuda(cudaMemcpy(f.data(), h->db.W32, tot * 4, cudaMemcpyDeviceToHost), "W"));
+        for (size_t e = 0; e < tot; ++e) buf[e] = f[e];
+    } else {
+        KV_TRY(h->cuda(cudaMemcpy(buf.data(), h->db.W64, tot * 8, cudaMemcpyDeviceToHost), "W"));
+    }
+    for (int w = 0; w < h->n_walkers; ++w) {
+        const double *base = buf.data() + (size_t)w * wblock;
+        for (int r = 0; r < N; ++r) {
+            if (W_up)
+                for (int c = 0; c < h->n_up; ++c)
+                    W_up[((size_t)w * N + r) * h->n_up + c] = base[(size_t)r * h->ld_up + c];
+            if (W_down)
+                for (int c = 0; c < h->n_dn; ++c)
+                    W_down[((size_t)w * N + r) * h->n_dn + c] = base[(size_t)N * h->ld_up + (size_t)r * h->ld_dn + c];
+        }
+    }
+    return KVMC_OK;
+}
+
+extern "C" int kvmc_walker_stats(kvmc_handle *h, double *sum_e, double *sum_e2, int64_t *n_meas, int64_t *accepted,
+                                 int64_t *proposals, int32_t *status) {
+    if (!h) return fail_global(KVMC_ERR_ARGUMENT, "null handle");
+    KV_TRY(set_device(h));
+    const size_t Wk = h->n_walkers;
+    auto &b = h->db;
+    if (sum_e) KV_TRY(h->cuda(cudaMemcpy(sum_e, b.sum_e, Wk * 8, cudaMemcpyDeviceToHost), "stats"));
+    if (sum_e2) KV_TRY(h->cuda(cudaMemcpy(sum_e2, b.sum_e2, Wk * 8, cudaMemcpyDeviceToHost), "stats"));
+    if (n_meas) KV_TRY(h->cuda(cudaMemcpy(n_meas, b.n_meas, Wk * 8, cudaMemcpyDeviceToHost), "stats"));
+    if (accepted) KV_TRY(h->cuda(cudaMemcpy(accepted, b.accepted, Wk * 8, cudaMemcpyDeviceToHost), "stats"));
+    if (proposals) KV_TRY(h->cuda(cudaMemcpy(proposals, b.proposals, Wk * 8, cudaMemcpyDeviceToHost), "stats"));
+    if (status) KV_TRY(h->cuda(cudaMemcpy(status, b.status, Wk * 4, cudaMemcpyDeviceToHost), "stats"));
+    return KVMC_OK;
+}

@@ -1,0 +1,84 @@
+// Internal interface between the host side of libkvmc (kvmc_api.cpp) and its
+// CUDA kernels (kvmc_kernels.cu).  Not part of the public C ABI.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace kvmc {
+
+// Device view of the model, shared by every walker.
+struct DevModel {
+    int n_sites;         // N
+    int n_up, n_dn;      // orbitals per spin; n_up + n_dn == N
+    int ld_up, ld_dn;    // padded row strides of W (multiples of 4)
+    int n_bonds;
+    const short2 *bonds; // [n_bonds] 0-based (i, j)
+    const int *nbr_off;  // [N+1] CSR adjacency built from the bond list
+    const short *nbr;    // [2*n_bonds]
+    const double *U_up;  // row-major [N][n_up]
+    const double *U_dn;  // row-major [N][n_dn]
+};
+
+// Device view of the batch state.
+struct DevBatch {
+    int n_walkers;
+    short *kappa_up;       // [W][N]  0 = empty, 1..n = label
+    short *kappa_dn;       // [W][N]
+    double *W64;           // plain form: [W][N*(ld_up+ld_dn)] (up block then down block)
+    float *W32;            // mixed form: same layout in FP32
+    long long *t;          // [W] proposals made (Philox counter)
+    long long *t_end;      // [W] target counter for the running kvmc_sweep
+    int *since;            // [W] accepted moves since the last refresh
+    double *sum_e;         // [W]
+    double *sum_e2;        // [W]
+    long long *n_meas;     // [W]
+    long long *accepted;   // [W]
+    long long *proposals;  // [W]
+    int *status;           // [W] bit flags (kStatus*)
+    double *logdet;        // [W][4] from the last refresh: log|det| up, down,
+                           // log(min|pivot|/max|pivot|) up, down
+    float *drift;          // [W] max |W32_old - W64_new| at the last refresh
+    double *energy_out;    // [W] scratch for kvmc_measure
+    unsigned long long *refresh_count;  // walker refreshes performed (one counter)
+};
+
+enum : int {
+    kStatusSingular = 1,
+    kStatusNonFinite = 2,
+};
+
+struct SweepParams {
+    unsigned long long seed;
+    int accept_rule;      // 0 reference, 1 metropolis
+    int refresh_every;    // mixed: accepted moves between refreshes
+    int measure_every;    // proposals between energy samples
+};
+
+// Launchers.  All enqueue on `stream` and return the launch error.
+// only_due: refresh only walkers whose `since` is negative (marked due by the
+// sweep kernel).  track_drift: record max |W_old - W_new| per walker.
+cudaError_t launch_refresh(const DevModel &m, const DevBatch &b, bool fp32_out,
+                           int only_due, int track_drift, cudaStream_t stream);
+// mixed=false: plain FP64 form (W in global memory, refresh every
+// p.refresh_every proposals).  mixed=true: FP32 form, W staged in shared
+// memory when smem_w (else read in place), refresh every p.refresh_every
+// accepted moves.  active (device int) counts walkers left short of t_end.
+cudaError_t launch_sweep(const DevModel &m, const DevBatch &b, const SweepParams &p,
+                         bool mixed, bool smem_w, int *active, cudaStream_t stream);
+cudaError_t launch_measure(const DevModel &m, const DevBatch &b, bool fp32, cudaStream_t stream);
+cudaError_t launch_eval_ratios(const DevModel &m, const DevBatch &b, bool fp32, int n_moves,
+                               const int *moves, double *out, cudaStream_t stream);
+cudaError_t launch_apply_moves(const DevModel &m, const DevBatch &b, bool fp32,
+                               const int *moves, cudaStream_t stream);
+cudaError_t launch_set_tend(const DevBatch &b, long long proposals, cudaStream_t stream);
+cudaError_t launch_init_random(const DevModel &m, const DevBatch &b, unsigned long long seed,
+                               const int *attempt, const int *redo, cudaStream_t stream);
+
+// Shared-memory bytes the mixed sweep kernel needs for this model (0 if it
+// cannot hold both W matrices on one SM).
+size_t mixed_sweep_smem(const DevModel &m);
+size_t refresh_smem(const DevModel &m);
+int max_smem_optin(int device);
+
+}  // namespace kvmc

@@ -1,0 +1,817 @@
+// CUDA kernels of libkvmc (sm_103a).
+//
+// Reference counterparts (KagomeDSL.jl):
+//   refresh_kernel      reevaluateW! + tilde_U      src/MonteCarlo.jl:55-115
+//   sweep_kernel        Carlo.sweep! + Z + update_configurations! + update_W!
+//                       src/MonteCarlo.jl:460-607, measure! :628-634,
+//                       getOL src/Hamiltonian.jl:762-778
+//   measure_kernel      getOL                       src/Hamiltonian.jl:762-778
+//   ratio_kernel        the ratio of src/MonteCarlo.jl:576-580
+//   apply_moves_kernel  update_configurations!      src/MonteCarlo.jl:497-511
+//   init_random_kernel  seeded random starts (replaces the QR start of
+//                       src/MonteCarlo.jl:326-357 for batches of walkers)
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "kvmc_internal.h"
+
+namespace kvmc {
+
+// ---------------------------------------------------------------------------
+// Philox4x32-10 (Salmon et al., SC'11): counter-based, so proposal t of
+// walker w is the same draw however the proposals are split across launches.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint4 philox4x32_10(uint4 c, uint2 k) {
+#pragma unroll
+    for (int r = 0; r < 10; ++r) {
+        const unsigned hi0 = __umulhi(0xD2511F53u, c.x);
+        const unsigned lo0 = 0xD2511F53u * c.x;
+        const unsigned hi1 = __umulhi(0xCD9E8D57u, c.z);
+        const unsigned lo1 = 0xCD9E8D57u * c.z;
+        c = make_uint4(hi1 ^ c.y ^ k.x, lo1, hi0 ^ c.w ^ k.y, lo0);
+        if (r < 9) {
+            k.x += 0x9E3779B9u;
+            k.y += 0xBB67AE85u;
+        }
+    }
+    return c;
+}
+
+// Proposal t of walker w: r uniform in [0,1) (53 bits) and a bond index.
+__device__ __forceinline__ void proposal_draw(unsigned long long seed, int walker, long long t,
+                                              int n_bonds, double &r, int &bond) {
+    const unsigned long long ut = (unsigned long long)t;
+    const uint4 x = philox4x32_10(make_uint4((unsigned)ut, (unsigned)(ut >> 32), (unsigned)walker, 0u),
+                                  make_uint2((unsigned)seed, (unsigned)(seed >> 32)));
+    const unsigned long long u53 = ((unsigned long long)(x.x >> 5) << 26) | (x.y >> 6);
+    r = (double)u53 * (1.0 / 9007199254740992.0);
+    bond = (int)(((unsigned long long)x.z * (unsigned long long)(unsigned)n_bonds) >> 32);
+}
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Block-wide FP64 sum; every thread gets the result.  `red` holds >= 33 doubles.
+__device__ double block_sum(double v, double *red) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    v = warp_sum(v);
+    __syncthreads();
+    if (lane == 0) red[warp] = v;
+    __syncthreads();
+    if (warp == 0) {
+        double s = lane < nw ? red[lane] : 0.0;
+        s = warp_sum(s);
+        if (lane == 0) red[32] = s;
+    }
+    __syncthreads();
+    return red[32];
+}
+
+// Block-wide FP64 max; every thread gets the result.
+__device__ double block_sum_max(double v, double *red) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+    __syncthreads();
+    if (lane == 0) red[warp] = v;
+    __syncthreads();
+    if (warp == 0) {
+        double s = lane < nw ? red[lane] : -INFINITY;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) s = fmax(s, __shfl_xor_sync(0xffffffffu, s, o));
+        if (lane == 0) red[32] = s;
+    }
+    __syncthreads();
+    return red[32];
+}
+
+__device__ __forceinline__ void atomic_max_nonneg(float *addr, float v) {
+    atomicMax(reinterpret_cast<int *>(addr), __float_as_int(v));
+}
+
+// ---------------------------------------------------------------------------
+// Refresh: W_sigma = U_sigma * tilde_U_sigma^{-1} in FP64.
+// One CTA per (walker, spin).  tilde_U (row l = U[R,:] with kappa[R] == l) is
+// LU-factorised with partial pivoting in shared memory; the rows of W at
+// sites not holding this spin are solved one warp per row (w * tilde_U = u,
+// forward with the upper factor, backward with the unit-lower factor, then
+// the pivot permutation), the rows at occupied sites are unit rows.
+// ---------------------------------------------------------------------------
+constexpr int kRefreshThreads = 256;
+
+template <int NQ, typename OutT>
+__device__ void solve_rows(const double *A, int lda, const double *invd, const int *perm,
+                           const double *U, int n, const short *rows, int n_rows,
+                           OutT *Wout, int ldw, float *drift_slot, bool track_drift) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    float dmax = 0.f;
+    for (int idx = warp; idx < n_rows; idx += nw) {
+        const int R = rows[idx];
+        double y[NQ];
+#pragma unroll
+        for (int q = 0; q < NQ; ++q) {
+            const int j = lane + 32 * q;
+            y[q] = j < n ? U[(size_t)R * n + j] : 0.0;
+        }
+        // forward: y * Uf = u  (Uf upper, stored in A on and above the diagonal)
+#pragma unroll
+        for (int q = 0; q < NQ; ++q) {
+            for (int s = 0; s < 32; ++s) {
+                const int i = 32 * q + s;
+                if (i >= n) break;
+                double yi = __shfl_sync(0xffffffffu, y[q], s) * invd[i];
+                if (lane == s) y[q] = yi;
+                const double *Ai = A + (size_t)i * lda;
+#pragma unroll
+                for (int q2 = q; q2 < NQ; ++q2) {
+                    const int j = lane + 32 * q2;
+                    if (j > i && j < n) y[q2] = fma(-yi, Ai[j], y[q2]);
+                }
+            }
+        }
+        // backward: v * L = y  (L unit lower, stored below the diagonal)
+#pragma unroll
+        for (int q = NQ - 1; q >= 0; --q) {
+            for (int s = 31; s >= 0; --s) {
+                const int j = 32 * q + s;
+                if (j >= n) continue;
+                const double vj = __shfl_sync(0xffffffffu, y[q], s);
+                const double *Aj = A + (size_t)j * lda;
+#pragma unroll
+                for (int q2 = 0; q2 <= q; ++q2) {
+                    const int i = lane + 32 * q2;
+                    if (i < j) y[q2] = fma(-vj, Aj[i], y[q2]);
+                }
+            }
+        }
+        // w[perm[i]] = v[i]
+        OutT *wr = Wout + (size_t)R * ldw;
+#pragma unroll
+        for (int q = 0; q < NQ; ++q) {
+            const int i = lane + 32 * q;
+            if (i < n) {
+                const OutT nv = (OutT)y[q];
+                if (track_drift) dmax = fmaxf(dmax, fabsf((float)wr[perm[i]] - (float)nv));
+                wr[perm[i]] = nv;
+            }
+        }
+    }
+    if (track_drift) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) dmax = fmaxf(dmax, __shfl_xor_sync(0xffffffffu, dmax, o));
+        if (lane == 0 && dmax > 0.f) atomic_max_nonneg(drift_slot, dmax);
+    }
+}
+
+template <typename OutT>
+__global__ void __launch_bounds__(kRefreshThreads)
+refresh_kernel(DevModel m, DevBatch b, int only_due, int track_drift) {
+    const int w = blockIdx.x;
+    const int spin = blockIdx.y;
+    if (only_due && b.since[w] >= 0) return;  // a negative `since` marks a refresh as due
+
+    if (spin == 0 && threadIdx.x == 0) atomicAdd(b.refresh_count, 1ull);
+    const int N = m.n_sites;
+    const int n = spin == 0 ? m.n_up : m.n_dn;
+    const int ldw = spin == 0 ? m.ld_up : m.ld_dn;
+    const double *U = spin == 0 ? m.U_up : m.U_dn;
+    const short *kappa = (spin == 0 ? b.kappa_up : b.kappa_dn) + (size_t)w * N;
+    const size_t wblock = (size_t)N * (m.ld_up + m.ld_dn);
+    OutT *W = (sizeof(OutT) == 8 ? (OutT *)b.W64 : (OutT *)b.W32) + (size_t)w * wblock +
+              (spin == 0 ? 0 : (size_t)N * m.ld_up);
+
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int lda = n + 1;  // odd stride: column reads hit distinct banks
+    double *A = reinterpret_cast<double *>(smem);
+    double *invd = A + (size_t)n * lda;
+    double *red = invd + n;                       // 33 doubles
+    int *perm = reinterpret_cast<int *>(red + 33);
+    short *rows = reinterpret_cast<short *>(perm + n);
+    __shared__ int s_piv, s_nrows;
+    __shared__ double s_pmax;
+
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nt = blockDim.x;
+
+    // gather tilde_U (zeroed first so that a configuration missing a label is singular)
+    for (int e = tid; e < n * lda; e += nt) A[e] = 0.0;
+    __syncthreads();
+    for (int R = warp; R < N; R += nt / 32) {
+        const int l = kappa[R];
+        if (l >= 1 && l <= n) {
+            const double *src = U + (size_t)R * n;
+            double *dst = A + (size_t)(l - 1) * lda;
+            for (int c = lane; c < n; c += 32) dst[c] = src[c];
+        }
+    }
+    for (int i = tid; i < n; i += nt) perm[i] = i;
+    if (tid == 0) s_nrows = 0;
+    __syncthreads();
+
+    // LU with partial pivoting (first maximal |pivot| wins, as LAPACK i*amax)
+    bool singular = false;
+    for (int k = 0; k < n; ++k) {
+        if (warp == 0) {
+            double best = -1.0;
+            int bi = n;
+            for (int i = k + lane; i < n; i += 32) {
+                const double v = fabs(A[(size_t)i * lda + k]);
+                if (v > best) { best = v; bi = i; }
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                const double ob = __shfl_xor_sync(0xffffffffu, best, o);
+                const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+                if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
+            }
+            if (lane == 0) { s_piv = bi; s_pmax = best; }
+        }
+        __syncthreads();
+        const int p = s_piv;
+        if (!(s_pmax > 0.0)) {  // exactly singular (or NaN): every thread sees it, stops
+            singular = true;
+            break;
+        }
+        if (p != k) {
+            for (int j = tid; j < n; j += nt) {
+                const double a = A[(size_t)k * lda + j];
+                A[(size_t)k * lda + j] = A[(size_t)p * lda + j];
+                A[(size_t)p * lda + j] = a;
+            }
+            if (tid == 0) { const int t = perm[k]; perm[k] = perm[p]; perm[p] = t; }
+        }
+        __syncthreads();
+        const double dinv = 1.0 / A[(size_t)k * lda + k];
+        for (int i = k + 1 + tid; i < n; i += nt) A[(size_t)i * lda + k] *= dinv;
+        __syncthreads();
+        // trailing update: warp rows, lane columns
+        for (int i = k + 1 + warp; i < n; i += nt / 32) {
+            const double aik = A[(size_t)i * lda + k];
+            double *Ai = A + (size_t)i * lda;
+            const double *Ak = A + (size_t)k * lda;
+            for (int j = k + 1 + lane; j < n; j += 32) Ai[j] = fma(-aik, Ak[j], Ai[j]);
+        }
+        __syncthreads();
+    }
+    if (singular) {
+        if (tid == 0) {
+            atomicOr(&b.status[w], kStatusSingular);
+            b.logdet[4 * w + spin] = -INFINITY;
+            b.logdet[4 * w + 2 + spin] = -INFINITY;
+        }
+        return;
+    }
+    // log|det|, log(min|u_kk| / max|u_kk|) and reciprocal pivots
+    double ld = 0.0, dmin = INFINITY, dmaxp = 0.0;
+    for (int i = tid; i < n; i += nt) {
+        const double d = A[(size_t)i * lda + i];
+        invd[i] = 1.0 / d;
+        ld += log(fabs(d));
+        dmin = fmin(dmin, fabs(d));
+        dmaxp = fmax(dmaxp, fabs(d));
+    }
+    ld = block_sum(ld, red);
+    dmin = -block_sum_max(-dmin, red);
+    dmaxp = block_sum_max(dmaxp, red);
+    if (tid == 0) {
+        b.logdet[4 * w + spin] = ld;
+        b.logdet[4 * w + 2 + spin] = log(dmin / dmaxp);
+    }
+
+    // rows to solve: sites not holding this spin, in site order
+    if (warp == 0) {
+        int base = 0;
+        for (int R0 = 0; R0 < N; R0 += 32) {
+            const int R = R0 + lane;
+            const bool un = R < N && kappa[R] == 0;
+            const unsigned bal = __ballot_sync(0xffffffffu, un);
+            if (un) rows[base + __popc(bal & ((1u << lane) - 1u))] = (short)R;
+            base += __popc(bal);
+        }
+        if (lane == 0) s_nrows = base;
+    }
+    // unit rows at occupied sites, zero padding columns
+    for (int R = warp; R < N; R += nt / 32) {
+        const int l = kappa[R];
+        if (l != 0) {
+            OutT *wr = W + (size_t)R * ldw;
+            float dmax = 0.f;
+            for (int c = lane; c < ldw; c += 32) {
+                const OutT nv = (OutT)((c == l - 1) ? 1.0 : 0.0);
+                if (track_drift) dmax = fmaxf(dmax, fabsf((float)wr[c] - (float)nv));
+                wr[c] = nv;
+            }
+            if (track_drift) {
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) dmax = fmaxf(dmax, __shfl_xor_sync(0xffffffffu, dmax, o));
+                if (lane == 0 && dmax > 0.f) atomic_max_nonneg(&b.drift[w], dmax);
+            }
+        } else {
+            OutT *wr = W + (size_t)R * ldw;
+            for (int c = n + lane; c < ldw; c += 32) wr[c] = (OutT)0;
+        }
+    }
+    __syncthreads();
+    const int nrows = s_nrows;
+    const int NQ = (n + 31) / 32;
+    float *dslot = &b.drift[w];
+    const bool td = track_drift != 0;
+    switch (NQ) {
+        case 1: solve_rows<1>(A, lda, invd, perm, U, n, rows, nrows, W, ldw, dslot, td); break;
+        case 2: solve_rows<2>(A, lda, invd, perm, U, n, rows, nrows, W, ldw, dslot, td); break;
+        case 3: solve_rows<3>(A, lda, invd, perm, U, n, rows, nrows, W, ldw, dslot, td); break;
+        case 4: solve_rows<4>(A, lda, invd, perm, U, n, rows, nrows, W, ldw, dslot, td); break;
+        default: solve_rows<5>(A, lda, invd, perm, U, n, rows, nrows, W, ldw, dslot, td); break;
+    }
+}
+
+size_t refresh_smem(const DevModel &m) {
+    const int n = m.n_up > m.n_dn ? m.n_up : m.n_dn;
+    return (size_t)n * (n + 1) * 8 + (size_t)n * 8 + 33 * 8 + (size_t)n * 4 + (size_t)m.n_sites * 2 + 16;
+}
+
+// ---------------------------------------------------------------------------
+// Sweep: proposals of one walker per CTA.
+//
+// Warp 0 evaluates proposals t..t+31 of its walker at once against the
+// current state; the first accepted lane is the next accepted move (all
+// earlier lanes were rejected against exactly the state they would have seen
+// one at a time, so the chain is the sequential one).  Then the whole CTA
+// applies the Sherman-Morrison update to both W matrices.
+//
+// T = double, W in global memory: the plain FP64 form.
+// T = float,  W staged in shared memory: the mixed form.
+// ---------------------------------------------------------------------------
+struct SweepCtl {
+    long long t, tend;
+    int since, zmu, state;
+    int Ku, lu, Kd, ld;
+    double red[33];
+};
+
+template <typename T>
+struct WPtr {
+    T *up, *dn;
+    int ld_up, ld_dn;
+    __device__ __forceinline__ T &U(int r, int c) const { return up[(size_t)r * ld_up + c]; }
+    __device__ __forceinline__ T &D(int r, int c) const { return dn[(size_t)r * ld_dn + c]; }
+};
+
+// Local energy of the state (src/Hamiltonian.jl:593-778), FP64 sums.
+template <typename T>
+__device__ double local_energy(const DevModel &m, const short2 *bonds, const short *kup,
+                               const short *kdn, const WPtr<T> &W, double *red) {
+    double acc = 0.0;
+    for (int e = threadIdx.x; e < m.n_bonds; e += blockDim.x) {
+        const short2 bd = bonds[e];
+        const int i = bd.x, j = bd.y;
+        const int ui = kup[i], uj = kup[j], di = kdn[i], dj = kdn[j];
+        acc += ((ui != 0) == (uj != 0)) ? 0.25 : -0.25;
+        if (uj != 0 && di != 0) acc -= 0.5 * (double)W.U(i, uj - 1) * (double)W.D(j, di - 1);
+        if (ui != 0 && dj != 0) acc -= 0.5 * (double)W.U(j, ui - 1) * (double)W.D(i, dj - 1);
+    }
+    return block_sum(acc, red);
+}
+
+// Antiparallel bonds touching sites a or b (each bond counted once).
+__device__ int incident_antiparallel(const DevModel &m, const short *kup, int a, int bsite) {
+    int c = 0;
+    for (int e = m.nbr_off[a]; e < m.nbr_off[a + 1]; ++e) {
+        const int k = m.nbr[e];
+        c += ((kup[a] != 0) != (kup[k] != 0));
+    }
+    for (int e = m.nbr_off[bsite]; e < m.nbr_off[bsite + 1]; ++e) {
+        const int k = m.nbr[e];
+        if (k == a) continue;
+        c += ((kup[bsite] != 0) != (kup[k] != 0));
+    }
+    return c;
+}
+
+// Sherman-Morrison update of both spins (src/MonteCarlo.jl:279-292):
+// W <- W - W[:,l] (W[K,:] - e_l) / W[K,l].  col/row staging buffers hold
+// N + ld entries per spin.
+template <typename T>
+__device__ void rank1_update(const WPtr<T> &W, int N, int Ku, int lu, int Kd, int ld, T *stg_col_u,
+                             T *stg_row_u, T *stg_col_d, T *stg_row_d) {
+    const int tid = threadIdx.x, nt = blockDim.x;
+    const T au = (T)(-1.0) / W.U(Ku, lu);
+    const T ad = (T)(-1.0) / W.D(Kd, ld);
+    for (int r = tid; r < N; r += nt) {
+        stg_col_u[r] = W.U(r, lu) * au;
+        stg_col_d[r] = W.D(r, ld) * ad;
+    }
+    for (int c = tid; c < W.ld_up; c += nt) stg_row_u[c] = W.U(Ku, c) - (c == lu ? (T)1 : (T)0);
+    for (int c = tid; c < W.ld_dn; c += nt) stg_row_d[c] = W.D(Kd, c) - (c == ld ? (T)1 : (T)0);
+    __syncthreads();
+    if constexpr (sizeof(T) == 4) {
+        const int q_up = W.ld_up >> 2, q_dn = W.ld_dn >> 2;
+        const int tot_up = N * q_up, tot = tot_up + N * q_dn;
+        for (int e = tid; e < tot; e += nt) {
+            const bool is_up = e < tot_up;
+            const int ee = is_up ? e : e - tot_up;
+            const int q = is_up ? q_up : q_dn;
+            const int r = ee / q, c4 = ee - r * q;
+            float4 *wp = reinterpret_cast<float4 *>(is_up ? W.up : W.dn) + (size_t)r * q + c4;
+            const float cv = is_up ? stg_col_u[r] : stg_col_d[r];
+            const float4 rv = reinterpret_cast<const float4 *>(is_up ? stg_row_u : stg_row_d)[c4];
+            float4 v = *wp;
+            v.x = fmaf(cv, rv.x, v.x);
+            v.y = fmaf(cv, rv.y, v.y);
+            v.z = fmaf(cv, rv.z, v.z);
+            v.w = fmaf(cv, rv.w, v.w);
+            *wp = v;
+        }
+    } else {
+        const int tot_up = N * W.ld_up, tot = tot_up + N * W.ld_dn;
+        for (int e = tid; e < tot; e += nt) {
+            const bool is_up = e < tot_up;
+            const int ee = is_up ? e : e - tot_up;
+            const int q = is_up ? W.ld_up : W.ld_dn;
+            const int r = ee / q, c = ee - r * q;
+            T *wp = (is_up ? W.up : W.dn) + (size_t)r * q + c;
+            const T cv = is_up ? stg_col_u[r] : stg_col_d[r];
+            const T rv = is_up ? stg_row_u[c] : stg_row_d[c];
+            *wp = fma(cv, rv, *wp);
+        }
+    }
+    __syncthreads();
+}
+
+template <typename T, bool kSmemW>
+__global__ void sweep_kernel(DevModel m, DevBatch b, SweepParams p, int refresh_by_proposals,
+                             int *active_count) {
+    const int w = blockIdx.x;
+    const int N = m.n_sites;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+
+    const long long t0 = b.t[w];
+    const long long tend = b.t_end[w];
+    if (t0 >= tend) return;
+
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ SweepCtl ctl;
+
+    const size_t wblock = (size_t)N * (m.ld_up + m.ld_dn);
+    T *gW = (sizeof(T) == 8 ? (T *)b.W64 : (T *)b.W32) + (size_t)w * wblock;
+    unsigned char *cur = smem;
+    WPtr<T> W;
+    W.ld_up = m.ld_up;
+    W.ld_dn = m.ld_dn;
+    if constexpr (kSmemW) {
+        T *sW = reinterpret_cast<T *>(cur);
+        const int nvec = (int)(wblock * sizeof(T) / 16);
+        const float4 *src = reinterpret_cast<const float4 *>(gW);
+        float4 *dst = reinterpret_cast<float4 *>(sW);
+        for (int e = tid; e < nvec; e += blockDim.x) dst[e] = src[e];
+        W.up = sW;
+        W.dn = sW + (size_t)N * m.ld_up;
+        cur += wblock * sizeof(T);
+    } else {
+        W.up = gW;
+        W.dn = gW + (size_t)N * m.ld_up;
+    }
+    T *stg_col_u = reinterpret_cast<T *>(cur); cur += (size_t)N * sizeof(T);
+    T *stg_col_d = reinterpret_cast<T *>(cur); cur += (size_t)N * sizeof(T);
+    T *stg_row_u = reinterpret_cast<T *>(cur); cur += (size_t)m.ld_up * sizeof(T);
+    T *stg_row_d = reinterpret_cast<T *>(cur); cur += (size_t)m.ld_dn * sizeof(T);
+    short2 *bonds = reinterpret_cast<short2 *>(cur); cur += (size_t)m.n_bonds * sizeof(short2);
+    short *kup = reinterpret_cast<short *>(cur); cur += (size_t)N * sizeof(short);
+    short *kdn = reinterpret_cast<short *>(cur);
+
+    for (int e = tid; e < m.n_bonds; e += blockDim.x) bonds[e] = m.bonds[e];
+    for (int s = tid; s < N; s += blockDim.x) {
+        kup[s] = b.kappa_up[(size_t)w * N + s];
+        kdn[s] = b.kappa_dn[(size_t)w * N + s];
+    }
+    __syncthreads();
+    // Z_mu (src/MonteCarlo.jl:460-474)
+    double zc = 0.0;
+    for (int e = tid; e < m.n_bonds; e += blockDim.x) {
+        const short2 bd = bonds[e];
+        zc += ((kup[bd.x] != 0 && kdn[bd.y] != 0) || (kup[bd.y] != 0 && kdn[bd.x] != 0)) ? 1.0 : 0.0;
+    }
+    zc = block_sum(zc, ctl.red);
+    if (tid == 0) {
+        ctl.t = t0;
+        ctl.tend = tend;
+        ctl.since = b.since[w] < 0 ? 0 : b.since[w];
+        ctl.zmu = (int)zc;
+    }
+    __syncthreads();
+
+    const int R = p.refresh_every;
+    const int M = p.measure_every;
+    const double nb_d = (double)m.n_bonds;
+    long long acc_count = 0, n_meas = 0;
+    double se = 0.0, se2 = 0.0;
+
+    while (true) {
+        if (warp == 0) {
+            long long t = ctl.t;
+            const int since = ctl.since;
+            int state = 2;  // 2 = stop, 1 = accepted move, 3 = measurement boundary
+            const double thr = p.accept_rule == 0 ? (double)ctl.zmu / nb_d : 1.0;
+            while (true) {
+                if (t >= tend) break;
+                if (!refresh_by_proposals && since >= R) break;
+                long long lim = tend - t;
+                const long long to_meas = (t / M + 1) * M - t;
+                if (to_meas < lim) lim = to_meas;
+                if (refresh_by_proposals) {
+                    const long long to_ref = (t / R + 1) * R - t;
+                    if (to_ref < lim) lim = to_ref;
+                }
+                const int win = lim < 32 ? (int)lim : 32;
+                bool acc = false;
+                int Ku = 0, lu = 0, Kd = 0, ld = 0;
+                if (lane < win) {
+                    double r;
+                    int bi;
+                    proposal_draw(p.seed, w, t + lane, m.n_bonds, r, bi);
+                    if (!(r > thr)) {
+                        const short2 bd = bonds[bi];
+                        const int i = bd.x, j = bd.y;
+                        const int kui = kup[i], kuj = kup[j], kdi = kdn[i], kdj = kdn[j];
+                        const bool f1 = kui != 0 && kdj != 0;
+                        const bool f2 = kuj != 0 && kdi != 0;
+                        if (f1 || f2) {
+                            if (f1) { Ku = j; lu = kui - 1; Kd = i; ld = kdj - 1; }
+                            else    { Ku = i; lu = kuj - 1; Kd = j; ld = kdi - 1; }
+                            const double ratio = (double)W.U(Ku, lu) * (double)W.D(Kd, ld);
+                            const double a = ratio * ratio;
+                            if (!isfinite(a)) {
+                                atomicOr(&b.status[w], kStatusNonFinite);
+                            } else if (p.accept_rule == 0) {
+                                acc = a >= 1.0 ? (r < thr) : (r < thr * a);
+                            } else {
+                                acc = a >= 1.0 || r < a;
+                            }
+                        }
+                    }
+                }
+                const unsigned mask = __ballot_sync(0xffffffffu, acc);
+                if (mask) {
+                    const int f = __ffs(mask) - 1;
+                    if (lane == f) { ctl.Ku = Ku; ctl.lu = lu; ctl.Kd = Kd; ctl.ld = ld; }
+                    t += f + 1;
+                    state = 1;
+                    break;
+                }
+                t += win;
+                if (t % M == 0 || (refresh_by_proposals && t % R == 0)) { state = 3; break; }
+            }
+            if (lane == 0) { ctl.t = t; ctl.state = state; }
+        }
+        __syncthreads();
+        const int state = ctl.state;
+        if (state == 2) break;
+        if (state == 1) {
+            const int Ku = ctl.Ku, lu = ctl.lu, Kd = ctl.Kd, ld = ctl.ld;
+            rank1_update<T>(W, N, Ku, lu, Kd, ld, stg_col_u, stg_row_u, stg_col_d, stg_row_d);
+            if (tid == 0) {
+                // the up spin moves Kd -> Ku, the down spin Ku -> Kd
+                const int before = incident_antiparallel(m, kup, Ku, Kd);
+                kup[Ku] = (short)(lu + 1); kup[Kd] = 0;
+                kdn[Kd] = (short)(ld + 1); kdn[Ku] = 0;
+                const int after = incident_antiparallel(m, kup, Ku, Kd);
+                ctl.zmu += after - before;
+                ctl.since += 1;
+            }
+            acc_count += 1;
+            __syncthreads();
+        }
+        const long long t = ctl.t;
+        if (t % M == 0) {
+            const double e = local_energy<T>(m, bonds, kup, kdn, W, ctl.red);
+            se += e;
+            se2 += e * e;
+            n_meas += 1;
+        }
+        if (refresh_by_proposals && t % R == 0) break;  // refresh boundary: hand over to refresh
+        __syncthreads();
+    }
+    __syncthreads();
+
+    // write back
+    if constexpr (kSmemW) {
+        const int nvec = (int)(wblock * sizeof(T) / 16);
+        const float4 *src = reinterpret_cast<const float4 *>(W.up);
+        float4 *dst = reinterpret_cast<float4 *>(gW);
+        for (int e = tid; e < nvec; e += blockDim.x) dst[e] = src[e];
+    }
+    for (int s = tid; s < N; s += blockDim.x) {
+        b.kappa_up[(size_t)w * N + s] = kup[s];
+        b.kappa_dn[(size_t)w * N + s] = kdn[s];
+    }
+    if (tid == 0) {
+        const long long t = ctl.t;
+        b.t[w] = t;
+        bool due;
+        if (refresh_by_proposals) due = (t % R == 0) && t > t0;
+        else due = ctl.since >= R;
+        b.since[w] = due ? -1 : ctl.since;
+        b.accepted[w] += acc_count;
+        b.proposals[w] += t - t0;
+        b.sum_e[w] += se;
+        b.sum_e2[w] += se2;
+        b.n_meas[w] += n_meas;
+        if (t < tend) atomicAdd(active_count, 1);
+    }
+}
+
+template <typename T, bool kSmemW>
+size_t sweep_smem_bytes(const DevModel &m) {
+    const size_t wblock = (size_t)m.n_sites * (m.ld_up + m.ld_dn);
+    size_t s = kSmemW ? wblock * sizeof(T) : 0;
+    s += (size_t)(2 * m.n_sites + m.ld_up + m.ld_dn) * sizeof(T);
+    s += (size_t)m.n_bonds * sizeof(short2);
+    s += (size_t)2 * m.n_sites * sizeof(short) + 16;
+    return s;
+}
+
+size_t mixed_sweep_smem(const DevModel &m) { return sweep_smem_bytes<float, true>(m); }
+
+// ---------------------------------------------------------------------------
+// Small kernels used by the Carlo-facing API and the parity tests.
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void measure_kernel(DevModel m, DevBatch b) {
+    const int w = blockIdx.x, N = m.n_sites;
+    __shared__ double red[33];
+    const size_t wblock = (size_t)N * (m.ld_up + m.ld_dn);
+    T *gW = (sizeof(T) == 8 ? (T *)b.W64 : (T *)b.W32) + (size_t)w * wblock;
+    WPtr<T> W{gW, gW + (size_t)N * m.ld_up, m.ld_up, m.ld_dn};
+    const double e = local_energy<T>(m, m.bonds, b.kappa_up + (size_t)w * N, b.kappa_dn + (size_t)w * N, W, red);
+    if (threadIdx.x == 0) b.energy_out[w] = e;
+}
+
+template <typename T>
+__global__ void ratio_kernel(DevModel m, DevBatch b, int n_moves, const int *moves, double *out) {
+    const int w = blockIdx.x, N = m.n_sites;
+    const size_t wblock = (size_t)N * (m.ld_up + m.ld_dn);
+    T *gW = (sizeof(T) == 8 ? (T *)b.W64 : (T *)b.W32) + (size_t)w * wblock;
+    WPtr<T> W{gW, gW + (size_t)N * m.ld_up, m.ld_up, m.ld_dn};
+    for (int k = threadIdx.x; k < n_moves; k += blockDim.x) {
+        const int *mv = moves + ((size_t)w * n_moves + k) * 4;
+        out[(size_t)w * n_moves + k] = (double)W.U(mv[0], mv[1] - 1) * (double)W.D(mv[2], mv[3] - 1);
+    }
+}
+
+template <typename T>
+__global__ void apply_moves_kernel(DevModel m, DevBatch b, const int *moves) {
+    const int w = blockIdx.x, N = m.n_sites;
+    const int *mv = moves + (size_t)w * 5;
+    const int flag = mv[0];
+    if (flag == 0) return;
+    const int i = mv[1], site = mv[2], l_up = mv[3], l_dn = mv[4];
+    extern __shared__ __align__(16) unsigned char smem[];
+    T *stg = reinterpret_cast<T *>(smem);
+    const size_t wblock = (size_t)N * (m.ld_up + m.ld_dn);
+    T *gW = (sizeof(T) == 8 ? (T *)b.W64 : (T *)b.W32) + (size_t)w * wblock;
+    WPtr<T> W{gW, gW + (size_t)N * m.ld_up, m.ld_up, m.ld_dn};
+    // flag 1: K_up = site, K_down = i; flag 2: K_up = i, K_down = site
+    const int Ku = flag == 1 ? site : i;
+    const int Kd = flag == 1 ? i : site;
+    rank1_update<T>(W, N, Ku, l_up - 1, Kd, l_dn - 1, stg, stg + 2 * N, stg + N, stg + 2 * N + m.ld_up);
+    if (threadIdx.x == 0) {
+        short *ku = b.kappa_up + (size_t)w * N, *kd = b.kappa_dn + (size_t)w * N;
+        if (flag == 1) {
+            ku[i] = 0; ku[site] = (short)l_up;
+            kd[i] = (short)l_dn; kd[site] = 0;
+        } else {
+            ku[i] = (short)l_up; ku[site] = 0;
+            kd[i] = 0; kd[site] = (short)l_dn;
+        }
+    }
+}
+
+// Seeded uniformly random start (Fisher-Yates over sites with Philox stream
+// 1, counter (word block, attempt, walker)); labels in increasing site order.
+__global__ void init_random_kernel(DevModel m, DevBatch b, unsigned long long seed, const int *attempt,
+                                   const int *redo) {
+    const int w = blockIdx.x, N = m.n_sites;
+    if (!redo[w]) return;
+    extern __shared__ __align__(16) unsigned char smem[];
+    short *perm = reinterpret_cast<short *>(smem);
+    short *up = perm + N;
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < N; ++s) { perm[s] = (short)s; up[s] = 0; }
+        unsigned words[4];
+        int nw = 0, ctr = 0;
+        const uint2 key = make_uint2((unsigned)seed, (unsigned)(seed >> 32));
+        for (int k = N - 1; k > 0; --k) {
+            if (nw == 0) {
+                const uint4 x = philox4x32_10(make_uint4((unsigned)ctr, (unsigned)attempt[w], (unsigned)w, 1u), key);
+                words[0] = x.x; words[1] = x.y; words[2] = x.z; words[3] = x.w;
+                nw = 4;
+                ++ctr;
+            }
+            const unsigned u = words[4 - nw];
+            --nw;
+            const int j = (int)(((unsigned long long)u * (unsigned long long)(k + 1)) >> 32);
+            const short tmp = perm[k]; perm[k] = perm[j]; perm[j] = tmp;
+        }
+        for (int q = 0; q < m.n_up; ++q) up[perm[q]] = 1;
+        int lu = 0, ld = 0;
+        short *ku = b.kappa_up + (size_t)w * N, *kd = b.kappa_dn + (size_t)w * N;
+        for (int s = 0; s < N; ++s) {
+            if (up[s]) { ku[s] = (short)(++lu); kd[s] = 0; }
+            else       { ku[s] = 0; kd[s] = (short)(++ld); }
+        }
+        b.status[w] = 0;
+    }
+}
+
+// t_end = t + proposals for every walker (the target of one kvmc_sweep call).
+__global__ void set_tend_kernel(DevBatch b, long long proposals) {
+    const int w = blockIdx.x * blockDim.x + threadIdx.x;
+    if (w < b.n_walkers) b.t_end[w] = b.t[w] + proposals;
+}
+
+// ---------------------------------------------------------------------------
+// Launchers
+// ---------------------------------------------------------------------------
+cudaError_t launch_set_tend(const DevBatch &b, long long proposals, cudaStream_t stream) {
+    set_tend_kernel<<<(b.n_walkers + 255) / 256, 256, 0, stream>>>(b, proposals);
+    return cudaGetLastError();
+}
+
+int max_smem_optin(int device) {
+    int v = 0;
+    cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, device);
+    return v;
+}
+
+cudaError_t launch_refresh(const DevModel &m, const DevBatch &b, bool fp32_out, int only_due,
+                           int track_drift, cudaStream_t stream) {
+    const size_t sm = refresh_smem(m);
+    const dim3 grid(b.n_walkers, 2);
+    if (fp32_out) {
+        cudaError_t e = cudaFuncSetAttribute(refresh_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        if (e != cudaSuccess) return e;
+        refresh_kernel<float><<<grid, kRefreshThreads, sm, stream>>>(m, b, only_due, track_drift);
+    } else {
+        cudaError_t e = cudaFuncSetAttribute(refresh_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        if (e != cudaSuccess) return e;
+        refresh_kernel<double><<<grid, kRefreshThreads, sm, stream>>>(m, b, only_due, track_drift);
+    }
+    return cudaGetLastError();
+}
+
+template <typename T, bool kSmemW>
+static cudaError_t launch_sweep_impl(const DevModel &m, const DevBatch &b, const SweepParams &p,
+                                     int by_proposals, int *active, int threads, cudaStream_t stream) {
+    const size_t sm = sweep_smem_bytes<T, kSmemW>(m);
+    cudaError_t e = cudaFuncSetAttribute(sweep_kernel<T, kSmemW>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    if (e != cudaSuccess) return e;
+    sweep_kernel<T, kSmemW><<<b.n_walkers, threads, sm, stream>>>(m, b, p, by_proposals, active);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_sweep(const DevModel &m, const DevBatch &b, const SweepParams &p, bool mixed,
+                         bool smem_w, int *active, cudaStream_t stream) {
+    if (!mixed) return launch_sweep_impl<double, false>(m, b, p, 1, active, 256, stream);
+    if (smem_w) return launch_sweep_impl<float, true>(m, b, p, 0, active, 512, stream);
+    return launch_sweep_impl<float, false>(m, b, p, 0, active, 512, stream);
+}
+
+cudaError_t launch_measure(const DevModel &m, const DevBatch &b, bool fp32, cudaStream_t stream) {
+    if (fp32) measure_kernel<float><<<b.n_walkers, 256, 0, stream>>>(m, b);
+    else measure_kernel<double><<<b.n_walkers, 256, 0, stream>>>(m, b);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_eval_ratios(const DevModel &m, const DevBatch &b, bool fp32, int n_moves, const int *moves,
+                               double *out, cudaStream_t stream) {
+    if (fp32) ratio_kernel<float><<<b.n_walkers, 128, 0, stream>>>(m, b, n_moves, moves, out);
+    else ratio_kernel<double><<<b.n_walkers, 128, 0, stream>>>(m, b, n_moves, moves, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_apply_moves(const DevModel &m, const DevBatch &b, bool fp32, const int *moves,
+                               cudaStream_t stream) {
+    const size_t elem = fp32 ? 4 : 8;
+    const size_t sm = (size_t)(2 * m.n_sites + m.ld_up + m.ld_dn) * elem + 16;
+    if (fp32) {
+        cudaError_t e = cudaFuncSetAttribute(apply_moves_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        if (e != cudaSuccess) return e;
+        apply_moves_kernel<float><<<b.n_walkers, 256, sm, stream>>>(m, b, moves);
+    } else {
+        cudaError_t e = cudaFuncSetAttribute(apply_moves_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        if (e != cudaSuccess) return e;
+        apply_moves_kernel<double><<<b.n_walkers, 256, sm, stream>>>(m, b, moves);
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_init_random(const DevModel &m, const DevBatch &b, unsigned long long seed, const int *attempt,
+                               const int *redo, cudaStream_t stream) {
+    const size_t sm = (size_t)2 * m.n_sites * sizeof(short) + 16;
+    init_random_kernel<<<b.n_walkers, 32, sm, stream>>>(m, b, seed, attempt, redo);
+    return cudaGetLastError();
+}
+
+}  // namespace kvmc

@@ -1,0 +1,289 @@
+"""GPU parity: libkvmc (through its C ABI) against the oracle and the golden fixtures.
+
+Tolerances (stated per result):
+  plain FP64 form: W, ratios, local energies within 1e-10 relative to the
+  oracle; chains follow the oracle's trajectory exactly.
+  mixed FP32 form: W within 1e-6 relative to max(1, |W|) after a refresh;
+  ratios and local energies within 1e-5 relative; chains follow the
+  oracle's trajectory (an FP32 rounding may flip a decision that sits within
+  ~1e-6 of its threshold, so at most one walker of a batch may diverge).
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+import kagome_oracle as o
+import oracle_c
+
+pytestmark = pytest.mark.gpu
+
+GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+CELLS = {24: (2, 2), 54: (3, 3), 96: (4, 4), 216: (6, 6)}
+
+
+@pytest.fixture(scope="module")
+def kv(built):
+    import kagomevmc
+
+    return kagomevmc
+
+
+@pytest.fixture(scope="module")
+def golden():
+    return json.load(open(os.path.join(GOLD, "golden.json")))
+
+
+def ham_for(kv, N):
+    a, b = CELLS[N]
+    ham = kv.Hamiltonian.build(N // 2, N // 2, kv.DoubleKagome(1.0, 2 * a, b, (True, True), (False, True)))
+    if N == 24:
+        U = np.load(os.path.join(GOLD, "u_N24.npy"))
+        ham = kv.Hamiltonian(12, 12, U, U.copy(), ham.H_mat, ham.nn)
+    return ham
+
+
+def oracle_ham(ham):
+    return o.Hamiltonian(ham.N_up, ham.N_down, ham.U_up, ham.U_down, ham.H_mat, [(i + 1, j + 1) for i, j in ham.nn])
+
+
+def close(a, b, rel):
+    a, b = np.asarray(a, float), np.asarray(b, float)
+    return np.all(np.abs(a - b) <= rel * np.maximum(1.0, np.abs(b)))
+
+
+@pytest.mark.parametrize("precision", ["plain", "mixed"])
+@pytest.mark.parametrize("N", [24, 54, 96, 216])
+def test_refresh_matches_oracle(kv, N, precision):
+    ham = ham_for(kv, N)
+    U = ham.U_up
+    starts = [o.seeded_start(13, w, U, U)[:2] for w in range(4)]
+    eng = kv.Engine(ham, 4, precision=precision, seed=13)
+    eng.init(np.stack([s[0] for s in starts]), np.stack([s[1] for s in starts]))
+    Wu, Wd = eng.get_w()
+    tol = 1e-10 if precision == "plain" else 1e-6
+    for w, (ku, kd) in enumerate(starts):
+        assert close(Wu[w], o.reevaluateW(U, ku), tol), (N, w)
+        assert close(Wd[w], o.reevaluateW(U, kd), tol), (N, w)
+    eng.close()
+
+
+@pytest.mark.parametrize("precision", ["plain", "mixed"])
+@pytest.mark.parametrize("N", [24, 54, 96])
+def test_ratios_and_local_energy_match_golden(kv, golden, N, precision):
+    ham = ham_for(kv, N)
+    cases = golden["configs"][str(N)]
+    eng = kv.Engine(ham, len(cases), precision=precision)
+    eng.init(np.array([c["kappa_up"] for c in cases]), np.array([c["kappa_down"] for c in cases]))
+    tol = 1e-10 if precision == "plain" else 1e-5
+    E = eng.measure()
+    for w, c in enumerate(cases):
+        assert abs(E[w] - c["local_energy"]) <= tol * max(1.0, abs(c["local_energy"])), (N, w, E[w])
+    nm = min(len(c["moves"]) for c in cases)
+    moves = np.array([c["moves"][:nm] for c in cases])
+    R = eng.eval_ratios(moves)
+    for w, c in enumerate(cases):
+        np.testing.assert_allclose(R[w], c["ratios"][:nm], rtol=tol, atol=tol)
+    eng.close()
+
+
+@pytest.mark.parametrize("precision", ["plain", "mixed"])
+@pytest.mark.parametrize("N", [24, 54])
+def test_chain_matches_golden(kv, golden, N, precision):
+    """Same Philox stream as the oracle: same accepted moves, same final configuration."""
+    g = golden["chains"][str(N)]
+    ham = ham_for(kv, N)
+    W = len(g["walkers"])
+    eng = kv.Engine(ham, W, precision=precision, seed=g["seed"], measure_interval=g["measure_every"])
+    eng.init(np.array([c["start_up"] for c in g["walkers"]]), np.array([c["start_down"] for c in g["walkers"]]))
+    st = eng.sweep(g["proposals"])
+    ku, kd, ct = eng.get_state()
+    ws = eng.walker_stats()
+    assert np.all(ct == g["proposals"])
+    match = 0
+    for w, c in enumerate(g["walkers"]):
+        if ku[w].tolist() == c["final_up"] and kd[w].tolist() == c["final_down"]:
+            match += 1
+            assert ws["accepted"][w] == c["accepted"]
+            assert ws["n_meas"][w] == len(c["energies"])
+            tol = 1e-9 if precision == "plain" else 1e-4
+            assert abs(ws["sum_e"][w] - sum(c["energies"])) <= tol * max(1.0, abs(sum(c["energies"])))
+    assert match >= W - (0 if precision == "plain" else 1)
+    assert st["bad_walkers"] == 0
+    eng.close()
+
+
+@pytest.mark.parametrize("precision", ["plain", "mixed"])
+@pytest.mark.parametrize("accept", ["reference", "metropolis"])
+def test_long_chains_match_c_oracle(kv, precision, accept):
+    N, walkers, proposals, seed = 96, 12, 3000, 21
+    ham = ham_for(kv, N)
+    eng = kv.Engine(ham, walkers, precision=precision, accept=accept, seed=seed, refresh_interval=(64 if precision == "mixed" else 0))
+    eng.init()
+    ku0, kd0, _ = eng.get_state()
+    eng.sweep(proposals)
+    ku1, kd1, _ = eng.get_state()
+    ws = eng.walker_stats()
+    m = oracle_c.OracleModel(ham.U_up, ham.U_down, ham.nn)
+    rule = 0 if accept == "reference" else 1
+    match = 0
+    for w in range(walkers):
+        ch = m.new_chain(ku0[w], kd0[w])
+        ch.run(seed, w, proposals, 48, 48, rule)
+        if np.array_equal(ch.ku, ku1[w]) and np.array_equal(ch.kd, kd1[w]):
+            match += 1
+            assert ch.c.accepted == ws["accepted"][w]
+            tol = 1e-8 if precision == "plain" else 1e-4
+            assert abs(ch.c.sum_e - ws["sum_e"][w]) <= tol * max(1.0, abs(ch.c.sum_e))
+    assert match >= walkers - (0 if precision == "plain" else 1)
+    eng.close()
+
+
+@pytest.mark.parametrize("precision", ["plain", "mixed"])
+def test_seeded_starts_match_oracle(kv, precision):
+    N, seed = 54, 77
+    ham = ham_for(kv, N)
+    eng = kv.Engine(ham, 6, precision=precision, seed=seed)
+    att = eng.init()
+    ku, kd, ct = eng.get_state()
+    for w in range(6):
+        oku, okd, a = o.seeded_start(seed, w, ham.U_up, ham.U_down)
+        assert ku[w].tolist() == oku.tolist() and kd[w].tolist() == okd.tolist()
+        assert att[w] == a + 1
+    assert np.all(ct == 0)
+    eng.close()
+
+
+@pytest.mark.parametrize("precision", ["plain", "mixed"])
+def test_apply_moves_match_oracle(kv, precision):
+    """update_configurations! with update_W! (src/MonteCarlo.jl:497-511, 279-292)."""
+    N = 54
+    ham = ham_for(kv, N)
+    U = ham.U_up
+    ku, kd, _ = o.seeded_start(5, 0, U, U)
+    st = o.ChainState(ku.copy(), kd.copy(), o.reevaluateW(U, ku), o.reevaluateW(U, kd))
+    eng = kv.Engine(ham, 1, precision=precision)
+    eng.init(ku, kd)
+    rng = np.random.default_rng(0)
+    nn = ham.nn
+    for step in range(6):
+        while True:
+            i, site = nn[rng.integers(len(nn))]
+            f1 = st.kappa_up[i] != 0 and st.kappa_down[site] != 0
+            f2 = st.kappa_up[site] != 0 and st.kappa_down[i] != 0
+            if f1 or f2:
+                break
+        flag = 1 if f1 else 2
+        l_up = int(st.kappa_up[i] if flag == 1 else st.kappa_up[site])
+        l_dn = int(st.kappa_down[site] if flag == 1 else st.kappa_down[i])
+        o.update_configurations(st, flag, i + 1, site + 1, l_up, l_dn)
+        eng.apply_moves([flag, i, site, l_up, l_dn])
+    gku, gkd, _ = eng.get_state()
+    assert gku[0].tolist() == st.kappa_up.tolist() and gkd[0].tolist() == st.kappa_down.tolist()
+    Wu, Wd = eng.get_w()
+    tol = 1e-9 if precision == "plain" else 1e-4
+    assert close(Wu[0], st.W_up, tol) and close(Wd[0], st.W_down, tol)
+    eng.close()
+
+
+def test_invalid_and_singular_configurations(kv):
+    ham = ham_for(kv, 24)
+    eng = kv.Engine(ham, 1)
+    ku, kd, _ = o.seeded_start(1, 0, ham.U_up, ham.U_down)
+    bad = kd.copy()
+    bad[np.argmax(ku > 0)] = 5   # doubly occupied
+    with pytest.raises(kv.ArgumentError):
+        eng.init(ku, bad)
+    bad = ku.copy()
+    bad[np.argmax(ku > 0)] = 99
+    with pytest.raises(kv.BoundsError):
+        eng.init(bad, kd)
+    eng.close()
+    # identical rows make every tilde_U singular (test/test-MonteCarlo.jl:429-477)
+    rng = np.random.default_rng(3)
+    Us = np.repeat(rng.random((1, 12)), 24, axis=0)
+    sing = kv.Hamiltonian(12, 12, Us, rng.random((24, 12)), ham.H_mat, ham.nn)
+    eng = kv.Engine(sing, 1)
+    with pytest.raises(kv.SingularException):
+        eng.init(ku, kd)
+    eng.close()
+
+
+def test_carlo_callbacks_and_checkpoint(kv):
+    params = dict(n1=4, n2=2, PBC=(True, True), antiPBC=(False, True), N_up=12, N_down=12, walkers=8,
+                  precision="mixed", proposals_per_sweep=12, seed=3)
+    mc = kv.MC(params)
+    ctx = kv.MCContext()
+    kv.init_(mc, ctx, params)
+    for _ in range(20):
+        kv.sweep_(mc, ctx)
+        ctx.sweeps += 1
+        kv.measure_(mc, ctx)
+    ev = kv.Evaluator()
+    kv.register_evaluables(kv.MC, ev, params)
+    res = ev.run(ctx.observables)
+    assert np.isfinite(res["energy"]) and -1.0 < res["energy"] < 0.0
+    assert len(ctx.observables["acc"]) == 20 and len(ctx.observables["OL"]) == 20
+    ck = {}
+    kv.write_checkpoint(mc, ck)
+    mc2 = kv.MC(params)
+    kv.read_checkpoint_(mc2, ck)
+    a, b = mc.engine.get_state(), mc2.engine.get_state()
+    assert all(np.array_equal(x, y) for x, y in zip(a, b))
+    np.testing.assert_allclose(mc.engine.measure(), mc2.engine.measure(), rtol=1e-5, atol=1e-5)
+    mc.engine.sweep(200)
+    mc2.engine.sweep(200)
+    a, b = mc.engine.get_state(), mc2.engine.get_state()
+    assert all(np.array_equal(x, y) for x, y in zip(a, b))
+
+
+def test_qr_start_singular_message(kv):
+    """The reference's singular-start error (src/MonteCarlo.jl:401-408) through the product."""
+    params = dict(n1=2, n2=2, PBC=(False, False), N_up=6, N_down=6, walkers=1)
+    mc = kv.MC(params)
+    rng = np.random.default_rng(3)
+    Us = np.repeat(rng.random((1, 6)), 12, axis=0)
+    mc.Ham = kv.Hamiltonian(6, 6, Us, rng.random((12, 6)), mc.Ham.H_mat, mc.Ham.nn)
+    mc.engine = kv.Engine(mc.Ham, 1)
+    with pytest.raises(RuntimeError, match="QR-based configuration is singular"):
+        kv.init_(mc, kv.MCContext(), params)
+
+
+@pytest.mark.parametrize("precision", ["plain", "mixed"])
+@pytest.mark.parametrize("accept,key", [("reference", "E_per_site_reference_rule"), ("metropolis", "E_per_site_psi2")])
+def test_energy_matches_exact_enumeration(kv, golden, precision, accept, key):
+    """N=24: E/N within 3 standard errors of the exact value for the rule's stationary law."""
+    ham = ham_for(kv, 24)
+    walkers = 2048
+    eng = kv.Engine(ham, walkers, precision=precision, accept=accept, seed=99)
+    eng.init()
+    eng.sweep(600)
+    eng.reset_stats()
+    eng.sweep(3600)
+    ws = eng.walker_stats()
+    m = ws["sum_e"] / ws["n_meas"]
+    e = m.mean() / 24
+    se = m.std(ddof=1) / np.sqrt(walkers) / 24
+    exact = golden["enum_N24"][key]
+    assert abs(e - exact) <= 3 * se + 1e-5, (e, exact, se)
+    eng.close()
+
+
+def test_mixed_vs_plain_energy_gate(kv):
+    """|dE/N| <= 1e-4 between the two forms on identical walkers and proposal streams."""
+    ham = ham_for(kv, 96)
+    walkers, seed = 256, 5
+    out = {}
+    for precision in ("plain", "mixed"):
+        eng = kv.Engine(ham, walkers, precision=precision, seed=seed, refresh_interval=(256 if precision == "mixed" else 0))
+        eng.init()
+        eng.sweep(2400)
+        ws = eng.walker_stats()
+        out[precision] = (ws["sum_e"].copy(), ws["n_meas"].copy(), eng.get_state())
+        eng.close()
+    (ep, npm, sp), (em, nmm, sm) = out["plain"], out["mixed"]
+    same = np.array([np.array_equal(sp[0][w], sm[0][w]) for w in range(walkers)])
+    assert same.mean() > 0.95
+    dE = abs(ep[same].sum() / npm[same].sum() - em[same].sum() / nmm[same].sum()) / 96
+    assert dE <= 1e-4, dE

@@ -1,0 +1,107 @@
+"""Host side of the library without a GPU: the C ABI loads and exports every
+declared symbol, the FP64 hopping-matrix builder and bond list match the
+oracle bit for bit, and argument errors carry the reference's error classes."""
+import ctypes as C
+import os
+import re
+
+import numpy as np
+import pytest
+
+import kagome_oracle as o
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_symbols():
+    txt = open(os.path.join(ROOT, "include", "kvmc.h")).read()
+    return sorted(set(re.findall(r"KVMC_API\s+int\s+(kvmc_\w+)\s*\(", txt)))
+
+
+def test_library_exports_every_declared_symbol(built):
+    import kagomevmc as kv
+
+    lib = kv.load()
+    names = declared_symbols()
+    assert len(names) >= 20
+    for n in names:
+        assert hasattr(lib, n), n
+    assert set(names) == set(kv.EXPORTS)
+
+
+def test_version(built):
+    import kagomevmc as kv
+
+    abi, arch = C.c_int32(), C.c_int32()
+    assert kv.load().kvmc_version(C.byref(abi), C.byref(arch)) == 0
+    assert abi.value == 1 and arch.value == 1030
+
+
+@pytest.mark.parametrize("n1,n2,pbc,anti,B", [
+    (4, 3, (False, False), (False, False), 0.0), (4, 3, (True, False), (False, False), 0.0),
+    (4, 3, (True, True), (True, True), 0.0), (4, 3, (True, True), (True, False), 0.1),
+    (4, 2, (True, True), (False, True), 0.0), (6, 3, (True, True), (False, True), 0.0),
+    (8, 4, (True, True), (False, True), 0.3), (2, 2, (False, False), (False, False), 0.0),
+    (12, 6, (True, True), (False, True), 0.0)])
+def test_hopping_matrix_and_bonds_match_oracle_exactly(built, n1, n2, pbc, anti, B):
+    import kagomevmc as kv
+
+    Ho = o.hmat(o.double_kagome(1.0, n1, n2, pbc, anti), B=B)
+    Hk = kv.Hmat(kv.DoubleKagome(1.0, n1, n2, pbc, anti), B=B)
+    assert np.array_equal(Ho, Hk)
+    assert kv.get_nn(Hk) == [(i - 1, j - 1) for i, j in o.get_nn(Ho)]
+
+
+def test_custom_links_zero_flux_shape(built):
+    """Custom link tables (the reference's link_in / link_inter keywords)."""
+    import kagomevmc as kv
+
+    lin = {k: abs(v) for k, v in kv.PI_LINK_IN.items()}
+    lint = {k: abs(v) for k, v in kv.PI_LINK_INTER.items()}
+    L = kv.DoubleKagome(1.0, 4, 2, (True, True), (False, True))
+    Lo = o.double_kagome(1.0, 4, 2, (True, True), (False, True))
+    assert np.array_equal(kv.Hmat(L, lin, lint), o.hmat(Lo, lin, lint))
+
+
+def test_lattice_errors(built):
+    import kagomevmc as kv
+
+    with pytest.raises(kv.ArgumentError):
+        kv.DoubleKagome(1.0, 3, 3, (False, False))
+    with pytest.raises(kv.ArgumentError):
+        kv.DoubleKagome(1.0, 4, 3, (False, False), (True, False))
+    assert kv.ns(kv.DoubleKagome(1.0, 4, 3, (False, False))) == 36
+
+
+def test_bad_link_table_is_rejected(built):
+    import kagomevmc as kv
+
+    with pytest.raises(kv.ArgumentError):
+        kv.Hmat(kv.DoubleKagome(1.0, 4, 2, (True, True)), {(1, 7): 1.0})
+
+
+def test_create_validates_before_touching_a_device(built):
+    import kagomevmc as kv
+
+    L = kv.DoubleKagome(1.0, 4, 2, (True, True), (False, True))
+    ham = kv.Hamiltonian.build(12, 12, L)
+    bad = kv.Hamiltonian(12, 11, ham.U_up, ham.U_down[:, :11], ham.H_mat, ham.nn)
+    with pytest.raises(kv.ArgumentError):
+        kv.Engine(bad, 2)
+    bad = kv.Hamiltonian(12, 12, ham.U_up, ham.U_down, ham.H_mat, [(0, 99)])
+    with pytest.raises(kv.BoundsError):
+        kv.Engine(bad, 2)
+
+
+def test_no_device_is_a_clean_error_on_cpu(built):
+    import kagomevmc as kv
+
+    try:
+        import torch
+        if torch.cuda.is_available():
+            pytest.skip("a GPU is present")
+    except ImportError:
+        pass
+    L = kv.DoubleKagome(1.0, 4, 2, (True, True), (False, True))
+    with pytest.raises(kv.DeviceError):
+        kv.Engine(kv.Hamiltonian.build(12, 12, L), 2)
