@@ -47,6 +47,9 @@ def args_():
     p.add_argument("--seed", type=int, default=2024)
     p.add_argument("--skip-plain", action="store_true")
     p.add_argument("--skip-cpu", action="store_true")
+    p.add_argument("--skip-gate", action="store_true")
+    p.add_argument("--skip-e2e", action="store_true")
+    p.add_argument("--no-peaks", action="store_true")
     return p.parse_args()
 
 
@@ -239,7 +242,7 @@ def gpu_arm(a):
 
     ham = model()
     n = N_SITES // 2
-    peaks = measure_peaks(local) if rank == 0 else {}
+    peaks = measure_peaks(local) if (rank == 0 and not a.no_peaks) else {}
     eng = kv.Engine(ham, a.walkers, precision="mixed", seed=a.seed + 104729 * rank, refresh_interval=a.refresh,
                     device=local)
     eng.init()
@@ -269,7 +272,7 @@ def gpu_arm(a):
     # configurations and stream counters go host -> device, the step runs,
     # configurations, counters and per-walker statistics come back.
     ku, kd, ct = eng.get_state()
-    e2e_steps = min(a.steps, 4)
+    e2e_steps = 0 if a.skip_e2e else min(a.steps, 4)
     e2e_acc = 0
     eng.region_start()
     for _ in range(e2e_steps):
@@ -281,8 +284,8 @@ def gpu_arm(a):
     e2e_ms = eng.region_stop()
     Wk = a.walkers
     h2d = ku.nbytes + kd.nbytes + ct.nbytes
-    d2h = ku.nbytes + kd.nbytes + ct.nbytes + sum(v.nbytes for v in ws.values())
-    e2e = {"value": e2e_acc / (e2e_ms * 1e-3), "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+    d2h = ku.nbytes + kd.nbytes + ct.nbytes + (sum(v.nbytes for v in ws.values()) if e2e_steps else 0)
+    e2e = {"value": e2e_acc / (e2e_ms * 1e-3) if e2e_steps else None, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
            "d2h_bytes_per_step": int(d2h), "steps": e2e_steps,
            "path": "kvmc_set_state (H2D + FP64 rebuild) -> kvmc_sweep -> kvmc_get_state + kvmc_walker_stats (D2H)"}
     eng.close()
@@ -303,7 +306,7 @@ def gpu_arm(a):
         pe.close()
         plain = {"value": ptot["accepted"] / (pms * 1e-3), "unit": UNIT, "ms": pms,
                  "proposals_per_walker": 8 * n, "accepted": ptot["accepted"]}
-    gate = energy_gate(ham, kv, 256, 4 * a.proposals, a.refresh, a.seed + 1)
+    gate = None if a.skip_gate else energy_gate(ham, kv, 256, 4 * a.proposals, a.refresh, a.seed + 1)
 
     # roofline of the dominant kernel
     refreshes = tot["refreshes"]

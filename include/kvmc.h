@@ -113,7 +113,9 @@ typedef struct {
                                  (plain: min(n_up,n_down) as src/MonteCarlo.jl:594-595) */
     int32_t measure_interval; /* proposals between local-energy samples; 0 = min(n_up,n_down)
                                  (src/MonteCarlo.jl:628-634) */
-    int32_t delay_k;          /* reserved: delayed-update depth, 0 or 1 = rank-1 */
+    int32_t delay_k;          /* mixed form: delayed-update depth; 0 = the largest of
+                                 16, 12, 8, 4 whose working set fits in shared memory,
+                                 1 = a rank-1 update per accepted move */
     int32_t device;           /* CUDA device ordinal */
     uint64_t seed;            /* Philox4x32-10 key for proposals and seeded starts */
 } kvmc_batch_desc;
@@ -206,6 +208,11 @@ KVMC_API int kvmc_reset_stats(kvmc_handle *h);
  * kind: 0 = sweep kernel, 1 = refresh kernel.  Totals since enabling. */
 KVMC_API int kvmc_enable_timing(kvmc_handle *h, int32_t on);
 KVMC_API int kvmc_kernel_time(kvmc_handle *h, int32_t kind, double *total_ms, int64_t *launches);
+
+/* The settings a handle resolved at creation: refresh and measurement
+ * intervals, delayed-update depth, and whether W is staged on chip. */
+KVMC_API int kvmc_get_config(kvmc_handle *h, int32_t *refresh_interval, int32_t *measure_interval,
+                             int32_t *delay_k, int32_t *w_on_chip);
 
 /* Device time of everything the handle enqueues between a call with
  * start=1 and a call with start=0 (CUDA events on the handle's stream);

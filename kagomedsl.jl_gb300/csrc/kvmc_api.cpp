@@ -48,6 +48,7 @@ struct kvmc_handle {
     bool smem_w = false;
     int refresh_every = 0;
     int measure_every = 0;
+    int delay_k = 1;  // mixed form: 1 = rank-1 updates, 4/8/12/16 = delayed-update depth
     std::string err;
 
     DevModel dm{};
@@ -514,6 +515,25 @@ extern "C" int kvmc_create(const kvmc_model_desc *model, const kvmc_batch_desc *
     if ((size_t)optin < kvmc::refresh_smem(m))
         return bail(h->fail(KVMC_ERR_UNSUPPORTED, "refresh needs %zu B shared memory, device offers %d", kvmc::refresh_smem(m), optin));
     h->smem_w = h->mixed && kvmc::mixed_sweep_smem(m) <= (size_t)optin;
+    // delayed-update depth: 0 = the largest depth whose working set fits on chip
+    const size_t budget = (size_t)optin - 1024;  // leave room for the kernel's static shared memory
+    if (h->mixed && h->smem_w) {
+        const int want = batch->delay_k;
+        if (want == 0) {
+            h->delay_k = 1;
+            for (int k : {16, 12, 8, 4})
+                if (kvmc::delayed_smem_bytes(m, k) <= budget) { h->delay_k = k; break; }
+        } else if (want == 1) {
+            h->delay_k = 1;
+        } else if (want == 4 || want == 8 || want == 12 || want == 16) {
+            if (kvmc::delayed_smem_bytes(m, want) > budget)
+                return bail(h->fail(KVMC_ERR_UNSUPPORTED, "delay_k=%d needs %zu B shared memory (device offers %d)", want,
+                                    kvmc::delayed_smem_bytes(m, want), optin));
+            h->delay_k = want;
+        } else {
+            return bail(h->fail(KVMC_ERR_ARGUMENT, "delay_k must be 0, 1, 4, 8, 12 or 16 (got %d)", want));
+        }
+    }
     for (auto &e : h->region)
         if ((rc = h->cuda(cudaEventCreate(&e), "event"))) return bail(rc);
     if ((rc = h->cuda(cudaDeviceSynchronize(), "create"))) return bail(rc);
@@ -557,7 +577,12 @@ extern "C" int kvmc_init(kvmc_handle *h, const int32_t *kappa_up, const int32_t 
         KV_TRY(h->cuda(cudaMemcpyAsync(h->d_attempt, att.data(), Wk * 4, cudaMemcpyHostToDevice, h->stream), "upload"));
         KV_TRY(h->cuda(cudaMemcpyAsync(h->d_redo, redo.data(), Wk * 4, cudaMemcpyHostToDevice, h->stream), "upload"));
         KV_TRY(h->cuda(kvmc::launch_init_random(h->dm, h->db, h->batch.seed, h->d_attempt, h->d_redo, h->stream), "init launch"));
-        KV_TRY(full_refresh(h, false));
+        // refresh only the walkers drawn this round (a negative `since` marks them)
+        std::vector<int> mark(Wk);
+        for (int w = 0; w < Wk; ++w) mark[w] = redo[w] ? -1 : 0;
+        KV_TRY(h->cuda(cudaMemcpyAsync(h->db.since, mark.data(), Wk * 4, cudaMemcpyHostToDevice, h->stream), "upload"));
+        KV_TRY(h->cuda(kvmc::launch_refresh(h->dm, h->db, h->mixed, 1, 0, h->stream), "refresh launch"));
+        KV_TRY(h->cuda(cudaStreamSynchronize(h->stream), "refresh"));
         KV_TRY(h->cuda(cudaMemcpy(ld.data(), h->db.logdet, ld.size() * 8, cudaMemcpyDeviceToHost), "logdet"));
         int left = 0;
         for (int w = 0; w < Wk; ++w) {
@@ -571,7 +596,8 @@ extern "C" int kvmc_init(kvmc_handle *h, const int32_t *kappa_up, const int32_t 
             return h->fail(KVMC_ERR_SINGULAR, "%d walker(s) found no non-singular start in %d draws", left, max_attempts);
     }
     KV_TRY(h->cuda(cudaMemsetAsync(h->db.status, 0, Wk * 4, h->stream), "memset"));
-    KV_TRY(full_refresh(h, false));
+    KV_TRY(h->cuda(cudaMemsetAsync(h->db.since, 0, Wk * 4, h->stream), "memset"));
+    KV_TRY(h->cuda(cudaStreamSynchronize(h->stream), "init"));
     if (attempts) for (int w = 0; w < Wk; ++w) attempts[w] = att[w] + 1;
     return check_status(h, nullptr);
 }
@@ -593,6 +619,16 @@ extern "C" int kvmc_region_timer(kvmc_handle *h, int32_t start, double *ms) {
     float t = 0.f;
     KV_TRY(h->cuda(cudaEventElapsedTime(&t, h->region[0], h->region[1]), "event time"));
     if (ms) *ms = t;
+    return KVMC_OK;
+}
+
+extern "C" int kvmc_get_config(kvmc_handle *h, int32_t *refresh_interval, int32_t *measure_interval,
+                               int32_t *delay_k, int32_t *w_on_chip) {
+    if (!h) return fail_global(KVMC_ERR_ARGUMENT, "null handle");
+    if (refresh_interval) *refresh_interval = h->refresh_every;
+    if (measure_interval) *measure_interval = h->measure_every;
+    if (delay_k) *delay_k = h->mixed ? h->delay_k : 1;
+    if (w_on_chip) *w_on_chip = h->smem_w ? 1 : 0;
     return KVMC_OK;
 }
 
@@ -675,6 +711,7 @@ extern "C" int kvmc_sweep(kvmc_handle *h, int64_t proposals_per_walker, kvmc_swe
     p.accept_rule = h->batch.accept_rule;
     p.refresh_every = h->refresh_every;
     p.measure_every = h->measure_every;
+    p.delay_k = h->delay_k;
     KV_TRY(h->cuda(kvmc::launch_set_tend(h->db, proposals_per_walker, h->stream), "set t_end"));
     KV_TRY(h->cuda(cudaMemsetAsync(h->db.drift, 0, sizeof(float) * h->n_walkers, h->stream), "memset"));
     int launches = 1;

@@ -53,6 +53,7 @@ struct SweepParams {
     int accept_rule;      // 0 reference, 1 metropolis
     int refresh_every;    // mixed: accepted moves between refreshes
     int measure_every;    // proposals between energy samples
+    int delay_k;          // mixed form: delayed-update depth (4, 8, 12, 16), else rank-1
 };
 
 // Launchers.  All enqueue on `stream` and return the launch error.
@@ -78,6 +79,7 @@ cudaError_t launch_init_random(const DevModel &m, const DevBatch &b, unsigned lo
 // Shared-memory bytes the mixed sweep kernel needs for this model (0 if it
 // cannot hold both W matrices on one SM).
 size_t mixed_sweep_smem(const DevModel &m);
+size_t delayed_smem_bytes(const DevModel &m, int K);
 size_t refresh_smem(const DevModel &m);
 int max_smem_optin(int device);
 

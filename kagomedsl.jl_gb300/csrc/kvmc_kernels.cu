@@ -10,6 +10,7 @@
 //   apply_moves_kernel  update_configurations!      src/MonteCarlo.jl:497-511
 //   init_random_kernel  seeded random starts (replaces the QR start of
 //                       src/MonteCarlo.jl:326-357 for batches of walkers)
+#include <algorithm>
 #include <cstdint>
 #include <cuda_runtime.h>
 
@@ -102,73 +103,52 @@ __device__ __forceinline__ void atomic_max_nonneg(float *addr, float v) {
 // ---------------------------------------------------------------------------
 constexpr int kRefreshThreads = 256;
 
-template <int NQ, typename OutT>
-__device__ void solve_rows(const double *A, int lda, const double *invd, const int *perm,
-                           const double *U, int n, const short *rows, int n_rows,
-                           OutT *Wout, int ldw, float *drift_slot, bool track_drift) {
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+// Rows of W at sites that do not hold this spin: w * tilde_U = u, one
+// thread per row.  With P tilde_U = L Uf (row pivots perm): y Uf = u
+// (forward), v L = y (backward, unit diagonal), w[perm[i]] = v[i].  Each
+// thread works on its own row of Y in shared memory; the factor entries it
+// reads are the same for every thread (broadcast), so no barrier is needed.
+template <typename OutT>
+__device__ void solve_rows_block(const double *A, int lda, const double *invd, const int *perm, const double *U,
+                                 int n, const short *rows, int n_rows, double *Y, int ldy, OutT *Wout, int ldw,
+                                 float *drift_slot, bool track_drift) {
+    const int tid = threadIdx.x;
     float dmax = 0.f;
-    for (int idx = warp; idx < n_rows; idx += nw) {
-        const int R = rows[idx];
-        double y[NQ];
-#pragma unroll
-        for (int q = 0; q < NQ; ++q) {
-            const int j = lane + 32 * q;
-            y[q] = j < n ? U[(size_t)R * n + j] : 0.0;
+    if (tid < n_rows) {
+        double *y = Y + (size_t)tid * ldy;
+        const int R = rows[tid];
+        for (int j = 0; j < n; ++j) y[j] = U[(size_t)R * n + j];
+        for (int i = 0; i < n; ++i) {
+            const double yi = y[i] * invd[i];
+            y[i] = yi;
+            const double *Ai = A + (size_t)i * lda;
+            for (int j = i + 1; j < n; ++j) y[j] = fma(-yi, Ai[j], y[j]);
         }
-        // forward: y * Uf = u  (Uf upper, stored in A on and above the diagonal)
-#pragma unroll
-        for (int q = 0; q < NQ; ++q) {
-            for (int s = 0; s < 32; ++s) {
-                const int i = 32 * q + s;
-                if (i >= n) break;
-                double yi = __shfl_sync(0xffffffffu, y[q], s) * invd[i];
-                if (lane == s) y[q] = yi;
-                const double *Ai = A + (size_t)i * lda;
-#pragma unroll
-                for (int q2 = q; q2 < NQ; ++q2) {
-                    const int j = lane + 32 * q2;
-                    if (j > i && j < n) y[q2] = fma(-yi, Ai[j], y[q2]);
-                }
-            }
+        for (int j = n - 1; j > 0; --j) {
+            const double vj = y[j];
+            const double *Aj = A + (size_t)j * lda;
+            for (int i = 0; i < j; ++i) y[i] = fma(-vj, Aj[i], y[i]);
         }
-        // backward: v * L = y  (L unit lower, stored below the diagonal)
-#pragma unroll
-        for (int q = NQ - 1; q >= 0; --q) {
-            for (int s = 31; s >= 0; --s) {
-                const int j = 32 * q + s;
-                if (j >= n) continue;
-                const double vj = __shfl_sync(0xffffffffu, y[q], s);
-                const double *Aj = A + (size_t)j * lda;
-#pragma unroll
-                for (int q2 = 0; q2 <= q; ++q2) {
-                    const int i = lane + 32 * q2;
-                    if (i < j) y[q2] = fma(-vj, Aj[i], y[q2]);
-                }
-            }
-        }
-        // w[perm[i]] = v[i]
         OutT *wr = Wout + (size_t)R * ldw;
-#pragma unroll
-        for (int q = 0; q < NQ; ++q) {
-            const int i = lane + 32 * q;
-            if (i < n) {
-                const OutT nv = (OutT)y[q];
-                if (track_drift) dmax = fmaxf(dmax, fabsf((float)wr[perm[i]] - (float)nv));
-                wr[perm[i]] = nv;
+        for (int i = 0; i < n; ++i) {
+            const OutT nv = (OutT)y[i];
+            if (track_drift) {
+                const float o = (float)wr[perm[i]];
+                dmax = fmaxf(dmax, fabsf(o - (float)nv) / (1.f + fabsf((float)nv)));
             }
+            wr[perm[i]] = nv;
         }
     }
     if (track_drift) {
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) dmax = fmaxf(dmax, __shfl_xor_sync(0xffffffffu, dmax, o));
-        if (lane == 0 && dmax > 0.f) atomic_max_nonneg(drift_slot, dmax);
+        if ((tid & 31) == 0 && dmax > 0.f) atomic_max_nonneg(drift_slot, dmax);
     }
 }
 
 template <typename OutT>
 __global__ void __launch_bounds__(kRefreshThreads)
-refresh_kernel(DevModel m, DevBatch b, int only_due, int track_drift) {
+refresh_kernel(DevModel m, DevBatch b, int only_due, int track_drift, int rows_per_pass) {
     const int w = blockIdx.x;
     const int spin = blockIdx.y;
     if (only_due && b.since[w] >= 0) return;  // a negative `since` marks a refresh as due
@@ -188,7 +168,8 @@ refresh_kernel(DevModel m, DevBatch b, int only_due, int track_drift) {
     double *A = reinterpret_cast<double *>(smem);
     double *invd = A + (size_t)n * lda;
     double *red = invd + n;                       // 33 doubles
-    int *perm = reinterpret_cast<int *>(red + 33);
+    double *Y = red + 33;                         // row block [rows_per_pass][n + 1]
+    int *perm = reinterpret_cast<int *>(Y + (size_t)rows_per_pass * lda);
     short *rows = reinterpret_cast<short *>(perm + n);
     __shared__ int s_piv, s_nrows;
     __shared__ double s_pmax;
@@ -300,7 +281,7 @@ refresh_kernel(DevModel m, DevBatch b, int only_due, int track_drift) {
             float dmax = 0.f;
             for (int c = lane; c < ldw; c += 32) {
                 const OutT nv = (OutT)((c == l - 1) ? 1.0 : 0.0);
-                if (track_drift) dmax = fmaxf(dmax, fabsf((float)wr[c] - (float)nv));
+                if (track_drift) dmax = fmaxf(dmax, fabsf((float)wr[c] - (float)nv) / (1.f + fabsf((float)nv)));
                 wr[c] = nv;
             }
             if (track_drift) {
@@ -315,22 +296,22 @@ refresh_kernel(DevModel m, DevBatch b, int only_due, int track_drift) {
     }
     __syncthreads();
     const int nrows = s_nrows;
-    const int NQ = (n + 31) / 32;
-    float *dslot = &b.drift[w];
-    const bool td = track_drift != 0;
-    switch (NQ) {
-        case 1: solve_rows<1>(A, lda, invd, perm, U, n, rows, nrows, W, ldw, dslot, td); break;
-        case 2: solve_rows<2>(A, lda, invd, perm, U, n, rows, nrows, W, ldw, dslot, td); break;
-        case 3: solve_rows<3>(A, lda, invd, perm, U, n, rows, nrows, W, ldw, dslot, td); break;
-        case 4: solve_rows<4>(A, lda, invd, perm, U, n, rows, nrows, W, ldw, dslot, td); break;
-        default: solve_rows<5>(A, lda, invd, perm, U, n, rows, nrows, W, ldw, dslot, td); break;
+    for (int r0 = 0; r0 < nrows; r0 += rows_per_pass) {
+        const int cnt = min(rows_per_pass, nrows - r0);
+        solve_rows_block<OutT>(A, lda, invd, perm, U, n, rows + r0, cnt, Y, lda, W, ldw, &b.drift[w], track_drift != 0);
     }
 }
 
-size_t refresh_smem(const DevModel &m) {
+// Shared memory of the refresh kernel when it solves rows_per_pass rows at a time.
+size_t refresh_smem_rows(const DevModel &m, int rows_per_pass) {
     const int n = m.n_up > m.n_dn ? m.n_up : m.n_dn;
-    return (size_t)n * (n + 1) * 8 + (size_t)n * 8 + 33 * 8 + (size_t)n * 4 + (size_t)m.n_sites * 2 + 16;
+    return (size_t)n * (n + 1) * 8 + (size_t)n * 8 + 33 * 8 + (size_t)rows_per_pass * (n + 1) * 8 + (size_t)n * 4 +
+           (size_t)m.n_sites * 2 + 16;
 }
+
+// Minimum footprint (one row per pass); the launcher widens the row block to
+// what fits.
+size_t refresh_smem(const DevModel &m) { return refresh_smem_rows(m, 1); }
 
 // ---------------------------------------------------------------------------
 // Sweep: proposals of one walker per CTA.
@@ -635,6 +616,354 @@ size_t sweep_smem_bytes(const DevModel &m) {
 size_t mixed_sweep_smem(const DevModel &m) { return sweep_smem_bytes<float, true>(m); }
 
 // ---------------------------------------------------------------------------
+// Mixed form with delayed updates (McDaniel, Mihm, Sanderson, Kent 2017,
+// "Delayed Slater determinant update algorithms for high efficiency quantum
+// Monte Carlo", J. Chem. Phys. 147, 174107).
+//
+// W (FP32) stays fixed in shared memory while up to K accepted moves collect
+// as a low-rank correction: W_eff = W - P Q^T, P: N x K, Q: ld x K (unused
+// columns kept at zero).  Move m (pivot W_eff[K,l]) appends
+//   P[:,m] = W_eff[:,l] / W_eff[K,l],   Q[:,m] = W_eff[K,:] - e_l,
+// which is the Sherman-Morrison update of src/MonteCarlo.jl:279-292 in
+// factored form.  Ratios and local energies read W_eff = W - P Q^T (a
+// K-term dot per element); after K moves one register-tiled pass applies
+// W -= P Q^T, touching each W element once per K moves instead of once per
+// move.
+// ---------------------------------------------------------------------------
+template <int K>
+struct DelayedSpin {
+    float *W;   // [N][ld]
+    float *P;   // [N][K]
+    float *Q;   // [ld][K]
+    int ld;
+    __device__ __forceinline__ float dotPQ(int r, int c) const {
+        const float4 *pr = reinterpret_cast<const float4 *>(P + (size_t)r * K);
+        const float4 *qc = reinterpret_cast<const float4 *>(Q + (size_t)c * K);
+        float acc = 0.f;
+#pragma unroll
+        for (int k = 0; k < K / 4; ++k) {
+            const float4 a = pr[k], b = qc[k];
+            acc = fmaf(a.x, b.x, acc);
+            acc = fmaf(a.y, b.y, acc);
+            acc = fmaf(a.z, b.z, acc);
+            acc = fmaf(a.w, b.w, acc);
+        }
+        return acc;
+    }
+    __device__ __forceinline__ float eff(int r, int c) const { return W[(size_t)r * ld + c] - dotPQ(r, c); }
+};
+
+// W -= P Q^T over all threads; each thread keeps the Q slab of its four
+// columns in registers and walks rows.
+template <int K>
+__device__ void delayed_flush(const DelayedSpin<K> &S, int N) {
+    const int qc = S.ld >> 2;
+    const int groups = blockDim.x / qc;
+    const int t = threadIdx.x;
+    if (t < groups * qc) {
+        const int c4 = t % qc, rp = t / qc;
+        float q[4][K];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const float4 *qr = reinterpret_cast<const float4 *>(S.Q + (size_t)(4 * c4 + j) * K);
+#pragma unroll
+            for (int k = 0; k < K / 4; ++k) {
+                const float4 v = qr[k];
+                q[j][4 * k] = v.x; q[j][4 * k + 1] = v.y; q[j][4 * k + 2] = v.z; q[j][4 * k + 3] = v.w;
+            }
+        }
+        for (int r = rp; r < N; r += groups) {
+            const float4 *pr = reinterpret_cast<const float4 *>(S.P + (size_t)r * K);
+            float p[K];
+#pragma unroll
+            for (int k = 0; k < K / 4; ++k) {
+                const float4 v = pr[k];
+                p[4 * k] = v.x; p[4 * k + 1] = v.y; p[4 * k + 2] = v.z; p[4 * k + 3] = v.w;
+            }
+            float4 *wp = reinterpret_cast<float4 *>(S.W + (size_t)r * S.ld) + c4;
+            float4 w = *wp;
+            float a0 = 0.f, a1 = 0.f, a2 = 0.f, a3 = 0.f;
+#pragma unroll
+            for (int k = 0; k < K; ++k) {
+                a0 = fmaf(p[k], q[0][k], a0);
+                a1 = fmaf(p[k], q[1][k], a1);
+                a2 = fmaf(p[k], q[2][k], a2);
+                a3 = fmaf(p[k], q[3][k], a3);
+            }
+            w.x -= a0; w.y -= a1; w.z -= a2; w.w -= a3;
+            *wp = w;
+        }
+    }
+}
+
+template <int K>
+__device__ void delayed_zero(const DelayedSpin<K> &S, int N) {
+    float4 *p = reinterpret_cast<float4 *>(S.P);
+    for (int e = threadIdx.x; e < N * K / 4; e += blockDim.x) p[e] = make_float4(0.f, 0.f, 0.f, 0.f);
+    float4 *q = reinterpret_cast<float4 *>(S.Q);
+    for (int e = threadIdx.x; e < S.ld * K / 4; e += blockDim.x) q[e] = make_float4(0.f, 0.f, 0.f, 0.f);
+}
+
+struct DelayedCtl {
+    long long t;
+    int since, zmu, state, m;
+    int Ku, lu, Kd, ld;
+    float piv_u, piv_d;
+    double red[33];
+};
+
+// Local energy with W_eff (src/Hamiltonian.jl:593-778), FP64 sums.
+template <int K>
+__device__ double delayed_local_energy(const DevModel &m, const short2 *bonds, const short *kup, const short *kdn,
+                                       const DelayedSpin<K> &U, const DelayedSpin<K> &D, double *red) {
+    double acc = 0.0;
+    for (int e = threadIdx.x; e < m.n_bonds; e += blockDim.x) {
+        const short2 bd = bonds[e];
+        const int i = bd.x, j = bd.y;
+        const int ui = kup[i], uj = kup[j], di = kdn[i], dj = kdn[j];
+        acc += ((ui != 0) == (uj != 0)) ? 0.25 : -0.25;
+        if (uj != 0 && di != 0) acc -= 0.5 * (double)U.eff(i, uj - 1) * (double)D.eff(j, di - 1);
+        if (ui != 0 && dj != 0) acc -= 0.5 * (double)U.eff(j, ui - 1) * (double)D.eff(i, dj - 1);
+    }
+    return block_sum(acc, red);
+}
+
+template <int K>
+__global__ void __launch_bounds__(512) sweep_delayed_kernel(DevModel m, DevBatch b, SweepParams p, int *active_count) {
+    const int w = blockIdx.x;
+    const int N = m.n_sites;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const long long t0 = b.t[w];
+    const long long tend = b.t_end[w];
+    if (t0 >= tend) return;
+
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ DelayedCtl ctl;
+    const size_t wblock = (size_t)N * (m.ld_up + m.ld_dn);
+    float *gW = b.W32 + (size_t)w * wblock;
+    unsigned char *cur = smem;
+    DelayedSpin<K> SU, SD;
+    SU.W = reinterpret_cast<float *>(cur);
+    SU.ld = m.ld_up;
+    SD.W = SU.W + (size_t)N * m.ld_up;
+    SD.ld = m.ld_dn;
+    cur += wblock * sizeof(float);
+    SU.P = reinterpret_cast<float *>(cur); cur += (size_t)N * K * sizeof(float);
+    SD.P = reinterpret_cast<float *>(cur); cur += (size_t)N * K * sizeof(float);
+    SU.Q = reinterpret_cast<float *>(cur); cur += (size_t)m.ld_up * K * sizeof(float);
+    SD.Q = reinterpret_cast<float *>(cur); cur += (size_t)m.ld_dn * K * sizeof(float);
+    float *stg_pu = reinterpret_cast<float *>(cur); cur += (size_t)N * sizeof(float);
+    float *stg_pd = reinterpret_cast<float *>(cur); cur += (size_t)N * sizeof(float);
+    float *stg_qu = reinterpret_cast<float *>(cur); cur += (size_t)m.ld_up * sizeof(float);
+    float *stg_qd = reinterpret_cast<float *>(cur); cur += (size_t)m.ld_dn * sizeof(float);
+    int *nbr_off = reinterpret_cast<int *>(cur); cur += (size_t)(N + 1) * sizeof(int);
+    short2 *bonds = reinterpret_cast<short2 *>(cur); cur += (size_t)m.n_bonds * sizeof(short2);
+    short *nbr = reinterpret_cast<short *>(cur); cur += (size_t)2 * m.n_bonds * sizeof(short);
+    short *kup = reinterpret_cast<short *>(cur); cur += (size_t)N * sizeof(short);
+    short *kdn = reinterpret_cast<short *>(cur);
+
+    {
+        const int nvec = (int)(wblock / 4);
+        const float4 *src = reinterpret_cast<const float4 *>(gW);
+        float4 *dst = reinterpret_cast<float4 *>(SU.W);
+        for (int e = tid; e < nvec; e += blockDim.x) dst[e] = src[e];
+    }
+    delayed_zero<K>(SU, N);
+    delayed_zero<K>(SD, N);
+    for (int e = tid; e < m.n_bonds; e += blockDim.x) bonds[e] = m.bonds[e];
+    for (int e = tid; e < 2 * m.n_bonds; e += blockDim.x) nbr[e] = m.nbr[e];
+    for (int e = tid; e <= N; e += blockDim.x) nbr_off[e] = m.nbr_off[e];
+    for (int s = tid; s < N; s += blockDim.x) {
+        kup[s] = b.kappa_up[(size_t)w * N + s];
+        kdn[s] = b.kappa_dn[(size_t)w * N + s];
+    }
+    __syncthreads();
+    double zc = 0.0;
+    for (int e = tid; e < m.n_bonds; e += blockDim.x) {
+        const short2 bd = bonds[e];
+        zc += ((kup[bd.x] != 0 && kdn[bd.y] != 0) || (kup[bd.y] != 0 && kdn[bd.x] != 0)) ? 1.0 : 0.0;
+    }
+    zc = block_sum(zc, ctl.red);
+    if (tid == 0) {
+        ctl.t = t0;
+        ctl.since = b.since[w] < 0 ? 0 : b.since[w];
+        ctl.zmu = (int)zc;
+        ctl.m = 0;
+    }
+    __syncthreads();
+
+    const int R = p.refresh_every;
+    const int M = p.measure_every;
+    const double nb_d = (double)m.n_bonds;
+    long long acc_count = 0, n_meas = 0;
+    double se = 0.0, se2 = 0.0;
+
+    while (true) {
+        if (warp == 0) {
+            long long t = ctl.t;
+            const int since = ctl.since;
+            int state = 2;
+            const double thr = p.accept_rule == 0 ? (double)ctl.zmu / nb_d : 1.0;
+            while (true) {
+                if (t >= tend || since >= R) break;
+                long long lim = tend - t;
+                const long long to_meas = (t / M + 1) * M - t;
+                if (to_meas < lim) lim = to_meas;
+                const int win = lim < 32 ? (int)lim : 32;
+                bool acc = false;
+                int Ku = 0, lu = 0, Kd = 0, ld = 0;
+                float pu = 0.f, pd = 0.f;
+                if (lane < win) {
+                    double r;
+                    int bi;
+                    proposal_draw(p.seed, w, t + lane, m.n_bonds, r, bi);
+                    if (!(r > thr)) {
+                        const short2 bd = bonds[bi];
+                        const int i = bd.x, j = bd.y;
+                        const int kui = kup[i], kuj = kup[j], kdi = kdn[i], kdj = kdn[j];
+                        const bool f1 = kui != 0 && kdj != 0;
+                        const bool f2 = kuj != 0 && kdi != 0;
+                        if (f1 || f2) {
+                            if (f1) { Ku = j; lu = kui - 1; Kd = i; ld = kdj - 1; }
+                            else    { Ku = i; lu = kuj - 1; Kd = j; ld = kdi - 1; }
+                            pu = SU.eff(Ku, lu);
+                            pd = SD.eff(Kd, ld);
+                            const double ratio = (double)pu * (double)pd;
+                            const double a = ratio * ratio;
+                            if (!isfinite(a)) {
+                                atomicOr(&b.status[w], kStatusNonFinite);
+                            } else if (p.accept_rule == 0) {
+                                acc = a >= 1.0 ? (r < thr) : (r < thr * a);
+                            } else {
+                                acc = a >= 1.0 || r < a;
+                            }
+                        }
+                    }
+                }
+                const unsigned mask = __ballot_sync(0xffffffffu, acc);
+                if (mask) {
+                    const int f = __ffs(mask) - 1;
+                    if (lane == f) {
+                        ctl.Ku = Ku; ctl.lu = lu; ctl.Kd = Kd; ctl.ld = ld;
+                        ctl.piv_u = pu; ctl.piv_d = pd;
+                    }
+                    t += f + 1;
+                    state = 1;
+                    break;
+                }
+                t += win;
+                if (t % M == 0) { state = 3; break; }
+            }
+            if (lane == 0) { ctl.t = t; ctl.state = state; }
+        }
+        __syncthreads();
+        const int state = ctl.state;
+        if (state == 2) break;
+        if (state == 1) {
+            const int Ku = ctl.Ku, lu = ctl.lu, Kd = ctl.Kd, ld = ctl.ld;
+            const float ipu = 1.f / ctl.piv_u, ipd = 1.f / ctl.piv_d;
+            // new factor columns into staging (reads of P/Q see only old columns)
+            for (int e = tid; e < 2 * N + m.ld_up + m.ld_dn; e += blockDim.x) {
+                if (e < N) stg_pu[e] = SU.eff(e, lu) * ipu;
+                else if (e < 2 * N) stg_pd[e - N] = SD.eff(e - N, ld) * ipd;
+                else if (e < 2 * N + m.ld_up) {
+                    const int c = e - 2 * N;
+                    stg_qu[c] = SU.eff(Ku, c) - (c == lu ? 1.f : 0.f);
+                } else {
+                    const int c = e - 2 * N - m.ld_up;
+                    stg_qd[c] = SD.eff(Kd, c) - (c == ld ? 1.f : 0.f);
+                }
+            }
+            if (warp == (blockDim.x >> 5) - 1) {
+                // Z_mu change: the up spin moves Kd -> Ku, the down spin Ku -> Kd
+                int dz = 0;
+                for (int e = nbr_off[Ku] + lane; e < nbr_off[Ku + 1]; e += 32) {
+                    const int k = nbr[e];
+                    if (k != Kd) dz += kup[k] == 0 ? 1 : -1;
+                }
+                for (int e = nbr_off[Kd] + lane; e < nbr_off[Kd + 1]; e += 32) {
+                    const int k = nbr[e];
+                    if (k != Ku) dz += kup[k] != 0 ? 1 : -1;
+                }
+                dz = __reduce_add_sync(0xffffffffu, dz);
+                if (lane == 0) {
+                    ctl.zmu += dz;
+                    ctl.since += 1;
+                }
+            }
+            __syncthreads();
+            const int mm = ctl.m;
+            for (int e = tid; e < 2 * N + m.ld_up + m.ld_dn; e += blockDim.x) {
+                if (e < N) SU.P[(size_t)e * K + mm] = stg_pu[e];
+                else if (e < 2 * N) SD.P[(size_t)(e - N) * K + mm] = stg_pd[e - N];
+                else if (e < 2 * N + m.ld_up) SU.Q[(size_t)(e - 2 * N) * K + mm] = stg_qu[e - 2 * N];
+                else SD.Q[(size_t)(e - 2 * N - m.ld_up) * K + mm] = stg_qd[e - 2 * N - m.ld_up];
+            }
+            if (tid == 0) {
+                kup[Ku] = (short)(lu + 1); kup[Kd] = 0;
+                kdn[Kd] = (short)(ld + 1); kdn[Ku] = 0;
+                ctl.m = mm + 1;
+            }
+            acc_count += 1;
+            __syncthreads();
+            if (mm + 1 == K) {
+                delayed_flush<K>(SU, N);
+                delayed_flush<K>(SD, N);
+                __syncthreads();
+                delayed_zero<K>(SU, N);
+                delayed_zero<K>(SD, N);
+                if (tid == 0) ctl.m = 0;
+                __syncthreads();
+            }
+        }
+        const long long t = ctl.t;
+        if (t % M == 0) {
+            const double e = delayed_local_energy<K>(m, bonds, kup, kdn, SU, SD, ctl.red);
+            se += e;
+            se2 += e * e;
+            n_meas += 1;
+        }
+        __syncthreads();
+    }
+    __syncthreads();
+    if (ctl.m > 0) {
+        delayed_flush<K>(SU, N);
+        delayed_flush<K>(SD, N);
+        __syncthreads();
+    }
+    {
+        const int nvec = (int)(wblock / 4);
+        const float4 *src = reinterpret_cast<const float4 *>(SU.W);
+        float4 *dst = reinterpret_cast<float4 *>(gW);
+        for (int e = tid; e < nvec; e += blockDim.x) dst[e] = src[e];
+    }
+    for (int s = tid; s < N; s += blockDim.x) {
+        b.kappa_up[(size_t)w * N + s] = kup[s];
+        b.kappa_dn[(size_t)w * N + s] = kdn[s];
+    }
+    if (tid == 0) {
+        const long long t = ctl.t;
+        b.t[w] = t;
+        b.since[w] = ctl.since >= R ? -1 : ctl.since;
+        b.accepted[w] += acc_count;
+        b.proposals[w] += t - t0;
+        b.sum_e[w] += se;
+        b.sum_e2[w] += se2;
+        b.n_meas[w] += n_meas;
+        if (t < tend) atomicAdd(active_count, 1);
+    }
+}
+
+size_t delayed_smem_bytes(const DevModel &m, int K) {
+    const size_t N = m.n_sites;
+    size_t s = N * (m.ld_up + m.ld_dn) * 4;                 // W
+    s += 2 * N * K * 4 + (size_t)(m.ld_up + m.ld_dn) * K * 4;  // P, Q
+    s += (2 * N + m.ld_up + m.ld_dn) * 4;                     // staging
+    s += (N + 1) * 4 + (size_t)m.n_bonds * 4 + (size_t)2 * m.n_bonds * 2 + 2 * N * 2 + 16;
+    return (s + 15) / 16 * 16;
+}
+
+// ---------------------------------------------------------------------------
 // Small kernels used by the Carlo-facing API and the parity tests.
 // ---------------------------------------------------------------------------
 template <typename T>
@@ -747,16 +1076,23 @@ int max_smem_optin(int device) {
 
 cudaError_t launch_refresh(const DevModel &m, const DevBatch &b, bool fp32_out, int only_due,
                            int track_drift, cudaStream_t stream) {
-    const size_t sm = refresh_smem(m);
+    int dev = 0;
+    cudaGetDevice(&dev);
+    const size_t cap = (size_t)max_smem_optin(dev) - 1024;
+    const int n = m.n_up > m.n_dn ? m.n_up : m.n_dn;
+    int rows = std::min(kRefreshThreads, m.n_sites - std::min(m.n_up, m.n_dn));
+    while (rows > 1 && refresh_smem_rows(m, rows) > cap) --rows;
+    (void)n;
+    const size_t sm = refresh_smem_rows(m, rows);
     const dim3 grid(b.n_walkers, 2);
     if (fp32_out) {
         cudaError_t e = cudaFuncSetAttribute(refresh_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
         if (e != cudaSuccess) return e;
-        refresh_kernel<float><<<grid, kRefreshThreads, sm, stream>>>(m, b, only_due, track_drift);
+        refresh_kernel<float><<<grid, kRefreshThreads, sm, stream>>>(m, b, only_due, track_drift, rows);
     } else {
         cudaError_t e = cudaFuncSetAttribute(refresh_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
         if (e != cudaSuccess) return e;
-        refresh_kernel<double><<<grid, kRefreshThreads, sm, stream>>>(m, b, only_due, track_drift);
+        refresh_kernel<double><<<grid, kRefreshThreads, sm, stream>>>(m, b, only_due, track_drift, rows);
     }
     return cudaGetLastError();
 }
@@ -771,9 +1107,23 @@ static cudaError_t launch_sweep_impl(const DevModel &m, const DevBatch &b, const
     return cudaGetLastError();
 }
 
+template <int K>
+static cudaError_t launch_delayed(const DevModel &m, const DevBatch &b, const SweepParams &p, int *active,
+                                  cudaStream_t stream) {
+    const size_t sm = delayed_smem_bytes(m, K);
+    cudaError_t e = cudaFuncSetAttribute(sweep_delayed_kernel<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    if (e != cudaSuccess) return e;
+    sweep_delayed_kernel<K><<<b.n_walkers, 512, sm, stream>>>(m, b, p, active);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_sweep(const DevModel &m, const DevBatch &b, const SweepParams &p, bool mixed,
                          bool smem_w, int *active, cudaStream_t stream) {
     if (!mixed) return launch_sweep_impl<double, false>(m, b, p, 1, active, 256, stream);
+    if (smem_w && p.delay_k == 4) return launch_delayed<4>(m, b, p, active, stream);
+    if (smem_w && p.delay_k == 8) return launch_delayed<8>(m, b, p, active, stream);
+    if (smem_w && p.delay_k == 12) return launch_delayed<12>(m, b, p, active, stream);
+    if (smem_w && p.delay_k == 16) return launch_delayed<16>(m, b, p, active, stream);
     if (smem_w) return launch_sweep_impl<float, true>(m, b, p, 0, active, 512, stream);
     return launch_sweep_impl<float, false>(m, b, p, 0, active, 512, stream);
 }

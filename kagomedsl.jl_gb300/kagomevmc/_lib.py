@@ -107,6 +107,7 @@ _SIGS = {
     "kvmc_enable_timing": [_P, C.c_int32],
     "kvmc_kernel_time": [_P, C.c_int32, C.POINTER(C.c_double), C.POINTER(C.c_int64)],
     "kvmc_region_timer": [_P, C.c_int32, C.POINTER(C.c_double)],
+    "kvmc_get_config": [_P, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(C.c_int32)],
     "kvmc_version": [C.POINTER(C.c_int32), C.POINTER(C.c_int32)],
 }
 EXPORTS = tuple(_SIGS)

@@ -23,7 +23,7 @@ class Engine:
     """A batch of walkers of one model on one GPU (a kvmc handle)."""
 
     def __init__(self, ham: Hamiltonian, n_walkers=1, precision="plain", accept="reference",
-                 refresh_interval=0, measure_interval=0, seed=0, device=0):
+                 refresh_interval=0, measure_interval=0, seed=0, device=0, delay_k=0):
         self.ham = ham
         self.N = int(ham.U_up.shape[0])
         self.n_up = int(ham.U_up.shape[1])
@@ -46,7 +46,7 @@ class Engine:
         bd = _lib.BatchDesc()
         bd.n_walkers, bd.precision, bd.accept_rule = self.n_walkers, prec, acc
         bd.refresh_interval, bd.measure_interval = int(refresh_interval), int(measure_interval)
-        bd.delay_k, bd.device, bd.seed = 0, int(device), int(seed) & 0xFFFFFFFFFFFFFFFF
+        bd.delay_k, bd.device, bd.seed = int(delay_k), int(device), int(seed) & 0xFFFFFFFFFFFFFFFF
         self._lib = _lib.load()
         h = C.c_void_p()
         _lib.check(self._lib.kvmc_create(C.byref(md), C.byref(bd), C.byref(h)))
@@ -138,6 +138,11 @@ class Engine:
     def enable_timing(self, on=True):
         self._check(self._lib.kvmc_enable_timing(self.h, int(bool(on))))
 
+    def config(self) -> dict:
+        r, m, k, on = (C.c_int32() for _ in range(4))
+        self._check(self._lib.kvmc_get_config(self.h, C.byref(r), C.byref(m), C.byref(k), C.byref(on)))
+        return dict(refresh_interval=r.value, measure_interval=m.value, delay_k=k.value, w_on_chip=bool(on.value))
+
     def region_start(self):
         self._check(self._lib.kvmc_region_timer(self.h, 1, None))
 
@@ -210,7 +215,8 @@ class MC:
         self.proposals_per_sweep = int(params.get("proposals_per_sweep", 1))
         self.engine = Engine(self.Ham, self.walkers, params.get("precision", "plain"),
                              params.get("accept", "reference"), params.get("refresh_interval", 0),
-                             params.get("measure_interval", 0), params.get("seed", 0), params.get("device", 0))
+                             params.get("measure_interval", 0), params.get("seed", 0), params.get("device", 0),
+                             params.get("delay_k", 0))
         self.n_occupied = min(self.Ham.N_up, self.Ham.N_down)
 
     @property
