@@ -243,8 +243,10 @@ def gpu_arm(a):
     ham = model()
     n = N_SITES // 2
     peaks = measure_peaks(local) if (rank == 0 and not a.no_peaks) else {}
-    eng = kv.Engine(ham, a.walkers, precision="mixed", seed=a.seed + 104729 * rank, refresh_interval=a.refresh,
-                    device=local)
+    from kagomevmc import replicas
+
+    eng = kv.Engine(ham, a.walkers, precision="mixed", seed=replicas.replica_seed(a.seed, rank),
+                    refresh_interval=a.refresh, device=local)
     eng.init()
     run_steps(eng, a.warmup, a.proposals)
     eng.enable_timing(True)
@@ -259,13 +261,8 @@ def gpu_arm(a):
     sweep_ms, sweep_n = eng.kernel_time(0)
     ref_ms, ref_n = eng.kernel_time(1)
     eng.enable_timing(False)
-    accepted = tot["accepted"]
-    if world > 1:
-        t = torch.tensor([ms, float(accepted)], dtype=torch.float64, device="cuda")
-        mx = t.clone()
-        torch.distributed.all_reduce(mx, op=torch.distributed.ReduceOp.MAX)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.SUM)
-        ms, accepted = float(mx[0]), float(t[1])
+    ms, red = replicas.reduce_run(ms, {"accepted": tot["accepted"]}, device=f"cuda:{local}" if world > 1 else None)
+    accepted = red["accepted"]
     value = accepted / (ms * 1e-3)
 
     # end to end through the public API with host buffers: the walkers'

@@ -499,6 +499,8 @@ extern "C" int kvmc_create(const kvmc_model_desc *model, const kvmc_batch_desc *
         (rc = h->alloc(&b.energy_out, Wk)) || (rc = h->alloc(&b.refresh_count, 1)) || (rc = h->alloc(&h->d_active, 1)) ||
         (rc = h->alloc(&h->d_attempt, Wk)) || (rc = h->alloc(&h->d_redo, Wk)))
         return bail(rc);
+    b.solve_block = kvmc::refresh_scratch_block(m);
+    if ((rc = h->alloc(&b.solve_scratch, b.solve_block * 2 * (size_t)Wk))) return bail(rc);
     if (h->mixed) cudaMemset(b.W32, 0, wblock * Wk * sizeof(float));
     else cudaMemset(b.W64, 0, wblock * Wk * sizeof(double));
     cudaMemset(b.kappa_up, 0, (size_t)Wk * N * 2);

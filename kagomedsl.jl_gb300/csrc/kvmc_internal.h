@@ -41,6 +41,8 @@ struct DevBatch {
     float *drift;          // [W] max |W32_old - W64_new| at the last refresh
     double *energy_out;    // [W] scratch for kvmc_measure
     unsigned long long *refresh_count;  // walker refreshes performed (one counter)
+    double *solve_scratch; // FP64 rows being solved by the refresh: [W][2][solve_block]
+    size_t solve_block;    // doubles per (walker, spin)
 };
 
 enum : int {
@@ -81,6 +83,7 @@ cudaError_t launch_init_random(const DevModel &m, const DevBatch &b, unsigned lo
 size_t mixed_sweep_smem(const DevModel &m);
 size_t delayed_smem_bytes(const DevModel &m, int K);
 size_t refresh_smem(const DevModel &m);
+size_t refresh_scratch_block(const DevModel &m);
 int max_smem_optin(int device);
 
 }  // namespace kvmc

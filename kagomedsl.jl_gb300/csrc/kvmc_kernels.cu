@@ -49,6 +49,16 @@ __device__ __forceinline__ void proposal_draw(unsigned long long seed, int walke
     bond = (int)(((unsigned long long)x.z * (unsigned long long)(unsigned)n_bonds) >> 32);
 }
 
+// The same draw as raw bits: u53 (r = u53 * 2^-53) and the bond index.
+__device__ __forceinline__ void proposal_bits(unsigned long long seed, int walker, long long t, int n_bonds,
+                                              unsigned long long &u53, int &bond) {
+    const unsigned long long ut = (unsigned long long)t;
+    const uint4 x = philox4x32_10(make_uint4((unsigned)ut, (unsigned)(ut >> 32), (unsigned)walker, 0u),
+                                  make_uint2((unsigned)seed, (unsigned)(seed >> 32)));
+    u53 = ((unsigned long long)(x.x >> 5) << 26) | (x.y >> 6);
+    bond = (int)(((unsigned long long)x.z * (unsigned long long)(unsigned)n_bonds) >> 32);
+}
+
 __device__ __forceinline__ double warp_sum(double v) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
@@ -105,33 +115,103 @@ constexpr int kRefreshThreads = 256;
 
 // Rows of W at sites that do not hold this spin: w * tilde_U = u, one
 // thread per row.  With P tilde_U = L Uf (row pivots perm): y Uf = u
-// (forward), v L = y (backward, unit diagonal), w[perm[i]] = v[i].  Each
-// thread works on its own row of Y in shared memory; the factor entries it
-// reads are the same for every thread (broadcast), so no barrier is needed.
+// (forward), v L = y (backward, unit diagonal), w[perm[i]] = v[i].
+// The rows live column-major in an FP64 scratch block (a warp's 32 rows
+// form one coalesced segment per column); each thread solves its row in
+// blocks of kSolveB columns held in registers, and applies a block to the
+// remaining columns eight at a time (eight independent FMA chains).  The
+// factor entries are the same for every thread (shared-memory broadcast),
+// so no barrier is needed.
+constexpr int kSolveB = 16;
+
 template <typename OutT>
-__device__ void solve_rows_block(const double *A, int lda, const double *invd, const int *perm, const double *U,
-                                 int n, const short *rows, int n_rows, double *Y, int ldy, OutT *Wout, int ldw,
-                                 float *drift_slot, bool track_drift) {
-    const int tid = threadIdx.x;
+__device__ void solve_rows_blocked(const double *A, int lda, const double *invd, const int *perm, const double *U,
+                                   int n, const short *rows, int n_rows, double *Y, OutT *Wout, int ldw,
+                                   float *drift_slot, bool track_drift) {
+    const int r = threadIdx.x;
     float dmax = 0.f;
-    if (tid < n_rows) {
-        double *y = Y + (size_t)tid * ldy;
-        const int R = rows[tid];
-        for (int j = 0; j < n; ++j) y[j] = U[(size_t)R * n + j];
-        for (int i = 0; i < n; ++i) {
-            const double yi = y[i] * invd[i];
-            y[i] = yi;
-            const double *Ai = A + (size_t)i * lda;
-            for (int j = i + 1; j < n; ++j) y[j] = fma(-yi, Ai[j], y[j]);
+    if (r < n_rows) {
+        const int ld = n_rows;
+        const int R = rows[r];
+        for (int j = 0; j < n; ++j) Y[(size_t)j * ld + r] = U[(size_t)R * n + j];
+        // forward: y * Uf = u
+        for (int jb = 0; jb < n; jb += kSolveB) {
+            const int nb = min(kSolveB, n - jb);
+            double yb[kSolveB];
+#pragma unroll
+            for (int q = 0; q < kSolveB; ++q) yb[q] = q < nb ? Y[(size_t)(jb + q) * ld + r] : 0.0;
+#pragma unroll
+            for (int ii = 0; ii < kSolveB; ++ii) {
+                if (ii < nb) {
+                    yb[ii] *= invd[jb + ii];
+                    const double *Ai = A + (size_t)(jb + ii) * lda + jb;
+#pragma unroll
+                    for (int jj = ii + 1; jj < kSolveB; ++jj)
+                        if (jj < nb) yb[jj] = fma(-yb[ii], Ai[jj], yb[jj]);
+                }
+            }
+#pragma unroll
+            for (int q = 0; q < kSolveB; ++q)
+                if (q < nb) Y[(size_t)(jb + q) * ld + r] = yb[q];
+            for (int j0 = jb + kSolveB; j0 < n; j0 += 8) {
+                const int cnt = min(8, n - j0);
+                double acc[8];
+#pragma unroll
+                for (int t = 0; t < 8; ++t) acc[t] = t < cnt ? Y[(size_t)(j0 + t) * ld + r] : 0.0;
+#pragma unroll
+                for (int ii = 0; ii < kSolveB; ++ii) {
+                    if (ii < nb) {
+                        const double *Ai = A + (size_t)(jb + ii) * lda + j0;
+#pragma unroll
+                        for (int t = 0; t < 8; ++t)
+                            if (t < cnt) acc[t] = fma(-yb[ii], Ai[t], acc[t]);
+                    }
+                }
+#pragma unroll
+                for (int t = 0; t < 8; ++t)
+                    if (t < cnt) Y[(size_t)(j0 + t) * ld + r] = acc[t];
+            }
         }
-        for (int j = n - 1; j > 0; --j) {
-            const double vj = y[j];
-            const double *Aj = A + (size_t)j * lda;
-            for (int i = 0; i < j; ++i) y[i] = fma(-vj, Aj[i], y[i]);
+        // backward: v * L = y (L unit lower, L[j][i] = A[j][i] for j > i)
+        const int last = ((n - 1) / kSolveB) * kSolveB;
+        for (int jb = last; jb >= 0; jb -= kSolveB) {
+            const int nb = min(kSolveB, n - jb);
+            double yb[kSolveB];
+#pragma unroll
+            for (int q = 0; q < kSolveB; ++q) yb[q] = q < nb ? Y[(size_t)(jb + q) * ld + r] : 0.0;
+#pragma unroll
+            for (int ii = kSolveB - 1; ii >= 0; --ii) {
+                if (ii < nb) {
+                    const double *Aj = A + (size_t)(jb + ii) * lda + jb;
+#pragma unroll
+                    for (int kk = 0; kk < ii; ++kk) yb[kk] = fma(-yb[ii], Aj[kk], yb[kk]);
+                }
+            }
+#pragma unroll
+            for (int q = 0; q < kSolveB; ++q)
+                if (q < nb) Y[(size_t)(jb + q) * ld + r] = yb[q];
+            for (int i0 = 0; i0 < jb; i0 += 8) {
+                const int cnt = min(8, jb - i0);
+                double acc[8];
+#pragma unroll
+                for (int t = 0; t < 8; ++t) acc[t] = t < cnt ? Y[(size_t)(i0 + t) * ld + r] : 0.0;
+#pragma unroll
+                for (int ii = 0; ii < kSolveB; ++ii) {
+                    if (ii < nb) {
+                        const double *Aj = A + (size_t)(jb + ii) * lda + i0;
+#pragma unroll
+                        for (int t = 0; t < 8; ++t)
+                            if (t < cnt) acc[t] = fma(-yb[ii], Aj[t], acc[t]);
+                    }
+                }
+#pragma unroll
+                for (int t = 0; t < 8; ++t)
+                    if (t < cnt) Y[(size_t)(i0 + t) * ld + r] = acc[t];
+            }
         }
         OutT *wr = Wout + (size_t)R * ldw;
         for (int i = 0; i < n; ++i) {
-            const OutT nv = (OutT)y[i];
+            const OutT nv = (OutT)Y[(size_t)i * ld + r];
             if (track_drift) {
                 const float o = (float)wr[perm[i]];
                 dmax = fmaxf(dmax, fabsf(o - (float)nv) / (1.f + fabsf((float)nv)));
@@ -142,13 +222,13 @@ __device__ void solve_rows_block(const double *A, int lda, const double *invd, c
     if (track_drift) {
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) dmax = fmaxf(dmax, __shfl_xor_sync(0xffffffffu, dmax, o));
-        if ((tid & 31) == 0 && dmax > 0.f) atomic_max_nonneg(drift_slot, dmax);
+        if ((threadIdx.x & 31) == 0 && dmax > 0.f) atomic_max_nonneg(drift_slot, dmax);
     }
 }
 
 template <typename OutT>
-__global__ void __launch_bounds__(kRefreshThreads)
-refresh_kernel(DevModel m, DevBatch b, int only_due, int track_drift, int rows_per_pass) {
+__global__ void __launch_bounds__(kRefreshThreads, 2)
+refresh_kernel(DevModel m, DevBatch b, int only_due, int track_drift) {
     const int w = blockIdx.x;
     const int spin = blockIdx.y;
     if (only_due && b.since[w] >= 0) return;  // a negative `since` marks a refresh as due
@@ -168,9 +248,10 @@ refresh_kernel(DevModel m, DevBatch b, int only_due, int track_drift, int rows_p
     double *A = reinterpret_cast<double *>(smem);
     double *invd = A + (size_t)n * lda;
     double *red = invd + n;                       // 33 doubles
-    double *Y = red + 33;                         // row block [rows_per_pass][n + 1]
-    int *perm = reinterpret_cast<int *>(Y + (size_t)rows_per_pass * lda);
+    int *perm = reinterpret_cast<int *>(red + 33);
     short *rows = reinterpret_cast<short *>(perm + n);
+    // FP64 scratch for the solved rows, [n][rows] column-major, one block per (walker, spin)
+    double *Y = b.solve_scratch + ((size_t)w * 2 + spin) * b.solve_block;
     __shared__ int s_piv, s_nrows;
     __shared__ double s_pmax;
 
@@ -296,22 +377,121 @@ refresh_kernel(DevModel m, DevBatch b, int only_due, int track_drift, int rows_p
     }
     __syncthreads();
     const int nrows = s_nrows;
-    for (int r0 = 0; r0 < nrows; r0 += rows_per_pass) {
-        const int cnt = min(rows_per_pass, nrows - r0);
-        solve_rows_block<OutT>(A, lda, invd, perm, U, n, rows + r0, cnt, Y, lda, W, ldw, &b.drift[w], track_drift != 0);
+    for (int r0 = 0; r0 < nrows; r0 += blockDim.x) {
+        const int cnt = min((int)blockDim.x, nrows - r0);
+        solve_rows_blocked<OutT>(A, lda, invd, perm, U, n, rows + r0, cnt, Y + (size_t)r0 * n, W, ldw, &b.drift[w],
+                                 track_drift != 0);
     }
 }
 
-// Shared memory of the refresh kernel when it solves rows_per_pass rows at a time.
-size_t refresh_smem_rows(const DevModel &m, int rows_per_pass) {
+size_t refresh_smem(const DevModel &m) {
     const int n = m.n_up > m.n_dn ? m.n_up : m.n_dn;
-    return (size_t)n * (n + 1) * 8 + (size_t)n * 8 + 33 * 8 + (size_t)rows_per_pass * (n + 1) * 8 + (size_t)n * 4 +
-           (size_t)m.n_sites * 2 + 16;
+    return (size_t)n * (n + 1) * 8 + (size_t)n * 8 + 33 * 8 + (size_t)n * 4 + (size_t)m.n_sites * 2 + 16;
 }
 
-// Minimum footprint (one row per pass); the launcher widens the row block to
-// what fits.
-size_t refresh_smem(const DevModel &m) { return refresh_smem_rows(m, 1); }
+// FP64 scratch doubles per (walker, spin) for the solved rows.
+size_t refresh_scratch_block(const DevModel &m) {
+    const int n = m.n_up > m.n_dn ? m.n_up : m.n_dn;
+    const int rows = m.n_sites - (m.n_up < m.n_dn ? m.n_up : m.n_dn);
+    return (size_t)n * rows;
+}
+
+// ---------------------------------------------------------------------------
+// Acceptance decisions without FP64 on the common path.
+//
+// The reference rejects when r > Z_mu/Z_max (src/MonteCarlo.jl:546-550),
+// then accepts when |ratio|^2 >= 1 and r < Z_mu/Z_max, or when
+// r < (Z_mu/Z_max) |ratio|^2 (:581-591), all in FP64 with one uniform r.
+// Here r = u53 * 2^-53 exactly, thr = fl(Z_mu/Z_max) is encoded once per
+// change of Z_mu as m * 2^(k-53), and "r vs thr" becomes an exact integer
+// comparison.  The second test runs in FP32 with a relative guard band of
+// 1e-5 (FP32 carries ~1e-7); only a lane inside the band recomputes it in
+// FP64, so every decision equals the FP64 one while the FP64 pipe (1/64 of
+// the FP32 rate on GB300) is almost never issued.
+// ---------------------------------------------------------------------------
+struct Thr {
+    double d;              // fl(zmu / n_bonds), or 1 for the Metropolis rule
+    float f;
+    unsigned long long m;  // thr = m * 2^(k - 53); m = 0 encodes thr = 0
+    int k;
+};
+
+__device__ __forceinline__ void make_thr(Thr &T, int zmu, int n_bonds, int rule) {
+    T.d = rule == 0 ? (double)zmu / (double)n_bonds : 1.0;
+    T.f = (float)T.d;
+    if (T.d == 0.0) { T.m = 0; T.k = 0; return; }
+    const unsigned long long bits = (unsigned long long)__double_as_longlong(T.d);
+    T.m = (bits & 0xFFFFFFFFFFFFFull) | (1ull << 52);
+    T.k = (int)((bits >> 52) & 0x7ff) - 1075 + 53;
+}
+
+// sign(r - thr) for r = u53 * 2^-53, exact.  thr >= 1/n_bonds keeps -k <= 11.
+__device__ __forceinline__ int cmp_r_thr(unsigned long long u53, const Thr &T) {
+    if (T.m == 0) return u53 > 0 ? 1 : 0;
+    unsigned long long L = u53, Rr = T.m;
+    if (T.k >= 0) Rr <<= T.k;
+    else L <<= -T.k;
+    return L > Rr ? 1 : (L < Rr ? -1 : 0);
+}
+
+__device__ __forceinline__ double r_of(unsigned long long u53) { return (double)u53 * (1.0 / 9007199254740992.0); }
+
+// r in FP32 to ~1e-7 relative (two 32-bit conversions, no FP64)
+__device__ __forceinline__ float r_f32(unsigned long long u53) {
+    return (float)(unsigned)(u53 >> 21) * 2.3283064365386963e-10f + (float)(unsigned)(u53 & 0x1FFFFF) * 1.1102230246251565e-16f;
+}
+
+// FP64 decision from the two ratio factors (the plain form's rule, and the
+// mixed form's fallback inside the guard band)
+__device__ __forceinline__ bool decide_f64(double pu, double pd, unsigned long long u53, int c, const Thr &T, int rule,
+                                           bool &bad) {
+    const double ratio = pu * pd;
+    const double a = ratio * ratio;
+    if (!isfinite(a)) { bad = true; return false; }
+    const double r = r_of(u53);
+    if (rule == 0) return a >= 1.0 ? (c < 0) : (r < T.d * a);
+    return a >= 1.0 || r < a;
+}
+
+__device__ __forceinline__ bool decide(double pu, double pd, unsigned long long u53, int c, const Thr &T, int rule,
+                                       bool &bad) {
+    return decide_f64(pu, pd, u53, c, T, rule, bad);
+}
+
+__device__ __forceinline__ bool decide(float pu, float pd, unsigned long long u53, int c, const Thr &T, int rule,
+                                       bool &bad) {
+    const float rt = pu * pd;
+    const float a = rt * rt;
+    if (isnan(a)) { bad = true; return false; }
+    constexpr float band = 1e-5f;
+    if (a >= 1.f + band) return rule == 0 ? (c < 0) : true;   // includes a = inf
+    if (a <= 1.f - band) {
+        const float x = rule == 0 ? T.f * a : a;
+        const float rf = r_f32(u53);
+        if (rf < x * (1.f - band)) return true;
+        if (rf > x * (1.f + band)) return false;
+    }
+    return decide_f64((double)pu, (double)pd, u53, c, T, rule, bad);
+}
+
+// Block sum of FP32 partials into FP64: FP32 within each warp, FP64 across
+// the warps (only warp 0 touches the FP64 pipe).  red holds >= 33 doubles.
+__device__ double block_sum_f32(float v, double *red) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    float *redf = reinterpret_cast<float *>(red);
+    __syncthreads();
+    if (lane == 0) redf[warp] = v;
+    __syncthreads();
+    if (warp == 0) {
+        double s = lane < nw ? (double)redf[lane] : 0.0;
+        s = warp_sum(s);
+        if (lane == 0) red[32] = s;
+    }
+    __syncthreads();
+    return red[32];
+}
 
 // ---------------------------------------------------------------------------
 // Sweep: proposals of one walker per CTA.
@@ -326,9 +506,10 @@ size_t refresh_smem(const DevModel &m) { return refresh_smem_rows(m, 1); }
 // T = float,  W staged in shared memory: the mixed form.
 // ---------------------------------------------------------------------------
 struct SweepCtl {
-    long long t, tend;
+    long long t, tend, next_meas, next_ref;
     int since, zmu, state;
     int Ku, lu, Kd, ld;
+    Thr thr;
     double red[33];
 };
 
@@ -340,20 +521,23 @@ struct WPtr {
     __device__ __forceinline__ T &D(int r, int c) const { return dn[(size_t)r * ld_dn + c]; }
 };
 
-// Local energy of the state (src/Hamiltonian.jl:593-778), FP64 sums.
+// Local energy of the state (src/Hamiltonian.jl:593-778): the plain form
+// sums in FP64 throughout; the FP32 form sums each thread's terms and each
+// warp in FP32 and the warp partials in FP64.
 template <typename T>
 __device__ double local_energy(const DevModel &m, const short2 *bonds, const short *kup,
                                const short *kdn, const WPtr<T> &W, double *red) {
-    double acc = 0.0;
+    T acc = 0;
     for (int e = threadIdx.x; e < m.n_bonds; e += blockDim.x) {
         const short2 bd = bonds[e];
         const int i = bd.x, j = bd.y;
         const int ui = kup[i], uj = kup[j], di = kdn[i], dj = kdn[j];
-        acc += ((ui != 0) == (uj != 0)) ? 0.25 : -0.25;
-        if (uj != 0 && di != 0) acc -= 0.5 * (double)W.U(i, uj - 1) * (double)W.D(j, di - 1);
-        if (ui != 0 && dj != 0) acc -= 0.5 * (double)W.U(j, ui - 1) * (double)W.D(i, dj - 1);
+        acc += ((ui != 0) == (uj != 0)) ? (T)0.25 : (T)-0.25;
+        if (uj != 0 && di != 0) acc -= (T)0.5 * W.U(i, uj - 1) * W.D(j, di - 1);
+        if (ui != 0 && dj != 0) acc -= (T)0.5 * W.U(j, ui - 1) * W.D(i, dj - 1);
     }
-    return block_sum(acc, red);
+    if constexpr (sizeof(T) == 4) return block_sum_f32(acc, red);
+    else return block_sum(acc, red);
 }
 
 // Antiparallel bonds touching sites a or b (each bond counted once).
@@ -475,17 +659,19 @@ __global__ void sweep_kernel(DevModel m, DevBatch b, SweepParams p, int refresh_
         zc += ((kup[bd.x] != 0 && kdn[bd.y] != 0) || (kup[bd.y] != 0 && kdn[bd.x] != 0)) ? 1.0 : 0.0;
     }
     zc = block_sum(zc, ctl.red);
+    const int R = p.refresh_every;
+    const int M = p.measure_every;
     if (tid == 0) {
         ctl.t = t0;
         ctl.tend = tend;
         ctl.since = b.since[w] < 0 ? 0 : b.since[w];
         ctl.zmu = (int)zc;
+        ctl.next_meas = (t0 / M + 1) * M;
+        ctl.next_ref = refresh_by_proposals ? (t0 / R + 1) * R : tend;
+        make_thr(ctl.thr, ctl.zmu, m.n_bonds, p.accept_rule);
     }
     __syncthreads();
 
-    const int R = p.refresh_every;
-    const int M = p.measure_every;
-    const double nb_d = (double)m.n_bonds;
     long long acc_count = 0, n_meas = 0;
     double se = 0.0, se2 = 0.0;
 
@@ -493,26 +679,23 @@ __global__ void sweep_kernel(DevModel m, DevBatch b, SweepParams p, int refresh_
         if (warp == 0) {
             long long t = ctl.t;
             const int since = ctl.since;
-            int state = 2;  // 2 = stop, 1 = accepted move, 3 = measurement boundary
-            const double thr = p.accept_rule == 0 ? (double)ctl.zmu / nb_d : 1.0;
+            const long long stop = min(tend, ctl.next_ref);
+            const long long next_meas = ctl.next_meas;
+            const Thr thr = ctl.thr;
+            int state = 2;  // 2 = stop, 1 = accepted move, 3 = measurement or refresh boundary
             while (true) {
-                if (t >= tend) break;
+                if (t >= stop) break;
                 if (!refresh_by_proposals && since >= R) break;
-                long long lim = tend - t;
-                const long long to_meas = (t / M + 1) * M - t;
-                if (to_meas < lim) lim = to_meas;
-                if (refresh_by_proposals) {
-                    const long long to_ref = (t / R + 1) * R - t;
-                    if (to_ref < lim) lim = to_ref;
-                }
+                const long long lim = min(stop, next_meas) - t;
                 const int win = lim < 32 ? (int)lim : 32;
-                bool acc = false;
+                bool acc = false, bad = false;
                 int Ku = 0, lu = 0, Kd = 0, ld = 0;
                 if (lane < win) {
-                    double r;
+                    unsigned long long u53;
                     int bi;
-                    proposal_draw(p.seed, w, t + lane, m.n_bonds, r, bi);
-                    if (!(r > thr)) {
+                    proposal_bits(p.seed, w, t + lane, m.n_bonds, u53, bi);
+                    const int c = cmp_r_thr(u53, thr);
+                    if (p.accept_rule != 0 || c <= 0) {
                         const short2 bd = bonds[bi];
                         const int i = bd.x, j = bd.y;
                         const int kui = kup[i], kuj = kup[j], kdi = kdn[i], kdj = kdn[j];
@@ -521,18 +704,11 @@ __global__ void sweep_kernel(DevModel m, DevBatch b, SweepParams p, int refresh_
                         if (f1 || f2) {
                             if (f1) { Ku = j; lu = kui - 1; Kd = i; ld = kdj - 1; }
                             else    { Ku = i; lu = kuj - 1; Kd = j; ld = kdi - 1; }
-                            const double ratio = (double)W.U(Ku, lu) * (double)W.D(Kd, ld);
-                            const double a = ratio * ratio;
-                            if (!isfinite(a)) {
-                                atomicOr(&b.status[w], kStatusNonFinite);
-                            } else if (p.accept_rule == 0) {
-                                acc = a >= 1.0 ? (r < thr) : (r < thr * a);
-                            } else {
-                                acc = a >= 1.0 || r < a;
-                            }
+                            acc = decide(W.U(Ku, lu), W.D(Kd, ld), u53, c, thr, p.accept_rule, bad);
                         }
                     }
                 }
+                if (__any_sync(0xffffffffu, bad) && bad) atomicOr(&b.status[w], kStatusNonFinite);
                 const unsigned mask = __ballot_sync(0xffffffffu, acc);
                 if (mask) {
                     const int f = __ffs(mask) - 1;
@@ -542,7 +718,7 @@ __global__ void sweep_kernel(DevModel m, DevBatch b, SweepParams p, int refresh_
                     break;
                 }
                 t += win;
-                if (t % M == 0 || (refresh_by_proposals && t % R == 0)) { state = 3; break; }
+                if (t == next_meas || t == ctl.next_ref) { state = 3; break; }
             }
             if (lane == 0) { ctl.t = t; ctl.state = state; }
         }
@@ -560,18 +736,20 @@ __global__ void sweep_kernel(DevModel m, DevBatch b, SweepParams p, int refresh_
                 const int after = incident_antiparallel(m, kup, Ku, Kd);
                 ctl.zmu += after - before;
                 ctl.since += 1;
+                make_thr(ctl.thr, ctl.zmu, m.n_bonds, p.accept_rule);
             }
             acc_count += 1;
             __syncthreads();
         }
         const long long t = ctl.t;
-        if (t % M == 0) {
+        if (t == ctl.next_meas) {
             const double e = local_energy<T>(m, bonds, kup, kdn, W, ctl.red);
             se += e;
             se2 += e * e;
             n_meas += 1;
+            if (tid == 0) ctl.next_meas += M;
         }
-        if (refresh_by_proposals && t % R == 0) break;  // refresh boundary: hand over to refresh
+        if (t == ctl.next_ref) break;  // refresh boundary (plain form): hand over to the refresh kernel
         __syncthreads();
     }
     __syncthreads();
@@ -591,7 +769,7 @@ __global__ void sweep_kernel(DevModel m, DevBatch b, SweepParams p, int refresh_
         const long long t = ctl.t;
         b.t[w] = t;
         bool due;
-        if (refresh_by_proposals) due = (t % R == 0) && t > t0;
+        if (refresh_by_proposals) due = t == ctl.next_ref;
         else due = ctl.since >= R;
         b.since[w] = due ? -1 : ctl.since;
         b.accepted[w] += acc_count;
@@ -705,10 +883,11 @@ __device__ void delayed_zero(const DelayedSpin<K> &S, int N) {
 }
 
 struct DelayedCtl {
-    long long t;
+    long long t, next_meas;
     int since, zmu, state, m;
     int Ku, lu, Kd, ld;
     float piv_u, piv_d;
+    Thr thr;
     double red[33];
 };
 
@@ -716,16 +895,16 @@ struct DelayedCtl {
 template <int K>
 __device__ double delayed_local_energy(const DevModel &m, const short2 *bonds, const short *kup, const short *kdn,
                                        const DelayedSpin<K> &U, const DelayedSpin<K> &D, double *red) {
-    double acc = 0.0;
+    float acc = 0.f;
     for (int e = threadIdx.x; e < m.n_bonds; e += blockDim.x) {
         const short2 bd = bonds[e];
         const int i = bd.x, j = bd.y;
         const int ui = kup[i], uj = kup[j], di = kdn[i], dj = kdn[j];
-        acc += ((ui != 0) == (uj != 0)) ? 0.25 : -0.25;
-        if (uj != 0 && di != 0) acc -= 0.5 * (double)U.eff(i, uj - 1) * (double)D.eff(j, di - 1);
-        if (ui != 0 && dj != 0) acc -= 0.5 * (double)U.eff(j, ui - 1) * (double)D.eff(i, dj - 1);
+        acc += ((ui != 0) == (uj != 0)) ? 0.25f : -0.25f;
+        if (uj != 0 && di != 0) acc -= 0.5f * U.eff(i, uj - 1) * D.eff(j, di - 1);
+        if (ui != 0 && dj != 0) acc -= 0.5f * U.eff(j, ui - 1) * D.eff(i, dj - 1);
     }
-    return block_sum(acc, red);
+    return block_sum_f32(acc, red);
 }
 
 template <int K>
@@ -784,17 +963,18 @@ __global__ void __launch_bounds__(512) sweep_delayed_kernel(DevModel m, DevBatch
         zc += ((kup[bd.x] != 0 && kdn[bd.y] != 0) || (kup[bd.y] != 0 && kdn[bd.x] != 0)) ? 1.0 : 0.0;
     }
     zc = block_sum(zc, ctl.red);
+    const int R = p.refresh_every;
+    const int M = p.measure_every;
     if (tid == 0) {
         ctl.t = t0;
         ctl.since = b.since[w] < 0 ? 0 : b.since[w];
         ctl.zmu = (int)zc;
         ctl.m = 0;
+        ctl.next_meas = (t0 / M + 1) * M;
+        make_thr(ctl.thr, ctl.zmu, m.n_bonds, p.accept_rule);
     }
     __syncthreads();
 
-    const int R = p.refresh_every;
-    const int M = p.measure_every;
-    const double nb_d = (double)m.n_bonds;
     long long acc_count = 0, n_meas = 0;
     double se = 0.0, se2 = 0.0;
 
@@ -802,22 +982,22 @@ __global__ void __launch_bounds__(512) sweep_delayed_kernel(DevModel m, DevBatch
         if (warp == 0) {
             long long t = ctl.t;
             const int since = ctl.since;
+            const long long next_meas = ctl.next_meas;
+            const Thr thr = ctl.thr;
             int state = 2;
-            const double thr = p.accept_rule == 0 ? (double)ctl.zmu / nb_d : 1.0;
             while (true) {
                 if (t >= tend || since >= R) break;
-                long long lim = tend - t;
-                const long long to_meas = (t / M + 1) * M - t;
-                if (to_meas < lim) lim = to_meas;
+                const long long lim = min(tend, next_meas) - t;
                 const int win = lim < 32 ? (int)lim : 32;
-                bool acc = false;
+                bool acc = false, bad = false;
                 int Ku = 0, lu = 0, Kd = 0, ld = 0;
                 float pu = 0.f, pd = 0.f;
                 if (lane < win) {
-                    double r;
+                    unsigned long long u53;
                     int bi;
-                    proposal_draw(p.seed, w, t + lane, m.n_bonds, r, bi);
-                    if (!(r > thr)) {
+                    proposal_bits(p.seed, w, t + lane, m.n_bonds, u53, bi);
+                    const int c = cmp_r_thr(u53, thr);
+                    if (p.accept_rule != 0 || c <= 0) {
                         const short2 bd = bonds[bi];
                         const int i = bd.x, j = bd.y;
                         const int kui = kup[i], kuj = kup[j], kdi = kdn[i], kdj = kdn[j];
@@ -828,18 +1008,11 @@ __global__ void __launch_bounds__(512) sweep_delayed_kernel(DevModel m, DevBatch
                             else    { Ku = i; lu = kuj - 1; Kd = j; ld = kdi - 1; }
                             pu = SU.eff(Ku, lu);
                             pd = SD.eff(Kd, ld);
-                            const double ratio = (double)pu * (double)pd;
-                            const double a = ratio * ratio;
-                            if (!isfinite(a)) {
-                                atomicOr(&b.status[w], kStatusNonFinite);
-                            } else if (p.accept_rule == 0) {
-                                acc = a >= 1.0 ? (r < thr) : (r < thr * a);
-                            } else {
-                                acc = a >= 1.0 || r < a;
-                            }
+                            acc = decide(pu, pd, u53, c, thr, p.accept_rule, bad);
                         }
                     }
                 }
+                if (__any_sync(0xffffffffu, bad) && bad) atomicOr(&b.status[w], kStatusNonFinite);
                 const unsigned mask = __ballot_sync(0xffffffffu, acc);
                 if (mask) {
                     const int f = __ffs(mask) - 1;
@@ -852,7 +1025,7 @@ __global__ void __launch_bounds__(512) sweep_delayed_kernel(DevModel m, DevBatch
                     break;
                 }
                 t += win;
-                if (t % M == 0) { state = 3; break; }
+                if (t == next_meas) { state = 3; break; }
             }
             if (lane == 0) { ctl.t = t; ctl.state = state; }
         }
@@ -889,6 +1062,7 @@ __global__ void __launch_bounds__(512) sweep_delayed_kernel(DevModel m, DevBatch
                 if (lane == 0) {
                     ctl.zmu += dz;
                     ctl.since += 1;
+                    make_thr(ctl.thr, ctl.zmu, m.n_bonds, p.accept_rule);
                 }
             }
             __syncthreads();
@@ -917,11 +1091,12 @@ __global__ void __launch_bounds__(512) sweep_delayed_kernel(DevModel m, DevBatch
             }
         }
         const long long t = ctl.t;
-        if (t % M == 0) {
+        if (t == ctl.next_meas) {
             const double e = delayed_local_energy<K>(m, bonds, kup, kdn, SU, SD, ctl.red);
             se += e;
             se2 += e * e;
             n_meas += 1;
+            if (tid == 0) ctl.next_meas += M;
         }
         __syncthreads();
     }
@@ -1076,23 +1251,16 @@ int max_smem_optin(int device) {
 
 cudaError_t launch_refresh(const DevModel &m, const DevBatch &b, bool fp32_out, int only_due,
                            int track_drift, cudaStream_t stream) {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    const size_t cap = (size_t)max_smem_optin(dev) - 1024;
-    const int n = m.n_up > m.n_dn ? m.n_up : m.n_dn;
-    int rows = std::min(kRefreshThreads, m.n_sites - std::min(m.n_up, m.n_dn));
-    while (rows > 1 && refresh_smem_rows(m, rows) > cap) --rows;
-    (void)n;
-    const size_t sm = refresh_smem_rows(m, rows);
+    const size_t sm = refresh_smem(m);
     const dim3 grid(b.n_walkers, 2);
     if (fp32_out) {
         cudaError_t e = cudaFuncSetAttribute(refresh_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
         if (e != cudaSuccess) return e;
-        refresh_kernel<float><<<grid, kRefreshThreads, sm, stream>>>(m, b, only_due, track_drift, rows);
+        refresh_kernel<float><<<grid, kRefreshThreads, sm, stream>>>(m, b, only_due, track_drift);
     } else {
         cudaError_t e = cudaFuncSetAttribute(refresh_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
         if (e != cudaSuccess) return e;
-        refresh_kernel<double><<<grid, kRefreshThreads, sm, stream>>>(m, b, only_due, track_drift, rows);
+        refresh_kernel<double><<<grid, kRefreshThreads, sm, stream>>>(m, b, only_due, track_drift);
     }
     return cudaGetLastError();
 }
