@@ -226,6 +226,137 @@ __device__ void solve_rows_blocked(const double *A, int lda, const double *invd,
     }
 }
 
+// tilde_U into A (row l = U[R,:] with kappa[R] == l; zero-filled first so a
+// configuration missing a label is singular), perm = identity.  All threads.
+template <typename KT>
+__device__ void gather_tilde_u(double *A, int lda, int *perm, const double *U, const KT *kappa, int N, int n) {
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nt = blockDim.x;
+    for (int e = tid; e < n * lda; e += nt) A[e] = 0.0;
+    __syncthreads();
+    for (int R = warp; R < N; R += nt / 32) {
+        const int l = (int)kappa[R];
+        if (l >= 1 && l <= n) {
+            const double *src = U + (size_t)R * n;
+            double *dst = A + (size_t)(l - 1) * lda;
+            for (int c = lane; c < n; c += 32) dst[c] = src[c];
+        }
+    }
+    for (int i = tid; i < n; i += nt) perm[i] = i;
+    __syncthreads();
+}
+
+// LU with partial pivoting of A in shared memory (first maximal |pivot|
+// wins, as LAPACK i*amax): P A = L Uf in place, perm tracks the row
+// pivots.  All threads; returns true when A is exactly singular.  Otherwise
+// invd receives 1/Uf[i][i], logdet = log|det A| and log_ratio =
+// log(min|Uf[i][i]| / max|Uf[i][i]|).
+__device__ bool lu_factor_shared(double *A, int lda, int n, int *perm, double *invd, double *red, double &logdet,
+                                 double &log_ratio) {
+    __shared__ int s_piv;
+    __shared__ double s_pmax;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nt = blockDim.x;
+    for (int k = 0; k < n; ++k) {
+        if (warp == 0) {
+            double best = -1.0;
+            int bi = n;
+            for (int i = k + lane; i < n; i += 32) {
+                const double v = fabs(A[(size_t)i * lda + k]);
+                if (v > best) { best = v; bi = i; }
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                const double ob = __shfl_xor_sync(0xffffffffu, best, o);
+                const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+                if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
+            }
+            if (lane == 0) { s_piv = bi; s_pmax = best; }
+        }
+        __syncthreads();
+        const int p = s_piv;
+        if (!(s_pmax > 0.0)) return true;  // exactly singular (or NaN): every thread sees it
+        if (p != k) {
+            for (int j = tid; j < n; j += nt) {
+                const double a = A[(size_t)k * lda + j];
+                A[(size_t)k * lda + j] = A[(size_t)p * lda + j];
+                A[(size_t)p * lda + j] = a;
+            }
+            if (tid == 0) { const int t = perm[k]; perm[k] = perm[p]; perm[p] = t; }
+        }
+        __syncthreads();
+        const double dinv = 1.0 / A[(size_t)k * lda + k];
+        for (int i = k + 1 + tid; i < n; i += nt) A[(size_t)i * lda + k] *= dinv;
+        __syncthreads();
+        // trailing update: warp rows, lane columns
+        for (int i = k + 1 + warp; i < n; i += nt / 32) {
+            const double aik = A[(size_t)i * lda + k];
+            double *Ai = A + (size_t)i * lda;
+            const double *Ak = A + (size_t)k * lda;
+            for (int j = k + 1 + lane; j < n; j += 32) Ai[j] = fma(-aik, Ak[j], Ai[j]);
+        }
+        __syncthreads();
+    }
+    double ld = 0.0, dmin = INFINITY, dmaxp = 0.0;
+    for (int i = tid; i < n; i += nt) {
+        const double d = A[(size_t)i * lda + i];
+        invd[i] = 1.0 / d;
+        ld += log(fabs(d));
+        dmin = fmin(dmin, fabs(d));
+        dmaxp = fmax(dmaxp, fabs(d));
+    }
+    logdet = block_sum(ld, red);
+    dmin = -block_sum_max(-dmin, red);
+    dmaxp = block_sum_max(dmaxp, red);
+    log_ratio = log(dmin / dmaxp);
+    return false;
+}
+
+// Sites not holding this spin, in site order (warp 0 fills rows; every
+// thread gets the count).
+template <typename KT>
+__device__ int collect_empty_rows(const KT *kappa, int N, short *rows) {
+    __shared__ int s_nrows;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (warp == 0) {
+        int base = 0;
+        for (int R0 = 0; R0 < N; R0 += 32) {
+            const int R = R0 + lane;
+            const bool un = R < N && kappa[R] == 0;
+            const unsigned bal = __ballot_sync(0xffffffffu, un);
+            if (un) rows[base + __popc(bal & ((1u << lane) - 1u))] = (short)R;
+            base += __popc(bal);
+        }
+        if (lane == 0) s_nrows = base;
+    }
+    __syncthreads();
+    return s_nrows;
+}
+
+// Unit rows at occupied sites (W[R][kappa[R]-1] = 1), zero padding columns
+// elsewhere.  All threads.
+template <typename KT, typename OutT>
+__device__ void write_unit_rows(const KT *kappa, int N, int n, OutT *W, int ldw, bool track_drift, float *drift_slot) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nt = blockDim.x;
+    for (int R = warp; R < N; R += nt / 32) {
+        const int l = (int)kappa[R];
+        OutT *wr = W + (size_t)R * ldw;
+        if (l != 0) {
+            float dmax = 0.f;
+            for (int c = lane; c < ldw; c += 32) {
+                const OutT nv = (OutT)((c == l - 1) ? 1.0 : 0.0);
+                if (track_drift) dmax = fmaxf(dmax, fabsf((float)wr[c] - (float)nv) / (1.f + fabsf((float)nv)));
+                wr[c] = nv;
+            }
+            if (track_drift) {
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) dmax = fmaxf(dmax, __shfl_xor_sync(0xffffffffu, dmax, o));
+                if (lane == 0 && dmax > 0.f) atomic_max_nonneg(drift_slot, dmax);
+            }
+        } else {
+            for (int c = n + lane; c < ldw; c += 32) wr[c] = (OutT)0;
+        }
+    }
+}
+
 template <typename OutT>
 __global__ void __launch_bounds__(kRefreshThreads, 2)
 refresh_kernel(DevModel m, DevBatch b, int only_due, int track_drift) {
@@ -252,131 +383,23 @@ refresh_kernel(DevModel m, DevBatch b, int only_due, int track_drift) {
     short *rows = reinterpret_cast<short *>(perm + n);
     // FP64 scratch for the solved rows, [n][rows] column-major, one block per (walker, spin)
     double *Y = b.solve_scratch + ((size_t)w * 2 + spin) * b.solve_block;
-    __shared__ int s_piv, s_nrows;
-    __shared__ double s_pmax;
 
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nt = blockDim.x;
-
-    // gather tilde_U (zeroed first so that a configuration missing a label is singular)
-    for (int e = tid; e < n * lda; e += nt) A[e] = 0.0;
-    __syncthreads();
-    for (int R = warp; R < N; R += nt / 32) {
-        const int l = kappa[R];
-        if (l >= 1 && l <= n) {
-            const double *src = U + (size_t)R * n;
-            double *dst = A + (size_t)(l - 1) * lda;
-            for (int c = lane; c < n; c += 32) dst[c] = src[c];
-        }
-    }
-    for (int i = tid; i < n; i += nt) perm[i] = i;
-    if (tid == 0) s_nrows = 0;
-    __syncthreads();
-
-    // LU with partial pivoting (first maximal |pivot| wins, as LAPACK i*amax)
-    bool singular = false;
-    for (int k = 0; k < n; ++k) {
-        if (warp == 0) {
-            double best = -1.0;
-            int bi = n;
-            for (int i = k + lane; i < n; i += 32) {
-                const double v = fabs(A[(size_t)i * lda + k]);
-                if (v > best) { best = v; bi = i; }
-            }
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) {
-                const double ob = __shfl_xor_sync(0xffffffffu, best, o);
-                const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
-                if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
-            }
-            if (lane == 0) { s_piv = bi; s_pmax = best; }
-        }
-        __syncthreads();
-        const int p = s_piv;
-        if (!(s_pmax > 0.0)) {  // exactly singular (or NaN): every thread sees it, stops
-            singular = true;
-            break;
-        }
-        if (p != k) {
-            for (int j = tid; j < n; j += nt) {
-                const double a = A[(size_t)k * lda + j];
-                A[(size_t)k * lda + j] = A[(size_t)p * lda + j];
-                A[(size_t)p * lda + j] = a;
-            }
-            if (tid == 0) { const int t = perm[k]; perm[k] = perm[p]; perm[p] = t; }
-        }
-        __syncthreads();
-        const double dinv = 1.0 / A[(size_t)k * lda + k];
-        for (int i = k + 1 + tid; i < n; i += nt) A[(size_t)i * lda + k] *= dinv;
-        __syncthreads();
-        // trailing update: warp rows, lane columns
-        for (int i = k + 1 + warp; i < n; i += nt / 32) {
-            const double aik = A[(size_t)i * lda + k];
-            double *Ai = A + (size_t)i * lda;
-            const double *Ak = A + (size_t)k * lda;
-            for (int j = k + 1 + lane; j < n; j += 32) Ai[j] = fma(-aik, Ak[j], Ai[j]);
-        }
-        __syncthreads();
-    }
-    if (singular) {
-        if (tid == 0) {
+    gather_tilde_u(A, lda, perm, U, kappa, N, n);
+    double logdet = 0.0, log_ratio = 0.0;
+    if (lu_factor_shared(A, lda, n, perm, invd, red, logdet, log_ratio)) {
+        if (threadIdx.x == 0) {
             atomicOr(&b.status[w], kStatusSingular);
             b.logdet[4 * w + spin] = -INFINITY;
             b.logdet[4 * w + 2 + spin] = -INFINITY;
         }
         return;
     }
-    // log|det|, log(min|u_kk| / max|u_kk|) and reciprocal pivots
-    double ld = 0.0, dmin = INFINITY, dmaxp = 0.0;
-    for (int i = tid; i < n; i += nt) {
-        const double d = A[(size_t)i * lda + i];
-        invd[i] = 1.0 / d;
-        ld += log(fabs(d));
-        dmin = fmin(dmin, fabs(d));
-        dmaxp = fmax(dmaxp, fabs(d));
+    if (threadIdx.x == 0) {
+        b.logdet[4 * w + spin] = logdet;
+        b.logdet[4 * w + 2 + spin] = log_ratio;
     }
-    ld = block_sum(ld, red);
-    dmin = -block_sum_max(-dmin, red);
-    dmaxp = block_sum_max(dmaxp, red);
-    if (tid == 0) {
-        b.logdet[4 * w + spin] = ld;
-        b.logdet[4 * w + 2 + spin] = log(dmin / dmaxp);
-    }
-
-    // rows to solve: sites not holding this spin, in site order
-    if (warp == 0) {
-        int base = 0;
-        for (int R0 = 0; R0 < N; R0 += 32) {
-            const int R = R0 + lane;
-            const bool un = R < N && kappa[R] == 0;
-            const unsigned bal = __ballot_sync(0xffffffffu, un);
-            if (un) rows[base + __popc(bal & ((1u << lane) - 1u))] = (short)R;
-            base += __popc(bal);
-        }
-        if (lane == 0) s_nrows = base;
-    }
-    // unit rows at occupied sites, zero padding columns
-    for (int R = warp; R < N; R += nt / 32) {
-        const int l = kappa[R];
-        if (l != 0) {
-            OutT *wr = W + (size_t)R * ldw;
-            float dmax = 0.f;
-            for (int c = lane; c < ldw; c += 32) {
-                const OutT nv = (OutT)((c == l - 1) ? 1.0 : 0.0);
-                if (track_drift) dmax = fmaxf(dmax, fabsf((float)wr[c] - (float)nv) / (1.f + fabsf((float)nv)));
-                wr[c] = nv;
-            }
-            if (track_drift) {
-#pragma unroll
-                for (int o = 16; o > 0; o >>= 1) dmax = fmaxf(dmax, __shfl_xor_sync(0xffffffffu, dmax, o));
-                if (lane == 0 && dmax > 0.f) atomic_max_nonneg(&b.drift[w], dmax);
-            }
-        } else {
-            OutT *wr = W + (size_t)R * ldw;
-            for (int c = n + lane; c < ldw; c += 32) wr[c] = (OutT)0;
-        }
-    }
-    __syncthreads();
-    const int nrows = s_nrows;
+    const int nrows = collect_empty_rows(kappa, N, rows);
+    write_unit_rows(kappa, N, n, W, ldw, track_drift != 0, &b.drift[w]);
     for (int r0 = 0; r0 < nrows; r0 += blockDim.x) {
         const int cnt = min((int)blockDim.x, nrows - r0);
         solve_rows_blocked<OutT>(A, lda, invd, perm, U, n, rows + r0, cnt, Y + (size_t)r0 * n, W, ldw, &b.drift[w],
