@@ -12,8 +12,10 @@
 //                       src/MonteCarlo.jl:326-357 for batches of walkers)
 #include <algorithm>
 #include <cstdint>
+#include <mutex>
 #include <cuda_runtime.h>
 
+#include "kvmc.h"
 #include "kvmc_internal.h"
 
 namespace kvmc {
@@ -1355,4 +1357,98 @@ cudaError_t launch_init_random(const DevModel &m, const DevBatch &b, unsigned lo
     return cudaGetLastError();
 }
 
+// ---------------------------------------------------------------------------
+// Refresh with no device allocation (kvmc_refresh_static).
+//
+// For callers that cannot allocate device memory: code running where every
+// byte of the GPU belongs to another allocator (a Julia CUDA.jl memory pool,
+// a framework's caching allocator) or where cudaMalloc's implicit device
+// synchronisation is not allowed in the middle of a Monte Carlo loop.  The
+// caller passes its own device buffers for inputs and outputs; the FP64
+// rows being solved live in the fixed array below, which the library
+// reserves on every GPU that loads it, for as long as the process runs.
+// ---------------------------------------------------------------------------
+constexpr size_t kStaticScratchBytes = 8u << 20;  // 8 MiB per device
+static __device__ __align__(256) double g_static_solve_scratch[kStaticScratchBytes / sizeof(double)];
+
+__global__ void __launch_bounds__(kRefreshThreads, 2)
+refresh_static_kernel(int N, int n, const double *U, const int *kappa, double *W, double *logdet, double *scratch) {
+    const int item = blockIdx.x;
+    const int *ki = kappa + (size_t)item * N;
+    double *Wi = W + (size_t)item * N * n;
+    double *Y = scratch + (size_t)item * n * (N - n);
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int lda = n + 1;
+    double *A = reinterpret_cast<double *>(smem);
+    double *invd = A + (size_t)n * lda;
+    double *red = invd + n;
+    int *perm = reinterpret_cast<int *>(red + 33);
+    short *rows = reinterpret_cast<short *>(perm + n);
+    // exactly N - n empty sites, or this item's rows would not fit its scratch block
+    const int nrows = collect_empty_rows(ki, N, rows);
+    if (nrows != N - n) {
+        if (threadIdx.x == 0 && logdet) logdet[item] = NAN;
+        return;
+    }
+    gather_tilde_u(A, lda, perm, U, ki, N, n);
+    double ld = 0.0, lr = 0.0;
+    if (lu_factor_shared(A, lda, n, perm, invd, red, ld, lr)) {
+        if (threadIdx.x == 0 && logdet) logdet[item] = -INFINITY;
+        return;
+    }
+    if (threadIdx.x == 0 && logdet) logdet[item] = ld;
+    write_unit_rows(ki, N, n, Wi, n, false, (float *)nullptr);
+    for (int r0 = 0; r0 < nrows; r0 += blockDim.x) {
+        const int cnt = min((int)blockDim.x, nrows - r0);
+        solve_rows_blocked<double>(A, lda, invd, perm, U, n, rows + r0, cnt, Y + (size_t)r0 * n, Wi, n,
+                                   (float *)nullptr, false);
+    }
+}
+
+namespace {
+constexpr int kMaxDevices = 64;
+void *g_static_scratch_ptr[kMaxDevices] = {};
+std::mutex g_static_setup_mu;
+
+// Once per device, with that device current: the device address of the
+// static array (its host-side name is only a stand-in) and the kernel's
+// shared-memory opt-in.
+cudaError_t static_scratch_setup(int device, void **ptr) {
+    std::lock_guard<std::mutex> lock(g_static_setup_mu);
+    if (!g_static_scratch_ptr[device]) {
+        void *p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_static_solve_scratch);
+        if (e != cudaSuccess) return e;
+        // the kernel's own static shared variables count against the opt-in limit
+        const int max_dyn = max_smem_optin(device) - 1024;
+        e = cudaFuncSetAttribute(refresh_static_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, max_dyn);
+        if (e != cudaSuccess) return e;
+        g_static_scratch_ptr[device] = p;
+    }
+    *ptr = g_static_scratch_ptr[device];
+    return cudaSuccess;
+}
+}  // namespace
+
 }  // namespace kvmc
+
+extern "C" KVMC_API int kvmc_refresh_static(int32_t n_sites, int32_t n_orb, int32_t batch, const double *U,
+                                            const int32_t *kappa, double *W, double *logdet, void *stream) {
+    using namespace kvmc;
+    if (n_sites <= 0 || n_sites > 30000 || n_orb <= 0 || n_orb >= n_sites || batch < 0 || !U || !kappa || !W)
+        return KVMC_ERR_ARGUMENT;
+    if (n_orb > 160) return KVMC_ERR_UNSUPPORTED;
+    if (batch == 0) return KVMC_OK;
+    const size_t need = (size_t)batch * n_orb * (n_sites - n_orb) * sizeof(double);
+    if (need > kStaticScratchBytes) return KVMC_ERR_ARGUMENT;  // batch * n_orb * (n_sites - n_orb) * 8 > 8 MiB
+    int device = 0;
+    if (cudaGetDevice(&device) != cudaSuccess || device < 0 || device >= kMaxDevices) return KVMC_ERR_NO_DEVICE;
+    void *scratch = nullptr;
+    if (static_scratch_setup(device, &scratch) != cudaSuccess) return KVMC_ERR_CUDA;
+    const size_t sm = (size_t)n_orb * (n_orb + 1) * 8 + (size_t)n_orb * 8 + 33 * 8 + (size_t)n_orb * 4 +
+                      (size_t)n_sites * 2 + 16;
+    if ((int)sm > max_smem_optin(device) - 1024) return KVMC_ERR_UNSUPPORTED;
+    refresh_static_kernel<<<batch, kRefreshThreads, sm, static_cast<cudaStream_t>(stream)>>>(
+        n_sites, n_orb, U, reinterpret_cast<const int *>(kappa), W, logdet, static_cast<double *>(scratch));
+    return cudaGetLastError() == cudaSuccess ? KVMC_OK : KVMC_ERR_CUDA;
+}

@@ -109,6 +109,7 @@ _SIGS = {
     "kvmc_region_timer": [_P, C.c_int32, C.POINTER(C.c_double)],
     "kvmc_get_config": [_P, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(C.c_int32)],
     "kvmc_version": [C.POINTER(C.c_int32), C.POINTER(C.c_int32)],
+    "kvmc_refresh_static": [C.c_int32, C.c_int32, C.c_int32, _P, _P, _P, _P, _P],
 }
 EXPORTS = tuple(_SIGS)
 
