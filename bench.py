@@ -4,10 +4,11 @@
 Workload (the headline configuration): 6x6 doubled kagome cells (N=216,
 n_up = n_down = 108), pi-flux parton orbitals, the reference's acceptance
 rule, 2048 independent walkers from seeded random starts.  One step = every
-walker makes `--proposals` exchange proposals (local energy every 108
-proposals), with W refreshed in FP64 every `--refresh` accepted moves
-(mixed form) or every 108 proposals (plain FP64 form).  The walkers' FP32 W
-state (2048 x 186.6 KB = 382 MB) is larger than L2, so no flush is needed.
+walker makes `--moves` accepted exchange moves (kvmc_advance; local energy
+every 108 proposals), with W refreshed in FP64 every `--refresh` accepted
+moves (mixed form) or every 108 proposals (plain FP64 form).  The walkers'
+FP32 W state (2048 x 186.6 KB = 382 MB) is larger than L2, so no flush is
+needed between steps.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
@@ -42,8 +43,8 @@ def args_():
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--walkers", type=int, default=2048)
-    p.add_argument("--proposals", type=int, default=2048, help="proposals per walker per step")
-    p.add_argument("--refresh", type=int, default=256, help="mixed form: accepted moves between FP64 refreshes")
+    p.add_argument("--moves", type=int, default=1024, help="accepted moves per walker per step")
+    p.add_argument("--refresh", type=int, default=1024, help="mixed form: accepted moves between FP64 refreshes")
     p.add_argument("--seed", type=int, default=2024)
     p.add_argument("--skip-plain", action="store_true")
     p.add_argument("--skip-cpu", action="store_true")
@@ -192,11 +193,11 @@ def measure_peaks(device):
     return out
 
 
-def run_steps(eng, steps, proposals):
+def run_steps(eng, steps, moves):
     tot = {"accepted": 0, "proposals": 0, "launches": 0, "refreshes": 0, "measurements": 0, "sum_energy": 0.0,
            "max_drift": 0.0, "bad_walkers": 0}
     for _ in range(steps):
-        st = eng.sweep(proposals)
+        st = eng.advance(moves)
         for k in ("accepted", "proposals", "launches", "refreshes", "measurements", "sum_energy", "bad_walkers"):
             tot[k] += st[k]
         tot["max_drift"] = max(tot["max_drift"], st["max_drift"])
@@ -248,19 +249,24 @@ def gpu_arm(a):
     eng = kv.Engine(ham, a.walkers, precision="mixed", seed=replicas.replica_seed(a.seed, rank),
                     refresh_interval=a.refresh, device=local)
     eng.init()
-    run_steps(eng, a.warmup, a.proposals)
+    run_steps(eng, a.warmup, a.moves)
     eng.enable_timing(True)
     clocks = ClockSampler(local)
     barrier()
     clocks.start()
     eng.region_start()
-    tot = run_steps(eng, a.steps, a.proposals)
+    tot = run_steps(eng, a.steps, a.moves)
     ms = eng.region_stop()
     clk = clocks.stop()
     barrier()
     sweep_ms, sweep_n = eng.kernel_time(0)
     ref_ms, ref_n = eng.kernel_time(1)
     eng.enable_timing(False)
+    import numpy as np
+    dr = eng.walker_drift()
+    drift = {"p50": float(np.percentile(dr, 50)), "p99": float(np.percentile(dr, 99)), "max": float(dr.max()),
+             "walker_refreshes_per_step": tot["refreshes"] / a.steps / a.walkers,
+             "what": "relative W drift max|W32 - W64|/(1+|W64|) per walker at its last refresh of the last step"}
     ms, red = replicas.reduce_run(ms, {"accepted": tot["accepted"]}, device=f"cuda:{local}" if world > 1 else None)
     accepted = red["accepted"]
     value = accepted / (ms * 1e-3)
@@ -274,7 +280,7 @@ def gpu_arm(a):
     eng.region_start()
     for _ in range(e2e_steps):
         eng.set_state(ku, kd, ct)
-        st = eng.sweep(a.proposals)
+        st = eng.advance(a.moves)
         ku, kd, ct = eng.get_state()
         ws = eng.walker_stats()
         e2e_acc += st["accepted"]
@@ -296,14 +302,14 @@ def gpu_arm(a):
     if not a.skip_plain:
         pe = kv.Engine(ham, a.walkers, precision="plain", seed=a.seed, device=local)
         pe.init()
-        run_steps(pe, 1, 2 * n)
+        run_steps(pe, 1, 16)
         pe.region_start()
-        ptot = run_steps(pe, 2, 4 * n)
+        ptot = run_steps(pe, 2, 64)
         pms = pe.region_stop()
         pe.close()
         plain = {"value": ptot["accepted"] / (pms * 1e-3), "unit": UNIT, "ms": pms,
-                 "proposals_per_walker": 8 * n, "accepted": ptot["accepted"]}
-    gate = None if a.skip_gate else energy_gate(ham, kv, 256, 4 * a.proposals, a.refresh, a.seed + 1)
+                 "moves_per_walker": 128, "accepted": ptot["accepted"]}
+    gate = None if a.skip_gate else energy_gate(ham, kv, 256, 8192, a.refresh, a.seed + 1)
 
     # roofline of the dominant kernel
     refreshes = tot["refreshes"]
@@ -344,13 +350,13 @@ def gpu_arm(a):
             "ms_per_step": ms / a.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32 (W, ratios, rank-1) + f64 (refresh, energy sums)", "data": "synthetic (seeded random starts)",
             "config": {"workload": "kagome VMC, 6x6 doubled cells (N=216), pi-flux partons, reference acceptance rule",
-                       "walkers_per_gpu": a.walkers, "proposals_per_walker_per_step": a.proposals,
+                       "walkers_per_gpu": a.walkers, "accepted_moves_per_walker_per_step": a.moves,
                        "refresh_every_accepted": a.refresh, "measure_every_proposals": n,
                        "parallelism": f"replicas x{world}", "l2": "inputs larger than L2 (W state 382 MB per GPU)"},
             "proposals_per_step": tot["proposals"] / a.steps * world, "acceptance": tot["accepted"] / tot["proposals"],
             "gpu_launches": tot["launches"], "e2e": e2e, "roofline": roof, "cpu_baseline": cpu,
             "plain_fp64": plain, "speedup_vs_plain_fp64": (value / plain["value"]) if plain else None,
-            "energy_gate": gate, "clocks": clk, "peaks_measured": peaks}
+            "energy_gate": gate, "drift": drift, "clocks": clk, "peaks_measured": peaks}
     print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()

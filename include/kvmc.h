@@ -161,6 +161,12 @@ typedef struct {
  * local energy at the configured intervals.  stats may be NULL. */
 KVMC_API int kvmc_sweep(kvmc_handle *h, int64_t proposals_per_walker, kvmc_sweep_stats *stats);
 
+/* Like kvmc_sweep, but every walker runs until it has made
+ * moves_per_walker more accepted moves, however many proposals that takes
+ * (the measurement and refresh cadences are unchanged).  Equal accepted
+ * work per walker keeps the batch's launches balanced. */
+KVMC_API int kvmc_advance(kvmc_handle *h, int64_t moves_per_walker, kvmc_sweep_stats *stats);
+
 /* Local energy of every walker's current state (getOL,
  * src/Hamiltonian.jl:762-778), FP64 result: local_energy[n_walkers]. */
 KVMC_API int kvmc_measure(kvmc_handle *h, double *local_energy);
@@ -202,6 +208,18 @@ KVMC_API int kvmc_get_w(kvmc_handle *h, double *W_up, double *W_down);
 KVMC_API int kvmc_walker_stats(kvmc_handle *h, double *sum_e, double *sum_e2, int64_t *n_meas,
                       int64_t *accepted, int64_t *proposals, int32_t *status);
 KVMC_API int kvmc_reset_stats(kvmc_handle *h);
+
+/* Each walker's largest relative W drift, max |W_fp32 - W_fp64| / (1 + |W_fp64|),
+ * seen by the refreshes of the last kvmc_sweep / kvmc_advance call (0 when
+ * the walker was not refreshed).  drift: [n_walkers]. */
+KVMC_API int kvmc_walker_drift(kvmc_handle *h, float *drift);
+
+/* Mixed form with delayed updates: after every flush of the K pending moves
+ * the rows of W at occupied sites, which are exact unit rows in exact
+ * arithmetic, are compared with their exact values; a walker whose largest
+ * deviation exceeds tol is refreshed in FP64 at once instead of waiting for
+ * refresh_interval accepted moves.  Default 1e-4. */
+KVMC_API int kvmc_set_drift_tolerance(kvmc_handle *h, double tol);
 
 /* Device-side timing of the kernels launched by kvmc_sweep, measured with
  * CUDA events on the handle's stream (enable before the calls to time).

@@ -49,6 +49,7 @@ struct kvmc_handle {
     int refresh_every = 0;
     int measure_every = 0;
     int delay_k = 1;  // mixed form: 1 = rank-1 updates, 4/8/12/16 = delayed-update depth
+    float drift_tol = 1e-4f;  // delayed form: early refresh past this unit-row deviation
     std::string err;
 
     DevModel dm{};
@@ -481,6 +482,22 @@ extern "C" int kvmc_create(const kvmc_model_desc *model, const kvmc_batch_desc *
     cudaMemcpy(dOff, off.data(), (N + 1) * sizeof(int), cudaMemcpyHostToDevice);
     cudaMemcpy(dNbr, nbr.data(), nbr.size() * sizeof(short), cudaMemcpyHostToDevice);
     m.U_up = dUu; m.U_dn = dUd; m.bonds = dB; m.nbr_off = dOff; m.nbr = dNbr;
+    // thresholds fl(z / n_bonds) for z = 0..n_bonds, with their exact binary form
+    std::vector<kvmc::ThrEntry> thr(nb + 1);
+    for (int z = 0; z <= nb; ++z) {
+        kvmc::ThrEntry &e = thr[z];
+        e.d = (double)z / (double)nb;
+        e.f = (float)e.d;
+        if (z == 0) { e.m = 0; e.k = 0; continue; }
+        unsigned long long bits;
+        std::memcpy(&bits, &e.d, 8);
+        e.m = (bits & 0xFFFFFFFFFFFFFull) | (1ull << 52);
+        e.k = (int)((bits >> 52) & 0x7ff) - 1075 + 53;
+    }
+    kvmc::ThrEntry *dThr;
+    if ((rc = h->alloc(&dThr, thr.size()))) return bail(rc);
+    cudaMemcpy(dThr, thr.data(), thr.size() * sizeof(kvmc::ThrEntry), cudaMemcpyHostToDevice);
+    m.thr_table = dThr;
 
     DevBatch &b = h->db;
     const int Wk = h->n_walkers;
@@ -492,7 +509,8 @@ extern "C" int kvmc_create(const kvmc_model_desc *model, const kvmc_batch_desc *
     else rc = h->alloc(&b.W64, wblock * Wk);
     if (rc) return bail(rc);
     if ((rc = h->alloc(&b.kappa_up, (size_t)Wk * N)) || (rc = h->alloc(&b.kappa_dn, (size_t)Wk * N)) ||
-        (rc = h->alloc(&b.t, Wk)) || (rc = h->alloc(&b.t_end, Wk)) || (rc = h->alloc(&b.since, Wk)) ||
+        (rc = h->alloc(&b.t, Wk)) || (rc = h->alloc(&b.t_end, Wk)) || (rc = h->alloc(&b.acc_end, Wk)) ||
+        (rc = h->alloc(&b.since, Wk)) ||
         (rc = h->alloc(&b.sum_e, Wk)) || (rc = h->alloc(&b.sum_e2, Wk)) || (rc = h->alloc(&b.n_meas, Wk)) ||
         (rc = h->alloc(&b.accepted, Wk)) || (rc = h->alloc(&b.proposals, Wk)) || (rc = h->alloc(&b.status, Wk)) ||
         (rc = h->alloc(&b.logdet, 4 * (size_t)Wk)) || (rc = h->alloc(&b.drift, Wk)) ||
@@ -507,6 +525,7 @@ extern "C" int kvmc_create(const kvmc_model_desc *model, const kvmc_batch_desc *
     cudaMemset(b.kappa_dn, 0, (size_t)Wk * N * 2);
     cudaMemset(b.t, 0, Wk * 8);
     cudaMemset(b.t_end, 0, Wk * 8);
+    cudaMemset(b.acc_end, 0, Wk * 8);
     cudaMemset(b.since, 0, Wk * 4);
     cudaMemset(b.status, 0, Wk * 4);
     cudaMemset(b.drift, 0, Wk * 4);
@@ -696,9 +715,24 @@ int snapshot(kvmc_handle *h, Snapshot &s) {
 
 }  // namespace
 
+namespace {
+int run_sweep(kvmc_handle *h, int64_t proposals_per_walker, int64_t moves_per_walker, kvmc_sweep_stats *stats);
+}
+
 extern "C" int kvmc_sweep(kvmc_handle *h, int64_t proposals_per_walker, kvmc_sweep_stats *stats) {
     if (!h) return fail_global(KVMC_ERR_ARGUMENT, "null handle");
     if (proposals_per_walker < 0) return h->fail(KVMC_ERR_ARGUMENT, "proposals_per_walker must be >= 0");
+    return run_sweep(h, proposals_per_walker, 0, stats);
+}
+
+extern "C" int kvmc_advance(kvmc_handle *h, int64_t moves_per_walker, kvmc_sweep_stats *stats) {
+    if (!h) return fail_global(KVMC_ERR_ARGUMENT, "null handle");
+    if (moves_per_walker < 0) return h->fail(KVMC_ERR_ARGUMENT, "moves_per_walker must be >= 0");
+    return run_sweep(h, 0, moves_per_walker, stats);
+}
+
+namespace {
+int run_sweep(kvmc_handle *h, int64_t proposals_per_walker, int64_t moves_per_walker, kvmc_sweep_stats *stats) {
     KV_TRY(set_device(h));
     Snapshot before;
     unsigned long long ref0 = 0, ref1 = 0;
@@ -707,14 +741,15 @@ extern "C" int kvmc_sweep(kvmc_handle *h, int64_t proposals_per_walker, kvmc_swe
         std::memset(stats, 0, sizeof *stats);
         KV_TRY(h->cuda(cudaMemcpy(&ref0, h->db.refresh_count, 8, cudaMemcpyDeviceToHost), "refresh count"));
     }
-    if (proposals_per_walker == 0) return KVMC_OK;
+    if (proposals_per_walker == 0 && moves_per_walker == 0) return KVMC_OK;
     kvmc::SweepParams p{};
     p.seed = h->batch.seed;
     p.accept_rule = h->batch.accept_rule;
     p.refresh_every = h->refresh_every;
     p.measure_every = h->measure_every;
     p.delay_k = h->delay_k;
-    KV_TRY(h->cuda(kvmc::launch_set_tend(h->db, proposals_per_walker, h->stream), "set t_end"));
+    p.drift_tol = h->drift_tol;
+    KV_TRY(h->cuda(kvmc::launch_set_tend(h->db, proposals_per_walker, moves_per_walker, h->stream), "set t_end"));
     KV_TRY(h->cuda(cudaMemsetAsync(h->db.drift, 0, sizeof(float) * h->n_walkers, h->stream), "memset"));
     int launches = 1;
     // Between host checks the loop issues a group of (sweep, refresh) pairs;
@@ -760,6 +795,7 @@ extern "C" int kvmc_sweep(kvmc_handle *h, int64_t proposals_per_walker, kvmc_swe
     }
     return KVMC_OK;
 }
+}  // namespace
 
 extern "C" int kvmc_measure(kvmc_handle *h, double *local_energy) {
     if (!h || !local_energy) return fail_global(KVMC_ERR_ARGUMENT, "null argument");
@@ -870,6 +906,19 @@ extern "C" int kvmc_get_w(kvmc_handle *h, double *W_up, double *W_down) {
         }
     }
     return KVMC_OK;
+}
+
+extern "C" int kvmc_set_drift_tolerance(kvmc_handle *h, double tol) {
+    if (!h) return fail_global(KVMC_ERR_ARGUMENT, "null handle");
+    if (!(tol > 0.0)) return h->fail(KVMC_ERR_ARGUMENT, "drift tolerance must be positive");
+    h->drift_tol = (float)tol;
+    return KVMC_OK;
+}
+
+extern "C" int kvmc_walker_drift(kvmc_handle *h, float *drift) {
+    if (!h || !drift) return fail_global(KVMC_ERR_ARGUMENT, "null argument");
+    KV_TRY(set_device(h));
+    return h->cuda(cudaMemcpy(drift, h->db.drift, sizeof(float) * h->n_walkers, cudaMemcpyDeviceToHost), "drift");
 }
 
 extern "C" int kvmc_walker_stats(kvmc_handle *h, double *sum_e, double *sum_e2, int64_t *n_meas, int64_t *accepted,

@@ -7,6 +7,15 @@
 
 namespace kvmc {
 
+// The acceptance threshold fl(z / n_bonds) for one Z_mu = z, also encoded
+// exactly as m * 2^(k - 53) (m = 0 encodes 0).  Filled on the host.
+struct ThrEntry {
+    double d;
+    unsigned long long m;
+    float f;
+    int k;
+};
+
 // Device view of the model, shared by every walker.
 struct DevModel {
     int n_sites;         // N
@@ -18,6 +27,7 @@ struct DevModel {
     const short *nbr;    // [2*n_bonds]
     const double *U_up;  // row-major [N][n_up]
     const double *U_dn;  // row-major [N][n_dn]
+    const ThrEntry *thr_table;  // [n_bonds + 1]
 };
 
 // Device view of the batch state.
@@ -29,6 +39,7 @@ struct DevBatch {
     float *W32;            // mixed form: same layout in FP32
     long long *t;          // [W] proposals made (Philox counter)
     long long *t_end;      // [W] target counter for the running kvmc_sweep
+    long long *acc_end;    // [W] target accepted count for the running kvmc_advance
     int *since;            // [W] accepted moves since the last refresh
     double *sum_e;         // [W]
     double *sum_e2;        // [W]
@@ -56,6 +67,7 @@ struct SweepParams {
     int refresh_every;    // mixed: accepted moves between refreshes
     int measure_every;    // proposals between energy samples
     int delay_k;          // mixed form: delayed-update depth (4, 8, 12, 16), else rank-1
+    float drift_tol;      // delayed form: unit-row deviation that triggers an early refresh
 };
 
 // Launchers.  All enqueue on `stream` and return the launch error.
@@ -74,7 +86,7 @@ cudaError_t launch_eval_ratios(const DevModel &m, const DevBatch &b, bool fp32, 
                                const int *moves, double *out, cudaStream_t stream);
 cudaError_t launch_apply_moves(const DevModel &m, const DevBatch &b, bool fp32,
                                const int *moves, cudaStream_t stream);
-cudaError_t launch_set_tend(const DevBatch &b, long long proposals, cudaStream_t stream);
+cudaError_t launch_set_tend(const DevBatch &b, long long proposals, long long moves, cudaStream_t stream);
 cudaError_t launch_init_random(const DevModel &m, const DevBatch &b, unsigned long long seed,
                                const int *attempt, const int *redo, cudaStream_t stream);
 

@@ -255,7 +255,7 @@ __device__ void gather_tilde_u(double *A, int lda, int *perm, const double *U, c
 __device__ bool lu_factor_shared(double *A, int lda, int n, int *perm, double *invd, double *red, double &logdet,
                                  double &log_ratio) {
     __shared__ int s_piv;
-    __shared__ double s_pmax;
+    __shared__ double s_pmax, s_dinv;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nt = blockDim.x;
     for (int k = 0; k < n; ++k) {
         if (warp == 0) {
@@ -271,7 +271,12 @@ __device__ bool lu_factor_shared(double *A, int lda, int n, int *perm, double *i
                 const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
                 if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
             }
-            if (lane == 0) { s_piv = bi; s_pmax = best; }
+            // one lane divides (FP64 division is a long FP64 sequence on this part)
+            if (lane == 0) {
+                s_piv = bi;
+                s_pmax = best;
+                s_dinv = best > 0.0 ? 1.0 / A[(size_t)bi * lda + k] : 0.0;
+            }
         }
         __syncthreads();
         const int p = s_piv;
@@ -285,7 +290,7 @@ __device__ bool lu_factor_shared(double *A, int lda, int n, int *perm, double *i
             if (tid == 0) { const int t = perm[k]; perm[k] = perm[p]; perm[p] = t; }
         }
         __syncthreads();
-        const double dinv = 1.0 / A[(size_t)k * lda + k];
+        const double dinv = s_dinv;
         for (int i = k + 1 + tid; i < n; i += nt) A[(size_t)i * lda + k] *= dinv;
         __syncthreads();
         // trailing update: warp rows, lane columns
@@ -441,13 +446,15 @@ struct Thr {
     int k;
 };
 
-__device__ __forceinline__ void make_thr(Thr &T, int zmu, int n_bonds, int rule) {
-    T.d = rule == 0 ? (double)zmu / (double)n_bonds : 1.0;
-    T.f = (float)T.d;
-    if (T.d == 0.0) { T.m = 0; T.k = 0; return; }
-    const unsigned long long bits = (unsigned long long)__double_as_longlong(T.d);
-    T.m = (bits & 0xFFFFFFFFFFFFFull) | (1ull << 52);
-    T.k = (int)((bits >> 52) & 0x7ff) - 1075 + 53;
+// thr for the current Z_mu: a lookup in the table the host filled with
+// fl(z / n_bonds) for every z (an FP64 division on the device would sit on
+// the critical path of every accepted move).
+__device__ __forceinline__ void make_thr(Thr &T, const ThrEntry *table, int zmu, int rule) {
+    const ThrEntry e = table[rule == 0 ? zmu : 0];
+    T.d = rule == 0 ? e.d : 1.0;
+    T.f = rule == 0 ? e.f : 1.f;
+    T.m = rule == 0 ? e.m : (1ull << 52);
+    T.k = rule == 0 ? e.k : 1;
 }
 
 // sign(r - thr) for r = u53 * 2^-53, exact.  thr >= 1/n_bonds keeps -k <= 11.
@@ -639,7 +646,12 @@ __global__ void sweep_kernel(DevModel m, DevBatch b, SweepParams p, int refresh_
 
     const long long t0 = b.t[w];
     const long long tend = b.t_end[w];
-    if (t0 >= tend) return;
+    const long long acc_left = b.acc_end[w] - b.accepted[w];  // accepted moves still wanted
+    if (t0 >= tend || acc_left <= 0) {
+        // nothing to do; a refresh marked due has run since (stream order), clear the mark
+        if (threadIdx.x == 0 && b.since[w] < 0) b.since[w] = 0;
+        return;
+    }
 
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ SweepCtl ctl;
@@ -693,7 +705,7 @@ __global__ void sweep_kernel(DevModel m, DevBatch b, SweepParams p, int refresh_
         ctl.zmu = (int)zc;
         ctl.next_meas = (t0 / M + 1) * M;
         ctl.next_ref = refresh_by_proposals ? (t0 / R + 1) * R : tend;
-        make_thr(ctl.thr, ctl.zmu, m.n_bonds, p.accept_rule);
+        make_thr(ctl.thr, m.thr_table, ctl.zmu, p.accept_rule);
     }
     __syncthreads();
 
@@ -709,7 +721,7 @@ __global__ void sweep_kernel(DevModel m, DevBatch b, SweepParams p, int refresh_
             const Thr thr = ctl.thr;
             int state = 2;  // 2 = stop, 1 = accepted move, 3 = measurement or refresh boundary
             while (true) {
-                if (t >= stop) break;
+                if (t >= stop || acc_count >= acc_left) break;
                 if (!refresh_by_proposals && since >= R) break;
                 const long long lim = min(stop, next_meas) - t;
                 const int win = lim < 32 ? (int)lim : 32;
@@ -761,7 +773,7 @@ __global__ void sweep_kernel(DevModel m, DevBatch b, SweepParams p, int refresh_
                 const int after = incident_antiparallel(m, kup, Ku, Kd);
                 ctl.zmu += after - before;
                 ctl.since += 1;
-                make_thr(ctl.thr, ctl.zmu, m.n_bonds, p.accept_rule);
+                make_thr(ctl.thr, m.thr_table, ctl.zmu, p.accept_rule);
             }
             acc_count += 1;
             __syncthreads();
@@ -769,10 +781,12 @@ __global__ void sweep_kernel(DevModel m, DevBatch b, SweepParams p, int refresh_
         const long long t = ctl.t;
         if (t == ctl.next_meas) {
             const double e = local_energy<T>(m, bonds, kup, kdn, W, ctl.red);
-            se += e;
-            se2 += e * e;
-            n_meas += 1;
-            if (tid == 0) ctl.next_meas += M;
+            if (tid == 0) {  // only thread 0 keeps the FP64 sums
+                se += e;
+                se2 += e * e;
+                n_meas += 1;
+                ctl.next_meas += M;
+            }
         }
         if (t == ctl.next_ref) break;  // refresh boundary (plain form): hand over to the refresh kernel
         __syncthreads();
@@ -802,7 +816,7 @@ __global__ void sweep_kernel(DevModel m, DevBatch b, SweepParams p, int refresh_
         b.sum_e[w] += se;
         b.sum_e2[w] += se2;
         b.n_meas[w] += n_meas;
-        if (t < tend) atomicAdd(active_count, 1);
+        if (t < tend && acc_count < acc_left) atomicAdd(active_count, 1);
     }
 }
 
@@ -842,29 +856,48 @@ struct DelayedSpin {
     __device__ __forceinline__ float dotPQ(int r, int c) const {
         const float4 *pr = reinterpret_cast<const float4 *>(P + (size_t)r * K);
         const float4 *qc = reinterpret_cast<const float4 *>(Q + (size_t)c * K);
-        float acc = 0.f;
+        float acc0 = 0.f, acc1 = 0.f;  // two chains: the window waits on this latency
 #pragma unroll
         for (int k = 0; k < K / 4; ++k) {
             const float4 a = pr[k], b = qc[k];
-            acc = fmaf(a.x, b.x, acc);
-            acc = fmaf(a.y, b.y, acc);
-            acc = fmaf(a.z, b.z, acc);
-            acc = fmaf(a.w, b.w, acc);
+            acc0 = fmaf(a.x, b.x, acc0);
+            acc1 = fmaf(a.y, b.y, acc1);
+            acc0 = fmaf(a.z, b.z, acc0);
+            acc1 = fmaf(a.w, b.w, acc1);
         }
-        return acc;
+        return acc0 + acc1;
     }
     __device__ __forceinline__ float eff(int r, int c) const { return W[(size_t)r * ld + c] - dotPQ(r, c); }
+    // W_eff over the first m factor columns only (column m is being written)
+    __device__ __forceinline__ float eff_lt(int r, int c, int m) const {
+        const float4 *pr = reinterpret_cast<const float4 *>(P + (size_t)r * K);
+        const float4 *qc = reinterpret_cast<const float4 *>(Q + (size_t)c * K);
+        float acc0 = 0.f, acc1 = 0.f;
+#pragma unroll
+        for (int k = 0; k < K / 4; ++k) {
+            const float4 a = pr[k], b = qc[k];
+            acc0 = fmaf(4 * k + 0 < m ? a.x : 0.f, b.x, acc0);
+            acc1 = fmaf(4 * k + 1 < m ? a.y : 0.f, b.y, acc1);
+            acc0 = fmaf(4 * k + 2 < m ? a.z : 0.f, b.z, acc0);
+            acc1 = fmaf(4 * k + 3 < m ? a.w : 0.f, b.w, acc1);
+        }
+        return W[(size_t)r * ld + c] - (acc0 + acc1);
+    }
 };
 
 // W -= P Q^T over all threads; each thread keeps the Q slab of its four
-// columns in registers and walks rows.
+// columns in registers and walks rows.  The rows of occupied sites should
+// come out as exact unit rows (W[R][kappa[R]-1] = 1, zeros elsewhere); their
+// largest deviation, the rounding accumulated since the last FP64 refresh,
+// is folded into *dev (float bits, atomicMax).
 template <int K>
-__device__ void delayed_flush(const DelayedSpin<K> &S, int N) {
+__device__ void delayed_flush(const DelayedSpin<K> &S, int N, const short *kappa, int *dev) {
     const int qc = S.ld >> 2;
     const int groups = blockDim.x / qc;
     const int t = threadIdx.x;
     if (t < groups * qc) {
         const int c4 = t % qc, rp = t / qc;
+        float dmax = 0.f;
         float q[4][K];
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
@@ -875,27 +908,55 @@ __device__ void delayed_flush(const DelayedSpin<K> &S, int N) {
                 q[j][4 * k] = v.x; q[j][4 * k + 1] = v.y; q[j][4 * k + 2] = v.z; q[j][4 * k + 3] = v.w;
             }
         }
-        for (int r = rp; r < N; r += groups) {
+        // two rows per pass: eight independent FMA chains per thread
+        for (int r = rp; r < N; r += 2 * groups) {
+            const int r2 = r + groups;
+            const bool two = r2 < N;
             const float4 *pr = reinterpret_cast<const float4 *>(S.P + (size_t)r * K);
-            float p[K];
+            const float4 *pr2 = reinterpret_cast<const float4 *>(S.P + (size_t)(two ? r2 : r) * K);
+            float p[K], p2[K];
 #pragma unroll
             for (int k = 0; k < K / 4; ++k) {
-                const float4 v = pr[k];
+                const float4 v = pr[k], v2 = pr2[k];
                 p[4 * k] = v.x; p[4 * k + 1] = v.y; p[4 * k + 2] = v.z; p[4 * k + 3] = v.w;
+                p2[4 * k] = v2.x; p2[4 * k + 1] = v2.y; p2[4 * k + 2] = v2.z; p2[4 * k + 3] = v2.w;
             }
             float4 *wp = reinterpret_cast<float4 *>(S.W + (size_t)r * S.ld) + c4;
-            float4 w = *wp;
-            float a0 = 0.f, a1 = 0.f, a2 = 0.f, a3 = 0.f;
+            float4 *wp2 = reinterpret_cast<float4 *>(S.W + (size_t)(two ? r2 : r) * S.ld) + c4;
+            float4 w = *wp, w2 = *wp2;
+            float a0 = 0.f, a1 = 0.f, a2 = 0.f, a3 = 0.f, b0 = 0.f, b1 = 0.f, b2 = 0.f, b3 = 0.f;
 #pragma unroll
             for (int k = 0; k < K; ++k) {
                 a0 = fmaf(p[k], q[0][k], a0);
                 a1 = fmaf(p[k], q[1][k], a1);
                 a2 = fmaf(p[k], q[2][k], a2);
                 a3 = fmaf(p[k], q[3][k], a3);
+                b0 = fmaf(p2[k], q[0][k], b0);
+                b1 = fmaf(p2[k], q[1][k], b1);
+                b2 = fmaf(p2[k], q[2][k], b2);
+                b3 = fmaf(p2[k], q[3][k], b3);
             }
             w.x -= a0; w.y -= a1; w.z -= a2; w.w -= a3;
             *wp = w;
+            const int c0 = 4 * c4;
+            int l = kappa[r] - 1;
+            if (l >= 0) {
+                const float d = fmaxf(fmaxf(fabsf(w.x - (c0 == l ? 1.f : 0.f)), fabsf(w.y - (c0 + 1 == l ? 1.f : 0.f))),
+                                      fmaxf(fabsf(w.z - (c0 + 2 == l ? 1.f : 0.f)), fabsf(w.w - (c0 + 3 == l ? 1.f : 0.f))));
+                dmax = fmaxf(dmax, d);
+            }
+            if (two) {
+                w2.x -= b0; w2.y -= b1; w2.z -= b2; w2.w -= b3;
+                *wp2 = w2;
+                l = kappa[r2] - 1;
+                if (l >= 0) {
+                    const float d = fmaxf(fmaxf(fabsf(w2.x - (c0 == l ? 1.f : 0.f)), fabsf(w2.y - (c0 + 1 == l ? 1.f : 0.f))),
+                                          fmaxf(fabsf(w2.z - (c0 + 2 == l ? 1.f : 0.f)), fabsf(w2.w - (c0 + 3 == l ? 1.f : 0.f))));
+                    dmax = fmaxf(dmax, d);
+                }
+            }
         }
+        if (dmax > 0.f) atomicMax(dev, __float_as_int(dmax));
     }
 }
 
@@ -909,7 +970,11 @@ __device__ void delayed_zero(const DelayedSpin<K> &S, int N) {
 
 struct DelayedCtl {
     long long t, next_meas;
+    long long cache_t;  // the draws below belong to proposals cache_t .. cache_t+31
+    unsigned long long cache_u53[32];
+    short2 cache_bond[32];  // the proposal's bond endpoints
     int since, zmu, state, m;
+    int dev;  // float bits: unit-row deviation seen at the last flush
     int Ku, lu, Kd, ld;
     float piv_u, piv_d;
     Thr thr;
@@ -939,7 +1004,12 @@ __global__ void __launch_bounds__(512) sweep_delayed_kernel(DevModel m, DevBatch
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const long long t0 = b.t[w];
     const long long tend = b.t_end[w];
-    if (t0 >= tend) return;
+    const long long acc_left = b.acc_end[w] - b.accepted[w];  // accepted moves still wanted
+    if (t0 >= tend || acc_left <= 0) {
+        // nothing to do; a refresh marked due has run since (stream order), clear the mark
+        if (threadIdx.x == 0 && b.since[w] < 0) b.since[w] = 0;
+        return;
+    }
 
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ DelayedCtl ctl;
@@ -956,10 +1026,6 @@ __global__ void __launch_bounds__(512) sweep_delayed_kernel(DevModel m, DevBatch
     SD.P = reinterpret_cast<float *>(cur); cur += (size_t)N * K * sizeof(float);
     SU.Q = reinterpret_cast<float *>(cur); cur += (size_t)m.ld_up * K * sizeof(float);
     SD.Q = reinterpret_cast<float *>(cur); cur += (size_t)m.ld_dn * K * sizeof(float);
-    float *stg_pu = reinterpret_cast<float *>(cur); cur += (size_t)N * sizeof(float);
-    float *stg_pd = reinterpret_cast<float *>(cur); cur += (size_t)N * sizeof(float);
-    float *stg_qu = reinterpret_cast<float *>(cur); cur += (size_t)m.ld_up * sizeof(float);
-    float *stg_qd = reinterpret_cast<float *>(cur); cur += (size_t)m.ld_dn * sizeof(float);
     int *nbr_off = reinterpret_cast<int *>(cur); cur += (size_t)(N + 1) * sizeof(int);
     short2 *bonds = reinterpret_cast<short2 *>(cur); cur += (size_t)m.n_bonds * sizeof(short2);
     short *nbr = reinterpret_cast<short *>(cur); cur += (size_t)2 * m.n_bonds * sizeof(short);
@@ -995,8 +1061,10 @@ __global__ void __launch_bounds__(512) sweep_delayed_kernel(DevModel m, DevBatch
         ctl.since = b.since[w] < 0 ? 0 : b.since[w];
         ctl.zmu = (int)zc;
         ctl.m = 0;
+        ctl.dev = 0;
+        ctl.cache_t = -1;
         ctl.next_meas = (t0 / M + 1) * M;
-        make_thr(ctl.thr, ctl.zmu, m.n_bonds, p.accept_rule);
+        make_thr(ctl.thr, m.thr_table, ctl.zmu, p.accept_rule);
     }
     __syncthreads();
 
@@ -1011,7 +1079,7 @@ __global__ void __launch_bounds__(512) sweep_delayed_kernel(DevModel m, DevBatch
             const Thr thr = ctl.thr;
             int state = 2;
             while (true) {
-                if (t >= tend || since >= R) break;
+                if (t >= tend || since >= R || acc_count >= acc_left) break;
                 const long long lim = min(tend, next_meas) - t;
                 const int win = lim < 32 ? (int)lim : 32;
                 bool acc = false, bad = false;
@@ -1019,11 +1087,17 @@ __global__ void __launch_bounds__(512) sweep_delayed_kernel(DevModel m, DevBatch
                 float pu = 0.f, pd = 0.f;
                 if (lane < win) {
                     unsigned long long u53;
-                    int bi;
-                    proposal_bits(p.seed, w, t + lane, m.n_bonds, u53, bi);
+                    short2 bd;
+                    if (t == ctl.cache_t) {  // drawn ahead during the previous update
+                        u53 = ctl.cache_u53[lane];
+                        bd = ctl.cache_bond[lane];
+                    } else {
+                        int bi;
+                        proposal_bits(p.seed, w, t + lane, m.n_bonds, u53, bi);
+                        bd = bonds[bi];
+                    }
                     const int c = cmp_r_thr(u53, thr);
                     if (p.accept_rule != 0 || c <= 0) {
-                        const short2 bd = bonds[bi];
                         const int i = bd.x, j = bd.y;
                         const int kui = kup[i], kuj = kup[j], kdi = kdn[i], kdj = kdn[j];
                         const bool f1 = kui != 0 && kdj != 0;
@@ -1060,17 +1134,30 @@ __global__ void __launch_bounds__(512) sweep_delayed_kernel(DevModel m, DevBatch
         if (state == 1) {
             const int Ku = ctl.Ku, lu = ctl.lu, Kd = ctl.Kd, ld = ctl.ld;
             const float ipu = 1.f / ctl.piv_u, ipd = 1.f / ctl.piv_d;
-            // new factor columns into staging (reads of P/Q see only old columns)
+            const int mm = ctl.m;
+            // new factor column mm, written in place: its entries read only the
+            // columns before mm, so writers and readers never touch the same word
             for (int e = tid; e < 2 * N + m.ld_up + m.ld_dn; e += blockDim.x) {
-                if (e < N) stg_pu[e] = SU.eff(e, lu) * ipu;
-                else if (e < 2 * N) stg_pd[e - N] = SD.eff(e - N, ld) * ipd;
+                if (e < N) SU.P[(size_t)e * K + mm] = SU.eff_lt(e, lu, mm) * ipu;
+                else if (e < 2 * N) SD.P[(size_t)(e - N) * K + mm] = SD.eff_lt(e - N, ld, mm) * ipd;
                 else if (e < 2 * N + m.ld_up) {
                     const int c = e - 2 * N;
-                    stg_qu[c] = SU.eff(Ku, c) - (c == lu ? 1.f : 0.f);
+                    SU.Q[(size_t)c * K + mm] = SU.eff_lt(Ku, c, mm) - (c == lu ? 1.f : 0.f);
                 } else {
                     const int c = e - 2 * N - m.ld_up;
-                    stg_qd[c] = SD.eff(Kd, c) - (c == ld ? 1.f : 0.f);
+                    SD.Q[(size_t)c * K + mm] = SD.eff_lt(Kd, c, mm) - (c == ld ? 1.f : 0.f);
                 }
+            }
+            if (warp == (blockDim.x >> 5) - 2) {
+                // draws for the next window, which starts at ctl.t
+                const long long tn = ctl.t;
+                unsigned long long u53;
+                int bi;
+                proposal_bits(p.seed, w, tn + lane, m.n_bonds, u53, bi);
+                ctl.cache_u53[lane] = u53;
+                ctl.cache_bond[lane] = bonds[bi];
+                __syncwarp();
+                if (lane == 0) ctl.cache_t = tn;
             }
             if (warp == (blockDim.x >> 5) - 1) {
                 // Z_mu change: the up spin moves Kd -> Ku, the down spin Ku -> Kd
@@ -1084,51 +1171,52 @@ __global__ void __launch_bounds__(512) sweep_delayed_kernel(DevModel m, DevBatch
                     if (k != Ku) dz += kup[k] != 0 ? 1 : -1;
                 }
                 dz = __reduce_add_sync(0xffffffffu, dz);
-                if (lane == 0) {
+                __syncwarp();
+                if (lane == 0) {   // nobody else reads kappa in this phase
                     ctl.zmu += dz;
                     ctl.since += 1;
-                    make_thr(ctl.thr, ctl.zmu, m.n_bonds, p.accept_rule);
+                    make_thr(ctl.thr, m.thr_table, ctl.zmu, p.accept_rule);
+                    kup[Ku] = (short)(lu + 1); kup[Kd] = 0;
+                    kdn[Kd] = (short)(ld + 1); kdn[Ku] = 0;
                 }
-            }
-            __syncthreads();
-            const int mm = ctl.m;
-            for (int e = tid; e < 2 * N + m.ld_up + m.ld_dn; e += blockDim.x) {
-                if (e < N) SU.P[(size_t)e * K + mm] = stg_pu[e];
-                else if (e < 2 * N) SD.P[(size_t)(e - N) * K + mm] = stg_pd[e - N];
-                else if (e < 2 * N + m.ld_up) SU.Q[(size_t)(e - 2 * N) * K + mm] = stg_qu[e - 2 * N];
-                else SD.Q[(size_t)(e - 2 * N - m.ld_up) * K + mm] = stg_qd[e - 2 * N - m.ld_up];
-            }
-            if (tid == 0) {
-                kup[Ku] = (short)(lu + 1); kup[Kd] = 0;
-                kdn[Kd] = (short)(ld + 1); kdn[Ku] = 0;
-                ctl.m = mm + 1;
             }
             acc_count += 1;
             __syncthreads();
+            // every thread has read ctl.m for this move before the barrier above
             if (mm + 1 == K) {
-                delayed_flush<K>(SU, N);
-                delayed_flush<K>(SD, N);
+                delayed_flush<K>(SU, N, kup, &ctl.dev);
+                delayed_flush<K>(SD, N, kdn, &ctl.dev);
                 __syncthreads();
                 delayed_zero<K>(SU, N);
                 delayed_zero<K>(SD, N);
-                if (tid == 0) ctl.m = 0;
+                if (tid == 0) {
+                    ctl.m = 0;
+                    // adaptive refresh: rounding past the tolerance ends this walker's
+                    // run here, so the FP64 refresh rebuilds W now
+                    if (__int_as_float(ctl.dev) > p.drift_tol) ctl.since = R;
+                    ctl.dev = 0;
+                }
                 __syncthreads();
+            } else if (tid == 0) {
+                ctl.m = mm + 1;  // read again only after the bottom barrier
             }
         }
         const long long t = ctl.t;
         if (t == ctl.next_meas) {
             const double e = delayed_local_energy<K>(m, bonds, kup, kdn, SU, SD, ctl.red);
-            se += e;
-            se2 += e * e;
-            n_meas += 1;
-            if (tid == 0) ctl.next_meas += M;
+            if (tid == 0) {  // only thread 0 keeps the FP64 sums
+                se += e;
+                se2 += e * e;
+                n_meas += 1;
+                ctl.next_meas += M;
+            }
         }
         __syncthreads();
     }
     __syncthreads();
     if (ctl.m > 0) {
-        delayed_flush<K>(SU, N);
-        delayed_flush<K>(SD, N);
+        delayed_flush<K>(SU, N, kup, &ctl.dev);
+        delayed_flush<K>(SD, N, kdn, &ctl.dev);
         __syncthreads();
     }
     {
@@ -1150,7 +1238,7 @@ __global__ void __launch_bounds__(512) sweep_delayed_kernel(DevModel m, DevBatch
         b.sum_e[w] += se;
         b.sum_e2[w] += se2;
         b.n_meas[w] += n_meas;
-        if (t < tend) atomicAdd(active_count, 1);
+        if (t < tend && acc_count < acc_left) atomicAdd(active_count, 1);
     }
 }
 
@@ -1158,7 +1246,6 @@ size_t delayed_smem_bytes(const DevModel &m, int K) {
     const size_t N = m.n_sites;
     size_t s = N * (m.ld_up + m.ld_dn) * 4;                 // W
     s += 2 * N * K * 4 + (size_t)(m.ld_up + m.ld_dn) * K * 4;  // P, Q
-    s += (2 * N + m.ld_up + m.ld_dn) * 4;                     // staging
     s += (N + 1) * 4 + (size_t)m.n_bonds * 4 + (size_t)2 * m.n_bonds * 2 + 2 * N * 2 + 16;
     return (s + 15) / 16 * 16;
 }
@@ -1254,17 +1341,21 @@ __global__ void init_random_kernel(DevModel m, DevBatch b, unsigned long long se
     }
 }
 
-// t_end = t + proposals for every walker (the target of one kvmc_sweep call).
-__global__ void set_tend_kernel(DevBatch b, long long proposals) {
+// Targets of one call: kvmc_sweep sets t_end = t + proposals (no accepted
+// target); kvmc_advance sets acc_end = accepted + moves (no proposal limit).
+__global__ void set_tend_kernel(DevBatch b, long long proposals, long long moves) {
     const int w = blockIdx.x * blockDim.x + threadIdx.x;
-    if (w < b.n_walkers) b.t_end[w] = b.t[w] + proposals;
+    if (w < b.n_walkers) {
+        b.t_end[w] = proposals > 0 ? b.t[w] + proposals : 0x3fffffffffffffffll;
+        b.acc_end[w] = moves > 0 ? b.accepted[w] + moves : 0x3fffffffffffffffll;
+    }
 }
 
 // ---------------------------------------------------------------------------
 // Launchers
 // ---------------------------------------------------------------------------
-cudaError_t launch_set_tend(const DevBatch &b, long long proposals, cudaStream_t stream) {
-    set_tend_kernel<<<(b.n_walkers + 255) / 256, 256, 0, stream>>>(b, proposals);
+cudaError_t launch_set_tend(const DevBatch &b, long long proposals, long long moves, cudaStream_t stream) {
+    set_tend_kernel<<<(b.n_walkers + 255) / 256, 256, 0, stream>>>(b, proposals, moves);
     return cudaGetLastError();
 }
 

@@ -95,6 +95,7 @@ _SIGS = {
     "kvmc_last_error": [_P, C.c_char_p, C.c_size_t],
     "kvmc_init": [_P, _P, _P, _P],
     "kvmc_sweep": [_P, C.c_int64, C.POINTER(SweepStats)],
+    "kvmc_advance": [_P, C.c_int64, C.POINTER(SweepStats)],
     "kvmc_measure": [_P, _P],
     "kvmc_eval_ratios": [_P, C.c_int32, _P, _P],
     "kvmc_apply_moves": [_P, _P],
@@ -104,6 +105,8 @@ _SIGS = {
     "kvmc_get_w": [_P, _P, _P],
     "kvmc_walker_stats": [_P, _P, _P, _P, _P, _P, _P],
     "kvmc_reset_stats": [_P],
+    "kvmc_walker_drift": [_P, _P],
+    "kvmc_set_drift_tolerance": [_P, C.c_double],
     "kvmc_enable_timing": [_P, C.c_int32],
     "kvmc_kernel_time": [_P, C.c_int32, C.POINTER(C.c_double), C.POINTER(C.c_int64)],
     "kvmc_region_timer": [_P, C.c_int32, C.POINTER(C.c_double)],

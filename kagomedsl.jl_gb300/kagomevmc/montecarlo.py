@@ -102,6 +102,12 @@ class Engine:
         self._check(self._lib.kvmc_sweep(self.h, int(proposals_per_walker), C.byref(st)))
         return {k: getattr(st, k) for k, _ in st._fields_}
 
+    def advance(self, moves_per_walker: int) -> dict:
+        """Every walker makes `moves_per_walker` more accepted moves."""
+        st = _lib.SweepStats()
+        self._check(self._lib.kvmc_advance(self.h, int(moves_per_walker), C.byref(st)))
+        return {k: getattr(st, k) for k, _ in st._fields_}
+
     def measure(self) -> np.ndarray:
         out = np.empty(self.n_walkers)
         self._check(self._lib.kvmc_measure(self.h, _lib.ptr(out)))
@@ -131,6 +137,14 @@ class Engine:
         self._check(self._lib.kvmc_walker_stats(self.h, _lib.ptr(se), _lib.ptr(se2), _lib.ptr(nm), _lib.ptr(acc),
                                                 _lib.ptr(prop), _lib.ptr(status)))
         return dict(sum_e=se, sum_e2=se2, n_meas=nm, accepted=acc, proposals=prop, status=status)
+
+    def walker_drift(self) -> np.ndarray:
+        d = np.empty(self.n_walkers, dtype=np.float32)
+        self._check(self._lib.kvmc_walker_drift(self.h, _lib.ptr(d)))
+        return d
+
+    def set_drift_tolerance(self, tol: float):
+        self._check(self._lib.kvmc_set_drift_tolerance(self.h, float(tol)))
 
     def reset_stats(self):
         self._check(self._lib.kvmc_reset_stats(self.h))

@@ -323,3 +323,83 @@ def test_n216_mixed_chain_matches_c_oracle(kv, delay_k):
             assert abs(ch.c.sum_e - ws["sum_e"][w]) <= 1e-4 * max(1.0, abs(ch.c.sum_e))
     assert match >= walkers - 1
     eng.close()
+
+
+@pytest.mark.parametrize("precision", ["plain", "mixed"])
+def test_advance_makes_exactly_the_asked_moves(kv, precision):
+    """kvmc_advance: every walker makes exactly A more accepted moves; the chain is the oracle's."""
+    N, walkers, seed, A = 54, 10, 17, 60
+    ham = ham_for(kv, N)
+    eng = kv.Engine(ham, walkers, precision=precision, seed=seed, refresh_interval=(32 if precision == "mixed" else 0))
+    eng.init()
+    ku0, kd0, _ = eng.get_state()
+    st = eng.advance(A)
+    ku1, kd1, ct = eng.get_state()
+    ws = eng.walker_stats()
+    assert np.all(ws["accepted"] == A) and st["accepted"] == walkers * A
+    assert np.all(ws["proposals"] == ct)
+    m = oracle_c.OracleModel(ham.U_up, ham.U_down, ham.nn)
+    match = 0
+    for w in range(walkers):
+        ch = m.new_chain(ku0[w], kd0[w])
+        ch.run(seed, w, int(ct[w]), 27, 27)
+        if np.array_equal(ch.ku, ku1[w]) and np.array_equal(ch.kd, kd1[w]):
+            match += 1
+            assert ch.c.accepted == A
+    assert match >= walkers - (0 if precision == "plain" else 1)
+    eng.close()
+
+
+@pytest.mark.parametrize("precision", ["plain", "mixed"])
+def test_unequal_spin_counts(kv, precision):
+    """N_up != N_down (src/MonteCarlo.jl:165-185 takes both): two W widths."""
+    N, n_up, seed, walkers, proposals = 54, 30, 23, 8, 1500
+    lat = kv.DoubleKagome(1.0, 6, 3, (True, True), (False, True))
+    H = kv.Hmat(lat)
+    Uu, Ud = kv.orbitals(H, n_up, N - n_up)
+    ham = kv.Hamiltonian(n_up, N - n_up, Uu, Ud, H, kv.get_nn(H))
+    eng = kv.Engine(ham, walkers, precision=precision, seed=seed)
+    eng.init()
+    ku0, kd0, _ = eng.get_state()
+    assert np.all((ku0 != 0).sum(1) == n_up) and np.all((kd0 != 0).sum(1) == N - n_up)
+    eng.sweep(proposals)
+    ku1, kd1, _ = eng.get_state()
+    ws = eng.walker_stats()
+    m = oracle_c.OracleModel(Uu, Ud, ham.nn)
+    match = 0
+    for w in range(walkers):
+        ch = m.new_chain(ku0[w], kd0[w])
+        ch.run(seed, w, proposals, 24, 24)
+        if np.array_equal(ch.ku, ku1[w]) and np.array_equal(ch.kd, kd1[w]):
+            match += 1
+            assert ch.c.accepted == ws["accepted"][w]
+            tol = 1e-8 if precision == "plain" else 1e-4
+            assert abs(ch.c.sum_e - ws["sum_e"][w]) <= tol * max(1.0, abs(ch.c.sum_e))
+    assert match >= walkers - (0 if precision == "plain" else 1)
+    Wu, Wd = eng.get_w()
+    assert Wu.shape[2] == n_up and Wd.shape[2] == N - n_up
+    eng.close()
+
+
+def test_custom_link_tables(kv):
+    """Zero-flux links (all amplitudes +1, as scripts/zero_flux.jl builds) through the whole path."""
+    lin = {k: 1.0 for k in kv.PI_LINK_IN}
+    lint = {k: 1.0 for k in kv.PI_LINK_INTER}
+    lat = kv.DoubleKagome(1.0, 6, 3, (True, True), (False, True))
+    Lo = o.double_kagome(1.0, 6, 3, (True, True), (False, True))
+    H = kv.Hmat(lat, lin, lint)
+    assert np.array_equal(H, o.hmat(Lo, lin, lint))
+    Uu, Ud = kv.orbitals(H, 27, 27)
+    ham = kv.Hamiltonian(27, 27, Uu, Ud, H, kv.get_nn(H))
+    seed, walkers, proposals = 29, 6, 1200
+    eng = kv.Engine(ham, walkers, precision="plain", seed=seed)
+    eng.init()
+    ku0, kd0, _ = eng.get_state()
+    eng.sweep(proposals)
+    ku1, kd1, _ = eng.get_state()
+    m = oracle_c.OracleModel(Uu, Ud, ham.nn)
+    for w in range(walkers):
+        ch = m.new_chain(ku0[w], kd0[w])
+        ch.run(seed, w, proposals, 27, 27)
+        assert np.array_equal(ch.ku, ku1[w]) and np.array_equal(ch.kd, kd1[w])
+    eng.close()
