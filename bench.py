@@ -326,10 +326,17 @@ def gpu_arm(a):
     dom = max(kern, key=lambda k: kern[k]["ms"])
     peak_key = "fp64_tflops" if dom == "refresh_fp64" else "fp32_tflops"
     peak = peaks.get(peak_key)
+    # DRAM bytes per launch from the ncu captures summarised in profiles/,
+    # scaled from the captured launch to this run's launches by the units
+    # each processes (walkers per sweep launch, walker-spins per refresh)
     traffic = None
     tfile = os.path.join(ROOT, "profiles", "traffic.json")
     if os.path.exists(tfile):
-        traffic = json.load(open(tfile)).get(dom)
+        tj = json.load(open(tfile))
+        if dom == "sweep_mixed" and kern[dom]["launches"]:
+            traffic = tj["sweep_mixed"]["bytes_per_walker_launch"] * a.walkers * a.steps / kern[dom]["launches"]
+        elif dom == "refresh_fp64" and kern[dom]["launches"]:
+            traffic = tj["refresh_fp64"]["bytes_per_walker_spin"] * 2 * refreshes / kern[dom]["launches"]
     ach = kern[dom]["achieved_tflops"]
     roof = {"bound": "fp64" if dom == "refresh_fp64" else "fp32", "kernel": dom,
             "achieved": ach, "peak": peak, "unit": "TFLOP/s",
