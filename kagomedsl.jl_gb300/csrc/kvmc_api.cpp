@@ -412,8 +412,8 @@ extern "C" int kvmc_create(const kvmc_model_desc *model, const kvmc_batch_desc *
         return fail_global(KVMC_ERR_ARGUMENT, "unknown accept rule %d", batch->accept_rule);
     if (batch->refresh_interval < 0 || batch->measure_interval < 0)
         return fail_global(KVMC_ERR_ARGUMENT, "intervals must be >= 0");
-    if (std::max(nu, nd) > 160)
-        return fail_global(KVMC_ERR_UNSUPPORTED, "more than 160 orbitals per spin is not supported by this build");
+    if (std::max(nu, nd) > 2048)
+        return fail_global(KVMC_ERR_UNSUPPORTED, "more than 2048 orbitals per spin is not supported by this build");
 
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
@@ -519,6 +519,13 @@ extern "C" int kvmc_create(const kvmc_model_desc *model, const kvmc_batch_desc *
         return bail(rc);
     b.solve_block = kvmc::refresh_scratch_block(m);
     if ((rc = h->alloc(&b.solve_scratch, b.solve_block * 2 * (size_t)Wk))) return bail(rc);
+    b.lu_block = 0;
+    b.lu_scratch = nullptr;
+    if (kvmc::refresh_needs_large(m)) {
+        const size_t nmax = (size_t)std::max(nu, nd);
+        b.lu_block = nmax * nmax;
+        if ((rc = h->alloc(&b.lu_scratch, b.lu_block * 2 * (size_t)Wk))) return bail(rc);
+    }
     if (h->mixed) cudaMemset(b.W32, 0, wblock * Wk * sizeof(float));
     else cudaMemset(b.W64, 0, wblock * Wk * sizeof(double));
     cudaMemset(b.kappa_up, 0, (size_t)Wk * N * 2);
@@ -533,8 +540,9 @@ extern "C" int kvmc_create(const kvmc_model_desc *model, const kvmc_batch_desc *
     if (int e = kvmc_reset_stats(h)) return bail(e);
     // shared-memory capacity decides whether the FP32 W can be staged on chip
     const int optin = kvmc::max_smem_optin(h->device);
-    if ((size_t)optin < kvmc::refresh_smem(m))
-        return bail(h->fail(KVMC_ERR_UNSUPPORTED, "refresh needs %zu B shared memory, device offers %d", kvmc::refresh_smem(m), optin));
+    const size_t rsm = kvmc::refresh_needs_large(m) ? kvmc::refresh_large_smem(m) : kvmc::refresh_smem(m);
+    if ((size_t)optin < rsm + 1024)
+        return bail(h->fail(KVMC_ERR_UNSUPPORTED, "refresh needs %zu B shared memory, device offers %d", rsm, optin));
     h->smem_w = h->mixed && kvmc::mixed_sweep_smem(m) <= (size_t)optin;
     // delayed-update depth: 0 = the largest depth whose working set fits on chip
     const size_t budget = (size_t)optin - 1024;  // leave room for the kernel's static shared memory

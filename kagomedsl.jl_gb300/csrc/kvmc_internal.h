@@ -54,6 +54,8 @@ struct DevBatch {
     unsigned long long *refresh_count;  // walker refreshes performed (one counter)
     double *solve_scratch; // FP64 rows being solved by the refresh: [W][2][solve_block]
     size_t solve_block;    // doubles per (walker, spin)
+    double *lu_scratch;    // more than 160 orbitals: tilde_U factorised in HBM, [W][2][lu_block]
+    size_t lu_block;       // doubles per (walker, spin), 0 when unused
 };
 
 enum : int {
@@ -96,6 +98,8 @@ size_t mixed_sweep_smem(const DevModel &m);
 size_t delayed_smem_bytes(const DevModel &m, int K);
 size_t refresh_smem(const DevModel &m);
 size_t refresh_scratch_block(const DevModel &m);
+size_t refresh_large_smem(const DevModel &m);
+bool refresh_needs_large(const DevModel &m);
 int max_smem_optin(int device);
 
 }  // namespace kvmc

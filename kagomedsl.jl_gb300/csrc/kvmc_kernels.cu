@@ -414,6 +414,241 @@ refresh_kernel(DevModel m, DevBatch b, int only_due, int track_drift) {
     }
 }
 
+// ---------------------------------------------------------------------------
+// Refresh for more than kSmemLuMaxN orbitals per spin: tilde_U no longer fits
+// in shared memory, so it is factorised in place in an FP64 scratch block in
+// HBM with a blocked right-looking LU (panel width kPanel, partial pivoting):
+//   1. the n - pb by kPanel panel is factorised in shared memory,
+//   2. its row swaps are applied to the columns outside the panel,
+//   3. U12 = L11^{-1} A12 (unit lower triangular solve, one thread per column),
+//   4. A22 -= L21 U12 (FP64 GEMM, 4 x 4 register tiles per thread).
+// The factors then feed the same row solver as the shared-memory path.
+// ---------------------------------------------------------------------------
+constexpr int kPanel = 32;
+constexpr int kSmemLuMaxN = 160;
+
+template <typename OutT>
+__global__ void __launch_bounds__(kRefreshThreads)
+refresh_large_kernel(DevModel m, DevBatch b, int only_due, int track_drift) {
+    const int w = blockIdx.x;
+    const int spin = blockIdx.y;
+    if (only_due && b.since[w] >= 0) return;
+    if (spin == 0 && threadIdx.x == 0) atomicAdd(b.refresh_count, 1ull);
+    const int N = m.n_sites;
+    const int n = spin == 0 ? m.n_up : m.n_dn;
+    const int ldw = spin == 0 ? m.ld_up : m.ld_dn;
+    const double *U = spin == 0 ? m.U_up : m.U_dn;
+    const short *kappa = (spin == 0 ? b.kappa_up : b.kappa_dn) + (size_t)w * N;
+    const size_t wblock = (size_t)N * (m.ld_up + m.ld_dn);
+    OutT *W = (sizeof(OutT) == 8 ? (OutT *)b.W64 : (OutT *)b.W32) + (size_t)w * wblock +
+              (spin == 0 ? 0 : (size_t)N * m.ld_up);
+    double *A = b.lu_scratch + ((size_t)w * 2 + spin) * b.lu_block;  // n x n, row-major, lda = n
+    double *Y = b.solve_scratch + ((size_t)w * 2 + spin) * b.solve_block;
+
+    extern __shared__ __align__(16) unsigned char smem[];
+    constexpr int ldp = kPanel + 1;
+    double *Pn = reinterpret_cast<double *>(smem);          // panel [n][ldp]
+    double *Ut = Pn + (size_t)n * ldp;                       // U12 tile [kPanel][64]
+    double *invd = Ut + kPanel * 64;
+    double *red = invd + n;
+    int *perm = reinterpret_cast<int *>(red + 33);
+    int *ipiv = perm + n;
+    short *rows = reinterpret_cast<short *>(ipiv + n);
+    __shared__ int s_piv;
+    __shared__ double s_pmax, s_dinv;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nt = blockDim.x;
+
+    // gather tilde_U into A (zeroed first)
+    for (size_t e = tid; e < (size_t)n * n; e += nt) A[e] = 0.0;
+    __syncthreads();
+    for (int R = warp; R < N; R += nt / 32) {
+        const int l = kappa[R];
+        if (l >= 1 && l <= n) {
+            const double *src = U + (size_t)R * n;
+            double *dst = A + (size_t)(l - 1) * n;
+            for (int c = lane; c < n; c += 32) dst[c] = src[c];
+        }
+    }
+    for (int i = tid; i < n; i += nt) perm[i] = i;
+    __syncthreads();
+
+    bool singular = false;
+    for (int pb = 0; pb < n && !singular; pb += kPanel) {
+        const int nb = min(kPanel, n - pb);
+        const int rp = n - pb;
+        // 1. panel into shared memory
+        for (int e = tid; e < rp * nb; e += nt) {
+            const int r = e / nb, c = e - r * nb;
+            Pn[(size_t)r * ldp + c] = A[(size_t)(pb + r) * n + pb + c];
+        }
+        __syncthreads();
+        for (int k = 0; k < nb; ++k) {
+            if (warp == 0) {
+                double best = -1.0;
+                int bi = rp;
+                for (int i = k + lane; i < rp; i += 32) {
+                    const double v = fabs(Pn[(size_t)i * ldp + k]);
+                    if (v > best) { best = v; bi = i; }
+                }
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) {
+                    const double ob = __shfl_xor_sync(0xffffffffu, best, o);
+                    const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+                    if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
+                }
+                if (lane == 0) {
+                    s_piv = bi;
+                    s_pmax = best;
+                    s_dinv = best > 0.0 ? 1.0 / Pn[(size_t)bi * ldp + k] : 0.0;
+                    ipiv[pb + k] = pb + bi;
+                }
+            }
+            __syncthreads();
+            if (!(s_pmax > 0.0)) { singular = true; break; }
+            const int p = s_piv;
+            if (p != k)
+                for (int j = tid; j < nb; j += nt) {
+                    const double a = Pn[(size_t)k * ldp + j];
+                    Pn[(size_t)k * ldp + j] = Pn[(size_t)p * ldp + j];
+                    Pn[(size_t)p * ldp + j] = a;
+                }
+            __syncthreads();
+            const double dinv = s_dinv;
+            for (int i = k + 1 + tid; i < rp; i += nt) Pn[(size_t)i * ldp + k] *= dinv;
+            __syncthreads();
+            for (int e = tid; e < (rp - k - 1) * (nb - k - 1); e += nt) {
+                const int i = k + 1 + e / (nb - k - 1), j = k + 1 + e % (nb - k - 1);
+                Pn[(size_t)i * ldp + j] = fma(-Pn[(size_t)i * ldp + k], Pn[(size_t)k * ldp + j], Pn[(size_t)i * ldp + j]);
+            }
+            __syncthreads();
+        }
+        if (singular) break;
+        // panel back to A
+        for (int e = tid; e < rp * nb; e += nt) {
+            const int r = e / nb, c = e - r * nb;
+            A[(size_t)(pb + r) * n + pb + c] = Pn[(size_t)r * ldp + c];
+        }
+        // 2. the panel's row swaps on the other columns, in order
+        for (int k = 0; k < nb; ++k) {
+            const int r1 = pb + k, r2 = ipiv[pb + k];
+            if (r1 != r2) {
+                for (int c = tid; c < n; c += nt) {
+                    if (c >= pb && c < pb + nb) continue;
+                    const double a = A[(size_t)r1 * n + c];
+                    A[(size_t)r1 * n + c] = A[(size_t)r2 * n + c];
+                    A[(size_t)r2 * n + c] = a;
+                }
+                if (tid == 0) { const int t = perm[r1]; perm[r1] = perm[r2]; perm[r2] = t; }
+            }
+            __syncthreads();
+        }
+        const int c0 = pb + nb;
+        if (c0 < n) {
+            // 3. U12 = L11^{-1} A12, one column per thread
+            for (int c = c0 + tid; c < n; c += nt) {
+                double x[kPanel];
+#pragma unroll
+                for (int i = 0; i < kPanel; ++i) x[i] = i < nb ? A[(size_t)(pb + i) * n + c] : 0.0;
+#pragma unroll
+                for (int i = 1; i < kPanel; ++i) {
+                    if (i < nb) {
+                        double acc = x[i];
+#pragma unroll
+                        for (int k = 0; k < i; ++k) acc = fma(-Pn[(size_t)i * ldp + k], x[k], acc);
+                        x[i] = acc;
+                    }
+                }
+#pragma unroll
+                for (int i = 0; i < kPanel; ++i)
+                    if (i < nb) A[(size_t)(pb + i) * n + c] = x[i];
+            }
+            __syncthreads();
+            // 4. A22 -= L21 U12: 64-column tiles of U12 staged in shared memory,
+            //    each thread a 4 x 4 tile (rows r0 + 4*ty + {0..3}, cols 4*tx + {0..3})
+            const int tx = tid & 15, ty = tid >> 4;
+            for (int cb = c0; cb < n; cb += 64) {
+                const int ncol = min(64, n - cb);
+                for (int e = tid; e < nb * 64; e += nt) {
+                    const int k = e >> 6, c = e & 63;
+                    Ut[e] = c < ncol ? A[(size_t)(pb + k) * n + cb + c] : 0.0;
+                }
+                __syncthreads();
+                for (int rb = c0; rb < n; rb += 64) {
+                    double acc[4][4];
+#pragma unroll
+                    for (int a = 0; a < 4; ++a)
+#pragma unroll
+                        for (int q = 0; q < 4; ++q) acc[a][q] = 0.0;
+                    for (int k = 0; k < nb; ++k) {
+                        double lv[4], uv[4];
+#pragma unroll
+                        for (int a = 0; a < 4; ++a) {
+                            const int r = rb + 4 * ty + a;
+                            lv[a] = r < n ? Pn[(size_t)(r - pb) * ldp + k] : 0.0;
+                        }
+#pragma unroll
+                        for (int q = 0; q < 4; ++q) uv[q] = Ut[k * 64 + 4 * tx + q];
+#pragma unroll
+                        for (int a = 0; a < 4; ++a)
+#pragma unroll
+                            for (int q = 0; q < 4; ++q) acc[a][q] = fma(lv[a], uv[q], acc[a][q]);
+                    }
+#pragma unroll
+                    for (int a = 0; a < 4; ++a) {
+                        const int r = rb + 4 * ty + a;
+                        if (r >= n) continue;
+#pragma unroll
+                        for (int q = 0; q < 4; ++q) {
+                            const int c = cb + 4 * tx + q;
+                            if (c < n) A[(size_t)r * n + c] -= acc[a][q];
+                        }
+                    }
+                }
+                __syncthreads();
+            }
+        }
+        __syncthreads();
+    }
+    if (singular) {
+        if (threadIdx.x == 0) {
+            atomicOr(&b.status[w], kStatusSingular);
+            b.logdet[4 * w + spin] = -INFINITY;
+            b.logdet[4 * w + 2 + spin] = -INFINITY;
+        }
+        return;
+    }
+    double ld = 0.0, dmin = INFINITY, dmaxp = 0.0;
+    for (int i = tid; i < n; i += nt) {
+        const double d = A[(size_t)i * n + i];
+        invd[i] = 1.0 / d;
+        ld += log(fabs(d));
+        dmin = fmin(dmin, fabs(d));
+        dmaxp = fmax(dmaxp, fabs(d));
+    }
+    ld = block_sum(ld, red);
+    dmin = -block_sum_max(-dmin, red);
+    dmaxp = block_sum_max(dmaxp, red);
+    if (tid == 0) {
+        b.logdet[4 * w + spin] = ld;
+        b.logdet[4 * w + 2 + spin] = log(dmin / dmaxp);
+    }
+    const int nrows = collect_empty_rows(kappa, N, rows);
+    write_unit_rows(kappa, N, n, W, ldw, track_drift != 0, &b.drift[w]);
+    for (int r0 = 0; r0 < nrows; r0 += blockDim.x) {
+        const int cnt = min((int)blockDim.x, nrows - r0);
+        solve_rows_blocked<OutT>(A, n, invd, perm, U, n, rows + r0, cnt, Y + (size_t)r0 * n, W, ldw, &b.drift[w],
+                                 track_drift != 0);
+    }
+}
+
+size_t refresh_large_smem(const DevModel &m) {
+    const int n = m.n_up > m.n_dn ? m.n_up : m.n_dn;
+    return (size_t)n * (kPanel + 1) * 8 + kPanel * 64 * 8 + (size_t)n * 8 + 33 * 8 + (size_t)n * 8 +
+           (size_t)m.n_sites * 2 + 16;
+}
+
+bool refresh_needs_large(const DevModel &m) { return (m.n_up > m.n_dn ? m.n_up : m.n_dn) > kSmemLuMaxN; }
+
 size_t refresh_smem(const DevModel &m) {
     const int n = m.n_up > m.n_dn ? m.n_up : m.n_dn;
     return (size_t)n * (n + 1) * 8 + (size_t)n * 8 + 33 * 8 + (size_t)n * 4 + (size_t)m.n_sites * 2 + 16;
@@ -1367,8 +1602,21 @@ int max_smem_optin(int device) {
 
 cudaError_t launch_refresh(const DevModel &m, const DevBatch &b, bool fp32_out, int only_due,
                            int track_drift, cudaStream_t stream) {
-    const size_t sm = refresh_smem(m);
     const dim3 grid(b.n_walkers, 2);
+    if (refresh_needs_large(m)) {
+        const size_t sm = refresh_large_smem(m);
+        if (fp32_out) {
+            cudaError_t e = cudaFuncSetAttribute(refresh_large_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+            if (e != cudaSuccess) return e;
+            refresh_large_kernel<float><<<grid, kRefreshThreads, sm, stream>>>(m, b, only_due, track_drift);
+        } else {
+            cudaError_t e = cudaFuncSetAttribute(refresh_large_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+            if (e != cudaSuccess) return e;
+            refresh_large_kernel<double><<<grid, kRefreshThreads, sm, stream>>>(m, b, only_due, track_drift);
+        }
+        return cudaGetLastError();
+    }
+    const size_t sm = refresh_smem(m);
     if (fp32_out) {
         cudaError_t e = cudaFuncSetAttribute(refresh_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
         if (e != cudaSuccess) return e;

@@ -20,7 +20,7 @@ import oracle_c
 pytestmark = pytest.mark.gpu
 
 GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
-CELLS = {24: (2, 2), 54: (3, 3), 96: (4, 4), 216: (6, 6)}
+CELLS = {24: (2, 2), 54: (3, 3), 96: (4, 4), 216: (6, 6), 384: (8, 8), 864: (12, 12)}
 
 
 @pytest.fixture(scope="module")
@@ -57,12 +57,15 @@ def close(a, b, rel):
 
 
 @pytest.mark.parametrize("precision", ["plain", "mixed"])
-@pytest.mark.parametrize("N", [24, 54, 96, 216])
+@pytest.mark.parametrize("N", [24, 54, 96, 216, 384, 864])
 def test_refresh_matches_oracle(kv, N, precision):
+    """N <= 320 factorises tilde_U in shared memory; N = 384 and 864 (192 and
+    432 orbitals per spin) take the blocked LU in HBM."""
     ham = ham_for(kv, N)
     U = ham.U_up
-    starts = [o.seeded_start(13, w, U, U)[:2] for w in range(4)]
-    eng = kv.Engine(ham, 4, precision=precision, seed=13)
+    nw = 4 if N <= 384 else 2
+    starts = [o.seeded_start(13, w, U, U)[:2] for w in range(nw)]
+    eng = kv.Engine(ham, nw, precision=precision, seed=13)
     eng.init(np.stack([s[0] for s in starts]), np.stack([s[1] for s in starts]))
     Wu, Wd = eng.get_w()
     tol = 1e-10 if precision == "plain" else 1e-6
@@ -402,4 +405,30 @@ def test_custom_link_tables(kv):
         ch = m.new_chain(ku0[w], kd0[w])
         ch.run(seed, w, proposals, 27, 27)
         assert np.array_equal(ch.ku, ku1[w]) and np.array_equal(ch.kd, kd1[w])
+    eng.close()
+
+
+@pytest.mark.parametrize("precision", ["plain", "mixed"])
+def test_large_lattice_chain(kv, precision):
+    """N=384 (8x8 doubled cells): blocked-LU refresh and W streamed from HBM."""
+    N, walkers, proposals, seed = 384, 4, 800, 41
+    ham = ham_for(kv, N)
+    eng = kv.Engine(ham, walkers, precision=precision, seed=seed, refresh_interval=(64 if precision == "mixed" else 0))
+    assert not eng.config()["w_on_chip"]
+    eng.init()
+    ku0, kd0, _ = eng.get_state()
+    eng.sweep(proposals)
+    ku1, kd1, _ = eng.get_state()
+    ws = eng.walker_stats()
+    m = oracle_c.OracleModel(ham.U_up, ham.U_down, ham.nn)
+    match = 0
+    for w in range(walkers):
+        ch = m.new_chain(ku0[w], kd0[w])
+        ch.run(seed, w, proposals, 192, 192)
+        if np.array_equal(ch.ku, ku1[w]) and np.array_equal(ch.kd, kd1[w]):
+            match += 1
+            assert ch.c.accepted == ws["accepted"][w]
+            tol = 1e-8 if precision == "plain" else 1e-4
+            assert abs(ch.c.sum_e - ws["sum_e"][w]) <= tol * max(1.0, abs(ch.c.sum_e))
+    assert match >= walkers - (0 if precision == "plain" else 1)
     eng.close()
