@@ -33,7 +33,7 @@ extern "C" {
 #define KVMC_API
 #endif
 
-#define KVMC_ABI_VERSION 1
+#define KVMC_ABI_VERSION 2
 
 enum kvmc_status {
     KVMC_OK = 0,
@@ -101,8 +101,15 @@ typedef struct {
     int32_t n_up, n_down;  /* n_up + n_down == n_sites (one spinon per site) */
     int32_t n_bonds;
     const int32_t *bonds;  /* [n_bonds][2], 0-based, as kvmc_bonds_from_hopping */
-    const double *U_up;    /* column-major n_sites x n_up (real orbitals) */
+    const double *U_up;    /* column-major n_sites x n_up (real parts of the orbitals) */
     const double *U_down;  /* column-major n_sites x n_down */
+    /* Imaginary parts, same layout; both NULL for real orbitals (B = 0).  A
+     * non-NULL pointer makes the handle complex, as the reference's
+     * ComplexF64 W for B != 0 (src/Hamiltonian.jl:201-204, :325-327); a
+     * complex handle supports at most 112 orbitals per spin and rank-1
+     * updates (delay_k 0 or 1). */
+    const double *U_up_imag;
+    const double *U_down_imag;
 } kvmc_model_desc;
 
 typedef struct {
@@ -174,7 +181,8 @@ KVMC_API int kvmc_measure(kvmc_handle *h, double *local_energy);
 /* Determinant ratios W_up[K_up, l_up] * W_down[K_down, l_down] for given
  * moves, read from the device W (src/MonteCarlo.jl:576-580).
  * moves: [n_walkers][n_moves][4] = {K_up, l_up, K_down, l_down}, sites
- * 0-based, labels 1-based; ratios: [n_walkers][n_moves]. */
+ * 0-based, labels 1-based; ratios: [n_walkers][n_moves], or
+ * [n_walkers][n_moves][2] as (re, im) for a complex handle. */
 KVMC_API int kvmc_eval_ratios(kvmc_handle *h, int32_t n_moves, const int32_t *moves,
                      double *ratios);
 
@@ -199,7 +207,8 @@ KVMC_API int kvmc_get_state(kvmc_handle *h, int32_t *kappa_up, int32_t *kappa_do
 KVMC_API int kvmc_set_state(kvmc_handle *h, const int32_t *kappa_up, const int32_t *kappa_down,
                    const int64_t *counters);
 
-/* Copies W to the host as FP64, row-major [n_walkers][n_sites][n]. */
+/* Copies W to the host as FP64, row-major [n_walkers][n_sites][n]; a
+ * complex handle writes [n_walkers][n_sites][n][2] as (re, im). */
 KVMC_API int kvmc_get_w(kvmc_handle *h, double *W_up, double *W_down);
 
 /* Per-walker accumulators since creation or the last kvmc_reset_stats:

@@ -45,6 +45,7 @@ struct kvmc_handle {
     kvmc_batch_desc batch{};
     int n_sites = 0, n_up = 0, n_dn = 0, ld_up = 0, ld_dn = 0, n_bonds = 0, n_walkers = 0;
     bool mixed = false;
+    bool cplx = false;  // complex orbitals and W (B != 0)
     bool smem_w = false;
     int refresh_every = 0;
     int measure_every = 0;
@@ -150,9 +151,20 @@ int upload_kappa(kvmc_handle *h, const int32_t *ku, const int32_t *kd) {
     return h->cuda(cudaStreamSynchronize(h->stream), "upload kappa");
 }
 
+// The real and the complex kernels behind one call each
+cudaError_t refresh_launch(kvmc_handle *h, int only_due, int track_drift) {
+    if (h->cplx) return kvmc::launch_refresh_c(h->dm, h->db, h->mixed, only_due, track_drift, h->stream);
+    return kvmc::launch_refresh(h->dm, h->db, h->mixed, only_due, track_drift, h->stream);
+}
+
+cudaError_t sweep_launch(kvmc_handle *h, const kvmc::SweepParams &p) {
+    if (h->cplx) return kvmc::launch_sweep_c(h->dm, h->db, p, h->mixed, h->d_active, h->stream);
+    return kvmc::launch_sweep(h->dm, h->db, p, h->mixed, h->smem_w, h->d_active, h->stream);
+}
+
 int full_refresh(kvmc_handle *h, bool track_drift) {
     KV_TRY(h->cuda(cudaMemsetAsync(h->db.drift, 0, sizeof(float) * h->n_walkers, h->stream), "memset"));
-    KV_TRY(h->cuda(kvmc::launch_refresh(h->dm, h->db, h->mixed, 0, track_drift ? 1 : 0, h->stream), "refresh launch"));
+    KV_TRY(h->cuda(refresh_launch(h, 0, track_drift ? 1 : 0), "refresh launch"));
     KV_TRY(h->cuda(cudaMemsetAsync(h->db.since, 0, sizeof(int) * h->n_walkers, h->stream), "memset"));
     return h->cuda(cudaStreamSynchronize(h->stream), "refresh");
 }
@@ -414,6 +426,9 @@ extern "C" int kvmc_create(const kvmc_model_desc *model, const kvmc_batch_desc *
         return fail_global(KVMC_ERR_ARGUMENT, "intervals must be >= 0");
     if (std::max(nu, nd) > 2048)
         return fail_global(KVMC_ERR_UNSUPPORTED, "more than 2048 orbitals per spin is not supported by this build");
+    if ((model->U_up_imag || model->U_down_imag) && std::max(nu, nd) > kvmc::complex_max_orbitals())
+        return fail_global(KVMC_ERR_UNSUPPORTED, "complex orbitals: at most %d per spin (got %d)",
+                           kvmc::complex_max_orbitals(), std::max(nu, nd));
 
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
@@ -434,6 +449,7 @@ extern "C" int kvmc_create(const kvmc_model_desc *model, const kvmc_batch_desc *
     h->ld_up = (nu + 3) / 4 * 4;
     h->ld_dn = (nd + 3) / 4 * 4;
     h->mixed = batch->precision == KVMC_MIXED_FP32;
+    h->cplx = model->U_up_imag != nullptr || model->U_down_imag != nullptr;
     const int nocc = std::min(nu, nd);
     h->measure_every = batch->measure_interval > 0 ? batch->measure_interval : nocc;
     if (h->mixed) h->refresh_every = batch->refresh_interval > 0 ? batch->refresh_interval : 128;
@@ -445,11 +461,20 @@ extern "C" int kvmc_create(const kvmc_model_desc *model, const kvmc_batch_desc *
 
     DevModel &m = h->dm;
     m.n_sites = N; m.n_up = nu; m.n_dn = nd; m.ld_up = h->ld_up; m.ld_dn = h->ld_dn; m.n_bonds = nb;
-    // orbitals row-major
-    std::vector<double> Uu((size_t)N * nu), Ud((size_t)N * nd);
+    // orbitals row-major; complex ones as interleaved (re, im)
+    const size_t cw = h->cplx ? 2 : 1;
+    std::vector<double> Uu((size_t)N * nu * cw), Ud((size_t)N * nd * cw);
     for (int r = 0; r < N; ++r) {
-        for (int c = 0; c < nu; ++c) Uu[(size_t)r * nu + c] = model->U_up[(size_t)r + (size_t)c * N];
-        for (int c = 0; c < nd; ++c) Ud[(size_t)r * nd + c] = model->U_down[(size_t)r + (size_t)c * N];
+        for (int c = 0; c < nu; ++c) {
+            const size_t src = (size_t)r + (size_t)c * N, dst = ((size_t)r * nu + c) * cw;
+            Uu[dst] = model->U_up[src];
+            if (h->cplx) Uu[dst + 1] = model->U_up_imag ? model->U_up_imag[src] : 0.0;
+        }
+        for (int c = 0; c < nd; ++c) {
+            const size_t src = (size_t)r + (size_t)c * N, dst = ((size_t)r * nd + c) * cw;
+            Ud[dst] = model->U_down[src];
+            if (h->cplx) Ud[dst + 1] = model->U_down_imag ? model->U_down_imag[src] : 0.0;
+        }
     }
     // bonds and adjacency
     std::vector<short2> bonds(nb);
@@ -502,7 +527,7 @@ extern "C" int kvmc_create(const kvmc_model_desc *model, const kvmc_batch_desc *
     DevBatch &b = h->db;
     const int Wk = h->n_walkers;
     b.n_walkers = Wk;
-    const size_t wblock = (size_t)N * (h->ld_up + h->ld_dn);
+    const size_t wblock = (size_t)N * (h->ld_up + h->ld_dn) * cw;  // W64/W32 elements per walker
     b.W64 = nullptr;
     b.W32 = nullptr;
     if (h->mixed) rc = h->alloc(&b.W32, wblock * Wk);
@@ -517,11 +542,11 @@ extern "C" int kvmc_create(const kvmc_model_desc *model, const kvmc_batch_desc *
         (rc = h->alloc(&b.energy_out, Wk)) || (rc = h->alloc(&b.refresh_count, 1)) || (rc = h->alloc(&h->d_active, 1)) ||
         (rc = h->alloc(&h->d_attempt, Wk)) || (rc = h->alloc(&h->d_redo, Wk)))
         return bail(rc);
-    b.solve_block = kvmc::refresh_scratch_block(m);
+    b.solve_block = kvmc::refresh_scratch_block(m) * cw;
     if ((rc = h->alloc(&b.solve_scratch, b.solve_block * 2 * (size_t)Wk))) return bail(rc);
     b.lu_block = 0;
     b.lu_scratch = nullptr;
-    if (kvmc::refresh_needs_large(m)) {
+    if (!h->cplx && kvmc::refresh_needs_large(m)) {
         const size_t nmax = (size_t)std::max(nu, nd);
         b.lu_block = nmax * nmax;
         if ((rc = h->alloc(&b.lu_scratch, b.lu_block * 2 * (size_t)Wk))) return bail(rc);
@@ -540,10 +565,14 @@ extern "C" int kvmc_create(const kvmc_model_desc *model, const kvmc_batch_desc *
     if (int e = kvmc_reset_stats(h)) return bail(e);
     // shared-memory capacity decides whether the FP32 W can be staged on chip
     const int optin = kvmc::max_smem_optin(h->device);
-    const size_t rsm = kvmc::refresh_needs_large(m) ? kvmc::refresh_large_smem(m) : kvmc::refresh_smem(m);
+    const size_t rsm = h->cplx ? kvmc::complex_refresh_smem(m)
+                               : kvmc::refresh_needs_large(m) ? kvmc::refresh_large_smem(m) : kvmc::refresh_smem(m);
     if ((size_t)optin < rsm + 1024)
         return bail(h->fail(KVMC_ERR_UNSUPPORTED, "refresh needs %zu B shared memory, device offers %d", rsm, optin));
-    h->smem_w = h->mixed && kvmc::mixed_sweep_smem(m) <= (size_t)optin;
+    h->smem_w = h->mixed && !h->cplx && kvmc::mixed_sweep_smem(m) <= (size_t)optin;
+    if (h->cplx && batch->delay_k != 0 && batch->delay_k != 1)
+        return bail(h->fail(KVMC_ERR_UNSUPPORTED, "complex orbitals use rank-1 updates: delay_k must be 0 or 1 (got %d)",
+                            batch->delay_k));
     // delayed-update depth: 0 = the largest depth whose working set fits on chip
     const size_t budget = (size_t)optin - 1024;  // leave room for the kernel's static shared memory
     if (h->mixed && h->smem_w) {
@@ -610,7 +639,7 @@ extern "C" int kvmc_init(kvmc_handle *h, const int32_t *kappa_up, const int32_t 
         std::vector<int> mark(Wk);
         for (int w = 0; w < Wk; ++w) mark[w] = redo[w] ? -1 : 0;
         KV_TRY(h->cuda(cudaMemcpyAsync(h->db.since, mark.data(), Wk * 4, cudaMemcpyHostToDevice, h->stream), "upload"));
-        KV_TRY(h->cuda(kvmc::launch_refresh(h->dm, h->db, h->mixed, 1, 0, h->stream), "refresh launch"));
+        KV_TRY(h->cuda(refresh_launch(h, 1, 0), "refresh launch"));
         KV_TRY(h->cuda(cudaStreamSynchronize(h->stream), "refresh"));
         KV_TRY(h->cuda(cudaMemcpy(ld.data(), h->db.logdet, ld.size() * 8, cudaMemcpyDeviceToHost), "logdet"));
         int left = 0;
@@ -766,10 +795,8 @@ int run_sweep(kvmc_handle *h, int64_t proposals_per_walker, int64_t moves_per_wa
     for (int iter = 0;; iter += group) {
         for (int g = 0; g < group; ++g) {
             KV_TRY(h->cuda(cudaMemsetAsync(h->d_active, 0, sizeof(int), h->stream), "memset"));
-            KV_TRY(timed(h, 0, [&] { return kvmc::launch_sweep(h->dm, h->db, p, h->mixed, h->smem_w, h->d_active, h->stream); },
-                         "sweep launch"));
-            KV_TRY(timed(h, 1, [&] { return kvmc::launch_refresh(h->dm, h->db, h->mixed, 1, h->mixed ? 1 : 0, h->stream); },
-                         "refresh launch"));
+            KV_TRY(timed(h, 0, [&] { return sweep_launch(h, p); }, "sweep launch"));
+            KV_TRY(timed(h, 1, [&] { return refresh_launch(h, 1, h->mixed ? 1 : 0); }, "refresh launch"));
             launches += 2;
         }
         int active = 0;
@@ -808,7 +835,8 @@ int run_sweep(kvmc_handle *h, int64_t proposals_per_walker, int64_t moves_per_wa
 extern "C" int kvmc_measure(kvmc_handle *h, double *local_energy) {
     if (!h || !local_energy) return fail_global(KVMC_ERR_ARGUMENT, "null argument");
     KV_TRY(set_device(h));
-    KV_TRY(h->cuda(kvmc::launch_measure(h->dm, h->db, h->mixed, h->stream), "measure launch"));
+    KV_TRY(h->cuda(h->cplx ? kvmc::launch_measure_c(h->dm, h->db, h->mixed, h->stream)
+                           : kvmc::launch_measure(h->dm, h->db, h->mixed, h->stream), "measure launch"));
     KV_TRY(h->cuda(cudaMemcpyAsync(local_energy, h->db.energy_out, sizeof(double) * h->n_walkers,
                                    cudaMemcpyDeviceToHost, h->stream), "measure"));
     return h->cuda(cudaStreamSynchronize(h->stream), "measure");
@@ -825,12 +853,15 @@ extern "C" int kvmc_eval_ratios(kvmc_handle *h, int32_t n_moves, const int32_t *
             return h->fail(KVMC_ERR_BOUNDS, "move %zu out of range", k);
     }
     void *scr = nullptr;
-    KV_TRY(h->scratch(cnt * 4 * sizeof(int) + cnt * sizeof(double) + 256, &scr));
+    const size_t per = h->cplx ? 2 : 1;  // doubles per ratio
+    KV_TRY(h->scratch(cnt * 4 * sizeof(int) + cnt * per * sizeof(double) + 256, &scr));
     int *d_moves = static_cast<int *>(scr);
     double *d_out = reinterpret_cast<double *>(static_cast<char *>(scr) + ((cnt * 16 + 255) / 256) * 256);
     KV_TRY(h->cuda(cudaMemcpyAsync(d_moves, moves, cnt * 16, cudaMemcpyHostToDevice, h->stream), "upload"));
-    KV_TRY(h->cuda(kvmc::launch_eval_ratios(h->dm, h->db, h->mixed, n_moves, d_moves, d_out, h->stream), "ratio launch"));
-    KV_TRY(h->cuda(cudaMemcpyAsync(ratios, d_out, cnt * 8, cudaMemcpyDeviceToHost, h->stream), "ratios"));
+    KV_TRY(h->cuda(h->cplx ? kvmc::launch_eval_ratios_c(h->dm, h->db, h->mixed, n_moves, d_moves, d_out, h->stream)
+                           : kvmc::launch_eval_ratios(h->dm, h->db, h->mixed, n_moves, d_moves, d_out, h->stream),
+                   "ratio launch"));
+    KV_TRY(h->cuda(cudaMemcpyAsync(ratios, d_out, cnt * per * 8, cudaMemcpyDeviceToHost, h->stream), "ratios"));
     return h->cuda(cudaStreamSynchronize(h->stream), "ratios");
 }
 
@@ -848,7 +879,9 @@ extern "C" int kvmc_apply_moves(kvmc_handle *h, const int32_t *moves) {
     void *scr = nullptr;
     KV_TRY(h->scratch((size_t)h->n_walkers * 5 * sizeof(int), &scr));
     KV_TRY(h->cuda(cudaMemcpyAsync(scr, moves, (size_t)h->n_walkers * 5 * sizeof(int), cudaMemcpyHostToDevice, h->stream), "upload"));
-    KV_TRY(h->cuda(kvmc::launch_apply_moves(h->dm, h->db, h->mixed, static_cast<int *>(scr), h->stream), "move launch"));
+    KV_TRY(h->cuda(h->cplx ? kvmc::launch_apply_moves_c(h->dm, h->db, h->mixed, static_cast<int *>(scr), h->stream)
+                           : kvmc::launch_apply_moves(h->dm, h->db, h->mixed, static_cast<int *>(scr), h->stream),
+                   "move launch"));
     return h->cuda(cudaStreamSynchronize(h->stream), "apply moves");
 }
 
@@ -892,7 +925,8 @@ extern "C" int kvmc_get_w(kvmc_handle *h, double *W_up, double *W_down) {
     if (!h) return fail_global(KVMC_ERR_ARGUMENT, "null handle");
     KV_TRY(set_device(h));
     const int N = h->n_sites;
-    const size_t wblock = (size_t)N * (h->ld_up + h->ld_dn);
+    const size_t cw = h->cplx ? 2 : 1;  // doubles per entry
+    const size_t wblock = (size_t)N * (h->ld_up + h->ld_dn) * cw;
     const size_t tot = wblock * h->n_walkers;
     std::vector<double> buf(tot);
     if (h->mixed) {
@@ -906,11 +940,12 @@ extern "C" int kvmc_get_w(kvmc_handle *h, double *W_up, double *W_down) {
         const double *base = buf.data() + (size_t)w * wblock;
         for (int r = 0; r < N; ++r) {
             if (W_up)
-                for (int c = 0; c < h->n_up; ++c)
-                    W_up[((size_t)w * N + r) * h->n_up + c] = base[(size_t)r * h->ld_up + c];
+                for (size_t c = 0; c < h->n_up * cw; ++c)
+                    W_up[((size_t)w * N + r) * h->n_up * cw + c] = base[(size_t)r * h->ld_up * cw + c];
             if (W_down)
-                for (int c = 0; c < h->n_dn; ++c)
-                    W_down[((size_t)w * N + r) * h->n_dn + c] = base[(size_t)N * h->ld_up + (size_t)r * h->ld_dn + c];
+                for (size_t c = 0; c < h->n_dn * cw; ++c)
+                    W_down[((size_t)w * N + r) * h->n_dn * cw + c] =
+                        base[((size_t)N * h->ld_up + (size_t)r * h->ld_dn) * cw + c];
         }
     }
     return KVMC_OK;

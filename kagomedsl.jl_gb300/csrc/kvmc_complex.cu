@@ -1,0 +1,583 @@
+// Complex-orbital kernels of libkvmc (sm_103a): the path for a hopping matrix
+// with Peierls phases (B != 0, src/Hamiltonian.jl:201-204, :325-327), where U,
+// tilde_U and W are complex as in the reference (ComplexF64 throughout,
+// src/Hamiltonian.jl:423-425, src/MonteCarlo.jl:181-182).
+//
+//   refresh_c_kernel   reevaluateW! / tilde_U   src/MonteCarlo.jl:55-115 (FP64 complex)
+//   sweep_c_kernel     Carlo.sweep! + update_W! src/MonteCarlo.jl:460-607, :279-292
+//                      (plain form: complex FP64 W; mixed form: complex FP32 W)
+//   measure_c_kernel   getOL                    src/Hamiltonian.jl:762-778 (real part)
+//   ratio_c_kernel, apply_moves_c_kernel: the API / test entry points
+//
+// The acceptance probability is |ratio|^2 = |W_up[K,l]|^2 |W_down[K',l']|^2
+// (src/MonteCarlo.jl:581); the local energy is the real part of its sum.
+#include <algorithm>
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "kvmc_device.cuh"
+#include "kvmc_internal.h"
+
+namespace kvmc {
+
+// ---- complex scalars -------------------------------------------------------
+struct __align__(16) cd { double x, y; };
+struct __align__(8) cf { float x, y; };
+
+template <typename C> struct Real;
+template <> struct Real<cd> { using T = double; };
+template <> struct Real<cf> { using T = float; };
+
+template <typename C> __device__ __forceinline__ C cmul(C a, C b) {
+    return C{a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x};
+}
+// c - a * b
+template <typename C> __device__ __forceinline__ C cfms(C a, C b, C c) {
+    return C{fma(-a.x, b.x, fma(a.y, b.y, c.x)), fma(-a.x, b.y, fma(-a.y, b.x, c.y))};
+}
+// c + a * b
+template <typename C> __device__ __forceinline__ C cfma(C a, C b, C c) {
+    return C{fma(a.x, b.x, fma(-a.y, b.y, c.x)), fma(a.x, b.y, fma(a.y, b.x, c.y))};
+}
+template <typename C> __device__ __forceinline__ C cinv(C a) {
+    const auto d = a.x * a.x + a.y * a.y;
+    return C{a.x / d, -a.y / d};
+}
+template <typename C> __device__ __forceinline__ typename Real<C>::T cabs2(C a) { return a.x * a.x + a.y * a.y; }
+// LAPACK's pivot magnitude for complex matrices, |re| + |im|
+__device__ __forceinline__ double cabs1(cd a) { return fabs(a.x) + fabs(a.y); }
+
+template <typename O> __device__ __forceinline__ O to_out(cd v);
+template <> __device__ __forceinline__ cd to_out<cd>(cd v) { return v; }
+template <> __device__ __forceinline__ cf to_out<cf>(cd v) { return cf{(float)v.x, (float)v.y}; }
+
+// ---------------------------------------------------------------------------
+// Refresh: W = U * tilde_U^{-1}, complex FP64.  One CTA per (walker, spin);
+// tilde_U is LU-factorised with partial pivoting in shared memory (n <= 112
+// orbitals per spin fit), the rows at sites not holding this spin are solved
+// one thread per row from a column-major FP64 scratch block.
+// ---------------------------------------------------------------------------
+constexpr int kThreadsC = 256;
+constexpr int kMaxComplexOrbitals = 112;
+
+template <typename OutC>
+__global__ void __launch_bounds__(kThreadsC)
+refresh_c_kernel(DevModel m, DevBatch b, int only_due, int track_drift) {
+    const int w = blockIdx.x, spin = blockIdx.y;
+    if (only_due && b.since[w] >= 0) return;
+    if (spin == 0 && threadIdx.x == 0) atomicAdd(b.refresh_count, 1ull);
+    const int N = m.n_sites;
+    const int n = spin == 0 ? m.n_up : m.n_dn;
+    const int ldw = spin == 0 ? m.ld_up : m.ld_dn;
+    const cd *U = reinterpret_cast<const cd *>(spin == 0 ? m.U_up : m.U_dn);
+    const short *kappa = (spin == 0 ? b.kappa_up : b.kappa_dn) + (size_t)w * N;
+    const size_t wblock = (size_t)N * (m.ld_up + m.ld_dn);
+    OutC *W = (sizeof(OutC) == 16 ? reinterpret_cast<OutC *>(b.W64) : reinterpret_cast<OutC *>(b.W32)) +
+              (size_t)w * wblock + (spin == 0 ? 0 : (size_t)N * m.ld_up);
+    cd *Y = reinterpret_cast<cd *>(b.solve_scratch) + ((size_t)w * 2 + spin) * (b.solve_block / 2);
+
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int lda = n + 1;
+    cd *A = reinterpret_cast<cd *>(smem);
+    cd *invd = A + (size_t)n * lda;
+    double *red = reinterpret_cast<double *>(invd + n);
+    int *perm = reinterpret_cast<int *>(red + 33);
+    short *rows = reinterpret_cast<short *>(perm + n);
+    __shared__ int s_piv, s_nrows;
+    __shared__ double s_pmax;
+    __shared__ cd s_dinv;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nt = blockDim.x;
+
+    for (int e = tid; e < n * lda; e += nt) A[e] = cd{0.0, 0.0};
+    __syncthreads();
+    for (int R = warp; R < N; R += nt / 32) {
+        const int l = kappa[R];
+        if (l >= 1 && l <= n)
+            for (int c = lane; c < n; c += 32) A[(size_t)(l - 1) * lda + c] = U[(size_t)R * n + c];
+    }
+    for (int i = tid; i < n; i += nt) perm[i] = i;
+    __syncthreads();
+
+    for (int k = 0; k < n; ++k) {
+        if (warp == 0) {
+            double best = -1.0;
+            int bi = n;
+            for (int i = k + lane; i < n; i += 32) {
+                const double v = cabs1(A[(size_t)i * lda + k]);
+                if (v > best) { best = v; bi = i; }
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                const double ob = __shfl_xor_sync(0xffffffffu, best, o);
+                const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+                if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
+            }
+            if (lane == 0) {
+                s_piv = bi;
+                s_pmax = best;
+                s_dinv = best > 0.0 ? cinv(A[(size_t)bi * lda + k]) : cd{0.0, 0.0};
+            }
+        }
+        __syncthreads();
+        if (!(s_pmax > 0.0)) {
+            if (tid == 0) {
+                atomicOr(&b.status[w], kStatusSingular);
+                b.logdet[4 * w + spin] = -INFINITY;
+                b.logdet[4 * w + 2 + spin] = -INFINITY;
+            }
+            return;
+        }
+        const int p = s_piv;
+        if (p != k) {
+            for (int j = tid; j < n; j += nt) {
+                const cd a = A[(size_t)k * lda + j];
+                A[(size_t)k * lda + j] = A[(size_t)p * lda + j];
+                A[(size_t)p * lda + j] = a;
+            }
+            if (tid == 0) { const int t = perm[k]; perm[k] = perm[p]; perm[p] = t; }
+        }
+        __syncthreads();
+        const cd dinv = s_dinv;
+        for (int i = k + 1 + tid; i < n; i += nt) A[(size_t)i * lda + k] = cmul(A[(size_t)i * lda + k], dinv);
+        __syncthreads();
+        for (int i = k + 1 + warp; i < n; i += nt / 32) {
+            const cd aik = A[(size_t)i * lda + k];
+            for (int j = k + 1 + lane; j < n; j += 32)
+                A[(size_t)i * lda + j] = cfms(aik, A[(size_t)k * lda + j], A[(size_t)i * lda + j]);
+        }
+        __syncthreads();
+    }
+    double ld = 0.0, dmin = INFINITY, dmaxp = 0.0;
+    for (int i = tid; i < n; i += nt) {
+        const cd d = A[(size_t)i * lda + i];
+        invd[i] = cinv(d);
+        const double mag = hypot(d.x, d.y);
+        ld += log(mag);
+        dmin = fmin(dmin, mag);
+        dmaxp = fmax(dmaxp, mag);
+    }
+    ld = block_sum(ld, red);
+    dmin = -block_sum_max(-dmin, red);
+    dmaxp = block_sum_max(dmaxp, red);
+    if (tid == 0) {
+        b.logdet[4 * w + spin] = ld;
+        b.logdet[4 * w + 2 + spin] = log(dmin / dmaxp);
+        s_nrows = 0;
+    }
+    // sites not holding this spin, in site order
+    if (warp == 0) {
+        int base = 0;
+        for (int R0 = 0; R0 < N; R0 += 32) {
+            const int R = R0 + lane;
+            const bool un = R < N && kappa[R] == 0;
+            const unsigned bal = __ballot_sync(0xffffffffu, un);
+            if (un) rows[base + __popc(bal & ((1u << lane) - 1u))] = (short)R;
+            base += __popc(bal);
+        }
+        if (lane == 0) s_nrows = base;
+    }
+    // unit rows at occupied sites, zero padding
+    float dmax = 0.f;
+    for (int R = warp; R < N; R += nt / 32) {
+        const int l = kappa[R];
+        OutC *wr = W + (size_t)R * ldw;
+        if (l != 0) {
+            for (int c = lane; c < ldw; c += 32) {
+                const cd nv = cd{c == l - 1 ? 1.0 : 0.0, 0.0};
+                if (track_drift) {
+                    const OutC o = wr[c];
+                    dmax = fmaxf(dmax, (float)(hypot((double)o.x - nv.x, (double)o.y) / (1.0 + hypot(nv.x, nv.y))));
+                }
+                wr[c] = to_out<OutC>(nv);
+            }
+        } else {
+            for (int c = n + lane; c < ldw; c += 32) wr[c] = to_out<OutC>(cd{0.0, 0.0});
+        }
+    }
+    __syncthreads();
+    const int nrows = s_nrows;
+    // w * tilde_U = u: forward with Uf, backward with unit L, then w[perm[i]] = v[i]
+    for (int r = tid; r < nrows; r += nt) {
+        const int R = rows[r];
+        cd *y = Y + r;  // column-major: y[j * nrows]
+        for (int j = 0; j < n; ++j) y[(size_t)j * nrows] = U[(size_t)R * n + j];
+        for (int i = 0; i < n; ++i) {
+            const cd yi = cmul(y[(size_t)i * nrows], invd[i]);
+            y[(size_t)i * nrows] = yi;
+            const cd *Ai = A + (size_t)i * lda;
+            for (int j = i + 1; j < n; ++j) y[(size_t)j * nrows] = cfms(yi, Ai[j], y[(size_t)j * nrows]);
+        }
+        for (int j = n - 1; j > 0; --j) {
+            const cd vj = y[(size_t)j * nrows];
+            const cd *Aj = A + (size_t)j * lda;
+            for (int i = 0; i < j; ++i) y[(size_t)i * nrows] = cfms(vj, Aj[i], y[(size_t)i * nrows]);
+        }
+        OutC *wr = W + (size_t)R * ldw;
+        for (int i = 0; i < n; ++i) {
+            const cd nv = y[(size_t)i * nrows];
+            if (track_drift) {
+                const OutC o = wr[perm[i]];
+                dmax = fmaxf(dmax, (float)(hypot((double)o.x - nv.x, (double)o.y - nv.y) / (1.0 + hypot(nv.x, nv.y))));
+            }
+            wr[perm[i]] = to_out<OutC>(nv);
+        }
+    }
+    if (track_drift) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) dmax = fmaxf(dmax, __shfl_xor_sync(0xffffffffu, dmax, o));
+        if (lane == 0 && dmax > 0.f) atomic_max_nonneg(&b.drift[w], dmax);
+    }
+}
+
+size_t refresh_c_smem(const DevModel &m) {
+    const int n = m.n_up > m.n_dn ? m.n_up : m.n_dn;
+    return (size_t)n * (n + 1) * 16 + (size_t)n * 16 + 33 * 8 + (size_t)n * 4 + (size_t)m.n_sites * 2 + 32;
+}
+
+// ---------------------------------------------------------------------------
+// Sweep with complex W (one walker per CTA, W in global memory).  The same
+// proposal window as the real kernels; the acceptance uses
+// a = |W_up[K,l]|^2 |W_down[K',l']|^2.
+// ---------------------------------------------------------------------------
+template <typename C>
+struct CPtr {
+    C *up, *dn;
+    int ld_up, ld_dn;
+    __device__ __forceinline__ C &U(int r, int c) const { return up[(size_t)r * ld_up + c]; }
+    __device__ __forceinline__ C &D(int r, int c) const { return dn[(size_t)r * ld_dn + c]; }
+};
+
+__device__ __forceinline__ bool decide_a(double a, unsigned long long u53, int c, const Thr &T, int rule, bool &bad) {
+    if (!isfinite(a)) { bad = true; return false; }
+    const double r = r_of(u53);
+    if (rule == 0) return a >= 1.0 ? (c < 0) : (r < T.d * a);
+    return a >= 1.0 || r < a;
+}
+
+__device__ __forceinline__ bool decide_c(cd pu, cd pd, unsigned long long u53, int c, const Thr &T, int rule, bool &bad) {
+    const double ratio_abs2 = cabs2(cmul(pu, pd));
+    return decide_a(ratio_abs2, u53, c, T, rule, bad);
+}
+
+// FP32 complex: the FP32 test with the 1e-5 guard band, FP64 inside it
+__device__ __forceinline__ bool decide_c(cf pu, cf pd, unsigned long long u53, int c, const Thr &T, int rule, bool &bad) {
+    const cf rt = cmul(pu, pd);
+    const float a = cabs2(rt);
+    if (isnan(a)) { bad = true; return false; }
+    constexpr float band = 1e-5f;
+    if (a >= 1.f + band) return rule == 0 ? (c < 0) : true;
+    if (a <= 1.f - band) {
+        const float x = rule == 0 ? T.f * a : a;
+        const float rf = r_f32(u53);
+        if (rf < x * (1.f - band)) return true;
+        if (rf > x * (1.f + band)) return false;
+    }
+    const cd r64 = cmul(cd{(double)pu.x, (double)pu.y}, cd{(double)pd.x, (double)pd.y});
+    return decide_a(cabs2(r64), u53, c, T, rule, bad);
+}
+
+template <typename C>
+__device__ double local_energy_c(const DevModel &m, const short *kup, const short *kdn, const CPtr<C> &W, double *red) {
+    using R = typename Real<C>::T;
+    R acc = 0;
+    for (int e = threadIdx.x; e < m.n_bonds; e += blockDim.x) {
+        const short2 bd = m.bonds[e];
+        const int i = bd.x, j = bd.y;
+        const int ui = kup[i], uj = kup[j], di = kdn[i], dj = kdn[j];
+        acc += ((ui != 0) == (uj != 0)) ? (R)0.25 : (R)-0.25;
+        if (uj != 0 && di != 0) acc -= (R)0.5 * cmul(W.U(i, uj - 1), W.D(j, di - 1)).x;
+        if (ui != 0 && dj != 0) acc -= (R)0.5 * cmul(W.U(j, ui - 1), W.D(i, dj - 1)).x;
+    }
+    if constexpr (sizeof(R) == 4) return block_sum_f32(acc, red);
+    else return block_sum(acc, red);
+}
+
+template <typename C>
+__device__ void rank1_update_c(const CPtr<C> &W, int N, int Ku, int lu, int Kd, int ld, C *cu, C *ru, C *cdn, C *rd) {
+    const int tid = threadIdx.x, nt = blockDim.x;
+    const C au = cinv(W.U(Ku, lu));
+    const C ad = cinv(W.D(Kd, ld));
+    for (int r = tid; r < N; r += nt) {
+        const C a = cmul(W.U(r, lu), au), d = cmul(W.D(r, ld), ad);
+        cu[r] = C{-a.x, -a.y};
+        cdn[r] = C{-d.x, -d.y};
+    }
+    for (int c = tid; c < W.ld_up; c += nt) { C v = W.U(Ku, c); if (c == lu) v.x -= 1; ru[c] = v; }
+    for (int c = tid; c < W.ld_dn; c += nt) { C v = W.D(Kd, c); if (c == ld) v.x -= 1; rd[c] = v; }
+    __syncthreads();
+    const int tot_up = N * W.ld_up, tot = tot_up + N * W.ld_dn;
+    for (int e = tid; e < tot; e += nt) {
+        const bool is_up = e < tot_up;
+        const int ee = is_up ? e : e - tot_up;
+        const int q = is_up ? W.ld_up : W.ld_dn;
+        const int r = ee / q, c = ee - r * q;
+        C *wp = (is_up ? W.up : W.dn) + (size_t)r * q + c;
+        *wp = cfma(is_up ? cu[r] : cdn[r], is_up ? ru[c] : rd[c], *wp);
+    }
+    __syncthreads();
+}
+
+struct SweepCtlC {
+    long long t, next_meas, next_ref;
+    int since, zmu, state;
+    int Ku, lu, Kd, ld;
+    Thr thr;
+    double red[33];
+};
+
+template <typename C>
+__global__ void __launch_bounds__(256) sweep_c_kernel(DevModel m, DevBatch b, SweepParams p, int refresh_by_proposals,
+                                                      int *active_count) {
+    const int w = blockIdx.x, N = m.n_sites;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const long long t0 = b.t[w], tend = b.t_end[w];
+    const long long acc_left = b.acc_end[w] - b.accepted[w];
+    if (t0 >= tend || acc_left <= 0) {
+        if (threadIdx.x == 0 && b.since[w] < 0) b.since[w] = 0;
+        return;
+    }
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ SweepCtlC ctl;
+    const size_t wblock = (size_t)N * (m.ld_up + m.ld_dn);
+    C *gW = (sizeof(C) == 16 ? reinterpret_cast<C *>(b.W64) : reinterpret_cast<C *>(b.W32)) + (size_t)w * wblock;
+    CPtr<C> W{gW, gW + (size_t)N * m.ld_up, m.ld_up, m.ld_dn};
+    C *cu = reinterpret_cast<C *>(smem);
+    C *cdn = cu + N;
+    C *ru = cdn + N;
+    C *rd = ru + m.ld_up;
+    short *kup = reinterpret_cast<short *>(rd + m.ld_dn);
+    short *kdn = kup + N;
+    for (int s = tid; s < N; s += blockDim.x) {
+        kup[s] = b.kappa_up[(size_t)w * N + s];
+        kdn[s] = b.kappa_dn[(size_t)w * N + s];
+    }
+    __syncthreads();
+    double zc = 0.0;
+    for (int e = tid; e < m.n_bonds; e += blockDim.x) {
+        const short2 bd = m.bonds[e];
+        zc += ((kup[bd.x] != 0 && kdn[bd.y] != 0) || (kup[bd.y] != 0 && kdn[bd.x] != 0)) ? 1.0 : 0.0;
+    }
+    zc = block_sum(zc, ctl.red);
+    const int R = p.refresh_every, M = p.measure_every;
+    if (tid == 0) {
+        ctl.t = t0;
+        ctl.since = b.since[w] < 0 ? 0 : b.since[w];
+        ctl.zmu = (int)zc;
+        ctl.next_meas = (t0 / M + 1) * M;
+        ctl.next_ref = refresh_by_proposals ? (t0 / R + 1) * R : tend;
+        make_thr(ctl.thr, m.thr_table, ctl.zmu, p.accept_rule);
+    }
+    __syncthreads();
+    long long acc_count = 0, n_meas = 0;
+    double se = 0.0, se2 = 0.0;
+    while (true) {
+        if (warp == 0) {
+            long long t = ctl.t;
+            const int since = ctl.since;
+            const long long stop = min(tend, ctl.next_ref);
+            const long long next_meas = ctl.next_meas;
+            const Thr thr = ctl.thr;
+            int state = 2;
+            while (true) {
+                if (t >= stop || acc_count >= acc_left) break;
+                if (!refresh_by_proposals && since >= R) break;
+                const long long lim = min(stop, next_meas) - t;
+                const int win = lim < 32 ? (int)lim : 32;
+                bool acc = false, bad = false;
+                int Ku = 0, lu = 0, Kd = 0, ld = 0;
+                if (lane < win) {
+                    unsigned long long u53;
+                    int bi;
+                    proposal_bits(p.seed, w, t + lane, m.n_bonds, u53, bi);
+                    const int c = cmp_r_thr(u53, thr);
+                    if (p.accept_rule != 0 || c <= 0) {
+                        const short2 bd = m.bonds[bi];
+                        const int i = bd.x, j = bd.y;
+                        const int kui = kup[i], kuj = kup[j], kdi = kdn[i], kdj = kdn[j];
+                        const bool f1 = kui != 0 && kdj != 0;
+                        const bool f2 = kuj != 0 && kdi != 0;
+                        if (f1 || f2) {
+                            if (f1) { Ku = j; lu = kui - 1; Kd = i; ld = kdj - 1; }
+                            else    { Ku = i; lu = kuj - 1; Kd = j; ld = kdi - 1; }
+                            acc = decide_c(W.U(Ku, lu), W.D(Kd, ld), u53, c, thr, p.accept_rule, bad);
+                        }
+                    }
+                }
+                if (__any_sync(0xffffffffu, bad) && bad) atomicOr(&b.status[w], kStatusNonFinite);
+                const unsigned mask = __ballot_sync(0xffffffffu, acc);
+                if (mask) {
+                    const int f = __ffs(mask) - 1;
+                    if (lane == f) { ctl.Ku = Ku; ctl.lu = lu; ctl.Kd = Kd; ctl.ld = ld; }
+                    t += f + 1;
+                    state = 1;
+                    break;
+                }
+                t += win;
+                if (t == next_meas || t == ctl.next_ref) { state = 3; break; }
+            }
+            if (lane == 0) { ctl.t = t; ctl.state = state; }
+        }
+        __syncthreads();
+        const int state = ctl.state;
+        if (state == 2) break;
+        if (state == 1) {
+            const int Ku = ctl.Ku, lu = ctl.lu, Kd = ctl.Kd, ld = ctl.ld;
+            rank1_update_c<C>(W, N, Ku, lu, Kd, ld, cu, ru, cdn, rd);
+            if (tid == 0) {
+                // the up spin moves Kd -> Ku, the down spin Ku -> Kd
+                const int before = incident_antiparallel(m, kup, Ku, Kd);
+                kup[Ku] = (short)(lu + 1); kup[Kd] = 0;
+                kdn[Kd] = (short)(ld + 1); kdn[Ku] = 0;
+                const int after = incident_antiparallel(m, kup, Ku, Kd);
+                ctl.zmu += after - before;
+                ctl.since += 1;
+                make_thr(ctl.thr, m.thr_table, ctl.zmu, p.accept_rule);
+            }
+            acc_count += 1;
+            __syncthreads();
+        }
+        const long long t = ctl.t;
+        if (t == ctl.next_meas) {
+            const double e = local_energy_c<C>(m, kup, kdn, W, ctl.red);
+            if (tid == 0) {
+                se += e;
+                se2 += e * e;
+                n_meas += 1;
+                ctl.next_meas += M;
+            }
+        }
+        if (t == ctl.next_ref) break;
+        __syncthreads();
+    }
+    __syncthreads();
+    for (int s = tid; s < N; s += blockDim.x) {
+        b.kappa_up[(size_t)w * N + s] = kup[s];
+        b.kappa_dn[(size_t)w * N + s] = kdn[s];
+    }
+    if (tid == 0) {
+        const long long t = ctl.t;
+        b.t[w] = t;
+        bool due;
+        if (refresh_by_proposals) due = t == ctl.next_ref;
+        else due = ctl.since >= R;
+        b.since[w] = due ? -1 : ctl.since;
+        b.accepted[w] += acc_count;
+        b.proposals[w] += t - t0;
+        b.sum_e[w] += se;
+        b.sum_e2[w] += se2;
+        b.n_meas[w] += n_meas;
+        if (t < tend && acc_count < acc_left) atomicAdd(active_count, 1);
+    }
+}
+
+template <typename C>
+size_t sweep_c_smem(const DevModel &m) {
+    return (size_t)(2 * m.n_sites + m.ld_up + m.ld_dn) * sizeof(C) + (size_t)2 * m.n_sites * 2 + 16;
+}
+
+// ---- API / test entry points ------------------------------------------------
+template <typename C>
+__global__ void measure_c_kernel(DevModel m, DevBatch b) {
+    const int w = blockIdx.x, N = m.n_sites;
+    __shared__ double red[33];
+    const size_t wblock = (size_t)N * (m.ld_up + m.ld_dn);
+    C *gW = (sizeof(C) == 16 ? reinterpret_cast<C *>(b.W64) : reinterpret_cast<C *>(b.W32)) + (size_t)w * wblock;
+    CPtr<C> W{gW, gW + (size_t)N * m.ld_up, m.ld_up, m.ld_dn};
+    const double e = local_energy_c<C>(m, b.kappa_up + (size_t)w * N, b.kappa_dn + (size_t)w * N, W, red);
+    if (threadIdx.x == 0) b.energy_out[w] = e;
+}
+
+// complex ratios, interleaved (re, im) into out
+template <typename C>
+__global__ void ratio_c_kernel(DevModel m, DevBatch b, int n_moves, const int *moves, double *out) {
+    const int w = blockIdx.x, N = m.n_sites;
+    const size_t wblock = (size_t)N * (m.ld_up + m.ld_dn);
+    C *gW = (sizeof(C) == 16 ? reinterpret_cast<C *>(b.W64) : reinterpret_cast<C *>(b.W32)) + (size_t)w * wblock;
+    CPtr<C> W{gW, gW + (size_t)N * m.ld_up, m.ld_up, m.ld_dn};
+    for (int k = threadIdx.x; k < n_moves; k += blockDim.x) {
+        const int *mv = moves + ((size_t)w * n_moves + k) * 4;
+        const C a = W.U(mv[0], mv[1] - 1), d = W.D(mv[2], mv[3] - 1);
+        const cd r = cmul(cd{(double)a.x, (double)a.y}, cd{(double)d.x, (double)d.y});
+        out[2 * ((size_t)w * n_moves + k)] = r.x;
+        out[2 * ((size_t)w * n_moves + k) + 1] = r.y;
+    }
+}
+
+template <typename C>
+__global__ void apply_moves_c_kernel(DevModel m, DevBatch b, const int *moves) {
+    const int w = blockIdx.x, N = m.n_sites;
+    const int *mv = moves + (size_t)w * 5;
+    const int flag = mv[0];
+    if (flag == 0) return;
+    const int i = mv[1], site = mv[2], l_up = mv[3], l_dn = mv[4];
+    extern __shared__ __align__(16) unsigned char smem[];
+    C *stg = reinterpret_cast<C *>(smem);
+    const size_t wblock = (size_t)N * (m.ld_up + m.ld_dn);
+    C *gW = (sizeof(C) == 16 ? reinterpret_cast<C *>(b.W64) : reinterpret_cast<C *>(b.W32)) + (size_t)w * wblock;
+    CPtr<C> W{gW, gW + (size_t)N * m.ld_up, m.ld_up, m.ld_dn};
+    const int Ku = flag == 1 ? site : i;
+    const int Kd = flag == 1 ? i : site;
+    rank1_update_c<C>(W, N, Ku, l_up - 1, Kd, l_dn - 1, stg, stg + 2 * N, stg + N, stg + 2 * N + m.ld_up);
+    if (threadIdx.x == 0) {
+        short *ku = b.kappa_up + (size_t)w * N, *kd = b.kappa_dn + (size_t)w * N;
+        if (flag == 1) { ku[i] = 0; ku[site] = (short)l_up; kd[i] = (short)l_dn; kd[site] = 0; }
+        else { ku[i] = (short)l_up; ku[site] = 0; kd[i] = 0; kd[site] = (short)l_dn; }
+    }
+}
+
+// ---- launchers ----------------------------------------------------------------
+int complex_max_orbitals() { return kMaxComplexOrbitals; }
+
+size_t complex_refresh_smem(const DevModel &m) { return refresh_c_smem(m); }
+
+cudaError_t launch_refresh_c(const DevModel &m, const DevBatch &b, bool fp32_out, int only_due, int track_drift,
+                             cudaStream_t stream) {
+    const size_t sm = refresh_c_smem(m);
+    const dim3 grid(b.n_walkers, 2);
+    if (fp32_out) {
+        cudaError_t e = cudaFuncSetAttribute(refresh_c_kernel<cf>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        if (e != cudaSuccess) return e;
+        refresh_c_kernel<cf><<<grid, kThreadsC, sm, stream>>>(m, b, only_due, track_drift);
+    } else {
+        cudaError_t e = cudaFuncSetAttribute(refresh_c_kernel<cd>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        if (e != cudaSuccess) return e;
+        refresh_c_kernel<cd><<<grid, kThreadsC, sm, stream>>>(m, b, only_due, track_drift);
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_sweep_c(const DevModel &m, const DevBatch &b, const SweepParams &p, bool mixed, int *active,
+                           cudaStream_t stream) {
+    if (mixed) {
+        const size_t sm = sweep_c_smem<cf>(m);
+        sweep_c_kernel<cf><<<b.n_walkers, 256, sm, stream>>>(m, b, p, 0, active);
+    } else {
+        const size_t sm = sweep_c_smem<cd>(m);
+        sweep_c_kernel<cd><<<b.n_walkers, 256, sm, stream>>>(m, b, p, 1, active);
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_measure_c(const DevModel &m, const DevBatch &b, bool fp32, cudaStream_t stream) {
+    if (fp32) measure_c_kernel<cf><<<b.n_walkers, 256, 0, stream>>>(m, b);
+    else measure_c_kernel<cd><<<b.n_walkers, 256, 0, stream>>>(m, b);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_eval_ratios_c(const DevModel &m, const DevBatch &b, bool fp32, int n_moves, const int *moves,
+                                 double *out, cudaStream_t stream) {
+    if (fp32) ratio_c_kernel<cf><<<b.n_walkers, 128, 0, stream>>>(m, b, n_moves, moves, out);
+    else ratio_c_kernel<cd><<<b.n_walkers, 128, 0, stream>>>(m, b, n_moves, moves, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_apply_moves_c(const DevModel &m, const DevBatch &b, bool fp32, const int *moves,
+                                 cudaStream_t stream) {
+    const size_t elem = fp32 ? sizeof(cf) : sizeof(cd);
+    const size_t sm = (size_t)(2 * m.n_sites + m.ld_up + m.ld_dn) * elem + 16;
+    if (fp32) apply_moves_c_kernel<cf><<<b.n_walkers, 256, sm, stream>>>(m, b, moves);
+    else apply_moves_c_kernel<cd><<<b.n_walkers, 256, sm, stream>>>(m, b, moves);
+    return cudaGetLastError();
+}
+
+}  // namespace kvmc

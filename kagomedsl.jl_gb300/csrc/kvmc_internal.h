@@ -102,4 +102,19 @@ size_t refresh_large_smem(const DevModel &m);
 bool refresh_needs_large(const DevModel &m);
 int max_smem_optin(int device);
 
+// Complex orbitals (kvmc_complex.cu).  U_up / U_dn then point at interleaved
+// (re, im) pairs, W64 / W32 at complex FP64 / FP32 pairs, and solve_block
+// counts doubles (two per complex entry).
+int complex_max_orbitals();
+size_t complex_refresh_smem(const DevModel &m);
+cudaError_t launch_refresh_c(const DevModel &m, const DevBatch &b, bool fp32_out, int only_due, int track_drift,
+                             cudaStream_t stream);
+cudaError_t launch_sweep_c(const DevModel &m, const DevBatch &b, const SweepParams &p, bool mixed, int *active,
+                           cudaStream_t stream);
+cudaError_t launch_measure_c(const DevModel &m, const DevBatch &b, bool fp32, cudaStream_t stream);
+cudaError_t launch_eval_ratios_c(const DevModel &m, const DevBatch &b, bool fp32, int n_moves, const int *moves,
+                                 double *out, cudaStream_t stream);
+cudaError_t launch_apply_moves_c(const DevModel &m, const DevBatch &b, bool fp32, const int *moves,
+                                 cudaStream_t stream);
+
 }  // namespace kvmc

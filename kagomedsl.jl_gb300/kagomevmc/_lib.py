@@ -68,7 +68,8 @@ class Link(C.Structure):
 
 class ModelDesc(C.Structure):
     _fields_ = [("n_sites", C.c_int32), ("n_up", C.c_int32), ("n_down", C.c_int32), ("n_bonds", C.c_int32),
-                ("bonds", C.POINTER(C.c_int32)), ("U_up", C.POINTER(C.c_double)), ("U_down", C.POINTER(C.c_double))]
+                ("bonds", C.POINTER(C.c_int32)), ("U_up", C.POINTER(C.c_double)), ("U_down", C.POINTER(C.c_double)),
+                ("U_up_imag", C.POINTER(C.c_double)), ("U_down_imag", C.POINTER(C.c_double))]
 
 
 class BatchDesc(C.Structure):

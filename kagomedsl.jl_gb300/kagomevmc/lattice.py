@@ -112,13 +112,14 @@ def orbitals(H: np.ndarray, N_up: int, N_down: int):
 
     Inside a degenerate Fermi shell the reference keeps whatever LAPACK
     returns; here the real symmetric H (B = 0) is diagonalised as a real
-    matrix by numpy's ``eigh`` so that the orbitals are real.
+    matrix by numpy's ``eigh`` so that the orbitals are real, and a complex
+    Hermitian H (B != 0) gives complex orbitals.
     """
     H = np.asarray(H)
     if np.iscomplexobj(H) and np.any(H.imag != 0):
-        raise ArgumentError(_lib.KVMC_ERR_UNSUPPORTED,
-                            "complex hopping (B != 0) needs complex orbitals, which this build does not run")
-    w, V = np.linalg.eigh(np.real(H))
+        w, V = np.linalg.eigh(H)
+    else:
+        w, V = np.linalg.eigh(np.real(H))
     p = np.argsort(w, kind="stable")
     V = V[:, p]
     return np.ascontiguousarray(V[:, :N_up]), np.ascontiguousarray(V[:, :N_down])

@@ -33,16 +33,21 @@ class Engine:
         acc = {"reference": _lib.ACCEPT_REFERENCE, "metropolis": _lib.ACCEPT_METROPOLIS}.get(accept, accept)
         self.mixed = prec == _lib.MIXED_FP32
         self._bonds = _lib.as_c(np.asarray(ham.nn, dtype=np.int32).reshape(-1), np.int32)
-        if np.iscomplexobj(ham.U_up) or np.iscomplexobj(ham.U_down):
-            raise ArgumentError(_lib.KVMC_ERR_UNSUPPORTED, "complex orbitals are not supported by this build")
-        self._Uu = np.asfortranarray(ham.U_up, dtype=np.float64)
-        self._Ud = np.asfortranarray(ham.U_down, dtype=np.float64)
+        # complex orbitals (B != 0) make a complex handle: W, ratios complex
+        self.complex = bool(np.iscomplexobj(ham.U_up) or np.iscomplexobj(ham.U_down))
+        self._Uu = np.asfortranarray(np.real(ham.U_up), dtype=np.float64)
+        self._Ud = np.asfortranarray(np.real(ham.U_down), dtype=np.float64)
         md = _lib.ModelDesc()
         md.n_sites, md.n_up, md.n_down = self.N, self.n_up, self.n_down
         md.n_bonds = len(ham.nn)
         md.bonds = self._bonds.ctypes.data_as(C.POINTER(C.c_int32))
         md.U_up = self._Uu.ctypes.data_as(C.POINTER(C.c_double))
         md.U_down = self._Ud.ctypes.data_as(C.POINTER(C.c_double))
+        if self.complex:
+            self._Uui = np.asfortranarray(np.imag(ham.U_up), dtype=np.float64)
+            self._Udi = np.asfortranarray(np.imag(ham.U_down), dtype=np.float64)
+            md.U_up_imag = self._Uui.ctypes.data_as(C.POINTER(C.c_double))
+            md.U_down_imag = self._Udi.ctypes.data_as(C.POINTER(C.c_double))
         bd = _lib.BatchDesc()
         bd.n_walkers, bd.precision, bd.accept_rule = self.n_walkers, prec, acc
         bd.refresh_interval, bd.measure_interval = int(refresh_interval), int(measure_interval)
@@ -91,8 +96,9 @@ class Engine:
         self._check(self._lib.kvmc_set_state(self.h, _lib.ptr(ku), _lib.ptr(kd), _lib.ptr(ct)))
 
     def get_w(self):
-        Wu = np.empty((self.n_walkers, self.N, self.n_up))
-        Wd = np.empty((self.n_walkers, self.N, self.n_down))
+        dt = np.complex128 if self.complex else np.float64
+        Wu = np.empty((self.n_walkers, self.N, self.n_up), dtype=dt)
+        Wd = np.empty((self.n_walkers, self.N, self.n_down), dtype=dt)
         self._check(self._lib.kvmc_get_w(self.h, _lib.ptr(Wu), _lib.ptr(Wd)))
         return Wu, Wd
 
@@ -121,7 +127,7 @@ class Engine:
         if mv.ndim == 2:
             mv = mv[None]
         mv = _lib.as_c(np.broadcast_to(mv, (self.n_walkers, mv.shape[1], 4)), np.int32)
-        out = np.empty((self.n_walkers, mv.shape[1]))
+        out = np.empty((self.n_walkers, mv.shape[1]), dtype=np.complex128 if self.complex else np.float64)
         self._check(self._lib.kvmc_eval_ratios(self.h, mv.shape[1], _lib.ptr(mv), _lib.ptr(out)))
         return out
 

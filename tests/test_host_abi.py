@@ -34,7 +34,7 @@ def test_version(built):
 
     abi, arch = C.c_int32(), C.c_int32()
     assert kv.load().kvmc_version(C.byref(abi), C.byref(arch)) == 0
-    assert abi.value == 1 and arch.value == 1030
+    assert abi.value == 2 and arch.value == 1030
 
 
 @pytest.mark.parametrize("n1,n2,pbc,anti,B", [
@@ -91,6 +91,21 @@ def test_create_validates_before_touching_a_device(built):
     bad = kv.Hamiltonian(12, 12, ham.U_up, ham.U_down, ham.H_mat, [(0, 99)])
     with pytest.raises(kv.BoundsError):
         kv.Engine(bad, 2)
+
+
+def test_complex_orbitals_beyond_the_limit_are_unsupported(built):
+    """A field at 8x10 cells (240 sites, 120 orbitals per spin) exceeds the
+    complex kernels' 112-orbital limit; kvmc_create says so before any device call."""
+    import math
+
+    import kagomevmc as kv
+
+    L = kv.DoubleKagome(1.0, 8, 10, (True, True), (False, True))
+    H = kv.Hmat(L, B=math.pi / (8 * 10 * 2 * math.sqrt(3)))
+    Uu, Ud = kv.orbitals(H, 120, 120)
+    assert np.iscomplexobj(Uu)
+    with pytest.raises(kv.KvmcError, match="complex orbitals: at most 112"):
+        kv.Engine(kv.Hamiltonian(120, 120, Uu, Ud, H, kv.get_nn(H)), 2)
 
 
 def test_no_device_is_a_clean_error_on_cpu(built):

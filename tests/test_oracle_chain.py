@@ -72,6 +72,30 @@ def test_complex_oracle_equals_real_at_zero_field():
     np.testing.assert_allclose(ea, eb, rtol=1e-10, atol=1e-10)
 
 
+def test_complex_oracle_matches_numpy_chain_in_field():
+    """B != 0 with N_up != N_down (scripts/LL.jl:21-25 shape, 6x3 cells): the
+    complex C oracle follows the numpy restatement's trajectory and energies."""
+    import math
+
+    n1, n2, imbalance = 6, 3, 2
+    L = o.double_kagome(1.0, n1, n2, (True, True), (False, True))
+    B = imbalance * math.pi / (n1 * n2 * 2 * math.sqrt(3))
+    N = n1 * n2 * 3
+    ham = o.hamiltonian(N // 2 + imbalance // 2, N // 2 - imbalance // 2, L, B=B)
+    assert np.iscomplexobj(ham.U_up) and np.abs(ham.U_up.imag).max() > 1e-3
+    bonds = [(i - 1, j - 1) for i, j in ham.nn]
+    m = oracle_c.OracleModel(ham.U_up, ham.U_down, bonds, "cplx")
+    for walker in range(2):
+        ku, kd, _ = o.seeded_start(4, walker, ham.U_up, ham.U_down)
+        st = o.ChainState(ku.copy(), kd.copy(), o.reevaluateW(ham.U_up, ku), o.reevaluateW(ham.U_down, kd))
+        o.run_chain(ham.nn, ham.U_up, ham.U_down, st, 4, walker, 400, 26, 26, ham=ham)
+        ch = m.new_chain(ku, kd)
+        _, e = ch.run(4, walker, 400, 26, 26)
+        assert ch.ku.tolist() == st.kappa_up.tolist() and ch.kd.tolist() == st.kappa_down.tolist()
+        assert ch.c.accepted == st.accepted and st.accepted > 0
+        np.testing.assert_allclose(e[:len(st.energies)], st.energies, rtol=1e-9, atol=1e-9)
+
+
 def test_threaded_chains_equal_serial():
     ham, U = model(24)
     m = oracle_c.OracleModel(U, U, [(i - 1, j - 1) for i, j in ham.nn])
