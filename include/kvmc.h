@@ -94,6 +94,30 @@ KVMC_API int kvmc_hopping_matrix(const kvmc_lattice_desc *lat,
 KVMC_API int kvmc_bonds_from_hopping(int32_t n_sites, const double *H, int32_t *n_bonds,
                             int32_t *bonds);
 
+/* Extended mean-field ansatz with three real variational parameters
+ * params = {t2, m, theta}.  No reference counterpart: the reference has the
+ * pi-flux hopping only; this is the parameterised family whose energy
+ * gradient the adjoint entry points below measure.  On top of the pi-flux H
+ * of kvmc_hopping_matrix (same tables, boundary conditions and field B):
+ *   theta: each nearest-neighbour hop i->j is multiplied by
+ *          exp(i*theta*s_ij/3), s_ij = +1 when i->j runs counter-clockwise
+ *          around its triangle; every triangle then carries flux theta and
+ *          every hexagon pi - 2*theta;
+ *   t2, m: second-neighbour hops i->k (the two ends of a bent path i->j->k
+ *          around a hexagon corner, |r_k - r_i| = sqrt(3) t) get
+ *          H_ik += -(t2 + i*m*nu_ijk) * g_ijk, where g_ijk = sign(H0_ij H0_jk)
+ *          carries the pi-flux gauge of the path and nu_ijk = +1 (-1) for a
+ *          left (right) turn at j: a chiral mass of opposite sign on the two
+ *          orientations.  Second-neighbour hops carry no Peierls phase.
+ * H: 2*N*N doubles as kvmc_hopping_matrix.  dH (may be NULL): 3 matrices
+ * dH/dt2, dH/dm, dH/dtheta in the same layout, 6*N*N doubles.  The
+ * Heisenberg bonds stay the nearest-neighbour ones: take them from
+ * kvmc_bonds_from_hopping on the params = 0 matrix. */
+KVMC_API int kvmc_ansatz_hopping(const kvmc_lattice_desc *lat,
+                        const kvmc_link *link_in, int32_t n_link_in,
+                        const kvmc_link *link_inter, int32_t n_link_inter,
+                        double B, const double *params, double *H, double *dH);
+
 /* ---- batched Monte Carlo state ----------------------------------------- */
 
 typedef struct {
@@ -232,7 +256,8 @@ KVMC_API int kvmc_set_drift_tolerance(kvmc_handle *h, double tol);
 
 /* Device-side timing of the kernels launched by kvmc_sweep, measured with
  * CUDA events on the handle's stream (enable before the calls to time).
- * kind: 0 = sweep kernel, 1 = refresh kernel.  Totals since enabling. */
+ * kind: 0 = sweep kernel, 1 = refresh kernel, 2 = adjoint kernel
+ * (kvmc_measure_grad).  Totals since enabling. */
 KVMC_API int kvmc_enable_timing(kvmc_handle *h, int32_t on);
 KVMC_API int kvmc_kernel_time(kvmc_handle *h, int32_t kind, double *total_ms, int64_t *launches);
 
@@ -275,6 +300,41 @@ KVMC_API int kvmc_region_timer(kvmc_handle *h, int32_t start, double *ms);
  * start at zero, since every element a call reads it first writes. */
 KVMC_API int kvmc_refresh_static(int32_t n_sites, int32_t n_orb, int32_t batch, const double *U,
                                  const int32_t *kappa, double *W, double *logdet, void *stream);
+
+/* ---- adjoint gradient over ansatz parameters ---------------------------
+ * No reference counterpart (the reference measures the energy only).  For P
+ * real parameters a with orbital derivatives dU_a = dU/da (from first-order
+ * eigenvector perturbation of kvmc_ansatz_hopping's H and dH, computed on the
+ * host), the estimator takes per configuration the log-derivatives
+ * O_a = d ln psi / d a = sum_spin tr(tilde_U^{-1} tilde_dU_a) and the complex
+ * local energy E_L, and accumulates per walker the weighted sums from which
+ *   dE/da  = 2 Re( <conj(O_a) E_L> - conj(<O_a>) <E_L> )
+ *   S_ab   = Re( <conj(O_a) O_b> - conj(<O_a>) <O_b> )   (the SR matrix)
+ * follow, <.> under |psi|^2: the weight is Z_mu for the reference acceptance
+ * rule (whose chain samples |psi|^2 / Z_mu) and 1 for the Metropolis rule. */
+
+/* dU_up: [n_params] column-major n_sites x n_up matrices (dU_up_imag the
+ * imaginary parts, NULL when real); likewise dU_down.  1 <= n_params <= 8.
+ * Resets the gradient sums. */
+KVMC_API int kvmc_set_log_derivatives(kvmc_handle *h, int32_t n_params,
+                             const double *dU_up, const double *dU_up_imag,
+                             const double *dU_down, const double *dU_down_imag);
+
+/* One adjoint evaluation at every walker's current configuration (run it
+ * between kvmc_sweep calls, e.g. once per n-proposal sweep), added into the
+ * sums.  Optional outputs: local_energy [n_walkers][2] (re, im) and
+ * log_derivative [n_walkers][n_params][2]. */
+KVMC_API int kvmc_measure_grad(kvmc_handle *h, double *local_energy, double *log_derivative);
+
+/* Per-walker sums, [n_walkers][L] with L = 3 + 4P + 2P^2: sum w, sum w E_L
+ * (re, im), sum w O_a (re, im)[P], sum w conj(O_a) E_L (re, im)[P],
+ * sum w conj(O_a) O_b (re, im)[P][P].  Zeroed by kvmc_reset_stats. */
+KVMC_API int kvmc_grad_sums(kvmc_handle *h, double *sums);
+
+/* log|det tilde_U| per spin from the last refresh, [n_walkers][2] (up,
+ * down): with kvmc_set_state it gives |psi'(x) / psi(x)|^2 between two
+ * ansatz points on the same configurations (correlated sampling). */
+KVMC_API int kvmc_walker_logdet(kvmc_handle *h, double *logdet);
 
 /* Library version / build facts: abi version, compiled arch (e.g. 1030). */
 KVMC_API int kvmc_version(int32_t *abi, int32_t *arch);

@@ -69,8 +69,17 @@ struct kvmc_handle {
     std::vector<cudaEvent_t> ev_pool;
     std::vector<std::pair<int, int>> ev_used;  // (kind, first event index)
     cudaEvent_t region[2] = {nullptr, nullptr};
-    double t_ms[2] = {0, 0};
-    long long t_launch[2] = {0, 0};
+    double t_ms[3] = {0, 0, 0};
+    long long t_launch[3] = {0, 0, 0};
+
+    // orbitals kept on the host (row-major, (re, im) pairs when complex) for
+    // the adjoint set-up, and the adjoint's device buffers
+    std::vector<double> U_up_host, U_dn_host;
+    int n_params = 0;
+    void *d_MT = nullptr;
+    double *d_gsums = nullptr;
+    double *d_gout = nullptr;
+    size_t gsum_stride = 0;
 
     int fail(int code, const char *fmt, ...) {
         char buf[512];
@@ -372,6 +381,112 @@ extern "C" int kvmc_bonds_from_hopping(int32_t n_sites, const double *H, int32_t
     return KVMC_OK;
 }
 
+// Extended ansatz: the pi-flux H with a triangle flux theta and second-
+// neighbour hops t2 + i*m*nu (the parameterisation is stated in kvmc.h).
+// Geometry comes from the site coordinates (src/Hamiltonian.jl:279-283) and
+// the minimum image over the periodic directions.
+extern "C" int kvmc_ansatz_hopping(const kvmc_lattice_desc *lat, const kvmc_link *link_in, int32_t n_link_in,
+                                   const kvmc_link *link_inter, int32_t n_link_inter, double B, const double *params,
+                                   double *H, double *dH) {
+    if (!lat || !params || !H) return fail_global(KVMC_ERR_ARGUMENT, "null argument");
+    int32_t N = 0;
+    if (int rc = kvmc_lattice_sites(lat, &N)) return rc;
+    const double t2 = params[0], mch = params[1], theta = params[2];
+    if (!std::isfinite(t2) || !std::isfinite(mch) || !std::isfinite(theta))
+        return fail_global(KVMC_ERR_ARGUMENT, "ansatz parameters must be finite");
+    std::vector<double> H0(2 * (size_t)N * N), Hpi(2 * (size_t)N * N);
+    if (int rc = kvmc_hopping_matrix(lat, link_in, n_link_in, link_inter, n_link_inter, B, H0.data())) return rc;
+    if (int rc = kvmc_hopping_matrix(lat, link_in, n_link_in, link_inter, n_link_inter, 0.0, Hpi.data())) return rc;
+    using cplx = std::complex<double>;
+    auto ix = [N](int i, int j) { return (size_t)i + (size_t)j * N; };
+    const LatticeGeom g = make_geom(lat);
+    const Vec2 L1 = {g.n1h * g.a1.x, g.n1h * g.a1.y}, L2 = {g.n2 * g.a2.x, g.n2 * g.a2.y};
+    std::vector<Vec2> pos(N);
+    for (int s = 0; s < N; ++s) pos[s] = g.site(s + 1);
+    const double t = lat->t, tol = 1e-9 * t * t;
+    // displacements r_j - r_i over the images at squared length want; n = how many
+    auto disp = [&](int i, int j, double want, Vec2 &d) {
+        int n = 0;
+        for (int p = -1; p <= 1; ++p) {
+            if (p != 0 && !g.pbc1) continue;
+            for (int q = -1; q <= 1; ++q) {
+                if (q != 0 && !g.pbc2) continue;
+                const Vec2 e = {pos[j].x - pos[i].x + p * L1.x + q * L2.x, pos[j].y - pos[i].y + p * L1.y + q * L2.y};
+                if (std::fabs(e.x * e.x + e.y * e.y - want) <= tol) { d = e; ++n; }
+            }
+        }
+        return n;
+    };
+    // nearest neighbours: the nonzeros of the pi-flux H, each at one image
+    std::vector<std::vector<int>> nbr(N);
+    std::vector<std::vector<Vec2>> dnb(N);
+    for (int i = 0; i < N; ++i)
+        for (int j = 0; j < N; ++j) {
+            if (i == j || (Hpi[2 * ix(i, j)] == 0.0 && Hpi[2 * ix(i, j) + 1] == 0.0)) continue;
+            Vec2 d{};
+            const int n = disp(i, j, t * t, d);
+            if (n != 1)
+                return fail_global(KVMC_ERR_ARGUMENT,
+                                   "lattice too small for the extended ansatz: sites %d and %d are %s", i, j,
+                                   n == 0 ? "not at nearest-neighbour distance" : "neighbours through several images");
+            nbr[i].push_back(j);
+            dnb[i].push_back(d);
+        }
+    auto cross = [](Vec2 a, Vec2 b) { return a.x * b.y - a.y * b.x; };
+    std::vector<cplx> Hx((size_t)N * N), dT2((size_t)N * N), dM((size_t)N * N), dTh((size_t)N * N);
+    for (int i = 0; i < N; ++i)
+        for (int j = 0; j < N; ++j) Hx[ix(i, j)] = cplx(H0[2 * ix(i, j)], H0[2 * ix(i, j) + 1]);
+    // theta: orientation of each nearest-neighbour hop in its triangle
+    for (int i = 0; i < N; ++i)
+        for (size_t a = 0; a < nbr[i].size(); ++a) {
+            const int j = nbr[i][a];
+            const Vec2 dij = dnb[i][a];
+            int found = 0;
+            double s = 0.0;
+            for (size_t b = 0; b < nbr[j].size(); ++b) {
+                const Vec2 djk = dnb[j][b];
+                const Vec2 dik = {dij.x + djk.x, dij.y + djk.y};
+                if (nbr[j][b] == i || std::fabs(dik.x * dik.x + dik.y * dik.y - t * t) > tol) continue;
+                s = cross(dij, djk) > 0 ? 1.0 : -1.0;
+                ++found;
+            }
+            if (found != 1)
+                return fail_global(KVMC_ERR_ARGUMENT, "bond (%d, %d) does not close exactly one triangle", i, j);
+            const cplx ph(std::cos(theta * s / 3.0), std::sin(theta * s / 3.0));
+            Hx[ix(i, j)] *= ph;
+            dTh[ix(i, j)] = Hx[ix(i, j)] * cplx(0.0, s / 3.0);
+        }
+    // second neighbours: bent paths i -> j -> k around a hexagon corner
+    for (int j = 0; j < N; ++j)
+        for (size_t a = 0; a < nbr[j].size(); ++a)
+            for (size_t b = 0; b < nbr[j].size(); ++b) {
+                if (a == b) continue;
+                const int i = nbr[j][a], k = nbr[j][b];
+                // r_j - r_i is minus the displacement from j to i
+                const Vec2 dij = {-dnb[j][a].x, -dnb[j][a].y}, djk = dnb[j][b];
+                const Vec2 dik = {dij.x + djk.x, dij.y + djk.y};
+                if (std::fabs(dik.x * dik.x + dik.y * dik.y - 3 * t * t) > tol) continue;
+                const double gij = Hpi[2 * ix(i, j)], gjk = Hpi[2 * ix(j, k)];
+                const double gs = (gij * gjk) > 0 ? 1.0 : -1.0;
+                const double nu = cross(dij, djk) > 0 ? 1.0 : -1.0;
+                Hx[ix(i, k)] += -cplx(t2, mch * nu) * gs;
+                dT2[ix(i, k)] += -gs;
+                dM[ix(i, k)] += cplx(0.0, -nu * gs);
+            }
+    for (size_t e = 0; e < (size_t)N * N; ++e) {
+        H[2 * e] = Hx[e].real();
+        H[2 * e + 1] = Hx[e].imag();
+        if (dH) {
+            const cplx *src[3] = {&dT2[e], &dM[e], &dTh[e]};
+            for (int q = 0; q < 3; ++q) {
+                dH[2 * ((size_t)q * N * N + e)] = src[q]->real();
+                dH[2 * ((size_t)q * N * N + e) + 1] = src[q]->imag();
+            }
+        }
+    }
+    return KVMC_OK;
+}
+
 // ===========================================================================
 // Handle
 // ===========================================================================
@@ -395,6 +510,9 @@ extern "C" int kvmc_destroy(kvmc_handle *h) {
     if (h->stream) cudaStreamSynchronize(h->stream);
     for (void *p : h->allocs) cudaFree(p);
     if (h->d_scratch) cudaFree(h->d_scratch);
+    if (h->d_MT) cudaFree(h->d_MT);
+    if (h->d_gsums) cudaFree(h->d_gsums);
+    if (h->d_gout) cudaFree(h->d_gout);
     for (auto &e : h->ev_pool) cudaEventDestroy(e);
     for (auto &e : h->region)
         if (e) cudaEventDestroy(e);
@@ -507,6 +625,8 @@ extern "C" int kvmc_create(const kvmc_model_desc *model, const kvmc_batch_desc *
     cudaMemcpy(dOff, off.data(), (N + 1) * sizeof(int), cudaMemcpyHostToDevice);
     cudaMemcpy(dNbr, nbr.data(), nbr.size() * sizeof(short), cudaMemcpyHostToDevice);
     m.U_up = dUu; m.U_dn = dUd; m.bonds = dB; m.nbr_off = dOff; m.nbr = dNbr;
+    h->U_up_host = std::move(Uu);
+    h->U_dn_host = std::move(Ud);
     // thresholds fl(z / n_bonds) for z = 0..n_bonds, with their exact binary form
     std::vector<kvmc::ThrEntry> thr(nb + 1);
     for (int z = 0; z <= nb; ++z) {
@@ -609,6 +729,7 @@ extern "C" int kvmc_reset_stats(kvmc_handle *h) {
     cudaMemsetAsync(b.n_meas, 0, Wk * 8, h->stream);
     cudaMemsetAsync(b.accepted, 0, Wk * 8, h->stream);
     cudaMemsetAsync(b.proposals, 0, Wk * 8, h->stream);
+    if (h->d_gsums) cudaMemsetAsync(h->d_gsums, 0, Wk * h->gsum_stride * 8, h->stream);
     return h->cuda(cudaStreamSynchronize(h->stream), "reset stats");
 }
 
@@ -663,8 +784,7 @@ extern "C" int kvmc_init(kvmc_handle *h, const int32_t *kappa_up, const int32_t 
 extern "C" int kvmc_enable_timing(kvmc_handle *h, int32_t on) {
     if (!h) return fail_global(KVMC_ERR_ARGUMENT, "null handle");
     h->timing = on != 0;
-    h->t_ms[0] = h->t_ms[1] = 0;
-    h->t_launch[0] = h->t_launch[1] = 0;
+    for (int k = 0; k < 3; ++k) h->t_ms[k] = 0, h->t_launch[k] = 0;
     return KVMC_OK;
 }
 
@@ -691,7 +811,7 @@ extern "C" int kvmc_get_config(kvmc_handle *h, int32_t *refresh_interval, int32_
 }
 
 extern "C" int kvmc_kernel_time(kvmc_handle *h, int32_t kind, double *total_ms, int64_t *launches) {
-    if (!h || kind < 0 || kind > 1) return fail_global(KVMC_ERR_ARGUMENT, "bad argument");
+    if (!h || kind < 0 || kind > 2) return fail_global(KVMC_ERR_ARGUMENT, "bad argument");
     if (total_ms) *total_ms = h->t_ms[kind];
     if (launches) *launches = h->t_launch[kind];
     return KVMC_OK;
@@ -699,7 +819,7 @@ extern "C" int kvmc_kernel_time(kvmc_handle *h, int32_t kind, double *total_ms, 
 
 namespace {
 
-// One launch with optional event timing (kind 0 sweep, 1 refresh).  The
+// One launch with optional event timing (kind 0 sweep, 1 refresh, 2 adjoint).  The
 // events are only read by collect_timing() after the stream is synchronised.
 template <typename F>
 int timed(kvmc_handle *h, int kind, F &&launch, const char *what) {
@@ -976,5 +1096,137 @@ extern "C" int kvmc_walker_stats(kvmc_handle *h, double *sum_e, double *sum_e2, 
     if (accepted) KV_TRY(h->cuda(cudaMemcpy(accepted, b.accepted, Wk * 8, cudaMemcpyDeviceToHost), "stats"));
     if (proposals) KV_TRY(h->cuda(cudaMemcpy(proposals, b.proposals, Wk * 8, cudaMemcpyDeviceToHost), "stats"));
     if (status) KV_TRY(h->cuda(cudaMemcpy(status, b.status, Wk * 4, cudaMemcpyDeviceToHost), "stats"));
+    return KVMC_OK;
+}
+
+// ===========================================================================
+// Adjoint gradient estimator
+// ===========================================================================
+
+extern "C" int kvmc_set_log_derivatives(kvmc_handle *h, int32_t n_params, const double *dU_up,
+                                        const double *dU_up_imag, const double *dU_down,
+                                        const double *dU_down_imag) {
+    if (!h) return fail_global(KVMC_ERR_ARGUMENT, "null handle");
+    if (n_params < 1 || n_params > kvmc::kMaxGradParams)
+        return h->fail(KVMC_ERR_ARGUMENT, "n_params must be in 1..%d (got %d)", kvmc::kMaxGradParams, n_params);
+    if (!dU_up || !dU_down) return h->fail(KVMC_ERR_ARGUMENT, "null orbital derivatives");
+    const int N = h->n_sites, P = n_params;
+    if (!h->cplx) {
+        for (int s = 0; s < 2; ++s) {
+            const double *im = s == 0 ? dU_up_imag : dU_down_imag;
+            const size_t cnt = (size_t)P * N * (s == 0 ? h->n_up : h->n_dn);
+            if (im)
+                for (size_t e = 0; e < cnt; ++e)
+                    if (im[e] != 0.0)
+                        return h->fail(KVMC_ERR_ARGUMENT, "complex orbital derivatives need a handle with complex orbitals");
+        }
+    }
+    KV_TRY(set_device(h));
+    // M_a,s = dU_a,s U_s^H in FP64, stored transposed: MT[a][s][R'][R] = M[R, R']
+    const size_t NN = (size_t)N * N;
+    std::vector<std::complex<double>> MT((size_t)P * 2 * NN);
+    for (int s = 0; s < 2; ++s) {
+        const int n = s == 0 ? h->n_up : h->n_dn;
+        const std::vector<double> &Uh = s == 0 ? h->U_up_host : h->U_dn_host;
+        const double *re = s == 0 ? dU_up : dU_down;
+        const double *im = s == 0 ? dU_up_imag : dU_down_imag;
+        std::vector<std::complex<double>> Ur((size_t)N * n), Dr((size_t)N * n);
+        for (int R = 0; R < N; ++R)
+            for (int c = 0; c < n; ++c)
+                Ur[(size_t)R * n + c] = h->cplx ? std::complex<double>(Uh[2 * ((size_t)R * n + c)], -Uh[2 * ((size_t)R * n + c) + 1])
+                                                : std::complex<double>(Uh[(size_t)R * n + c], 0.0);  // conj(U)
+        for (int a = 0; a < P; ++a) {
+            for (int R = 0; R < N; ++R)
+                for (int c = 0; c < n; ++c) {
+                    const size_t src = (size_t)a * N * n + (size_t)c * N + R;
+                    Dr[(size_t)R * n + c] = std::complex<double>(re[src], im ? im[src] : 0.0);
+                }
+            std::complex<double> *dst = MT.data() + ((size_t)a * 2 + s) * NN;
+            for (int R = 0; R < N; ++R) {
+                const std::complex<double> *d = Dr.data() + (size_t)R * n;
+                for (int Rp = 0; Rp < N; ++Rp) {
+                    const std::complex<double> *u = Ur.data() + (size_t)Rp * n;
+                    std::complex<double> acc = 0.0;
+                    for (int c = 0; c < n; ++c) acc += d[c] * u[c];
+                    dst[(size_t)Rp * N + R] = acc;
+                }
+            }
+        }
+    }
+    // the working scalar of the handle: (complex) FP64 plain, (complex) FP32 mixed
+    const size_t per = (h->cplx ? 2 : 1) * (h->mixed ? 4 : 8);
+    std::vector<unsigned char> buf(MT.size() * per);
+    for (size_t e = 0; e < MT.size(); ++e) {
+        if (h->mixed) {
+            float *f = reinterpret_cast<float *>(buf.data()) + e * (h->cplx ? 2 : 1);
+            f[0] = (float)MT[e].real();
+            if (h->cplx) f[1] = (float)MT[e].imag();
+        } else {
+            double *d = reinterpret_cast<double *>(buf.data()) + e * (h->cplx ? 2 : 1);
+            d[0] = MT[e].real();
+            if (h->cplx) d[1] = MT[e].imag();
+        }
+    }
+    if (h->d_MT) { cudaFree(h->d_MT); h->d_MT = nullptr; }
+    if (h->d_gsums) { cudaFree(h->d_gsums); h->d_gsums = nullptr; }
+    if (h->d_gout) { cudaFree(h->d_gout); h->d_gout = nullptr; }
+    h->n_params = 0;
+    const size_t Wk = h->n_walkers;
+    const size_t L = 3 + 4 * (size_t)P + 2 * (size_t)P * P;
+    KV_TRY(h->cuda(cudaMalloc(&h->d_MT, buf.size()), "cudaMalloc"));
+    KV_TRY(h->cuda(cudaMalloc(reinterpret_cast<void **>(&h->d_gsums), Wk * L * 8), "cudaMalloc"));
+    KV_TRY(h->cuda(cudaMalloc(reinterpret_cast<void **>(&h->d_gout), Wk * (2 + 2 * (size_t)P) * 8), "cudaMalloc"));
+    KV_TRY(h->cuda(cudaMemcpy(h->d_MT, buf.data(), buf.size(), cudaMemcpyHostToDevice), "upload"));
+    KV_TRY(h->cuda(cudaMemset(h->d_gsums, 0, Wk * L * 8), "memset"));
+    h->gsum_stride = L;
+    h->n_params = P;
+    return KVMC_OK;
+}
+
+extern "C" int kvmc_measure_grad(kvmc_handle *h, double *local_energy, double *log_derivative) {
+    if (!h) return fail_global(KVMC_ERR_ARGUMENT, "null handle");
+    if (h->n_params == 0) return h->fail(KVMC_ERR_ARGUMENT, "kvmc_set_log_derivatives has not been called");
+    KV_TRY(set_device(h));
+    kvmc::GradModel g{};
+    g.n_params = h->n_params;
+    g.MT = h->d_MT;
+    g.W = h->mixed ? static_cast<const void *>(h->db.W32) : static_cast<const void *>(h->db.W64);
+    g.sums = h->d_gsums;
+    g.sum_stride = h->gsum_stride;
+    g.out = h->d_gout;
+    KV_TRY(timed(h, 2, [&] { return kvmc::launch_grad(h->dm, h->db, g, h->mixed, h->cplx, h->batch.accept_rule, h->stream); },
+                 "adjoint launch"));
+    KV_TRY(h->cuda(cudaStreamSynchronize(h->stream), "adjoint"));
+    KV_TRY(collect_timing(h));
+    if (local_energy || log_derivative) {
+        const size_t Wk = h->n_walkers, row = 2 + 2 * (size_t)h->n_params;
+        std::vector<double> o(Wk * row);
+        KV_TRY(h->cuda(cudaMemcpy(o.data(), h->d_gout, o.size() * 8, cudaMemcpyDeviceToHost), "adjoint"));
+        for (size_t w = 0; w < Wk; ++w) {
+            if (local_energy) { local_energy[2 * w] = o[w * row]; local_energy[2 * w + 1] = o[w * row + 1]; }
+            if (log_derivative)
+                for (size_t k = 0; k < row - 2; ++k) log_derivative[w * (row - 2) + k] = o[w * row + 2 + k];
+        }
+    }
+    return KVMC_OK;
+}
+
+extern "C" int kvmc_grad_sums(kvmc_handle *h, double *sums) {
+    if (!h || !sums) return fail_global(KVMC_ERR_ARGUMENT, "null argument");
+    if (h->n_params == 0) return h->fail(KVMC_ERR_ARGUMENT, "kvmc_set_log_derivatives has not been called");
+    KV_TRY(set_device(h));
+    return h->cuda(cudaMemcpy(sums, h->d_gsums, (size_t)h->n_walkers * h->gsum_stride * 8, cudaMemcpyDeviceToHost),
+                   "adjoint sums");
+}
+
+extern "C" int kvmc_walker_logdet(kvmc_handle *h, double *logdet) {
+    if (!h || !logdet) return fail_global(KVMC_ERR_ARGUMENT, "null argument");
+    KV_TRY(set_device(h));
+    std::vector<double> ld(4 * (size_t)h->n_walkers);
+    KV_TRY(h->cuda(cudaMemcpy(ld.data(), h->db.logdet, ld.size() * 8, cudaMemcpyDeviceToHost), "logdet"));
+    for (int w = 0; w < h->n_walkers; ++w) {
+        logdet[2 * w] = ld[4 * (size_t)w];
+        logdet[2 * w + 1] = ld[4 * (size_t)w + 1];
+    }
     return KVMC_OK;
 }

@@ -20,33 +20,6 @@
 
 namespace kvmc {
 
-// ---- complex scalars -------------------------------------------------------
-struct __align__(16) cd { double x, y; };
-struct __align__(8) cf { float x, y; };
-
-template <typename C> struct Real;
-template <> struct Real<cd> { using T = double; };
-template <> struct Real<cf> { using T = float; };
-
-template <typename C> __device__ __forceinline__ C cmul(C a, C b) {
-    return C{a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x};
-}
-// c - a * b
-template <typename C> __device__ __forceinline__ C cfms(C a, C b, C c) {
-    return C{fma(-a.x, b.x, fma(a.y, b.y, c.x)), fma(-a.x, b.y, fma(-a.y, b.x, c.y))};
-}
-// c + a * b
-template <typename C> __device__ __forceinline__ C cfma(C a, C b, C c) {
-    return C{fma(a.x, b.x, fma(-a.y, b.y, c.x)), fma(a.x, b.y, fma(a.y, b.x, c.y))};
-}
-template <typename C> __device__ __forceinline__ C cinv(C a) {
-    const auto d = a.x * a.x + a.y * a.y;
-    return C{a.x / d, -a.y / d};
-}
-template <typename C> __device__ __forceinline__ typename Real<C>::T cabs2(C a) { return a.x * a.x + a.y * a.y; }
-// LAPACK's pivot magnitude for complex matrices, |re| + |im|
-__device__ __forceinline__ double cabs1(cd a) { return fabs(a.x) + fabs(a.y); }
-
 template <typename O> __device__ __forceinline__ O to_out(cd v);
 template <> __device__ __forceinline__ cd to_out<cd>(cd v) { return v; }
 template <> __device__ __forceinline__ cf to_out<cf>(cd v) { return cf{(float)v.x, (float)v.y}; }

@@ -102,6 +102,19 @@ size_t refresh_large_smem(const DevModel &m);
 bool refresh_needs_large(const DevModel &m);
 int max_smem_optin(int device);
 
+// Adjoint gradient estimator (kvmc_grad.cu).
+constexpr int kMaxGradParams = 8;
+struct GradModel {
+    int n_params;
+    const void *MT;     // [P][2][N][N] of the working scalar: MT[a][s][R'][R] = (dU_a,s U_s^H)[R, R']
+    const void *W;      // the handle's W (W64 or W32)
+    double *sums;       // [n_walkers][sum_stride], see kvmc_grad_sums
+    size_t sum_stride;
+    double *out;        // [n_walkers][2 + 2P]: E_L (re, im), then O_a (re, im); may be null
+};
+cudaError_t launch_grad(const DevModel &m, const DevBatch &b, const GradModel &g, bool mixed, bool complex_w, int rule,
+                        cudaStream_t stream);
+
 // Complex orbitals (kvmc_complex.cu).  U_up / U_dn then point at interleaved
 // (re, im) pairs, W64 / W32 at complex FP64 / FP32 pairs, and solve_block
 // counts doubles (two per complex entry).

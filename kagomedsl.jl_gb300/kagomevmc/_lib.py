@@ -114,6 +114,12 @@ _SIGS = {
     "kvmc_get_config": [_P, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(C.c_int32)],
     "kvmc_version": [C.POINTER(C.c_int32), C.POINTER(C.c_int32)],
     "kvmc_refresh_static": [C.c_int32, C.c_int32, C.c_int32, _P, _P, _P, _P, _P],
+    "kvmc_ansatz_hopping": [C.POINTER(LatticeDesc), C.POINTER(Link), C.c_int32, C.POINTER(Link), C.c_int32,
+                            C.c_double, _P, _P, _P],
+    "kvmc_set_log_derivatives": [_P, C.c_int32, _P, _P, _P, _P],
+    "kvmc_measure_grad": [_P, _P, _P],
+    "kvmc_grad_sums": [_P, _P],
+    "kvmc_walker_logdet": [_P, _P],
 }
 EXPORTS = tuple(_SIGS)
 

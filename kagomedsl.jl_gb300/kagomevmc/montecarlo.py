@@ -32,6 +32,7 @@ class Engine:
         prec = {"plain": _lib.PLAIN_FP64, "mixed": _lib.MIXED_FP32}.get(precision, precision)
         acc = {"reference": _lib.ACCEPT_REFERENCE, "metropolis": _lib.ACCEPT_METROPOLIS}.get(accept, accept)
         self.mixed = prec == _lib.MIXED_FP32
+        self.n_params = 0
         self._bonds = _lib.as_c(np.asarray(ham.nn, dtype=np.int32).reshape(-1), np.int32)
         # complex orbitals (B != 0) make a complex handle: W, ratios complex
         self.complex = bool(np.iscomplexobj(ham.U_up) or np.iscomplexobj(ham.U_down))
@@ -143,6 +144,44 @@ class Engine:
         self._check(self._lib.kvmc_walker_stats(self.h, _lib.ptr(se), _lib.ptr(se2), _lib.ptr(nm), _lib.ptr(acc),
                                                 _lib.ptr(prop), _lib.ptr(status)))
         return dict(sum_e=se, sum_e2=se2, n_meas=nm, accepted=acc, proposals=prop, status=status)
+
+    # --- adjoint gradient ------------------------------------------------------
+    def set_log_derivatives(self, dU_up, dU_down):
+        """dU_sigma: [P][N][n_sigma] orbital derivatives (complex or real)."""
+        dU_up, dU_down = np.asarray(dU_up), np.asarray(dU_down)
+        P = dU_up.shape[0]
+        # [P][n][N] C order = P column-major N x n matrices
+        def split(d):
+            t = np.ascontiguousarray(np.transpose(d, (0, 2, 1)))
+            return (np.ascontiguousarray(t.real, dtype=np.float64),
+                    np.ascontiguousarray(t.imag, dtype=np.float64) if np.iscomplexobj(t) else None)
+        ur, ui = split(dU_up)
+        dr, di = split(dU_down)
+        self._check(self._lib.kvmc_set_log_derivatives(self.h, P, _lib.ptr(ur), _lib.ptr(ui), _lib.ptr(dr),
+                                                       _lib.ptr(di)))
+        self.n_params = P
+
+    def measure_grad(self, want=False):
+        """One adjoint evaluation at every walker's configuration; with want=True
+        returns (E_L complex [W], O complex [W][P])."""
+        if not want:
+            self._check(self._lib.kvmc_measure_grad(self.h, None, None))
+            return None
+        e = np.empty((self.n_walkers, 2))
+        o = np.empty((self.n_walkers, self.n_params, 2))
+        self._check(self._lib.kvmc_measure_grad(self.h, _lib.ptr(e), _lib.ptr(o)))
+        return e[:, 0] + 1j * e[:, 1], o[..., 0] + 1j * o[..., 1]
+
+    def grad_sums(self) -> np.ndarray:
+        P = self.n_params
+        out = np.empty((self.n_walkers, 3 + 4 * P + 2 * P * P))
+        self._check(self._lib.kvmc_grad_sums(self.h, _lib.ptr(out)))
+        return out
+
+    def walker_logdet(self) -> np.ndarray:
+        out = np.empty((self.n_walkers, 2))
+        self._check(self._lib.kvmc_walker_logdet(self.h, _lib.ptr(out)))
+        return out
 
     def walker_drift(self) -> np.ndarray:
         d = np.empty(self.n_walkers, dtype=np.float32)

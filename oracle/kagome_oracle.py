@@ -695,3 +695,193 @@ def enumerate_energy(U, nn, chunk=100000):
         numz += (p / Zm * EL).sum()
         denz += (p / Zm).sum()
     return num / den / N, numz / denz / N
+
+
+# ---------------------------------------------------------------------------
+# Extended ansatz and its energy gradient (oracle addition, no reference
+# counterpart).  The reference has the pi-flux hopping only; the family
+# below adds a triangle flux theta and second-neighbour hops t2 + i*m*nu, and
+# the gradient of E(t2, m, theta) is computed exactly (enumeration) from the
+# log-derivatives O_a(x) = d ln psi(x) / d a.
+# ---------------------------------------------------------------------------
+
+
+def _min_image(lat, i, j, want):
+    """Displacements r_j - r_i (0-based sites) over the periodic images whose
+    squared length equals `want` to 1e-9 t^2."""
+    ri, rj = get_site_coord(lat, i + 1), get_site_coord(lat, j + 1)
+    L1, L2 = (lat.n1 // 2) * lat.a1, lat.n2 * lat.a2
+    out = []
+    for p in ((-1, 0, 1) if lat.PBC[0] else (0,)):
+        for q in ((-1, 0, 1) if lat.PBC[1] else (0,)):
+            d = rj - ri + p * L1 + q * L2
+            if abs(d @ d - want) <= 1e-9 * lat.t ** 2:
+                out.append(d)
+    return out
+
+
+def ansatz_hmat(lat, params, B=0.0, link_in=PI_LINK_IN, link_inter=PI_LINK_INTER):
+    """H(t2, m, theta) and [dH/dt2, dH/dm, dH/dtheta].
+
+    Triangles are found as mutually adjacent triples of the pi-flux H and
+    oriented by the sign of their area; each directed edge i->j of a
+    triangle gets exp(i theta s/3) with s = +1 counter-clockwise.  Second
+    neighbours are the pairs at sqrt(3) t through a common neighbour j;
+    H_ik += -(t2 + i m nu) g with g = sign(H0_ij H0_jk) and nu = +1 for a left
+    turn at j.
+    """
+    t2, m, theta = (float(x) for x in params)
+    H0 = hmat(lat, link_in, link_inter, B)
+    Hp = hmat(lat, link_in, link_inter, 0.0)
+    N = H0.shape[0]
+    t = lat.t
+    adj = [set(np.nonzero(Hp[i])[0]) - {i} for i in range(N)]
+    disp = {}
+    for i in range(N):
+        for j in adj[i]:
+            d = _min_image(lat, i, j, t * t)
+            if len(d) != 1:
+                raise ValueError(f"lattice too small for the extended ansatz ({i}, {j})")
+            disp[i, j] = d[0]
+    H = H0.astype(complex).copy()
+    dT, dM, dTh = (np.zeros((N, N), complex) for _ in range(3))
+    s_edge = {}
+    for i in range(N):
+        for j in adj[i]:
+            for k in adj[i] & adj[j]:
+                if i < j < k:
+                    a = disp[i, j]
+                    b = disp[i, k]
+                    ccw = (a[0] * b[1] - a[1] * b[0]) > 0
+                    order = (i, j, k) if ccw else (i, k, j)
+                    for x, y in zip(order, order[1:] + order[:1]):
+                        s_edge[x, y] = 1.0
+                        s_edge[y, x] = -1.0
+    for (i, j), s in s_edge.items():
+        ph = complex(math.cos(theta * s / 3.0), math.sin(theta * s / 3.0))
+        H[i, j] = H0[i, j] * ph
+        dTh[i, j] = H[i, j] * complex(0.0, s / 3.0)
+    for j in range(N):
+        for i in adj[j]:
+            for k in adj[j]:
+                if i == k or k in adj[i]:
+                    continue
+                d = disp[i, j] + disp[j, k]
+                if abs(d @ d - 3 * t * t) > 1e-9 * t * t:
+                    continue
+                g = 1.0 if Hp[i, j].real * Hp[j, k].real > 0 else -1.0
+                cr = disp[i, j][0] * disp[j, k][1] - disp[i, j][1] * disp[j, k][0]
+                nu = 1.0 if cr > 0 else -1.0
+                H[i, k] += -complex(t2, m * nu) * g
+                dT[i, k] += -g
+                dM[i, k] += complex(0.0, -nu * g)
+    return H, [dT, dM, dTh]
+
+
+def orbital_derivatives(H, dHs, N_up, N_down):
+    """U_sigma = lowest-N_sigma eigenvectors of H (as ``orbitals``) and their
+    first-order derivatives dU[:, c] = sum_{m unoccupied} v_m (v_m^H dH v_c) / (e_c - e_m).
+
+    Occupied-occupied mixing is left out: it rotates U inside its own span,
+    which multiplies every determinant by one constant and so drops out of
+    every expectation value.  Requires a gap above the last occupied level.
+    """
+    Hh = np.asarray(H)
+    cplx = np.any(Hh.imag != 0) or any(np.any(np.asarray(d).imag != 0) for d in dHs)
+    w, V = np.linalg.eigh(Hh if cplx else Hh.real)
+    p = np.argsort(w, kind="stable")
+    w, V = w[p], V[:, p]
+    out = []
+    for n in (N_up, N_down):
+        if w[n] - w[n - 1] <= 1e-10:
+            raise ValueError(f"no gap above level {n}: {w[n - 1]} {w[n]}")
+        U, Vu = V[:, :n], V[:, n:]
+        den = w[:n][None, :] - w[n:][:, None]          # (N - n) x n: e_c - e_m
+        D = []
+        for dH in dHs:
+            dH = np.asarray(dH) if cplx else np.asarray(dH).real
+            Bm = (Vu.conj().T @ dH @ U) / den
+            D.append(Vu @ Bm)
+        out.append((U.copy(), np.array(D)))
+    return out[0][0], out[1][0], out[0][1], out[1][1]
+
+
+def log_derivative(U, D, kappa):
+    """O_a = tr(tilde_U^{-1} tilde_D_a) for one spin: d ln det tilde_U / d a."""
+    tU = tilde_U(U, kappa)
+    inv = np.linalg.inv(tU)
+    return np.array([np.trace(inv @ tilde_U(Da, kappa)) for Da in D])
+
+
+def local_energy_complex(nn, W_up, W_down, kappa_up, kappa_down):
+    """E_L with its imaginary part kept (src/Hamiltonian.jl:762-778 before the real part is taken)."""
+    E = 0.0 + 0.0j
+    for (i, j) in nn:
+        a, b = i - 1, j - 1
+        E += 0.25 if (kappa_up[a] != 0) == (kappa_up[b] != 0) else -0.25
+        for x, y in ((b, a), (a, b)):
+            if kappa_up[x] != 0 and kappa_down[y] != 0:
+                E -= 0.5 * W_up[y, kappa_up[x] - 1] * W_down[x, kappa_down[y] - 1]
+    return E
+
+
+def enumerate_gradient(U_up, U_down, D_up, D_down, nn, chunk=50000):
+    """Exact E, dE/da and the SR matrix over all configurations with
+    sum(kappa_up != 0) = N_up under |psi|^2 (oracle addition).
+
+    Returns a dict with E (total energy), grad (dE/da), S (Re <O*_a O_b> -
+    Re <O*_a><O_b>) and O (<O_a>).  Configurations with log|det| below
+    LOGDET_MIN for either spin carry weight below exp(-50) relative and are
+    skipped.
+    """
+    U_up, U_down = np.asarray(U_up, complex), np.asarray(U_down, complex)
+    D_up, D_down = np.asarray(D_up, complex), np.asarray(D_down, complex)
+    N, nu = U_up.shape
+    nd = U_down.shape[1]
+    A_ = len(D_up)
+    nn0 = np.asarray(nn, dtype=np.int64) - 1
+    combos = np.array(list(itertools.combinations(range(N), nu)), dtype=np.int16)
+    ref = None
+    acc = dict(w=0.0, E=0j, O=np.zeros(A_, complex), OE=np.zeros(A_, complex), OO=np.zeros((A_, A_), complex))
+    for s in range(0, len(combos), chunk):
+        A = combos[s:s + chunk]
+        c = len(A)
+        up = np.zeros((c, N), bool)
+        up[np.arange(c)[:, None], A] = True
+        dn = ~up
+        Bd = np.nonzero(dn)[1].reshape(c, nd)
+        Uu, Ud = U_up[A], U_down[Bd]
+        _, lu = np.linalg.slogdet(Uu)
+        _, ld = np.linalg.slogdet(Ud)
+        ok = (lu > LOGDET_MIN) & (ld > LOGDET_MIN)
+        A, Bd, Uu, Ud, lu, ld, up, dn = A[ok], Bd[ok], Uu[ok], Ud[ok], lu[ok], ld[ok], up[ok], dn[ok]
+        c = len(A)
+        iu, idn = np.linalg.inv(Uu), np.linalg.inv(Ud)
+        Wu, Wd = U_up[None] @ iu, U_down[None] @ idn
+        rku = np.cumsum(up, 1) - 1
+        rkd = np.cumsum(dn, 1) - 1
+        ar = np.arange(c)
+        sz = np.where(up, 0.5, -0.5)
+        EL = np.zeros(c, complex)
+        for i, j in nn0:
+            EL += sz[:, i] * sz[:, j]
+            for a, b in ((j, i), (i, j)):
+                msk = up[:, a] & dn[:, b]
+                EL += np.where(msk, -0.5 * Wu[ar, b, rku[:, a]] * Wd[ar, a, rkd[:, b]], 0.0)
+        O = np.zeros((c, A_), complex)
+        for k in range(A_):
+            O[:, k] = np.einsum("cij,cji->c", iu, D_up[k][A]) + np.einsum("cij,cji->c", idn, D_down[k][Bd])
+        L = 2 * (lu + ld)
+        if ref is None:
+            ref = L.max()
+        p = np.exp(L - ref)
+        acc["w"] += p.sum()
+        acc["E"] += (p * EL).sum()
+        acc["O"] += (p[:, None] * O).sum(0)
+        acc["OE"] += (p[:, None] * O.conj() * EL[:, None]).sum(0)
+        acc["OO"] += np.einsum("c,ca,cb->ab", p, O.conj(), O)
+    w = acc["w"]
+    E, O, OE, OO = acc["E"] / w, acc["O"] / w, acc["OE"] / w, acc["OO"] / w
+    grad = 2 * np.real(OE - O.conj() * E)
+    S = np.real(OO - np.outer(O.conj(), O))
+    return dict(E=float(E.real), E_imag=float(E.imag), grad=grad, S=S, O=O)

@@ -9,7 +9,11 @@ Writes
                  exact basis choice.
   golden.json    exact N=24 energies by enumeration; per-configuration local
                  energies and determinant ratios at N=24/54/96 on seeded
-                 configurations; short seeded chains at N=24/54.
+                 configurations; short seeded chains at N=24/54; the exact
+                 N=24 energy, gradient and SR matrix of the extended ansatz
+                 at one parameter point (key grad_N24).
+
+    python tests/golden/make_golden.py grad_N24     # rebuilds that key only
 
 The oracle itself is pinned separately against the literal values of the
 reference's test-suite (tests/test_oracle_pins.py).
@@ -75,7 +79,30 @@ def chain_case(N, U, ham, seed=5, walkers=4, proposals=1500):
     return dict(seed=seed, proposals=proposals, refresh_every=n, measure_every=n, walkers=out)
 
 
+# A parameter point of the extended ansatz (t2, m, theta) with an open gap
+# at half filling on 2x2 doubled cells (the pi-flux shell there is degenerate).
+ALPHA_N24 = (-0.2515, 0.1215, -0.0494)
+
+
+def grad_case():
+    lat = o.double_kagome(1.0, 4, 2, (True, True), (False, True))
+    H, dH = o.ansatz_hmat(lat, ALPHA_N24)
+    Uu, Ud, Du, Dd = o.orbital_derivatives(H, dH, 12, 12)
+    nn = o.get_nn(o.hmat(lat))
+    r = o.enumerate_gradient(Uu, Ud, Du, Dd, nn)
+    return dict(alpha=list(ALPHA_N24), E_per_site=r["E"] / 24, grad_per_site=(r["grad"] / 24).tolist(),
+                S=r["S"].tolist())
+
+
 def main():
+    if sys.argv[1:] == ["grad_N24"]:
+        path = os.path.join(HERE, "golden.json")
+        g = json.load(open(path))
+        g["grad_N24"] = grad_case()
+        with open(path, "w") as f:
+            json.dump(g, f)
+        print("updated grad_N24 in", path)
+        return
     ham24, U24 = model(24)
     if not os.path.exists(os.path.join(HERE, "u_N24.npy")):
         np.save(os.path.join(HERE, "u_N24.npy"), U24)
@@ -90,6 +117,7 @@ def main():
     for N in (24, 54):
         ham, U = model(N)
         g["chains"][str(N)] = chain_case(N, U, ham)
+    g["grad_N24"] = grad_case()
     with open(os.path.join(HERE, "golden.json"), "w") as f:
         json.dump(g, f)
     print("wrote", os.path.join(HERE, "golden.json"))
