@@ -51,6 +51,7 @@ def args_():
     p.add_argument("--skip-gate", action="store_true")
     p.add_argument("--skip-e2e", action="store_true")
     p.add_argument("--no-peaks", action="store_true")
+    p.add_argument("--skip-grad", action="store_true")
     return p.parse_args()
 
 
@@ -223,6 +224,41 @@ def energy_gate(ham, kv, walkers, proposals, refresh, seed):
             "identical_chains": int(same.sum()), "max_w_drift_at_refresh": float(drift), "pass": bool(dE <= 1e-4)}
 
 
+def adjoint_run(kv, seed, device, walkers=1024, sweeps=20):
+    """The differentiation workload: 4x4 doubled cells (N=96), the pi-flux
+    ansatz extended by (t2, m, theta) drawn from `seed`, 1024 chains (complex
+    FP32 W, reference acceptance rule), one adjoint evaluation of dE/da and the
+    3x3 SR matrix per 48-proposal sweep.  Reports the adjoint kernel's time
+    against the sweep (and refresh) kernels' time per sweep."""
+    import numpy as np
+
+    alpha = kv.ansatz.draw_alpha(seed)
+    A = kv.Ansatz.build(kv.DoubleKagome(1.0, 8, 4, (True, True), (False, True)), 48, 48, *alpha)
+    eng = kv.Engine(A.ham, walkers, precision="mixed", seed=seed, refresh_interval=64, device=device)
+    eng.set_log_derivatives(A.dU_up, A.dU_down)
+    eng.init()
+    eng.sweep(960)
+    eng.reset_stats()
+    eng.enable_timing(True)
+    eng.region_start()
+    for _ in range(sweeps):
+        eng.sweep(48)
+        eng.measure_grad()
+    wall = eng.region_stop()
+    k0, _ = eng.kernel_time(0)
+    k1, _ = eng.kernel_time(1)
+    k2, n2 = eng.kernel_time(2)
+    res = kv.estimate(eng.grad_sums(), 3)
+    eng.close()
+    return {"workload": "kagome VMC, 4x4 doubled cells (N=96), extended ansatz (t2, m, theta) drawn from seed "
+                        f"{seed}, {walkers} chains, mixed complex FP32 W, 48 proposals + 1 adjoint per sweep",
+            "alpha": list(alpha), "sweeps": sweeps,
+            "sweep_ms_per_sweep": (k0 + k1) / sweeps, "adjoint_ms_per_sweep": k2 / sweeps,
+            "adjoint_over_sweep": k2 / (k0 + k1) if k0 + k1 > 0 else None, "target_ratio": 2.0,
+            "wall_ms": wall, "E_per_site": res["E"] / 96, "grad_per_site": (res["grad"] / 96).tolist(),
+            "se_grad_per_site": (np.asarray(res["se_grad"]) / 96).tolist(), "S": res["S"].tolist()}
+
+
 def gpu_arm(a):
     import numpy as np
 
@@ -310,6 +346,7 @@ def gpu_arm(a):
         plain = {"value": ptot["accepted"] / (pms * 1e-3), "unit": UNIT, "ms": pms,
                  "moves_per_walker": 128, "accepted": ptot["accepted"]}
     gate = None if a.skip_gate else energy_gate(ham, kv, 256, 8192, a.refresh, a.seed + 1)
+    adjoint = None if a.skip_grad else adjoint_run(kv, 4, local)
 
     # roofline of the dominant kernel
     refreshes = tot["refreshes"]
@@ -363,7 +400,7 @@ def gpu_arm(a):
             "proposals_per_step": tot["proposals"] / a.steps * world, "acceptance": tot["accepted"] / tot["proposals"],
             "gpu_launches": tot["launches"], "e2e": e2e, "roofline": roof, "cpu_baseline": cpu,
             "plain_fp64": plain, "speedup_vs_plain_fp64": (value / plain["value"]) if plain else None,
-            "energy_gate": gate, "drift": drift, "clocks": clk, "peaks_measured": peaks}
+            "energy_gate": gate, "adjoint": adjoint, "drift": drift, "clocks": clk, "peaks_measured": peaks}
     print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
