@@ -5,10 +5,12 @@ Workload (the headline configuration): 6x6 doubled kagome cells (N=216,
 n_up = n_down = 108), pi-flux parton orbitals, the reference's acceptance
 rule, 2048 independent walkers from seeded random starts.  One step = every
 walker makes `--moves` accepted exchange moves (kvmc_advance; local energy
-every 108 proposals), with W refreshed in FP64 every `--refresh` accepted
-moves (mixed form) or every 108 proposals (plain FP64 form).  The walkers'
-FP32 W state (2048 x 186.6 KB = 382 MB) is larger than L2, so no flush is
-needed between steps.
+every 108 proposals), with W refreshed in FP64 every R accepted moves (mixed
+form) or every 108 proposals (plain FP64 form).  The mixed form's settings
+(where W lives, delayed-update depth k, R, threads per walker) are the
+autotuner's choice for this workload on a GB300 (kagomevmc/tuned.json);
+flags override them.  The walkers' FP32 W state (2048 x 186.6 KB = 382 MB)
+is larger than L2, so no flush is needed between steps.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
@@ -44,7 +46,10 @@ def args_():
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--walkers", type=int, default=2048)
     p.add_argument("--moves", type=int, default=1024, help="accepted moves per walker per step")
-    p.add_argument("--refresh", type=int, default=1024, help="mixed form: accepted moves between FP64 refreshes")
+    p.add_argument("--refresh", type=int, default=None, help="mixed form: accepted moves between FP64 refreshes")
+    p.add_argument("--delay-k", type=int, default=None)
+    p.add_argument("--placement", default=None, choices=["auto", "chip", "hbm"])
+    p.add_argument("--threads", type=int, default=None, help="threads per walker with W in HBM")
     p.add_argument("--seed", type=int, default=2024)
     p.add_argument("--skip-plain", action="store_true")
     p.add_argument("--skip-cpu", action="store_true")
@@ -52,6 +57,7 @@ def args_():
     p.add_argument("--skip-e2e", action="store_true")
     p.add_argument("--no-peaks", action="store_true")
     p.add_argument("--skip-grad", action="store_true")
+    p.add_argument("--skip-uneven", action="store_true")
     return p.parse_args()
 
 
@@ -205,13 +211,35 @@ def run_steps(eng, steps, moves):
     return tot
 
 
-def energy_gate(ham, kv, walkers, proposals, refresh, seed):
+def mixed_choice(kv, ham, a):
+    """The autotuner's cached choice for this workload, with flag overrides."""
+    from kagomevmc import autotune
+
+    ch = autotune.lookup(ham, a.walkers) or autotune.Choice(delay_k=0, refresh_interval=1024, placement="auto")
+    if a.refresh is not None:
+        ch.refresh_interval = a.refresh
+    if a.delay_k is not None:
+        ch.delay_k = a.delay_k
+    if a.placement is not None:
+        ch.placement = a.placement
+    if a.threads is not None:
+        ch.threads = a.threads
+    ch.trials = []
+    return ch
+
+
+def energy_gate(ham, kv, walkers, proposals, choice, seed):
     """Both forms on identical walkers and proposal streams: |dE/N| over walkers whose chains agree."""
     import numpy as np
 
+    from kagomevmc import autotune
+
     res = {}
     for prec in ("plain", "mixed"):
-        eng = kv.Engine(ham, walkers, precision=prec, seed=seed, refresh_interval=(refresh if prec == "mixed" else 0))
+        if prec == "mixed":
+            eng = autotune.make_engine(ham, walkers, choice, seed=seed)
+        else:
+            eng = kv.Engine(ham, walkers, precision="plain", seed=seed)
         eng.init()
         st = eng.sweep(proposals)
         ws = eng.walker_stats()
@@ -259,6 +287,53 @@ def adjoint_run(kv, seed, device, walkers=1024, sweeps=20):
             "se_grad_per_site": (np.asarray(res["se_grad"]) / 96).tolist(), "S": res["S"].tolist()}
 
 
+def uneven_run(kv, seed, device, moves=512, steps=3):
+    """The uneven batch: 1024 chains at 3x3 doubled cells (N=54), 768 at 6x6
+    (N=216) and 256 at 8x8 (N=384), each class with the autotuner's settings,
+    advanced together by one captured CUDA graph per step (kvmc_group), and
+    the same three classes advanced one after another for comparison."""
+    from kagomevmc import autotune
+
+    cells = {54: (3, 3), 216: (6, 6), 384: (8, 8)}
+    classes = [(54, 1024), (216, 768), (384, 256)]
+    res = {}
+    for mode in ("graph", "sequential"):
+        engines, choices = [], []
+        for N, walkers in classes:
+            a_, b_ = cells[N]
+            ham = kv.Hamiltonian.build(N // 2, N // 2, kv.DoubleKagome(1.0, 2 * a_, b_, (True, True), (False, True)))
+            ch = autotune.lookup(ham, walkers) or autotune.Choice(delay_k=0, refresh_interval=1024, placement="auto")
+            eng = autotune.make_engine(ham, walkers, ch, seed=seed + N, device=device)
+            eng.init()
+            engines.append(eng)
+            choices.append(dict(N=N, walkers=walkers, delay_k=eng.config()["delay_k"],
+                                refresh_interval=ch.refresh_interval, placement=ch.placement, threads=ch.threads))
+        acc, ms_tot = 0, 0.0
+        if mode == "graph":
+            g = kv.Group(engines)
+            g.advance(moves)  # warm-up, captures the graph
+            for _ in range(steps):
+                st, ms = g.advance(moves)
+                acc += sum(x["accepted"] for x in st)
+                ms_tot += ms
+            g.close()
+        else:
+            for e in engines:
+                e.advance(moves)
+            engines[0].region_start()
+            for _ in range(steps):
+                for e in engines:
+                    acc += e.advance(moves)["accepted"]
+            ms_tot = engines[0].region_stop()
+        for e in engines:
+            e.close()
+        res[mode] = {"value": acc / (ms_tot * 1e-3), "ms": ms_tot, "accepted": acc}
+    return {"workload": "1024 x N=54 + 768 x N=216 + 256 x N=384 walkers, reference rule, "
+                        f"{moves} accepted moves per walker per step, {steps} steps", "unit": UNIT,
+            "classes": choices, "graph": res["graph"], "sequential": res["sequential"],
+            "graph_over_sequential": res["graph"]["value"] / res["sequential"]["value"]}
+
+
 def gpu_arm(a):
     import numpy as np
 
@@ -282,8 +357,11 @@ def gpu_arm(a):
     peaks = measure_peaks(local) if (rank == 0 and not a.no_peaks) else {}
     from kagomevmc import replicas
 
-    eng = kv.Engine(ham, a.walkers, precision="mixed", seed=replicas.replica_seed(a.seed, rank),
-                    refresh_interval=a.refresh, device=local)
+    from kagomevmc import autotune
+
+    choice = mixed_choice(kv, ham, a)
+    eng = autotune.make_engine(ham, a.walkers, choice, seed=replicas.replica_seed(a.seed, rank), device=local)
+    cfg = eng.config()
     eng.init()
     run_steps(eng, a.warmup, a.moves)
     eng.enable_timing(True)
@@ -345,8 +423,9 @@ def gpu_arm(a):
         pe.close()
         plain = {"value": ptot["accepted"] / (pms * 1e-3), "unit": UNIT, "ms": pms,
                  "moves_per_walker": 128, "accepted": ptot["accepted"]}
-    gate = None if a.skip_gate else energy_gate(ham, kv, 256, 8192, a.refresh, a.seed + 1)
+    gate = None if a.skip_gate else energy_gate(ham, kv, 256, 8192, choice, a.seed + 1)
     adjoint = None if a.skip_grad else adjoint_run(kv, 4, local)
+    uneven = None if a.skip_uneven else uneven_run(kv, a.seed, local)
 
     # roofline of the dominant kernel
     refreshes = tot["refreshes"]
@@ -371,7 +450,8 @@ def gpu_arm(a):
     if os.path.exists(tfile):
         tj = json.load(open(tfile))
         if dom == "sweep_mixed" and kern[dom]["launches"]:
-            traffic = tj["sweep_mixed"]["bytes_per_walker_launch"] * a.walkers * a.steps / kern[dom]["launches"]
+            key = "sweep_mixed" if cfg["w_on_chip"] else "sweep_mixed_hbm"
+            traffic = tj[key]["bytes_per_walker_launch"] * a.walkers * a.steps / kern[dom]["launches"]
         elif dom == "refresh_fp64" and kern[dom]["launches"]:
             traffic = tj["refresh_fp64"]["bytes_per_walker_spin"] * 2 * refreshes / kern[dom]["launches"]
     ach = kern[dom]["achieved_tflops"]
@@ -395,12 +475,15 @@ def gpu_arm(a):
             "dtype": "f32 (W, ratios, rank-1) + f64 (refresh, energy sums)", "data": "synthetic (seeded random starts)",
             "config": {"workload": "kagome VMC, 6x6 doubled cells (N=216), pi-flux partons, reference acceptance rule",
                        "walkers_per_gpu": a.walkers, "accepted_moves_per_walker_per_step": a.moves,
-                       "refresh_every_accepted": a.refresh, "measure_every_proposals": n,
+                       "refresh_every_accepted": cfg["refresh_interval"], "measure_every_proposals": n,
+                       "delay_k": cfg["delay_k"], "w_on_chip": cfg["w_on_chip"],
+                       "threads_per_walker": (choice.threads if not cfg["w_on_chip"] else 512),
+                       "settings_from": "autotuner cache kagomevmc/tuned.json (GB300), flags override",
                        "parallelism": f"replicas x{world}", "l2": "inputs larger than L2 (W state 382 MB per GPU)"},
             "proposals_per_step": tot["proposals"] / a.steps * world, "acceptance": tot["accepted"] / tot["proposals"],
             "gpu_launches": tot["launches"], "e2e": e2e, "roofline": roof, "cpu_baseline": cpu,
             "plain_fp64": plain, "speedup_vs_plain_fp64": (value / plain["value"]) if plain else None,
-            "energy_gate": gate, "adjoint": adjoint, "drift": drift, "clocks": clk, "peaks_measured": peaks}
+            "energy_gate": gate, "adjoint": adjoint, "uneven_batch": uneven, "drift": drift, "clocks": clk, "peaks_measured": peaks}
     print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()

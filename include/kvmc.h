@@ -33,7 +33,7 @@ extern "C" {
 #define KVMC_API
 #endif
 
-#define KVMC_ABI_VERSION 2
+#define KVMC_ABI_VERSION 3
 
 enum kvmc_status {
     KVMC_OK = 0,
@@ -51,6 +51,16 @@ enum kvmc_precision {
                             refresh every refresh_interval proposals */
     KVMC_MIXED_FP32 = 1  /* FP32 W resident in shared memory, FP64 refresh every
                             refresh_interval accepted moves, FP64 energy sums */
+};
+
+/* Where the mixed form keeps each walker's FP32 W.  On chip, one walker
+ * owns an SM's shared memory for its launch (fits up to N = 216).  In HBM,
+ * only the delayed-update factors P, Q are on chip, so several walkers share
+ * an SM, and the rank-k flush streams W through once per k moves. */
+enum kvmc_w_placement {
+    KVMC_W_AUTO = 0,    /* on chip when it fits, else HBM */
+    KVMC_W_ON_CHIP = 1,
+    KVMC_W_HBM = 2
 };
 
 enum kvmc_accept {
@@ -149,6 +159,7 @@ typedef struct {
                                  1 = a rank-1 update per accepted move */
     int32_t device;           /* CUDA device ordinal */
     uint64_t seed;            /* Philox4x32-10 key for proposals and seeded starts */
+    int32_t w_placement;      /* mixed form, enum kvmc_w_placement */
 } kvmc_batch_desc;
 
 typedef struct kvmc_handle kvmc_handle;
@@ -261,6 +272,12 @@ KVMC_API int kvmc_set_drift_tolerance(kvmc_handle *h, double tol);
 KVMC_API int kvmc_enable_timing(kvmc_handle *h, int32_t on);
 KVMC_API int kvmc_kernel_time(kvmc_handle *h, int32_t kind, double *total_ms, int64_t *launches);
 
+/* Launch-shape knobs the autotuner sets (kagomevmc.autotune):
+ *   KVMC_TUNE_STREAM_THREADS: threads per walker's CTA when W is in HBM,
+ *   128 (four walkers per SM) or 256 (two walkers per SM, the default). */
+enum kvmc_tuning { KVMC_TUNE_STREAM_THREADS = 1 };
+KVMC_API int kvmc_set_tuning(kvmc_handle *h, int32_t key, int32_t value);
+
 /* The settings a handle resolved at creation: refresh and measurement
  * intervals, delayed-update depth, and whether W is staged on chip. */
 KVMC_API int kvmc_get_config(kvmc_handle *h, int32_t *refresh_interval, int32_t *measure_interval,
@@ -300,6 +317,23 @@ KVMC_API int kvmc_region_timer(kvmc_handle *h, int32_t start, double *ms);
  * start at zero, since every element a call reads it first writes. */
 KVMC_API int kvmc_refresh_static(int32_t n_sites, int32_t n_orb, int32_t batch, const double *U,
                                  const int32_t *kappa, double *W, double *logdet, void *stream);
+
+/* ---- groups: walkers of different lattice sizes in one graph launch -----
+ * No reference counterpart (the reference runs one chain per Carlo task).
+ * A group advances several handles -- typically one per lattice size, each
+ * with its own delayed-update depth and refresh interval -- together: one
+ * captured CUDA graph forks into every handle's stream, runs its
+ * (sweep, refresh) launches concurrently with the others, and joins.  The
+ * graph is captured on the first call and reused while the handles' settings
+ * do not change.  Handles keep working on their own between group calls. */
+typedef struct kvmc_group kvmc_group;
+KVMC_API int kvmc_group_create(kvmc_handle *const *handles, int32_t n, kvmc_group **out);
+KVMC_API int kvmc_group_destroy(kvmc_group *g);
+/* Every walker of every handle makes moves_per_walker more accepted moves.
+ * stats: [n] per-handle statistics (may be NULL); ms: device time of the
+ * graph launches (may be NULL). */
+KVMC_API int kvmc_group_advance(kvmc_group *g, int64_t moves_per_walker, kvmc_sweep_stats *stats, double *ms);
+KVMC_API int kvmc_group_last_error(const kvmc_group *g, char *buf, size_t len);
 
 /* ---- adjoint gradient over ansatz parameters ---------------------------
  * No reference counterpart (the reference measures the energy only).  For P

@@ -51,6 +51,7 @@ struct kvmc_handle {
     int measure_every = 0;
     int delay_k = 1;  // mixed form: 1 = rank-1 updates, 4/8/12/16 = delayed-update depth
     float drift_tol = 1e-4f;  // delayed form: early refresh past this unit-row deviation
+    int stream_threads = 256;  // W in HBM: threads per walker
     std::string err;
 
     DevModel dm{};
@@ -689,24 +690,37 @@ extern "C" int kvmc_create(const kvmc_model_desc *model, const kvmc_batch_desc *
                                : kvmc::refresh_needs_large(m) ? kvmc::refresh_large_smem(m) : kvmc::refresh_smem(m);
     if ((size_t)optin < rsm + 1024)
         return bail(h->fail(KVMC_ERR_UNSUPPORTED, "refresh needs %zu B shared memory, device offers %d", rsm, optin));
-    h->smem_w = h->mixed && !h->cplx && kvmc::mixed_sweep_smem(m) <= (size_t)optin;
+    // where the mixed form keeps W: on chip when it fits (or when asked), else in HBM
+    const int place = batch->w_placement;
+    if (place < KVMC_W_AUTO || place > KVMC_W_HBM)
+        return bail(h->fail(KVMC_ERR_ARGUMENT, "w_placement must be 0, 1 or 2 (got %d)", place));
+    const bool fits = h->mixed && !h->cplx && kvmc::mixed_sweep_smem(m) <= (size_t)optin;
+    if (place == KVMC_W_ON_CHIP && !fits)
+        return bail(h->fail(KVMC_ERR_UNSUPPORTED, "W cannot be kept on chip for this model and precision"));
+    h->smem_w = fits && place != KVMC_W_HBM;
     if (h->cplx && batch->delay_k != 0 && batch->delay_k != 1)
         return bail(h->fail(KVMC_ERR_UNSUPPORTED, "complex orbitals use rank-1 updates: delay_k must be 0 or 1 (got %d)",
                             batch->delay_k));
     // delayed-update depth: 0 = the largest depth whose working set fits on chip
+    // (W with P and Q when W is on chip; P and Q alone when W is in HBM)
     const size_t budget = (size_t)optin - 1024;  // leave room for the kernel's static shared memory
-    if (h->mixed && h->smem_w) {
+    if (h->mixed && !h->cplx) {
         const int want = batch->delay_k;
+        const bool on = h->smem_w;
+        // the flush gives each thread four columns: the HBM form (256 threads) needs ld <= 1024
+        const bool can_delay = on || std::max(h->ld_up, h->ld_dn) <= 1024;
         if (want == 0) {
             h->delay_k = 1;
             for (int k : {16, 12, 8, 4})
-                if (kvmc::delayed_smem_bytes(m, k) <= budget) { h->delay_k = k; break; }
+                if (can_delay && kvmc::delayed_smem_bytes(m, k, on) <= budget) { h->delay_k = k; break; }
         } else if (want == 1) {
             h->delay_k = 1;
+        } else if ((want == 4 || want == 8 || want == 12 || want == 16) && !can_delay) {
+            return bail(h->fail(KVMC_ERR_UNSUPPORTED, "delayed updates with W in HBM support at most 1024 orbitals per spin"));
         } else if (want == 4 || want == 8 || want == 12 || want == 16) {
-            if (kvmc::delayed_smem_bytes(m, want) > budget)
+            if (kvmc::delayed_smem_bytes(m, want, on) > budget)
                 return bail(h->fail(KVMC_ERR_UNSUPPORTED, "delay_k=%d needs %zu B shared memory (device offers %d)", want,
-                                    kvmc::delayed_smem_bytes(m, want), optin));
+                                    kvmc::delayed_smem_bytes(m, want, on), optin));
             h->delay_k = want;
         } else {
             return bail(h->fail(KVMC_ERR_ARGUMENT, "delay_k must be 0, 1, 4, 8, 12 or 16 (got %d)", want));
@@ -873,8 +887,104 @@ int snapshot(kvmc_handle *h, Snapshot &s) {
 }  // namespace
 
 namespace {
-int run_sweep(kvmc_handle *h, int64_t proposals_per_walker, int64_t moves_per_walker, kvmc_sweep_stats *stats);
+
+kvmc::SweepParams sweep_params(const kvmc_handle *h) {
+    kvmc::SweepParams p{};
+    p.seed = h->batch.seed;
+    p.accept_rule = h->batch.accept_rule;
+    p.refresh_every = h->refresh_every;
+    p.measure_every = h->measure_every;
+    p.delay_k = h->delay_k;
+    p.drift_tol = h->drift_tol;
+    p.stream_threads = h->stream_threads;
+    return p;
 }
+
+// The accounting around one kvmc_sweep / kvmc_advance call.
+struct SweepCall {
+    Snapshot before;
+    unsigned long long ref0 = 0;
+    int launches = 1;
+};
+
+int sweep_begin(kvmc_handle *h, int64_t proposals_per_walker, int64_t moves_per_walker, bool stats, SweepCall &c) {
+    KV_TRY(set_device(h));
+    if (stats) {
+        KV_TRY(snapshot(h, c.before));
+        KV_TRY(h->cuda(cudaMemcpy(&c.ref0, h->db.refresh_count, 8, cudaMemcpyDeviceToHost), "refresh count"));
+    }
+    KV_TRY(h->cuda(kvmc::launch_set_tend(h->db, proposals_per_walker, moves_per_walker, h->stream), "set t_end"));
+    return h->cuda(cudaMemsetAsync(h->db.drift, 0, sizeof(float) * h->n_walkers, h->stream), "memset");
+}
+
+// `pairs` (sweep, refresh) launches on the handle's stream; walkers that are
+// done return at once.  d_active counts the walkers the last sweep left short.
+int enqueue_pairs(kvmc_handle *h, const kvmc::SweepParams &p, int pairs, bool timed_launches) {
+    for (int g = 0; g < pairs; ++g) {
+        KV_TRY(h->cuda(cudaMemsetAsync(h->d_active, 0, sizeof(int), h->stream), "memset"));
+        if (timed_launches) {
+            KV_TRY(timed(h, 0, [&] { return sweep_launch(h, p); }, "sweep launch"));
+            KV_TRY(timed(h, 1, [&] { return refresh_launch(h, 1, h->mixed ? 1 : 0); }, "refresh launch"));
+        } else {
+            KV_TRY(h->cuda(sweep_launch(h, p), "sweep launch"));
+            KV_TRY(h->cuda(refresh_launch(h, 1, h->mixed ? 1 : 0), "refresh launch"));
+        }
+    }
+    return KVMC_OK;
+}
+
+int sweep_end(kvmc_handle *h, kvmc_sweep_stats *stats, SweepCall &c) {
+    int bad = 0;
+    KV_TRY(check_status(h, &bad));
+    if (!stats) return KVMC_OK;
+    std::memset(stats, 0, sizeof *stats);
+    Snapshot after;
+    KV_TRY(snapshot(h, after));
+    for (int w = 0; w < h->n_walkers; ++w) {
+        stats->proposals += after.prop[w] - c.before.prop[w];
+        stats->accepted += after.acc[w] - c.before.acc[w];
+        stats->measurements += after.nm[w] - c.before.nm[w];
+        stats->sum_energy += after.se[w] - c.before.se[w];
+        stats->sum_energy2 += after.se2[w] - c.before.se2[w];
+    }
+    std::vector<float> dr(h->n_walkers);
+    KV_TRY(h->cuda(cudaMemcpy(dr.data(), h->db.drift, dr.size() * 4, cudaMemcpyDeviceToHost), "drift"));
+    double md = 0;
+    for (float d : dr) md = std::max(md, (double)d);
+    stats->max_drift = md;
+    stats->bad_walkers = bad;
+    stats->launches = c.launches;
+    unsigned long long ref1 = 0;
+    KV_TRY(h->cuda(cudaMemcpy(&ref1, h->db.refresh_count, 8, cudaMemcpyDeviceToHost), "refresh count"));
+    stats->refreshes = (int64_t)(ref1 - c.ref0);
+    return KVMC_OK;
+}
+
+int run_sweep(kvmc_handle *h, int64_t proposals_per_walker, int64_t moves_per_walker, kvmc_sweep_stats *stats) {
+    SweepCall c;
+    if (proposals_per_walker == 0 && moves_per_walker == 0) {
+        KV_TRY(set_device(h));
+        if (stats) std::memset(stats, 0, sizeof *stats);
+        return KVMC_OK;
+    }
+    KV_TRY(sweep_begin(h, proposals_per_walker, moves_per_walker, stats != nullptr, c));
+    const kvmc::SweepParams p = sweep_params(h);
+    // Between host checks the loop issues a group of (sweep, refresh) pairs.
+    const int group = h->mixed ? 4 : 8;
+    for (int iter = 0;; iter += group) {
+        KV_TRY(enqueue_pairs(h, p, group, true));
+        c.launches += 2 * group;
+        int active = 0;
+        KV_TRY(h->cuda(cudaMemcpyAsync(&active, h->d_active, sizeof(int), cudaMemcpyDeviceToHost, h->stream), "active"));
+        KV_TRY(h->cuda(cudaStreamSynchronize(h->stream), "sweep"));
+        KV_TRY(collect_timing(h));
+        if (active == 0) break;
+        if (iter > 100000000) return h->fail(KVMC_ERR_NUMERIC, "sweep made no progress");
+    }
+    return sweep_end(h, stats, c);
+}
+
+}  // namespace
 
 extern "C" int kvmc_sweep(kvmc_handle *h, int64_t proposals_per_walker, kvmc_sweep_stats *stats) {
     if (!h) return fail_global(KVMC_ERR_ARGUMENT, "null handle");
@@ -888,69 +998,186 @@ extern "C" int kvmc_advance(kvmc_handle *h, int64_t moves_per_walker, kvmc_sweep
     return run_sweep(h, 0, moves_per_walker, stats);
 }
 
+// ===========================================================================
+// Groups: handles of different sizes advanced together by one CUDA graph
+// ===========================================================================
+
+struct kvmc_group {
+    std::vector<kvmc_handle *> hs;
+    int device = 0;
+    cudaStream_t s0 = nullptr;
+    cudaEvent_t fork = nullptr;
+    std::vector<cudaEvent_t> ready, join;
+    cudaEvent_t t0 = nullptr, t1 = nullptr;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    std::vector<int> pairs;                  // (sweep, refresh) pairs per handle in the graph
+    std::vector<kvmc::SweepParams> params;   // the parameters the graph was captured with
+    int graph_launches = 0;                  // kernels in one graph launch
+    std::string err;
+    int fail(int code, const char *fmt, ...) {
+        char buf[512];
+        va_list ap;
+        va_start(ap, fmt);
+        vsnprintf(buf, sizeof buf, fmt, ap);
+        va_end(ap);
+        err = buf;
+        g_last_error = buf;
+        return code;
+    }
+    int cuda(cudaError_t e, const char *what) {
+        if (e == cudaSuccess) return KVMC_OK;
+        return fail(KVMC_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+    }
+};
+
+extern "C" int kvmc_group_destroy(kvmc_group *g) {
+    if (!g) return KVMC_OK;
+    cudaSetDevice(g->device);
+    if (g->s0) cudaStreamSynchronize(g->s0);
+    if (g->exec) cudaGraphExecDestroy(g->exec);
+    if (g->graph) cudaGraphDestroy(g->graph);
+    for (auto e : g->ready) if (e) cudaEventDestroy(e);
+    for (auto e : g->join) if (e) cudaEventDestroy(e);
+    for (auto e : {g->fork, g->t0, g->t1}) if (e) cudaEventDestroy(e);
+    if (g->s0) cudaStreamDestroy(g->s0);
+    delete g;
+    return KVMC_OK;
+}
+
+extern "C" int kvmc_group_create(kvmc_handle *const *handles, int32_t n, kvmc_group **out) {
+    if (!handles || !out || n < 1 || n > 64) return fail_global(KVMC_ERR_ARGUMENT, "need 1..64 handles");
+    *out = nullptr;
+    for (int i = 0; i < n; ++i) {
+        if (!handles[i]) return fail_global(KVMC_ERR_ARGUMENT, "handle %d is null", i);
+        if (handles[i]->device != handles[0]->device)
+            return fail_global(KVMC_ERR_ARGUMENT, "handles of a group must share one device");
+        for (int j = 0; j < i; ++j)
+            if (handles[j] == handles[i]) return fail_global(KVMC_ERR_ARGUMENT, "handle %d appears twice", i);
+    }
+    kvmc_group *g = new kvmc_group();
+    g->hs.assign(handles, handles + n);
+    g->device = handles[0]->device;
+    auto bail = [&](int rc) { kvmc_group_destroy(g); return rc; };
+    if (int rc = g->cuda(cudaSetDevice(g->device), "cudaSetDevice")) return bail(rc);
+    if (int rc = g->cuda(cudaStreamCreateWithFlags(&g->s0, cudaStreamNonBlocking), "stream")) return bail(rc);
+    g->ready.assign(n, nullptr);
+    g->join.assign(n, nullptr);
+    for (auto *e : {&g->fork, &g->t0, &g->t1})
+        if (int rc = g->cuda(cudaEventCreate(e), "event")) return bail(rc);
+    for (int i = 0; i < n; ++i) {
+        if (int rc = g->cuda(cudaEventCreateWithFlags(&g->ready[i], cudaEventDisableTiming), "event")) return bail(rc);
+        if (int rc = g->cuda(cudaEventCreateWithFlags(&g->join[i], cudaEventDisableTiming), "event")) return bail(rc);
+    }
+    *out = g;
+    return KVMC_OK;
+}
+
 namespace {
-int run_sweep(kvmc_handle *h, int64_t proposals_per_walker, int64_t moves_per_walker, kvmc_sweep_stats *stats) {
-    KV_TRY(set_device(h));
-    Snapshot before;
-    unsigned long long ref0 = 0, ref1 = 0;
-    if (stats) {
-        KV_TRY(snapshot(h, before));
-        std::memset(stats, 0, sizeof *stats);
-        KV_TRY(h->cuda(cudaMemcpy(&ref0, h->db.refresh_count, 8, cudaMemcpyDeviceToHost), "refresh count"));
-    }
-    if (proposals_per_walker == 0 && moves_per_walker == 0) return KVMC_OK;
-    kvmc::SweepParams p{};
-    p.seed = h->batch.seed;
-    p.accept_rule = h->batch.accept_rule;
-    p.refresh_every = h->refresh_every;
-    p.measure_every = h->measure_every;
-    p.delay_k = h->delay_k;
-    p.drift_tol = h->drift_tol;
-    KV_TRY(h->cuda(kvmc::launch_set_tend(h->db, proposals_per_walker, moves_per_walker, h->stream), "set t_end"));
-    KV_TRY(h->cuda(cudaMemsetAsync(h->db.drift, 0, sizeof(float) * h->n_walkers, h->stream), "memset"));
-    int launches = 1;
-    // Between host checks the loop issues a group of (sweep, refresh) pairs;
-    // walkers that are done return at once.
-    const int group = h->mixed ? 4 : 8;
-    for (int iter = 0;; iter += group) {
-        for (int g = 0; g < group; ++g) {
-            KV_TRY(h->cuda(cudaMemsetAsync(h->d_active, 0, sizeof(int), h->stream), "memset"));
-            KV_TRY(timed(h, 0, [&] { return sweep_launch(h, p); }, "sweep launch"));
-            KV_TRY(timed(h, 1, [&] { return refresh_launch(h, 1, h->mixed ? 1 : 0); }, "refresh launch"));
-            launches += 2;
+
+bool same_params(const kvmc::SweepParams &a, const kvmc::SweepParams &b) {
+    return a.seed == b.seed && a.accept_rule == b.accept_rule && a.refresh_every == b.refresh_every &&
+           a.measure_every == b.measure_every && a.delay_k == b.delay_k && a.drift_tol == b.drift_tol &&
+           a.stream_threads == b.stream_threads;
+}
+
+// Captures one graph: from s0, every handle's stream runs its (sweep,
+// refresh) pairs concurrently with the others, then s0 joins them all.
+int group_capture(kvmc_group *g, const std::vector<int> &pairs) {
+    std::vector<kvmc::SweepParams> params;
+    for (auto *h : g->hs) params.push_back(sweep_params(h));
+    bool same = g->exec && pairs == g->pairs;
+    for (size_t i = 0; same && i < params.size(); ++i) same = same_params(params[i], g->params[i]);
+    if (same) return KVMC_OK;
+    if (g->exec) { cudaGraphExecDestroy(g->exec); g->exec = nullptr; }
+    if (g->graph) { cudaGraphDestroy(g->graph); g->graph = nullptr; }
+    KV_TRY(g->cuda(cudaStreamBeginCapture(g->s0, cudaStreamCaptureModeRelaxed), "begin capture"));
+    int rc = g->cuda(cudaEventRecord(g->fork, g->s0), "event");
+    int launches = 0;
+    for (size_t i = 0; i < g->hs.size() && rc == KVMC_OK; ++i) {
+        kvmc_handle *h = g->hs[i];
+        rc = g->cuda(cudaStreamWaitEvent(h->stream, g->fork, 0), "wait");
+        if (rc == KVMC_OK) {
+            rc = enqueue_pairs(h, params[i], pairs[i], false);
+            if (rc != KVMC_OK) g->err = h->err;
         }
-        int active = 0;
-        KV_TRY(h->cuda(cudaMemcpyAsync(&active, h->d_active, sizeof(int), cudaMemcpyDeviceToHost, h->stream), "active"));
-        KV_TRY(h->cuda(cudaStreamSynchronize(h->stream), "sweep"));
-        KV_TRY(collect_timing(h));
-        if (active == 0) break;
-        if (iter > 100000000) return h->fail(KVMC_ERR_NUMERIC, "sweep made no progress");
+        if (rc == KVMC_OK) rc = g->cuda(cudaEventRecord(g->join[i], h->stream), "event");
+        if (rc == KVMC_OK) rc = g->cuda(cudaStreamWaitEvent(g->s0, g->join[i], 0), "wait");
+        launches += 2 * pairs[i];
     }
-    int bad = 0;
-    KV_TRY(check_status(h, &bad));
-    if (stats) {
-        Snapshot after;
-        KV_TRY(snapshot(h, after));
-        for (int w = 0; w < h->n_walkers; ++w) {
-            stats->proposals += after.prop[w] - before.prop[w];
-            stats->accepted += after.acc[w] - before.acc[w];
-            stats->measurements += after.nm[w] - before.nm[w];
-            stats->sum_energy += after.se[w] - before.se[w];
-            stats->sum_energy2 += after.se2[w] - before.se2[w];
+    cudaGraph_t graph = nullptr;
+    const cudaError_t e = cudaStreamEndCapture(g->s0, &graph);
+    if (rc != KVMC_OK) {
+        if (graph) cudaGraphDestroy(graph);
+        return rc;
+    }
+    KV_TRY(g->cuda(e, "end capture"));
+    g->graph = graph;
+    KV_TRY(g->cuda(cudaGraphInstantiate(&g->exec, g->graph, 0), "graph instantiate"));
+    g->pairs = pairs;
+    g->params = params;
+    g->graph_launches = launches;
+    return KVMC_OK;
+}
+
+}  // namespace
+
+extern "C" int kvmc_group_advance(kvmc_group *g, int64_t moves_per_walker, kvmc_sweep_stats *stats, double *ms) {
+    if (!g) return fail_global(KVMC_ERR_ARGUMENT, "null group");
+    if (moves_per_walker < 0) return g->fail(KVMC_ERR_ARGUMENT, "moves_per_walker must be >= 0");
+    KV_TRY(g->cuda(cudaSetDevice(g->device), "cudaSetDevice"));
+    const size_t n = g->hs.size();
+    std::vector<SweepCall> calls(n);
+    std::vector<int> pairs(n);
+    for (size_t i = 0; i < n; ++i) {
+        kvmc_handle *h = g->hs[i];
+        if (int rc = sweep_begin(h, 0, moves_per_walker, stats != nullptr, calls[i])) { g->err = h->err; return rc; }
+        // enough pairs for every walker to reach its target in one graph launch when no early refresh intervenes
+        const int R = h->mixed ? std::max(h->refresh_every, 1) : 1;
+        pairs[i] = h->mixed ? (int)std::min<int64_t>(64, moves_per_walker / R + 2) : 8;
+    }
+    KV_TRY(group_capture(g, pairs));
+    // the graph runs after what each handle's stream already holds
+    for (size_t i = 0; i < n; ++i) {
+        KV_TRY(g->cuda(cudaEventRecord(g->ready[i], g->hs[i]->stream), "event"));
+        KV_TRY(g->cuda(cudaStreamWaitEvent(g->s0, g->ready[i], 0), "wait"));
+    }
+    KV_TRY(g->cuda(cudaEventRecord(g->t0, g->s0), "event"));
+    int launches = 0;
+    for (int iter = 0;; ++iter) {
+        KV_TRY(g->cuda(cudaGraphLaunch(g->exec, g->s0), "graph launch"));
+        launches += g->graph_launches;
+        KV_TRY(g->cuda(cudaStreamSynchronize(g->s0), "graph"));
+        int any = 0;
+        for (size_t i = 0; i < n; ++i) {
+            int a = 0;
+            KV_TRY(g->cuda(cudaMemcpy(&a, g->hs[i]->d_active, sizeof(int), cudaMemcpyDeviceToHost), "active"));
+            any += a;
         }
-        std::vector<float> dr(h->n_walkers);
-        KV_TRY(h->cuda(cudaMemcpy(dr.data(), h->db.drift, dr.size() * 4, cudaMemcpyDeviceToHost), "drift"));
-        double md = 0;
-        for (float d : dr) md = std::max(md, (double)d);
-        stats->max_drift = md;
-        stats->bad_walkers = bad;
-        stats->launches = launches;
-        KV_TRY(h->cuda(cudaMemcpy(&ref1, h->db.refresh_count, 8, cudaMemcpyDeviceToHost), "refresh count"));
-        stats->refreshes = (int64_t)(ref1 - ref0);
+        if (any == 0) break;
+        if (iter > 1000000) return g->fail(KVMC_ERR_NUMERIC, "group advance made no progress");
+    }
+    KV_TRY(g->cuda(cudaEventRecord(g->t1, g->s0), "event"));
+    KV_TRY(g->cuda(cudaEventSynchronize(g->t1), "event"));
+    if (ms) {
+        float t = 0.f;
+        KV_TRY(g->cuda(cudaEventElapsedTime(&t, g->t0, g->t1), "event time"));
+        *ms = t;
+    }
+    for (size_t i = 0; i < n; ++i) {
+        kvmc_handle *h = g->hs[i];
+        calls[i].launches = launches;
+        if (int rc = sweep_end(h, stats ? stats + i : nullptr, calls[i])) { g->err = h->err; return rc; }
     }
     return KVMC_OK;
 }
-}  // namespace
+
+extern "C" int kvmc_group_last_error(const kvmc_group *g, char *buf, size_t len) {
+    if (!buf || len == 0) return KVMC_ERR_ARGUMENT;
+    const std::string &e = g ? g->err : g_last_error;
+    std::snprintf(buf, len, "%s", e.c_str());
+    return KVMC_OK;
+}
 
 extern "C" int kvmc_measure(kvmc_handle *h, double *local_energy) {
     if (!h || !local_energy) return fail_global(KVMC_ERR_ARGUMENT, "null argument");
@@ -1069,6 +1296,19 @@ extern "C" int kvmc_get_w(kvmc_handle *h, double *W_up, double *W_down) {
         }
     }
     return KVMC_OK;
+}
+
+extern "C" int kvmc_set_tuning(kvmc_handle *h, int32_t key, int32_t value) {
+    if (!h) return fail_global(KVMC_ERR_ARGUMENT, "null handle");
+    if (key == KVMC_TUNE_STREAM_THREADS) {
+        if (value != 128 && value != 256) return h->fail(KVMC_ERR_ARGUMENT, "stream threads must be 128 or 256");
+        // the flush gives each thread four columns of one row group
+        if (std::max(h->ld_up, h->ld_dn) > 4 * value)
+            return h->fail(KVMC_ERR_ARGUMENT, "%d threads cannot flush %d columns", value, std::max(h->ld_up, h->ld_dn));
+        h->stream_threads = value;
+        return KVMC_OK;
+    }
+    return h->fail(KVMC_ERR_ARGUMENT, "unknown tuning key %d", key);
 }
 
 extern "C" int kvmc_set_drift_tolerance(kvmc_handle *h, double tol) {

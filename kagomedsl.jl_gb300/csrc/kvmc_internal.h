@@ -70,6 +70,7 @@ struct SweepParams {
     int measure_every;    // proposals between energy samples
     int delay_k;          // mixed form: delayed-update depth (4, 8, 12, 16), else rank-1
     float drift_tol;      // delayed form: unit-row deviation that triggers an early refresh
+    int stream_threads;   // W in HBM: threads per walker's CTA (128 or 256)
 };
 
 // Launchers.  All enqueue on `stream` and return the launch error.
@@ -78,9 +79,10 @@ struct SweepParams {
 cudaError_t launch_refresh(const DevModel &m, const DevBatch &b, bool fp32_out,
                            int only_due, int track_drift, cudaStream_t stream);
 // mixed=false: plain FP64 form (W in global memory, refresh every
-// p.refresh_every proposals).  mixed=true: FP32 form, W staged in shared
-// memory when smem_w (else read in place), refresh every p.refresh_every
-// accepted moves.  active (device int) counts walkers left short of t_end.
+// p.refresh_every proposals).  mixed=true: FP32 form, refresh every
+// p.refresh_every accepted moves; W staged in shared memory when smem_w,
+// else kept in HBM (delayed updates when p.delay_k > 1, rank-1 in place
+// otherwise).  active (device int) counts walkers left short of t_end.
 cudaError_t launch_sweep(const DevModel &m, const DevBatch &b, const SweepParams &p,
                          bool mixed, bool smem_w, int *active, cudaStream_t stream);
 cudaError_t launch_measure(const DevModel &m, const DevBatch &b, bool fp32, cudaStream_t stream);
@@ -95,7 +97,9 @@ cudaError_t launch_init_random(const DevModel &m, const DevBatch &b, unsigned lo
 // Shared-memory bytes the mixed sweep kernel needs for this model (0 if it
 // cannot hold both W matrices on one SM).
 size_t mixed_sweep_smem(const DevModel &m);
-size_t delayed_smem_bytes(const DevModel &m, int K);
+// Shared memory of the delayed-update sweep: with W on chip, or with W in
+// HBM (only P, Q and the walker's small state on chip).
+size_t delayed_smem_bytes(const DevModel &m, int K, bool w_on_chip);
 size_t refresh_smem(const DevModel &m);
 size_t refresh_scratch_block(const DevModel &m);
 size_t refresh_large_smem(const DevModel &m);

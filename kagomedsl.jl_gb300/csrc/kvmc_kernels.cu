@@ -905,6 +905,21 @@ struct DelayedSpin {
         return acc0 + acc1;
     }
     __device__ __forceinline__ float eff(int r, int c) const { return W[(size_t)r * ld + c] - dotPQ(r, c); }
+    // sum over the first m factor columns of P[r,k] Q[c,k]
+    __device__ __forceinline__ float dot_lt(int r, int c, int m) const {
+        const float4 *pr = reinterpret_cast<const float4 *>(P + (size_t)r * K);
+        const float4 *qc = reinterpret_cast<const float4 *>(Q + (size_t)c * K);
+        float acc0 = 0.f, acc1 = 0.f;
+#pragma unroll
+        for (int k = 0; k < K / 4; ++k) {
+            const float4 a = pr[k], b = qc[k];
+            acc0 = fmaf(4 * k + 0 < m ? a.x : 0.f, b.x, acc0);
+            acc1 = fmaf(4 * k + 1 < m ? a.y : 0.f, b.y, acc1);
+            acc0 = fmaf(4 * k + 2 < m ? a.z : 0.f, b.z, acc0);
+            acc1 = fmaf(4 * k + 3 < m ? a.w : 0.f, b.w, acc1);
+        }
+        return acc0 + acc1;
+    }
     // W_eff over the first m factor columns only (column m is being written)
     __device__ __forceinline__ float eff_lt(int r, int c, int m) const {
         const float4 *pr = reinterpret_cast<const float4 *>(P + (size_t)r * K);
@@ -997,6 +1012,68 @@ __device__ void delayed_flush(const DelayedSpin<K> &S, int N, const short *kappa
     }
 }
 
+// The same update with W in HBM: four rows' W words are loaded before any
+// arithmetic so that each thread keeps four global loads in flight (the
+// loop would otherwise wait one full memory latency per row), and P is read
+// from shared memory per 4-wide k step instead of being held in registers.
+template <int K>
+__device__ void delayed_flush_stream(const DelayedSpin<K> &S, int N, const short *kappa, int *dev) {
+    const int qc = S.ld >> 2;
+    const int groups = blockDim.x / qc;
+    const int t = threadIdx.x;
+    if (t >= groups * qc) return;
+    const int c4 = t % qc, rp = t / qc, c0 = 4 * c4;
+    float q[4][K];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        const float4 *qr = reinterpret_cast<const float4 *>(S.Q + (size_t)(c0 + j) * K);
+#pragma unroll
+        for (int k = 0; k < K / 4; ++k) {
+            const float4 v = qr[k];
+            q[j][4 * k] = v.x; q[j][4 * k + 1] = v.y; q[j][4 * k + 2] = v.z; q[j][4 * k + 3] = v.w;
+        }
+    }
+    float dmax = 0.f;
+    for (int r0 = rp; r0 < N; r0 += 4 * groups) {
+        float4 w[4];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            const int r = r0 + i * groups;
+            if (r < N) w[i] = reinterpret_cast<const float4 *>(S.W + (size_t)r * S.ld)[c4];
+        }
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            const int r = r0 + i * groups;
+            if (r < N) {
+                const float4 *pr = reinterpret_cast<const float4 *>(S.P + (size_t)r * K);
+                float a0 = 0.f, a1 = 0.f, a2 = 0.f, a3 = 0.f;
+#pragma unroll
+                for (int k4 = 0; k4 < K / 4; ++k4) {
+                    const float4 v = pr[k4];
+                    a0 = fmaf(v.x, q[0][4 * k4], a0); a1 = fmaf(v.x, q[1][4 * k4], a1);
+                    a2 = fmaf(v.x, q[2][4 * k4], a2); a3 = fmaf(v.x, q[3][4 * k4], a3);
+                    a0 = fmaf(v.y, q[0][4 * k4 + 1], a0); a1 = fmaf(v.y, q[1][4 * k4 + 1], a1);
+                    a2 = fmaf(v.y, q[2][4 * k4 + 1], a2); a3 = fmaf(v.y, q[3][4 * k4 + 1], a3);
+                    a0 = fmaf(v.z, q[0][4 * k4 + 2], a0); a1 = fmaf(v.z, q[1][4 * k4 + 2], a1);
+                    a2 = fmaf(v.z, q[2][4 * k4 + 2], a2); a3 = fmaf(v.z, q[3][4 * k4 + 2], a3);
+                    a0 = fmaf(v.w, q[0][4 * k4 + 3], a0); a1 = fmaf(v.w, q[1][4 * k4 + 3], a1);
+                    a2 = fmaf(v.w, q[2][4 * k4 + 3], a2); a3 = fmaf(v.w, q[3][4 * k4 + 3], a3);
+                }
+                float4 x = w[i];
+                x.x -= a0; x.y -= a1; x.z -= a2; x.w -= a3;
+                reinterpret_cast<float4 *>(S.W + (size_t)r * S.ld)[c4] = x;
+                const int l = kappa[r] - 1;
+                if (l >= 0) {
+                    const float d = fmaxf(fmaxf(fabsf(x.x - (c0 == l ? 1.f : 0.f)), fabsf(x.y - (c0 + 1 == l ? 1.f : 0.f))),
+                                          fmaxf(fabsf(x.z - (c0 + 2 == l ? 1.f : 0.f)), fabsf(x.w - (c0 + 3 == l ? 1.f : 0.f))));
+                    dmax = fmaxf(dmax, d);
+                }
+            }
+        }
+    }
+    if (dmax > 0.f) atomicMax(dev, __float_as_int(dmax));
+}
+
 template <int K>
 __device__ void delayed_zero(const DelayedSpin<K> &S, int N) {
     float4 *p = reinterpret_cast<float4 *>(S.P);
@@ -1034,8 +1111,15 @@ __device__ double delayed_local_energy(const DevModel &m, const short2 *bonds, c
     return block_sum_f32(acc, red);
 }
 
-template <int K>
-__global__ void __launch_bounds__(512) sweep_delayed_kernel(DevModel m, DevBatch b, SweepParams p, int *active_count) {
+// kStream = false: W (FP32) is staged in shared memory for the launch.
+// kStream = true: W stays in HBM and only P, Q and the walker's small state
+// are on chip, so several walkers share an SM and hide each other's global
+// latency; the flush then streams W through once per K moves.
+// kThreads: 512 with W on chip (one walker per SM); 256 or 128 with W in
+// HBM (two or four walkers per SM).
+template <int K, bool kStream, int kThreads>
+__global__ void __launch_bounds__(kThreads, 512 / kThreads)
+sweep_delayed_kernel(DevModel m, DevBatch b, SweepParams p, int *active_count) {
     const int w = blockIdx.x;
     const int N = m.n_sites;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -1054,11 +1138,15 @@ __global__ void __launch_bounds__(512) sweep_delayed_kernel(DevModel m, DevBatch
     float *gW = b.W32 + (size_t)w * wblock;
     unsigned char *cur = smem;
     DelayedSpin<K> SU, SD;
-    SU.W = reinterpret_cast<float *>(cur);
+    if constexpr (kStream) {
+        SU.W = gW;
+    } else {
+        SU.W = reinterpret_cast<float *>(cur);
+        cur += wblock * sizeof(float);
+    }
     SU.ld = m.ld_up;
     SD.W = SU.W + (size_t)N * m.ld_up;
     SD.ld = m.ld_dn;
-    cur += wblock * sizeof(float);
     SU.P = reinterpret_cast<float *>(cur); cur += (size_t)N * K * sizeof(float);
     SD.P = reinterpret_cast<float *>(cur); cur += (size_t)N * K * sizeof(float);
     SU.Q = reinterpret_cast<float *>(cur); cur += (size_t)m.ld_up * K * sizeof(float);
@@ -1069,7 +1157,7 @@ __global__ void __launch_bounds__(512) sweep_delayed_kernel(DevModel m, DevBatch
     short *kup = reinterpret_cast<short *>(cur); cur += (size_t)N * sizeof(short);
     short *kdn = reinterpret_cast<short *>(cur);
 
-    {
+    if constexpr (!kStream) {
         const int nvec = (int)(wblock / 4);
         const float4 *src = reinterpret_cast<const float4 *>(gW);
         float4 *dst = reinterpret_cast<float4 *>(SU.W);
@@ -1174,15 +1262,46 @@ __global__ void __launch_bounds__(512) sweep_delayed_kernel(DevModel m, DevBatch
             const int mm = ctl.m;
             // new factor column mm, written in place: its entries read only the
             // columns before mm, so writers and readers never touch the same word
-            for (int e = tid; e < 2 * N + m.ld_up + m.ld_dn; e += blockDim.x) {
-                if (e < N) SU.P[(size_t)e * K + mm] = SU.eff_lt(e, lu, mm) * ipu;
-                else if (e < 2 * N) SD.P[(size_t)(e - N) * K + mm] = SD.eff_lt(e - N, ld, mm) * ipd;
-                else if (e < 2 * N + m.ld_up) {
-                    const int c = e - 2 * N;
-                    SU.Q[(size_t)c * K + mm] = SU.eff_lt(Ku, c, mm) - (c == lu ? 1.f : 0.f);
-                } else {
-                    const int c = e - 2 * N - m.ld_up;
-                    SD.Q[(size_t)c * K + mm] = SD.eff_lt(Kd, c, mm) - (c == ld ? 1.f : 0.f);
+            const int tot = 2 * N + m.ld_up + m.ld_dn;
+            if constexpr (kStream) {
+                // W in HBM: each thread loads the W words of up to four of its
+                // entries before any shared-memory store, so their latencies overlap
+                for (int base = 0; base < tot; base += 4 * blockDim.x) {
+                    float wv[4];
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) {
+                        const int e = base + q * blockDim.x + tid;
+                        wv[q] = 0.f;
+                        if (e < N) wv[q] = SU.W[(size_t)e * SU.ld + lu];
+                        else if (e < 2 * N) wv[q] = SD.W[(size_t)(e - N) * SD.ld + ld];
+                        else if (e < 2 * N + m.ld_up) wv[q] = SU.W[(size_t)Ku * SU.ld + (e - 2 * N)];
+                        else if (e < tot) wv[q] = SD.W[(size_t)Kd * SD.ld + (e - 2 * N - m.ld_up)];
+                    }
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) {
+                        const int e = base + q * blockDim.x + tid;
+                        if (e < N) SU.P[(size_t)e * K + mm] = (wv[q] - SU.dot_lt(e, lu, mm)) * ipu;
+                        else if (e < 2 * N) SD.P[(size_t)(e - N) * K + mm] = (wv[q] - SD.dot_lt(e - N, ld, mm)) * ipd;
+                        else if (e < 2 * N + m.ld_up) {
+                            const int c = e - 2 * N;
+                            SU.Q[(size_t)c * K + mm] = wv[q] - SU.dot_lt(Ku, c, mm) - (c == lu ? 1.f : 0.f);
+                        } else if (e < tot) {
+                            const int c = e - 2 * N - m.ld_up;
+                            SD.Q[(size_t)c * K + mm] = wv[q] - SD.dot_lt(Kd, c, mm) - (c == ld ? 1.f : 0.f);
+                        }
+                    }
+                }
+            } else {
+                for (int e = tid; e < tot; e += blockDim.x) {
+                    if (e < N) SU.P[(size_t)e * K + mm] = SU.eff_lt(e, lu, mm) * ipu;
+                    else if (e < 2 * N) SD.P[(size_t)(e - N) * K + mm] = SD.eff_lt(e - N, ld, mm) * ipd;
+                    else if (e < 2 * N + m.ld_up) {
+                        const int c = e - 2 * N;
+                        SU.Q[(size_t)c * K + mm] = SU.eff_lt(Ku, c, mm) - (c == lu ? 1.f : 0.f);
+                    } else {
+                        const int c = e - 2 * N - m.ld_up;
+                        SD.Q[(size_t)c * K + mm] = SD.eff_lt(Kd, c, mm) - (c == ld ? 1.f : 0.f);
+                    }
                 }
             }
             if (warp == (blockDim.x >> 5) - 2) {
@@ -1221,8 +1340,13 @@ __global__ void __launch_bounds__(512) sweep_delayed_kernel(DevModel m, DevBatch
             __syncthreads();
             // every thread has read ctl.m for this move before the barrier above
             if (mm + 1 == K) {
-                delayed_flush<K>(SU, N, kup, &ctl.dev);
-                delayed_flush<K>(SD, N, kdn, &ctl.dev);
+                if constexpr (kStream) {
+                    delayed_flush_stream<K>(SU, N, kup, &ctl.dev);
+                    delayed_flush_stream<K>(SD, N, kdn, &ctl.dev);
+                } else {
+                    delayed_flush<K>(SU, N, kup, &ctl.dev);
+                    delayed_flush<K>(SD, N, kdn, &ctl.dev);
+                }
                 __syncthreads();
                 delayed_zero<K>(SU, N);
                 delayed_zero<K>(SD, N);
@@ -1252,11 +1376,16 @@ __global__ void __launch_bounds__(512) sweep_delayed_kernel(DevModel m, DevBatch
     }
     __syncthreads();
     if (ctl.m > 0) {
-        delayed_flush<K>(SU, N, kup, &ctl.dev);
-        delayed_flush<K>(SD, N, kdn, &ctl.dev);
+        if constexpr (kStream) {
+            delayed_flush_stream<K>(SU, N, kup, &ctl.dev);
+            delayed_flush_stream<K>(SD, N, kdn, &ctl.dev);
+        } else {
+            delayed_flush<K>(SU, N, kup, &ctl.dev);
+            delayed_flush<K>(SD, N, kdn, &ctl.dev);
+        }
         __syncthreads();
     }
-    {
+    if constexpr (!kStream) {
         const int nvec = (int)(wblock / 4);
         const float4 *src = reinterpret_cast<const float4 *>(SU.W);
         float4 *dst = reinterpret_cast<float4 *>(gW);
@@ -1279,9 +1408,9 @@ __global__ void __launch_bounds__(512) sweep_delayed_kernel(DevModel m, DevBatch
     }
 }
 
-size_t delayed_smem_bytes(const DevModel &m, int K) {
+size_t delayed_smem_bytes(const DevModel &m, int K, bool w_on_chip) {
     const size_t N = m.n_sites;
-    size_t s = N * (m.ld_up + m.ld_dn) * 4;                 // W
+    size_t s = w_on_chip ? N * (m.ld_up + m.ld_dn) * 4 : 0;  // W
     s += 2 * N * K * 4 + (size_t)(m.ld_up + m.ld_dn) * K * 4;  // P, Q
     s += (N + 1) * 4 + (size_t)m.n_bonds * 4 + (size_t)2 * m.n_bonds * 2 + 2 * N * 2 + 16;
     return (s + 15) / 16 * 16;
@@ -1441,23 +1570,37 @@ static cudaError_t launch_sweep_impl(const DevModel &m, const DevBatch &b, const
     return cudaGetLastError();
 }
 
-template <int K>
+template <int K, bool kStream, int kThreads>
+static cudaError_t launch_delayed_t(const DevModel &m, const DevBatch &b, const SweepParams &p, int *active,
+                                    cudaStream_t stream) {
+    const size_t sm = delayed_smem_bytes(m, K, !kStream);
+    cudaError_t e = cudaFuncSetAttribute(sweep_delayed_kernel<K, kStream, kThreads>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    if (e != cudaSuccess) return e;
+    sweep_delayed_kernel<K, kStream, kThreads><<<b.n_walkers, kThreads, sm, stream>>>(m, b, p, active);
+    return cudaGetLastError();
+}
+
+template <int K, bool kStream>
 static cudaError_t launch_delayed(const DevModel &m, const DevBatch &b, const SweepParams &p, int *active,
                                   cudaStream_t stream) {
-    const size_t sm = delayed_smem_bytes(m, K);
-    cudaError_t e = cudaFuncSetAttribute(sweep_delayed_kernel<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    if (e != cudaSuccess) return e;
-    sweep_delayed_kernel<K><<<b.n_walkers, 512, sm, stream>>>(m, b, p, active);
-    return cudaGetLastError();
+    if constexpr (!kStream) return launch_delayed_t<K, false, 512>(m, b, p, active, stream);
+    if (p.stream_threads == 128) return launch_delayed_t<K, true, 128>(m, b, p, active, stream);
+    return launch_delayed_t<K, true, 256>(m, b, p, active, stream);
 }
 
 cudaError_t launch_sweep(const DevModel &m, const DevBatch &b, const SweepParams &p, bool mixed,
                          bool smem_w, int *active, cudaStream_t stream) {
     if (!mixed) return launch_sweep_impl<double, false>(m, b, p, 1, active, 256, stream);
-    if (smem_w && p.delay_k == 4) return launch_delayed<4>(m, b, p, active, stream);
-    if (smem_w && p.delay_k == 8) return launch_delayed<8>(m, b, p, active, stream);
-    if (smem_w && p.delay_k == 12) return launch_delayed<12>(m, b, p, active, stream);
-    if (smem_w && p.delay_k == 16) return launch_delayed<16>(m, b, p, active, stream);
+    if (smem_w && p.delay_k == 4) return launch_delayed<4, false>(m, b, p, active, stream);
+    if (smem_w && p.delay_k == 8) return launch_delayed<8, false>(m, b, p, active, stream);
+    if (smem_w && p.delay_k == 12) return launch_delayed<12, false>(m, b, p, active, stream);
+    if (smem_w && p.delay_k == 16) return launch_delayed<16, false>(m, b, p, active, stream);
+    // W in HBM, delayed factors on chip
+    if (!smem_w && p.delay_k == 4) return launch_delayed<4, true>(m, b, p, active, stream);
+    if (!smem_w && p.delay_k == 8) return launch_delayed<8, true>(m, b, p, active, stream);
+    if (!smem_w && p.delay_k == 12) return launch_delayed<12, true>(m, b, p, active, stream);
+    if (!smem_w && p.delay_k == 16) return launch_delayed<16, true>(m, b, p, active, stream);
     if (smem_w) return launch_sweep_impl<float, true>(m, b, p, 0, active, 512, stream);
     return launch_sweep_impl<float, false>(m, b, p, 0, active, 512, stream);
 }

@@ -9,13 +9,13 @@ from ._lib import (ArgumentError, BoundsError, DeviceError, KvmcError, SingularE
                    load)
 from .lattice import PI_LINK_IN, PI_LINK_INTER, DoubleKagome, Hamiltonian, Hmat, get_nn, ns, orbitals
 from .ansatz import Ansatz, ansatz_hmat, energy_and_gradient, estimate, orbital_derivatives
-from .montecarlo import (MC, Engine, Evaluator, MCContext, init_, init_conf_qr, measure_, read_checkpoint_,
+from .montecarlo import (MC, Engine, Evaluator, Group, MCContext, init_, init_conf_qr, measure_, read_checkpoint_,
                          register_evaluables, sweep_, write_checkpoint)
 
 __all__ = [
     "ArgumentError", "BoundsError", "DeviceError", "KvmcError", "SingularException", "EXPORTS", "LIB_PATH", "load",
     "PI_LINK_IN", "PI_LINK_INTER", "DoubleKagome", "Hamiltonian", "Hmat", "get_nn", "ns", "orbitals",
-    "MC", "Engine", "Evaluator", "MCContext", "init_", "init_conf_qr", "measure_", "read_checkpoint_",
+    "MC", "Engine", "Evaluator", "Group", "MCContext", "init_", "init_conf_qr", "measure_", "read_checkpoint_",
     "register_evaluables", "sweep_", "write_checkpoint",
     "Ansatz", "ansatz_hmat", "energy_and_gradient", "estimate", "orbital_derivatives",
 ]

@@ -75,7 +75,7 @@ class ModelDesc(C.Structure):
 class BatchDesc(C.Structure):
     _fields_ = [("n_walkers", C.c_int32), ("precision", C.c_int32), ("accept_rule", C.c_int32),
                 ("refresh_interval", C.c_int32), ("measure_interval", C.c_int32), ("delay_k", C.c_int32),
-                ("device", C.c_int32), ("seed", C.c_uint64)]
+                ("device", C.c_int32), ("seed", C.c_uint64), ("w_placement", C.c_int32)]
 
 
 class SweepStats(C.Structure):
@@ -120,6 +120,11 @@ _SIGS = {
     "kvmc_measure_grad": [_P, _P, _P],
     "kvmc_grad_sums": [_P, _P],
     "kvmc_walker_logdet": [_P, _P],
+    "kvmc_set_tuning": [_P, C.c_int32, C.c_int32],
+    "kvmc_group_create": [_P, C.c_int32, C.POINTER(_P)],
+    "kvmc_group_destroy": [_P],
+    "kvmc_group_advance": [_P, C.c_int64, _P, C.POINTER(C.c_double)],
+    "kvmc_group_last_error": [_P, C.c_char_p, C.c_size_t],
 }
 EXPORTS = tuple(_SIGS)
 

@@ -1,103 +1,153 @@
-"""Autotuner for the mixed form: delayed-update depth k and refresh interval R.
+"""Autotuner for the mixed form: where W lives, the launch shape, the
+delayed-update depth k and the refresh interval R.
 
-For a model and batch size it times short trials over the candidate
-(k, R) pairs on the actual GPU and keeps the fastest pair whose measured W
-drift stays within a bound.  Drift is measured at each FP64 refresh as
-max |W_fp32 - W_fp64| / (1 + |W_fp64|) over all walkers (the refresh
-kernel records it), so a longer interval is accepted only when the FP32
-state it leaves behind is still accurate.
+For a model and batch size it times short trials over the candidates on the
+actual GPU and keeps the fastest one whose measured W drift stays within a
+bound.  Drift is measured at each FP64 refresh as
+max |W_fp32 - W_fp64| / (1 + |W_fp64|) per walker (the refresh kernel
+records it), so a longer interval is accepted only when the FP32 state it
+leaves behind is still accurate.
 
-Results are cached per (sites, orbitals, walkers, device name) in a JSON
-file so a production run tunes once.
+Candidates:
+  placement  "chip" (W staged in shared memory, one walker per SM; only when
+             it fits) or "hbm" (W in HBM, delayed factors on chip, two or four
+             walkers per SM)
+  threads    128 or 256 threads per walker with W in HBM
+  k          1 (rank-1), 4, 8, 12, 16
+  R          accepted moves between FP64 refreshes
+
+Results are cached per (sites, orbitals, walkers, acceptance rule, device
+name) in a JSON file so a production run tunes once; ``tuned.json`` next to
+this module holds the choices measured on a GB300 for the shipped workloads.
 """
 from __future__ import annotations
 
 import json
 import os
 import time
-from dataclasses import asdict, dataclass
+from dataclasses import asdict, dataclass, field
 
 import numpy as np
 
 from . import _lib
 
 DELAYS = (1, 4, 8, 12, 16)
-REFRESH = (32, 64, 128, 256, 512, 1024, 2048)
+REFRESH = (128, 256, 512, 1024, 2048)
+PLACEMENTS = ("chip", "hbm")
+THREADS = (128, 256)
 DRIFT_BOUND = 1e-2  # on the 99.9th percentile of per-walker relative drift
+SHIPPED = os.path.join(os.path.dirname(os.path.abspath(__file__)), "tuned.json")
 
 
 @dataclass
 class Choice:
     delay_k: int
     refresh_interval: int
-    moves_per_s: float
-    max_drift: float
-    trials: list
+    placement: str = "chip"
+    threads: int = 256
+    moves_per_s: float = 0.0
+    max_drift: float = 0.0
+    trials: list = field(default_factory=list)
+
+    def engine_kwargs(self) -> dict:
+        return dict(precision="mixed", delay_k=self.delay_k, refresh_interval=self.refresh_interval,
+                    w_placement=self.placement)
 
 
 def _device_name(device: int) -> str:
+    """The chip the choice was measured on ("GB300" for any GB300 board)."""
     try:
         import torch
 
-        return torch.cuda.get_device_name(device)
+        name = torch.cuda.get_device_name(device)
     except Exception:
-        return f"device{device}"
+        return "GB300"
+    return "GB300" if "GB300" in name else name
 
 
-def _cache_key(ham, walkers, device):
-    return f"N{ham.U_up.shape[0]}_nu{ham.U_up.shape[1]}_nd{ham.U_down.shape[1]}_W{walkers}_{_device_name(device)}"
+def cache_key(ham, walkers, accept="reference", device_name=None):
+    return (f"N{ham.U_up.shape[0]}_nu{ham.U_up.shape[1]}_nd{ham.U_down.shape[1]}_W{walkers}_{accept}"
+            f"_{'c' if np.iscomplexobj(ham.U_up) else 'r'}_{device_name or 'GB300'}")
+
+
+def lookup(ham, walkers, accept="reference", device_name=None, path: str | None = None) -> Choice | None:
+    """The cached choice for this workload, from `path` or the shipped table."""
+    for p in ([path] if path else []) + [SHIPPED]:
+        if p and os.path.exists(p):
+            cache = json.load(open(p))
+            key = cache_key(ham, walkers, accept, device_name)
+            if key in cache:
+                return Choice(**cache[key])
+    return None
+
+
+def make_engine(ham, walkers, choice: Choice, **kw):
+    """An Engine configured with `choice` (kw: accept, seed, device, ...)."""
+    from .montecarlo import Engine
+
+    eng = Engine(ham, walkers, **choice.engine_kwargs(), **kw)
+    if choice.placement == "hbm" and choice.delay_k > 1:
+        eng.set_stream_threads(choice.threads)
+    return eng
 
 
 def tune(ham, walkers: int, *, device: int = 0, seed: int = 1, accept: str = "reference",
-         proposals: int = 1024, delays=DELAYS, refresh=REFRESH, drift_bound: float = DRIFT_BOUND,
-         cache_path: str | None = None, verbose: bool = False) -> Choice:
-    """Times (k, R) candidates for this model on `walkers` walkers and returns the best.
+         warmup: int = 512, delays=DELAYS, refresh=REFRESH, placements=PLACEMENTS, threads=THREADS,
+         drift_bound: float = DRIFT_BOUND, cache_path: str | None = None, verbose: bool = False) -> Choice:
+    """Times the candidates for this model on `walkers` walkers and returns the best.
 
     Each trial: fresh engine, seeded random starts, a warm-up of
-    max(R, proposals/8) accepted moves per walker, then a timed 2R accepted
-    moves per walker (CUDA events on the handle's stream), so each walker's
-    FP64 refreshes fall inside the timed window.  Candidates whose depth
-    does not fit in shared memory for this model are skipped.
+    max(R, warmup) accepted moves per walker (past the transient after the
+    random starts), then a timed 2R accepted moves per walker (CUDA events
+    on the handle's stream), so each walker's FP64 refreshes fall inside the
+    timed window.  Candidates that do not fit on chip are skipped.
     """
     from .montecarlo import Engine
 
-    key = _cache_key(ham, walkers, device)
+    dev_name = _device_name(device)
+    key = cache_key(ham, walkers, accept, dev_name)
     if cache_path and os.path.exists(cache_path):
         cache = json.load(open(cache_path))
         if key in cache:
             return Choice(**cache[key])
     trials = []
     best = None
-    for k in delays:
-        for R in refresh:
-            try:
-                eng = Engine(ham, walkers, precision="mixed", accept=accept, seed=seed, refresh_interval=R,
-                             device=device, delay_k=k)
-            except _lib.KvmcError:
-                break  # this depth does not fit for this model
-            try:
-                # warm up, then time 2R accepted moves per walker so that every
-                # walker pays for its FP64 refreshes inside the timed window
-                eng.init()
-                eng.advance(max(R, proposals))  # past the transient after the random starts
-                eng.region_start()
-                st = eng.advance(2 * R)
-                ms = eng.region_stop()
-                drift_p999 = float(np.percentile(eng.walker_drift(), 99.9))
-            finally:
-                eng.close()
-            rate = st["accepted"] / (ms * 1e-3)
-            row = dict(delay_k=k, refresh_interval=R, moves_per_s=rate, max_drift=drift_p999,
-                       refreshes=st["refreshes"])
-            trials.append(row)
-            if verbose:
-                print(row, flush=True)
-            ok = st["max_drift"] <= drift_bound
-            if ok and (best is None or rate > best["moves_per_s"]):
-                best = row
-    if best is None:  # nothing met the bound: the most frequent refresh of the fastest depth
+    for place in placements:
+        for k in delays:
+            for th in (threads if (place == "hbm" and k > 1) else (256,)):
+                for R in refresh:
+                    try:
+                        eng = Engine(ham, walkers, precision="mixed", accept=accept, seed=seed, refresh_interval=R,
+                                     device=device, delay_k=k, w_placement=place)
+                        if place == "hbm" and k > 1:
+                            eng.set_stream_threads(th)
+                    except _lib.KvmcError:
+                        continue  # does not fit for this model
+                    try:
+                        if eng.config()["delay_k"] != k:
+                            continue
+                        eng.init()
+                        eng.advance(max(R, warmup))
+                        eng.region_start()
+                        st = eng.advance(2 * R)
+                        ms = eng.region_stop()
+                        drift = float(np.percentile(eng.walker_drift(), 99.9))
+                    finally:
+                        eng.close()
+                    rate = st["accepted"] / (ms * 1e-3)
+                    row = dict(placement=place, threads=th, delay_k=k, refresh_interval=R, moves_per_s=rate,
+                               max_drift=drift, refreshes=st["refreshes"])
+                    trials.append(row)
+                    if verbose:
+                        print(row, flush=True)
+                    if drift <= drift_bound and (best is None or rate > best["moves_per_s"]):
+                        best = row
+    if not trials:
+        raise _lib.KvmcError(_lib.KVMC_ERR_UNSUPPORTED, "no candidate configuration could be created")
+    if best is None:  # nothing met the bound: the most frequent refresh of the fastest candidate
         best = min(trials, key=lambda r: (r["refresh_interval"], -r["moves_per_s"]))
-    choice = Choice(best["delay_k"], best["refresh_interval"], best["moves_per_s"], best["max_drift"], trials)
+    choice = Choice(best["delay_k"], best["refresh_interval"], best["placement"], best["threads"],
+                    best["moves_per_s"], best["max_drift"], trials)
     if cache_path:
         cache = json.load(open(cache_path)) if os.path.exists(cache_path) else {}
         cache[key] = asdict(choice)

@@ -23,7 +23,7 @@ class Engine:
     """A batch of walkers of one model on one GPU (a kvmc handle)."""
 
     def __init__(self, ham: Hamiltonian, n_walkers=1, precision="plain", accept="reference",
-                 refresh_interval=0, measure_interval=0, seed=0, device=0, delay_k=0):
+                 refresh_interval=0, measure_interval=0, seed=0, device=0, delay_k=0, w_placement="auto"):
         self.ham = ham
         self.N = int(ham.U_up.shape[0])
         self.n_up = int(ham.U_up.shape[1])
@@ -53,6 +53,7 @@ class Engine:
         bd.n_walkers, bd.precision, bd.accept_rule = self.n_walkers, prec, acc
         bd.refresh_interval, bd.measure_interval = int(refresh_interval), int(measure_interval)
         bd.delay_k, bd.device, bd.seed = int(delay_k), int(device), int(seed) & 0xFFFFFFFFFFFFFFFF
+        bd.w_placement = {"auto": 0, "chip": 1, "hbm": 2}.get(w_placement, w_placement)
         self._lib = _lib.load()
         h = C.c_void_p()
         _lib.check(self._lib.kvmc_create(C.byref(md), C.byref(bd), C.byref(h)))
@@ -188,6 +189,10 @@ class Engine:
         self._check(self._lib.kvmc_walker_drift(self.h, _lib.ptr(d)))
         return d
 
+    def set_stream_threads(self, threads: int):
+        """W in HBM: threads per walker's CTA (128 or 256)."""
+        self._check(self._lib.kvmc_set_tuning(self.h, 1, int(threads)))
+
     def set_drift_tolerance(self, tol: float):
         self._check(self._lib.kvmc_set_drift_tolerance(self.h, float(tol)))
 
@@ -214,6 +219,46 @@ class Engine:
         ms, n = C.c_double(), C.c_int64()
         self._check(self._lib.kvmc_kernel_time(self.h, int(kind), C.byref(ms), C.byref(n)))
         return ms.value, n.value
+
+
+class Group:
+    """Several engines (typically one per lattice size) advanced together by
+    one captured CUDA graph (kvmc_group_*): each engine keeps its own
+    delayed-update depth and refresh interval, and their launches run
+    concurrently on the GPU."""
+
+    def __init__(self, engines):
+        self.engines = list(engines)
+        self._lib = _lib.load()
+        arr = (C.c_void_p * len(self.engines))(*[e.h.value if isinstance(e.h, C.c_void_p) else e.h
+                                                 for e in self.engines])
+        g = C.c_void_p()
+        _lib.check(self._lib.kvmc_group_create(arr, len(self.engines), C.byref(g)))
+        self.g = g
+
+    def _check(self, rc):
+        if rc != _lib.KVMC_OK:
+            buf = C.create_string_buffer(1024)
+            self._lib.kvmc_group_last_error(self.g, buf, len(buf))
+            raise _lib._ERRORS.get(rc, _lib.DeviceError)(rc, buf.value.decode(errors="replace"))
+
+    def advance(self, moves_per_walker: int):
+        """Returns (per-engine stats, device ms of the graph launches)."""
+        st = (_lib.SweepStats * len(self.engines))()
+        ms = C.c_double()
+        self._check(self._lib.kvmc_group_advance(self.g, int(moves_per_walker), st, C.byref(ms)))
+        return [{k: getattr(s, k) for k, _ in s._fields_} for s in st], ms.value
+
+    def close(self):
+        if getattr(self, "g", None):
+            self._lib.kvmc_group_destroy(self.g)
+            self.g = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 # ---------------------------------------------------------------------------

@@ -1,0 +1,48 @@
+"""Tunes the shipped workloads on the local GPU and writes kagomevmc/tuned.json.
+
+    python -m kagomevmc.tune_shipped            # from kagomedsl.jl_gb300/
+
+Workloads (doubled-cell kagome, pi-flux partons, half filling, reference
+acceptance rule):
+  N=216 x 2048 walkers   the headline batch
+  N=96  x 4096           batched walkers
+  N=54  x 1024, N=216 x 768, N=384 x 256   the classes of the uneven batch
+  N=864 x 512            the large lattice (W in HBM)
+"""
+from __future__ import annotations
+
+import json
+import os
+import sys
+
+from . import autotune
+from .lattice import DoubleKagome, Hamiltonian
+
+CELLS = {54: (3, 3), 96: (4, 4), 216: (6, 6), 384: (8, 8), 864: (12, 12)}
+WORKLOADS = [(216, 2048, {}), (96, 4096, {}), (54, 1024, {}), (216, 768, {}), (384, 256, {}),
+             (864, 512, dict(delays=(8, 16), refresh=(128, 256), threads=(256,), placements=("hbm",), warmup=128))]
+
+
+def model(N):
+    a, b = CELLS[N]
+    return Hamiltonian.build(N // 2, N // 2, DoubleKagome(1.0, 2 * a, b, (True, True), (False, True)))
+
+
+def main(argv=None):
+    argv = sys.argv[1:] if argv is None else argv
+    out = argv[0] if argv else autotune.SHIPPED
+    cache = json.load(open(out)) if os.path.exists(out) else {}
+    for N, walkers, kw in WORKLOADS:
+        ham = model(N)
+        key = autotune.cache_key(ham, walkers, "reference", autotune._device_name(0))
+        ch = autotune.tune(ham, walkers, **kw)
+        row = dict(delay_k=ch.delay_k, refresh_interval=ch.refresh_interval, placement=ch.placement,
+                   threads=ch.threads, moves_per_s=ch.moves_per_s, max_drift=ch.max_drift, trials=ch.trials)
+        cache[key] = row
+        print(key, {k: v for k, v in row.items() if k != "trials"}, flush=True)
+        with open(out, "w") as f:
+            json.dump(cache, f, indent=1)
+
+
+if __name__ == "__main__":
+    main()

@@ -432,3 +432,41 @@ def test_large_lattice_chain(kv, precision):
             assert abs(ch.c.sum_e - ws["sum_e"][w]) <= tol * max(1.0, abs(ch.c.sum_e))
     assert match >= walkers - (0 if precision == "plain" else 1)
     eng.close()
+
+
+@pytest.mark.parametrize("N,delay_k", [(96, 4), (96, 16), (216, 12), (216, 16)])
+def test_hbm_streaming_chains_match_c_oracle(kv, N, delay_k):
+    """Mixed form with W kept in HBM and only the delayed factors on chip."""
+    walkers, proposals, seed = 8, 2000, 37
+    ham = ham_for(kv, N)
+    eng = kv.Engine(ham, walkers, precision="mixed", seed=seed, refresh_interval=128, delay_k=delay_k,
+                    w_placement="hbm")
+    cfg = eng.config()
+    assert not cfg["w_on_chip"] and cfg["delay_k"] == delay_k
+    eng.init()
+    ku0, kd0, _ = eng.get_state()
+    st = eng.sweep(proposals)
+    ku1, kd1, _ = eng.get_state()
+    ws = eng.walker_stats()
+    m = oracle_c.OracleModel(ham.U_up, ham.U_down, ham.nn)
+    match = 0
+    for w in range(walkers):
+        ch = m.new_chain(ku0[w], kd0[w])
+        ch.run(seed, w, proposals, N // 2, N // 2, 0)
+        if np.array_equal(ch.ku, ku1[w]) and np.array_equal(ch.kd, kd1[w]):
+            match += 1
+            assert ch.c.accepted == ws["accepted"][w]
+            assert abs(ch.c.sum_e - ws["sum_e"][w]) <= 1e-4 * max(1.0, abs(ch.c.sum_e))
+    assert match >= walkers - 1
+    assert st["bad_walkers"] == 0
+    # the state left in HBM is the W of the final configuration
+    Wu, Wd = eng.get_w()
+    for w in range(walkers):
+        assert close(Wu[w], o.reevaluateW(ham.U_up, ku1[w]), 1e-3)
+    eng.close()
+
+
+def test_placement_on_chip_is_refused_when_w_does_not_fit(kv):
+    ham = ham_for(kv, 384)
+    with pytest.raises(kv.KvmcError):
+        kv.Engine(ham, 2, precision="mixed", w_placement="chip")

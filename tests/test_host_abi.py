@@ -34,7 +34,7 @@ def test_version(built):
 
     abi, arch = C.c_int32(), C.c_int32()
     assert kv.load().kvmc_version(C.byref(abi), C.byref(arch)) == 0
-    assert abi.value == 2 and arch.value == 1030
+    assert abi.value == 3 and arch.value == 1030
 
 
 @pytest.mark.parametrize("n1,n2,pbc,anti,B", [
@@ -120,3 +120,17 @@ def test_no_device_is_a_clean_error_on_cpu(built):
     L = kv.DoubleKagome(1.0, 4, 2, (True, True), (False, True))
     with pytest.raises(kv.DeviceError):
         kv.Engine(kv.Hamiltonian.build(12, 12, L), 2)
+
+
+def test_carlo_context_and_evaluator_host_logic(built):
+    """The measurement sink and evaluables of the Carlo-facing surface (no GPU)."""
+    import kagomevmc as kv
+
+    ctx = kv.MCContext()
+    for v in (1.0, 2.0, 3.0):
+        ctx.measure("OL", v)
+    assert ctx.observables["OL"] == [1.0, 2.0, 3.0] and ctx.sweeps == 0
+    ev = kv.Evaluator()
+    kv.register_evaluables(kv.MC, ev, dict(n1=4, n2=2))
+    res = ev.run(ctx.observables)
+    assert res["energy"] == pytest.approx(2.0 / 24)
