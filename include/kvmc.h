@@ -274,8 +274,12 @@ KVMC_API int kvmc_kernel_time(kvmc_handle *h, int32_t kind, double *total_ms, in
 
 /* Launch-shape knobs the autotuner sets (kagomevmc.autotune):
  *   KVMC_TUNE_STREAM_THREADS: threads per walker's CTA when W is in HBM,
- *   128 (four walkers per SM) or 256 (two walkers per SM, the default). */
-enum kvmc_tuning { KVMC_TUNE_STREAM_THREADS = 1 };
+ *   128 (four walkers per SM) or 256 (two walkers per SM, the default).
+ *   KVMC_TUNE_PIPELINE: 1 = with delayed updates, one warp scans for the next
+ *   accepted move while the others write the factor column of the last one
+ *   (the scan applies that move as a Sherman-Morrison correction), the
+ *   default; 0 = the two phases one after the other. */
+enum kvmc_tuning { KVMC_TUNE_STREAM_THREADS = 1, KVMC_TUNE_PIPELINE = 2 };
 KVMC_API int kvmc_set_tuning(kvmc_handle *h, int32_t key, int32_t value);
 
 /* The settings a handle resolved at creation: refresh and measurement

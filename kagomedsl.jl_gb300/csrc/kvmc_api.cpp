@@ -52,6 +52,7 @@ struct kvmc_handle {
     int delay_k = 1;  // mixed form: 1 = rank-1 updates, 4/8/12/16 = delayed-update depth
     float drift_tol = 1e-4f;  // delayed form: early refresh past this unit-row deviation
     int stream_threads = 256;  // W in HBM: threads per walker
+    int pipeline = 1;          // delayed form: pipelined scan / factor-column write
     std::string err;
 
     DevModel dm{};
@@ -897,6 +898,7 @@ kvmc::SweepParams sweep_params(const kvmc_handle *h) {
     p.delay_k = h->delay_k;
     p.drift_tol = h->drift_tol;
     p.stream_threads = h->stream_threads;
+    p.pipeline = h->pipeline;
     return p;
 }
 
@@ -1078,7 +1080,7 @@ namespace {
 bool same_params(const kvmc::SweepParams &a, const kvmc::SweepParams &b) {
     return a.seed == b.seed && a.accept_rule == b.accept_rule && a.refresh_every == b.refresh_every &&
            a.measure_every == b.measure_every && a.delay_k == b.delay_k && a.drift_tol == b.drift_tol &&
-           a.stream_threads == b.stream_threads;
+           a.stream_threads == b.stream_threads && a.pipeline == b.pipeline;
 }
 
 // Captures one graph: from s0, every handle's stream runs its (sweep,
@@ -1306,6 +1308,11 @@ extern "C" int kvmc_set_tuning(kvmc_handle *h, int32_t key, int32_t value) {
         if (std::max(h->ld_up, h->ld_dn) > 4 * value)
             return h->fail(KVMC_ERR_ARGUMENT, "%d threads cannot flush %d columns", value, std::max(h->ld_up, h->ld_dn));
         h->stream_threads = value;
+        return KVMC_OK;
+    }
+    if (key == KVMC_TUNE_PIPELINE) {
+        if (value != 0 && value != 1) return h->fail(KVMC_ERR_ARGUMENT, "pipeline must be 0 or 1");
+        h->pipeline = value;
         return KVMC_OK;
     }
     return h->fail(KVMC_ERR_ARGUMENT, "unknown tuning key %d", key);

@@ -71,6 +71,7 @@ struct SweepParams {
     int delay_k;          // mixed form: delayed-update depth (4, 8, 12, 16), else rank-1
     float drift_tol;      // delayed form: unit-row deviation that triggers an early refresh
     int stream_threads;   // W in HBM: threads per walker's CTA (128 or 256)
+    int pipeline;         // delayed form: scan for the next move while the last one's factor column is written
 };
 
 // Launchers.  All enqueue on `stream` and return the launch error.

@@ -1408,6 +1408,319 @@ sweep_delayed_kernel(DevModel m, DevBatch b, SweepParams p, int *active_count) {
     }
 }
 
+// ---------------------------------------------------------------------------
+// Pipelined delayed-update sweep: the same chain as sweep_delayed_kernel, but
+// the scan for the next accepted move (warp 0) runs while the other warps
+// write the factor column of the move accepted last.  The scan sees that
+// pending move (K, l, pivot) through its Sherman-Morrison correction on top
+// of the m complete factor columns,
+//   W_eff'(r, c) = W_eff(r, c) - W_eff(r, l) (W_eff(K, c) - [c == l]) / pivot,
+// every W_eff term over columns [0, m) only, which the writers do not touch.
+// The configuration, Z_mu and threshold of an accepted move are applied after
+// the flush that may follow, so the flush's unit-row check sees the sites W
+// describes.
+// ---------------------------------------------------------------------------
+struct PendingMove {
+    int Ku, lu, Kd, ld;
+    float piv_u, piv_d;
+};
+
+struct PipeCtl {
+    long long t, next_meas, acc;
+    int since, zmu, m, state, pend, slot, dz;
+    int dev;
+    PendingMove mv[2];
+    Thr thr;
+    double red[33];
+};
+
+template <int K>
+__device__ __forceinline__ float eff_after(const DelayedSpin<K> &S, int r, int c, int mm, bool pend, int Kp, int lp,
+                                           float ipiv) {
+    float v = S.eff_lt(r, c, mm);
+    if (pend) {
+        const float a = S.eff_lt(r, lp, mm);
+        const float q = S.eff_lt(Kp, c, mm) - (c == lp ? 1.f : 0.f);
+        v = fmaf(-a * ipiv, q, v);
+    }
+    return v;
+}
+
+template <int K, bool kStream, int kThreads>
+__global__ void __launch_bounds__(kThreads, 512 / kThreads)
+sweep_pipe_kernel(DevModel m, DevBatch b, SweepParams p, int *active_count) {
+    const int w = blockIdx.x;
+    const int N = m.n_sites;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const long long t0 = b.t[w];
+    const long long tend = b.t_end[w];
+    const long long acc_left = b.acc_end[w] - b.accepted[w];
+    if (t0 >= tend || acc_left <= 0) {
+        if (threadIdx.x == 0 && b.since[w] < 0) b.since[w] = 0;
+        return;
+    }
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ PipeCtl ctl;
+    const size_t wblock = (size_t)N * (m.ld_up + m.ld_dn);
+    float *gW = b.W32 + (size_t)w * wblock;
+    unsigned char *cur = smem;
+    DelayedSpin<K> SU, SD;
+    if constexpr (kStream) {
+        SU.W = gW;
+    } else {
+        SU.W = reinterpret_cast<float *>(cur);
+        cur += wblock * sizeof(float);
+    }
+    SU.ld = m.ld_up;
+    SD.W = SU.W + (size_t)N * m.ld_up;
+    SD.ld = m.ld_dn;
+    SU.P = reinterpret_cast<float *>(cur); cur += (size_t)N * K * sizeof(float);
+    SD.P = reinterpret_cast<float *>(cur); cur += (size_t)N * K * sizeof(float);
+    SU.Q = reinterpret_cast<float *>(cur); cur += (size_t)m.ld_up * K * sizeof(float);
+    SD.Q = reinterpret_cast<float *>(cur); cur += (size_t)m.ld_dn * K * sizeof(float);
+    int *nbr_off = reinterpret_cast<int *>(cur); cur += (size_t)(N + 1) * sizeof(int);
+    short2 *bonds = reinterpret_cast<short2 *>(cur); cur += (size_t)m.n_bonds * sizeof(short2);
+    short *nbr = reinterpret_cast<short *>(cur); cur += (size_t)2 * m.n_bonds * sizeof(short);
+    short *kup = reinterpret_cast<short *>(cur); cur += (size_t)N * sizeof(short);
+    short *kdn = reinterpret_cast<short *>(cur);
+
+    if constexpr (!kStream) {
+        const int nvec = (int)(wblock / 4);
+        const float4 *src = reinterpret_cast<const float4 *>(gW);
+        float4 *dst = reinterpret_cast<float4 *>(SU.W);
+        for (int e = tid; e < nvec; e += blockDim.x) dst[e] = src[e];
+    }
+    delayed_zero<K>(SU, N);
+    delayed_zero<K>(SD, N);
+    for (int e = tid; e < m.n_bonds; e += blockDim.x) bonds[e] = m.bonds[e];
+    for (int e = tid; e < 2 * m.n_bonds; e += blockDim.x) nbr[e] = m.nbr[e];
+    for (int e = tid; e <= N; e += blockDim.x) nbr_off[e] = m.nbr_off[e];
+    for (int s = tid; s < N; s += blockDim.x) {
+        kup[s] = b.kappa_up[(size_t)w * N + s];
+        kdn[s] = b.kappa_dn[(size_t)w * N + s];
+    }
+    __syncthreads();
+    double zc = 0.0;
+    for (int e = tid; e < m.n_bonds; e += blockDim.x) {
+        const short2 bd = bonds[e];
+        zc += ((kup[bd.x] != 0 && kdn[bd.y] != 0) || (kup[bd.y] != 0 && kdn[bd.x] != 0)) ? 1.0 : 0.0;
+    }
+    zc = block_sum(zc, ctl.red);
+    const int R = p.refresh_every;
+    const int M = p.measure_every;
+    if (tid == 0) {
+        ctl.t = t0;
+        ctl.acc = 0;
+        ctl.since = b.since[w] < 0 ? 0 : b.since[w];
+        ctl.zmu = (int)zc;
+        ctl.m = 0;
+        ctl.pend = 0;
+        ctl.slot = 0;
+        ctl.dev = 0;
+        ctl.next_meas = (t0 / M + 1) * M;
+        make_thr(ctl.thr, m.thr_table, ctl.zmu, p.accept_rule);
+    }
+    __syncthreads();
+
+    long long n_meas = 0;
+    double se = 0.0, se2 = 0.0;
+    while (true) {
+        const int pend = ctl.pend, slot = ctl.slot, mm = ctl.m;
+        if (warp == 0) {
+            // scan for the next accepted move
+            const PendingMove pm = ctl.mv[slot];
+            const float ipu = pend ? 1.f / pm.piv_u : 0.f, ipd = pend ? 1.f / pm.piv_d : 0.f;
+            long long t = ctl.t;
+            const long long acc = ctl.acc, next_meas = ctl.next_meas;
+            const int since = ctl.since;
+            const Thr thr = ctl.thr;
+            int state = 2;
+            while (true) {
+                if (t == next_meas) { state = 3; break; }
+                if (t >= tend || since >= R || acc >= acc_left) break;
+                const long long lim = min(tend, next_meas) - t;
+                const int win = lim < 32 ? (int)lim : 32;
+                bool accd = false, bad = false;
+                int Ku = 0, lu = 0, Kd = 0, ld = 0;
+                float pu = 0.f, pd = 0.f;
+                if (lane < win) {
+                    unsigned long long u53;
+                    int bi;
+                    proposal_bits(p.seed, w, t + lane, m.n_bonds, u53, bi);
+                    const short2 bd = bonds[bi];
+                    const int c = cmp_r_thr(u53, thr);
+                    if (p.accept_rule != 0 || c <= 0) {
+                        const int i = bd.x, j = bd.y;
+                        const int kui = kup[i], kuj = kup[j], kdi = kdn[i], kdj = kdn[j];
+                        const bool f1 = kui != 0 && kdj != 0;
+                        const bool f2 = kuj != 0 && kdi != 0;
+                        if (f1 || f2) {
+                            if (f1) { Ku = j; lu = kui - 1; Kd = i; ld = kdj - 1; }
+                            else    { Ku = i; lu = kuj - 1; Kd = j; ld = kdi - 1; }
+                            pu = eff_after<K>(SU, Ku, lu, mm, pend, pm.Ku, pm.lu, ipu);
+                            pd = eff_after<K>(SD, Kd, ld, mm, pend, pm.Kd, pm.ld, ipd);
+                            accd = decide(pu, pd, u53, c, thr, p.accept_rule, bad);
+                        }
+                    }
+                }
+                if (__any_sync(0xffffffffu, bad) && bad) atomicOr(&b.status[w], kStatusNonFinite);
+                const unsigned mask = __ballot_sync(0xffffffffu, accd);
+                if (mask) {
+                    const int f = __ffs(mask) - 1;
+                    if (lane == f) ctl.mv[slot ^ 1] = PendingMove{Ku, lu, Kd, ld, pu, pd};
+                    t += f + 1;
+                    state = 1;
+                    break;
+                }
+                t += win;
+            }
+            if (state == 1) {
+                __syncwarp();
+                const PendingMove nm = ctl.mv[slot ^ 1];
+                // Z_mu change of the move (configuration before it): the up spin
+                // moves Kd -> Ku, the down spin Ku -> Kd
+                int dz = 0;
+                for (int e = nbr_off[nm.Ku] + lane; e < nbr_off[nm.Ku + 1]; e += 32) {
+                    const int k = nbr[e];
+                    if (k != nm.Kd) dz += kup[k] == 0 ? 1 : -1;
+                }
+                for (int e = nbr_off[nm.Kd] + lane; e < nbr_off[nm.Kd + 1]; e += 32) {
+                    const int k = nbr[e];
+                    if (k != nm.Ku) dz += kup[k] != 0 ? 1 : -1;
+                }
+                dz = __reduce_add_sync(0xffffffffu, dz);
+                if (lane == 0) ctl.dz = dz;
+            }
+            if (lane == 0) { ctl.t = t; ctl.state = state; }
+        } else if (pend) {
+            // factor column mm of the pending move, over columns [0, mm)
+            const PendingMove pm = ctl.mv[slot];
+            const float ipu = 1.f / pm.piv_u, ipd = 1.f / pm.piv_d;
+            const int tot = 2 * N + m.ld_up + m.ld_dn;
+            const int nt = blockDim.x - 32, id = tid - 32;
+            if constexpr (kStream) {
+                for (int base = 0; base < tot; base += 4 * nt) {
+                    float wv[4];
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) {
+                        const int e = base + q * nt + id;
+                        wv[q] = 0.f;
+                        if (e < N) wv[q] = SU.W[(size_t)e * SU.ld + pm.lu];
+                        else if (e < 2 * N) wv[q] = SD.W[(size_t)(e - N) * SD.ld + pm.ld];
+                        else if (e < 2 * N + m.ld_up) wv[q] = SU.W[(size_t)pm.Ku * SU.ld + (e - 2 * N)];
+                        else if (e < tot) wv[q] = SD.W[(size_t)pm.Kd * SD.ld + (e - 2 * N - m.ld_up)];
+                    }
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) {
+                        const int e = base + q * nt + id;
+                        if (e < N) SU.P[(size_t)e * K + mm] = (wv[q] - SU.dot_lt(e, pm.lu, mm)) * ipu;
+                        else if (e < 2 * N) SD.P[(size_t)(e - N) * K + mm] = (wv[q] - SD.dot_lt(e - N, pm.ld, mm)) * ipd;
+                        else if (e < 2 * N + m.ld_up) {
+                            const int c = e - 2 * N;
+                            SU.Q[(size_t)c * K + mm] = wv[q] - SU.dot_lt(pm.Ku, c, mm) - (c == pm.lu ? 1.f : 0.f);
+                        } else if (e < tot) {
+                            const int c = e - 2 * N - m.ld_up;
+                            SD.Q[(size_t)c * K + mm] = wv[q] - SD.dot_lt(pm.Kd, c, mm) - (c == pm.ld ? 1.f : 0.f);
+                        }
+                    }
+                }
+            } else {
+                for (int e = id; e < tot; e += nt) {
+                    if (e < N) SU.P[(size_t)e * K + mm] = SU.eff_lt(e, pm.lu, mm) * ipu;
+                    else if (e < 2 * N) SD.P[(size_t)(e - N) * K + mm] = SD.eff_lt(e - N, pm.ld, mm) * ipd;
+                    else if (e < 2 * N + m.ld_up) {
+                        const int c = e - 2 * N;
+                        SU.Q[(size_t)c * K + mm] = SU.eff_lt(pm.Ku, c, mm) - (c == pm.lu ? 1.f : 0.f);
+                    } else {
+                        const int c = e - 2 * N - m.ld_up;
+                        SD.Q[(size_t)c * K + mm] = SD.eff_lt(pm.Kd, c, mm) - (c == pm.ld ? 1.f : 0.f);
+                    }
+                }
+            }
+        }
+        __syncthreads();
+        const int state = ctl.state;
+        const int mnew = pend ? mm + 1 : mm;
+        if (mnew == K) {
+            if constexpr (kStream) {
+                delayed_flush_stream<K>(SU, N, kup, &ctl.dev);
+                delayed_flush_stream<K>(SD, N, kdn, &ctl.dev);
+            } else {
+                delayed_flush<K>(SU, N, kup, &ctl.dev);
+                delayed_flush<K>(SD, N, kdn, &ctl.dev);
+            }
+            __syncthreads();
+            delayed_zero<K>(SU, N);
+            delayed_zero<K>(SD, N);
+        }
+        if (tid == 0) {
+            int since = ctl.since;
+            ctl.m = mnew == K ? 0 : mnew;
+            if (mnew == K) {
+                // adaptive refresh: rounding past the tolerance ends this walker's run
+                if (__int_as_float(ctl.dev) > p.drift_tol) since = R;
+                ctl.dev = 0;
+            }
+            if (state == 1) {
+                // apply the move just accepted: configuration, Z_mu, threshold
+                const PendingMove nm = ctl.mv[slot ^ 1];
+                kup[nm.Ku] = (short)(nm.lu + 1); kup[nm.Kd] = 0;
+                kdn[nm.Kd] = (short)(nm.ld + 1); kdn[nm.Ku] = 0;
+                ctl.zmu += ctl.dz;
+                make_thr(ctl.thr, m.thr_table, ctl.zmu, p.accept_rule);
+                since += 1;
+                ctl.acc += 1;
+                ctl.slot = slot ^ 1;
+            }
+            ctl.since = since;
+            ctl.pend = state == 1;
+        }
+        __syncthreads();
+        if (state == 3) {
+            const double e = delayed_local_energy<K>(m, bonds, kup, kdn, SU, SD, ctl.red);
+            if (tid == 0) {
+                se += e;
+                se2 += e * e;
+                n_meas += 1;
+                ctl.next_meas += M;
+            }
+            __syncthreads();
+        }
+        if (state == 2) break;
+    }
+    if (ctl.m > 0) {
+        if constexpr (kStream) {
+            delayed_flush_stream<K>(SU, N, kup, &ctl.dev);
+            delayed_flush_stream<K>(SD, N, kdn, &ctl.dev);
+        } else {
+            delayed_flush<K>(SU, N, kup, &ctl.dev);
+            delayed_flush<K>(SD, N, kdn, &ctl.dev);
+        }
+        __syncthreads();
+    }
+    if constexpr (!kStream) {
+        const int nvec = (int)(wblock / 4);
+        const float4 *src = reinterpret_cast<const float4 *>(SU.W);
+        float4 *dst = reinterpret_cast<float4 *>(gW);
+        for (int e = tid; e < nvec; e += blockDim.x) dst[e] = src[e];
+    }
+    for (int s = tid; s < N; s += blockDim.x) {
+        b.kappa_up[(size_t)w * N + s] = kup[s];
+        b.kappa_dn[(size_t)w * N + s] = kdn[s];
+    }
+    if (tid == 0) {
+        const long long t = ctl.t;
+        b.t[w] = t;
+        b.since[w] = ctl.since >= R ? -1 : ctl.since;
+        b.accepted[w] += ctl.acc;
+        b.proposals[w] += t - t0;
+        b.sum_e[w] += se;
+        b.sum_e2[w] += se2;
+        b.n_meas[w] += n_meas;
+        if (t < tend && ctl.acc < acc_left) atomicAdd(active_count, 1);
+    }
+}
+
 size_t delayed_smem_bytes(const DevModel &m, int K, bool w_on_chip) {
     const size_t N = m.n_sites;
     size_t s = w_on_chip ? N * (m.ld_up + m.ld_dn) * 4 : 0;  // W
@@ -1581,9 +1894,25 @@ static cudaError_t launch_delayed_t(const DevModel &m, const DevBatch &b, const 
     return cudaGetLastError();
 }
 
+template <int K, bool kStream, int kThreads>
+static cudaError_t launch_pipe_t(const DevModel &m, const DevBatch &b, const SweepParams &p, int *active,
+                                 cudaStream_t stream) {
+    const size_t sm = delayed_smem_bytes(m, K, !kStream);
+    cudaError_t e = cudaFuncSetAttribute(sweep_pipe_kernel<K, kStream, kThreads>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    if (e != cudaSuccess) return e;
+    sweep_pipe_kernel<K, kStream, kThreads><<<b.n_walkers, kThreads, sm, stream>>>(m, b, p, active);
+    return cudaGetLastError();
+}
+
 template <int K, bool kStream>
 static cudaError_t launch_delayed(const DevModel &m, const DevBatch &b, const SweepParams &p, int *active,
                                   cudaStream_t stream) {
+    if (p.pipeline) {
+        if constexpr (!kStream) return launch_pipe_t<K, false, 512>(m, b, p, active, stream);
+        if (p.stream_threads == 128) return launch_pipe_t<K, true, 128>(m, b, p, active, stream);
+        return launch_pipe_t<K, true, 256>(m, b, p, active, stream);
+    }
     if constexpr (!kStream) return launch_delayed_t<K, false, 512>(m, b, p, active, stream);
     if (p.stream_threads == 128) return launch_delayed_t<K, true, 128>(m, b, p, active, stream);
     return launch_delayed_t<K, true, 256>(m, b, p, active, stream);

@@ -189,6 +189,10 @@ class Engine:
         self._check(self._lib.kvmc_walker_drift(self.h, _lib.ptr(d)))
         return d
 
+    def set_pipeline(self, on: bool = True):
+        """Delayed form: scan for the next move while the last one's factor column is written."""
+        self._check(self._lib.kvmc_set_tuning(self.h, 2, int(bool(on))))
+
     def set_stream_threads(self, threads: int):
         """W in HBM: threads per walker's CTA (128 or 256)."""
         self._check(self._lib.kvmc_set_tuning(self.h, 1, int(threads)))

@@ -130,6 +130,7 @@ def test_long_chains_match_c_oracle(kv, precision, delay_k, accept):
                     refresh_interval=(64 if precision == "mixed" else 0), delay_k=delay_k)
     if precision == "mixed":
         assert eng.config()["delay_k"] == max(delay_k, 1)
+        eng.set_pipeline(False)   # the sequential scan / column-write kernel; the pipelined one is the default
     eng.init()
     ku0, kd0, _ = eng.get_state()
     eng.sweep(proposals)
@@ -470,3 +471,38 @@ def test_placement_on_chip_is_refused_when_w_does_not_fit(kv):
     ham = ham_for(kv, 384)
     with pytest.raises(kv.KvmcError):
         kv.Engine(ham, 2, precision="mixed", w_placement="chip")
+
+
+@pytest.mark.parametrize("N,delay_k,placement", [(96, 4, "chip"), (96, 16, "chip"), (96, 8, "hbm"), (216, 12, "hbm"),
+                                                 (216, 12, "chip"), (384, 8, "hbm")])
+def test_pipelined_scan_chains_match_c_oracle(kv, N, delay_k, placement):
+    """The scan for the next move overlapping the factor-column write of the last one."""
+    walkers, proposals, seed = 8, 2400, 53
+    ham = ham_for(kv, N)
+    eng = kv.Engine(ham, walkers, precision="mixed", seed=seed, refresh_interval=96, delay_k=delay_k,
+                    w_placement=placement)
+    eng.set_pipeline(True)
+    eng.init()
+    ku0, kd0, _ = eng.get_state()
+    st = eng.sweep(proposals)
+    ku1, kd1, _ = eng.get_state()
+    ws = eng.walker_stats()
+    m = oracle_c.OracleModel(ham.U_up, ham.U_down, ham.nn)
+    match = 0
+    for w in range(walkers):
+        ch = m.new_chain(ku0[w], kd0[w])
+        ch.run(seed, w, proposals, N // 2, N // 2, 0)
+        if np.array_equal(ch.ku, ku1[w]) and np.array_equal(ch.kd, kd1[w]):
+            match += 1
+            assert ch.c.accepted == ws["accepted"][w]
+            assert ws["n_meas"][w] == proposals // (N // 2)
+            assert abs(ch.c.sum_e - ws["sum_e"][w]) <= 1e-4 * max(1.0, abs(ch.c.sum_e))
+    assert match >= walkers - 1
+    assert st["bad_walkers"] == 0
+    Wu, Wd = eng.get_w()
+    for w in range(walkers):
+        assert close(Wu[w], o.reevaluateW(ham.U_up, ku1[w]), 1e-3)
+    # advance: exact move counts with the pipelined scan
+    st = eng.advance(77)
+    assert np.all(eng.walker_stats()["accepted"] == ws["accepted"] + 77)
+    eng.close()
