@@ -58,6 +58,7 @@ def args_():
     p.add_argument("--no-peaks", action="store_true")
     p.add_argument("--skip-grad", action="store_true")
     p.add_argument("--skip-uneven", action="store_true")
+    p.add_argument("--skip-large", action="store_true")
     return p.parse_args()
 
 
@@ -334,6 +335,46 @@ def uneven_run(kv, seed, device, moves=512, steps=3):
             "graph_over_sequential": res["graph"]["value"] / res["sequential"]["value"]}
 
 
+def large_run(kv, seed, device, walkers=512, moves=128, steps=2):
+    """The large lattice: 12x12 doubled cells (N=864, 432 orbitals per spin),
+    512 walkers, W (2 x 864 x 432 FP32 = 2.99 MB per walker, 1.53 GB in all)
+    in HBM with rank-16 delayed updates, FP64 refresh every 128 accepted
+    moves; and the plain FP64 form on the same walkers."""
+    from kagomevmc import autotune
+
+    ham = kv.Hamiltonian.build(432, 432, kv.DoubleKagome(1.0, 24, 12, (True, True), (False, True)))
+    ch = autotune.Choice(delay_k=16, refresh_interval=128, placement="hbm", threads=256)
+    eng = autotune.make_engine(ham, walkers, ch, seed=seed, device=device)
+    eng.set_drift_tolerance(1e-2)
+    eng.init()
+    eng.advance(moves)
+    eng.enable_timing(True)
+    eng.region_start()
+    acc = 0
+    for _ in range(steps):
+        acc += eng.advance(moves)["accepted"]
+    ms = eng.region_stop()
+    k0, _ = eng.kernel_time(0)
+    k1, _ = eng.kernel_time(1)
+    eng.close()
+    w_bytes = 2 * 864 * 432 * 4
+    flush_bytes = 2 * w_bytes / 16 * acc          # W read + written once per 16 accepted moves
+    pe = kv.Engine(ham, walkers, precision="plain", seed=seed, device=device)
+    pe.init()
+    pe.advance(8)
+    pe.region_start()
+    pacc = pe.advance(32)["accepted"]
+    pms = pe.region_stop()
+    pe.close()
+    return {"workload": f"kagome VMC, 12x12 doubled cells (N=864), {walkers} walkers, W in HBM, delayed k=16, "
+                        f"FP64 refresh every 128 accepted moves, {steps} x {moves} accepted moves per walker",
+            "value": acc / (ms * 1e-3), "unit": UNIT, "ms": ms, "sweep_ms": k0, "refresh_ms": k1,
+            "sweep_only_moves_per_s": acc / (k0 * 1e-3) if k0 else None,
+            "flush_hbm_gbs_in_sweep": flush_bytes / (k0 * 1e-3) / 1e9 if k0 else None,
+            "plain_fp64": {"value": pacc / (pms * 1e-3), "unit": UNIT, "moves_per_walker": 32},
+            "note": "refresh-bound: one walker refresh is 2*((2/3)n^3 + 2(N-n)n^2) = 0.86 GFLOP FP64"}
+
+
 def gpu_arm(a):
     import numpy as np
 
@@ -426,6 +467,7 @@ def gpu_arm(a):
     gate = None if a.skip_gate else energy_gate(ham, kv, 256, 8192, choice, a.seed + 1)
     adjoint = None if a.skip_grad else adjoint_run(kv, 4, local)
     uneven = None if a.skip_uneven else uneven_run(kv, a.seed, local)
+    large = None if a.skip_large else large_run(kv, a.seed, local)
 
     # roofline of the dominant kernel
     refreshes = tot["refreshes"]
@@ -483,7 +525,8 @@ def gpu_arm(a):
             "proposals_per_step": tot["proposals"] / a.steps * world, "acceptance": tot["accepted"] / tot["proposals"],
             "gpu_launches": tot["launches"], "e2e": e2e, "roofline": roof, "cpu_baseline": cpu,
             "plain_fp64": plain, "speedup_vs_plain_fp64": (value / plain["value"]) if plain else None,
-            "energy_gate": gate, "adjoint": adjoint, "uneven_batch": uneven, "drift": drift, "clocks": clk, "peaks_measured": peaks}
+            "energy_gate": gate, "adjoint": adjoint, "uneven_batch": uneven, "large_lattice": large,
+            "drift": drift, "clocks": clk, "peaks_measured": peaks}
     print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
