@@ -278,8 +278,11 @@ KVMC_API int kvmc_kernel_time(kvmc_handle *h, int32_t kind, double *total_ms, in
  *   KVMC_TUNE_PIPELINE: 1 = with delayed updates, one warp scans for the next
  *   accepted move while the others write the factor column of the last one
  *   (the scan applies that move as a Sherman-Morrison correction), the
- *   default; 0 = the two phases one after the other. */
-enum kvmc_tuning { KVMC_TUNE_STREAM_THREADS = 1, KVMC_TUNE_PIPELINE = 2 };
+ *   default; 0 = the two phases one after the other.
+ *   KVMC_TUNE_TC_FLUSH: 1 = with W in HBM, the rank-k flush W -= P Q^T runs
+ *   on the tensor cores (tcgen05, TF32 operands split in high and low parts,
+ *   three products accumulated in FP32 in tensor memory); 0 = FP32 FMA. */
+enum kvmc_tuning { KVMC_TUNE_STREAM_THREADS = 1, KVMC_TUNE_PIPELINE = 2, KVMC_TUNE_TC_FLUSH = 3 };
 KVMC_API int kvmc_set_tuning(kvmc_handle *h, int32_t key, int32_t value);
 
 /* The settings a handle resolved at creation: refresh and measurement

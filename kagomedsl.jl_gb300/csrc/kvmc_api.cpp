@@ -53,6 +53,7 @@ struct kvmc_handle {
     float drift_tol = 1e-4f;  // delayed form: early refresh past this unit-row deviation
     int stream_threads = 256;  // W in HBM: threads per walker
     int pipeline = 1;          // delayed form: pipelined scan / factor-column write
+    int tc_flush = 0;          // W in HBM: rank-k flush on the tensor cores
     std::string err;
 
     DevModel dm{};
@@ -190,6 +191,8 @@ int check_status(kvmc_handle *h, int *bad) {
     if (nb) {
         if (code & kvmc::kStatusSingular)
             return h->fail(KVMC_ERR_SINGULAR, "%d walker(s) have a singular tilde_U (first: walker %d)", nb, first);
+        if (code & kvmc::kStatusTimeout)
+            return h->fail(KVMC_ERR_CUDA, "%d walker(s): a tensor-core wait timed out (first: walker %d)", nb, first);
         return h->fail(KVMC_ERR_NUMERIC, "%d walker(s) produced a non-finite ratio (first: walker %d)", nb, first);
     }
     return KVMC_OK;
@@ -899,6 +902,7 @@ kvmc::SweepParams sweep_params(const kvmc_handle *h) {
     p.drift_tol = h->drift_tol;
     p.stream_threads = h->stream_threads;
     p.pipeline = h->pipeline;
+    p.tc_flush = h->tc_flush;
     return p;
 }
 
@@ -1080,7 +1084,7 @@ namespace {
 bool same_params(const kvmc::SweepParams &a, const kvmc::SweepParams &b) {
     return a.seed == b.seed && a.accept_rule == b.accept_rule && a.refresh_every == b.refresh_every &&
            a.measure_every == b.measure_every && a.delay_k == b.delay_k && a.drift_tol == b.drift_tol &&
-           a.stream_threads == b.stream_threads && a.pipeline == b.pipeline;
+           a.stream_threads == b.stream_threads && a.pipeline == b.pipeline && a.tc_flush == b.tc_flush;
 }
 
 // Captures one graph: from s0, every handle's stream runs its (sweep,
@@ -1308,6 +1312,19 @@ extern "C" int kvmc_set_tuning(kvmc_handle *h, int32_t key, int32_t value) {
         if (std::max(h->ld_up, h->ld_dn) > 4 * value)
             return h->fail(KVMC_ERR_ARGUMENT, "%d threads cannot flush %d columns", value, std::max(h->ld_up, h->ld_dn));
         h->stream_threads = value;
+        return KVMC_OK;
+    }
+    if (key == KVMC_TUNE_TC_FLUSH) {
+        if (value != 0 && value != 1) return h->fail(KVMC_ERR_ARGUMENT, "tensor-core flush must be 0 or 1");
+        if (value == 1) {
+            if (!h->mixed || h->cplx || h->smem_w || h->delay_k < 4)
+                return h->fail(KVMC_ERR_UNSUPPORTED,
+                               "the tensor-core flush serves the mixed real form with W in HBM and delayed updates");
+            const size_t need = kvmc::delayed_smem_bytes(h->dm, h->delay_k, false) + kvmc::tc_flush_smem_bytes();
+            if (need + 1024 > (size_t)kvmc::max_smem_optin(h->device))
+                return h->fail(KVMC_ERR_UNSUPPORTED, "the tensor-core flush needs %zu B shared memory", need);
+        }
+        h->tc_flush = value;
         return KVMC_OK;
     }
     if (key == KVMC_TUNE_PIPELINE) {

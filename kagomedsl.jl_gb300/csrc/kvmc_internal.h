@@ -61,6 +61,7 @@ struct DevBatch {
 enum : int {
     kStatusSingular = 1,
     kStatusNonFinite = 2,
+    kStatusTimeout = 4,   // a bounded wait on the tensor cores gave up
 };
 
 struct SweepParams {
@@ -72,6 +73,7 @@ struct SweepParams {
     float drift_tol;      // delayed form: unit-row deviation that triggers an early refresh
     int stream_threads;   // W in HBM: threads per walker's CTA (128 or 256)
     int pipeline;         // delayed form: scan for the next move while the last one's factor column is written
+    int tc_flush;         // W in HBM: rank-k flush on the tensor cores (tcgen05, 3xTF32)
 };
 
 // Launchers.  All enqueue on `stream` and return the launch error.
@@ -101,6 +103,8 @@ size_t mixed_sweep_smem(const DevModel &m);
 // Shared memory of the delayed-update sweep: with W on chip, or with W in
 // HBM (only P, Q and the walker's small state on chip).
 size_t delayed_smem_bytes(const DevModel &m, int K, bool w_on_chip);
+// Extra shared memory of the tensor-core flush (its operand tiles).
+size_t tc_flush_smem_bytes();
 size_t refresh_smem(const DevModel &m);
 size_t refresh_scratch_block(const DevModel &m);
 size_t refresh_large_smem(const DevModel &m);

@@ -1074,6 +1074,214 @@ __device__ void delayed_flush_stream(const DelayedSpin<K> &S, int N, const short
     if (dmax > 0.f) atomicMax(dev, __float_as_int(dmax));
 }
 
+// ---------------------------------------------------------------------------
+// The rank-k flush W -= P Q^T on the tensor cores (tcgen05, kind::tf32),
+// for W in HBM.  P (N x K) and Q (ld x K) are split into TF32 high and low
+// parts (hi = x with the low 13 mantissa bits cleared, lo = x - hi, exact),
+// and D = Ph Qh^T + Ph Ql^T + Pl Qh^T accumulates in TMEM in FP32: the
+// product to FP32 accuracy (3xTF32).  Operand tiles sit in shared memory in
+// the no-swizzle K-major layout, core matrices of 8 rows x 16 bytes:
+// element (row, k) of a tile with kk columns at float index
+// ((row/8) * (kk/4) + k/4) * 32 + (row%8) * 4 + k%4, so the leading-dimension
+// offset (next 4 k) is 128 bytes and the stride offset (next 8 rows) is
+// kk * 32 bytes.  One thread issues the MMAs of a 128-row tile of P against
+// a chunk of up to 128 columns of Q and commits them to an mbarrier; every
+// warp then reads its 32 TMEM lanes (rows) of D, half of the columns each,
+// and updates its rows of W in place.
+// ---------------------------------------------------------------------------
+namespace tc {
+
+constexpr int kTileM = 128;   // rows of P per MMA tile (TMEM lanes)
+constexpr int kChunkN = 128;  // columns of Q per chunk (TMEM columns allocated)
+constexpr int kMaxKK = 16;    // K padded to a multiple of 8
+constexpr uint32_t kWaitLimit = 1u << 20;
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ int canon(int row, int k, int kk) {
+    return ((row >> 3) * (kk >> 2) + (k >> 2)) * 32 + (row & 7) * 4 + (k & 3);
+}
+
+__device__ __forceinline__ uint64_t sdesc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+    uint64_t d = (uint64_t)((addr >> 4) & 0x3FFF);
+    d |= (uint64_t)((lbo >> 4) & 0x3FFF) << 16;
+    d |= (uint64_t)((sbo >> 4) & 0x3FFF) << 32;
+    d |= (uint64_t)1 << 46;  // descriptor version for this architecture; no swizzle, base offset 0
+    return d;
+}
+
+// kind::tf32: FP32 accumulator, TF32 A and B, both K-major, M x N
+__device__ __forceinline__ uint32_t idesc_tf32(int m, int n) {
+    return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(m >> 4) << 24);
+}
+
+__device__ __forceinline__ void mma(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t idesc, uint32_t accumulate) {
+    asm volatile("{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+                 "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}"
+                 :: "r"(d_tmem), "l"(a), "l"(b), "r"(idesc), "r"(accumulate));
+}
+
+__device__ __forceinline__ void commit(uint64_t *mbar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" :: "r"(smem_u32(mbar)));
+}
+
+// bounded wait for the mbarrier phase with this parity; false when it gave up
+__device__ __forceinline__ bool wait(uint64_t *mbar, uint32_t parity) {
+    uint32_t done = 0;
+    for (uint32_t it = 0; it < kWaitLimit && !done; ++it)
+        asm volatile("{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}"
+                     : "=r"(done) : "r"(smem_u32(mbar)), "r"(parity));
+    return done != 0;
+}
+
+__device__ __forceinline__ void ld8(uint32_t taddr, float (&v)[8]) {
+    uint32_t r[8];
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+                 : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;");
+#pragma unroll
+    for (int j = 0; j < 8; ++j) v[j] = __uint_as_float(r[j]);
+}
+
+__device__ __forceinline__ void fence_before() { asm volatile("tcgen05.fence::before_thread_sync;"); }
+__device__ __forceinline__ void fence_after() { asm volatile("tcgen05.fence::after_thread_sync;"); }
+
+__device__ __forceinline__ void split_tf32(float x, float &hi, float &lo) {
+    hi = __uint_as_float(__float_as_uint(x) & 0xFFFFE000u);
+    lo = x - hi;
+}
+
+// Per-CTA tensor-core state: TMEM columns, the commit barrier and its phase.
+struct State {
+    float *a_hi, *a_lo, *b_hi, *b_lo;  // operand tiles in shared memory
+    uint64_t *mbar;
+    uint32_t tmem;
+    uint32_t phase;
+};
+
+// warp 0 allocates kChunkN TMEM columns; thread 0 initialises the barrier
+__device__ void setup(State &st, uint32_t *tmem_slot) {
+    if (threadIdx.x == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(smem_u32(st.mbar)));
+        asm volatile("fence.mbarrier_init.release.cluster;");
+    }
+    if ((threadIdx.x >> 5) == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
+                     :: "r"(smem_u32(tmem_slot)), "r"((uint32_t)kChunkN));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    fence_before();
+    __syncthreads();
+    fence_after();
+    st.tmem = *tmem_slot;
+    st.phase = 0;
+}
+
+__device__ void teardown(const State &st) {
+    fence_before();
+    __syncthreads();
+    fence_after();
+    if ((threadIdx.x >> 5) == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" :: "r"(st.tmem), "r"((uint32_t)kChunkN));
+}
+
+}  // namespace tc
+
+template <int K>
+__device__ void delayed_flush_tc(const DelayedSpin<K> &S, int N, const short *kappa, int *dev, tc::State &st,
+                                 int *status) {
+    constexpr int KK = (K + 7) / 8 * 8;
+    static_assert(KK <= tc::kMaxKK, "delay depth beyond the operand tiles");
+    const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5, nwarps = nt >> 5;
+    const int quarter = warp & 3, half = warp >> 2, halves = nwarps >> 2;  // lanes 32*quarter.. of TMEM
+    const uint32_t lbo = 128, sbo = KK * 32;
+    float dmax = 0.f;
+    for (int c0 = 0; c0 < S.ld; c0 += tc::kChunkN) {
+        const int nvalid = min(tc::kChunkN, S.ld - c0);
+        const int nc = (nvalid + 15) / 16 * 16;
+        for (int e = tid; e < nc * KK; e += nt) {
+            const int row = e / KK, k = e - row * KK;
+            const float x = (row < nvalid && k < K) ? S.Q[(size_t)(c0 + row) * K + k] : 0.f;
+            float hi, lo;
+            tc::split_tf32(x, hi, lo);
+            st.b_hi[tc::canon(row, k, KK)] = hi;
+            st.b_lo[tc::canon(row, k, KK)] = lo;
+        }
+        const uint32_t idesc = tc::idesc_tf32(tc::kTileM, nc);
+        for (int r0 = 0; r0 < N; r0 += tc::kTileM) {
+            for (int e = tid; e < tc::kTileM * KK; e += nt) {
+                const int row = e / KK, k = e - row * KK;
+                const float x = (r0 + row < N && k < K) ? S.P[(size_t)(r0 + row) * K + k] : 0.f;
+                float hi, lo;
+                tc::split_tf32(x, hi, lo);
+                st.a_hi[tc::canon(row, k, KK)] = hi;
+                st.a_lo[tc::canon(row, k, KK)] = lo;
+            }
+            asm volatile("fence.proxy.async.shared::cta;");
+            tc::fence_before();
+            __syncthreads();
+            tc::fence_after();
+            if (tid == 0) {
+                const float *As[3] = {st.a_hi, st.a_hi, st.a_lo};
+                const float *Bs[3] = {st.b_hi, st.b_lo, st.b_hi};
+                uint32_t acc = 0;
+#pragma unroll
+                for (int s = 0; s < KK / 8; ++s) {
+#pragma unroll
+                    for (int q = 0; q < 3; ++q) {
+                        const uint64_t ad = tc::sdesc(tc::smem_u32(As[q]) + s * 2 * lbo, lbo, sbo);
+                        const uint64_t bd = tc::sdesc(tc::smem_u32(Bs[q]) + s * 2 * lbo, lbo, sbo);
+                        tc::mma(st.tmem, ad, bd, idesc, acc);
+                        acc = 1;
+                    }
+                }
+                tc::commit(st.mbar);
+            }
+            const bool ok = tc::wait(st.mbar, st.phase);
+            st.phase ^= 1u;
+            if (!ok && lane == 0) atomicOr(status, kStatusTimeout);
+            tc::fence_after();
+            // epilogue: row r0 + 32*quarter + lane, this warp's share of the chunk's columns
+            const int r = r0 + 32 * quarter + lane;
+            const int l = r < N ? kappa[r] - 1 : -1;
+            float *wr = S.W + (size_t)(r < N ? r : 0) * S.ld + c0;
+            for (int cc = 8 * half; cc < nc; cc += 8 * halves) {
+                float d[8];
+                tc::ld8(st.tmem + ((uint32_t)(32 * quarter) << 16) + (uint32_t)cc, d);
+                if (r < N && ok) {
+                    if (cc + 8 <= nvalid) {
+                        float4 *p4 = reinterpret_cast<float4 *>(wr + cc);
+                        float4 x0 = p4[0], x1 = p4[1];
+                        x0.x -= d[0]; x0.y -= d[1]; x0.z -= d[2]; x0.w -= d[3];
+                        x1.x -= d[4]; x1.y -= d[5]; x1.z -= d[6]; x1.w -= d[7];
+                        p4[0] = x0;
+                        p4[1] = x1;
+                        if (l >= 0) {
+                            const float v[8] = {x0.x, x0.y, x0.z, x0.w, x1.x, x1.y, x1.z, x1.w};
+#pragma unroll
+                            for (int j = 0; j < 8; ++j)
+                                dmax = fmaxf(dmax, fabsf(v[j] - (c0 + cc + j == l ? 1.f : 0.f)));
+                        }
+                    } else {
+                        for (int j = 0; j < 8 && cc + j < nvalid; ++j) {
+                            const float v = wr[cc + j] - d[j];
+                            wr[cc + j] = v;
+                            if (l >= 0) dmax = fmaxf(dmax, fabsf(v - (c0 + cc + j == l ? 1.f : 0.f)));
+                        }
+                    }
+                }
+            }
+            tc::fence_before();
+            __syncthreads();  // the next tile rewrites the operand tiles and TMEM
+            tc::fence_after();
+        }
+    }
+    if (dmax > 0.f) atomicMax(dev, __float_as_int(dmax));
+}
+
+size_t tc_flush_smem_bytes() { return (size_t)2 * (tc::kTileM + tc::kChunkN) * tc::kMaxKK * 4 + 128; }
+
 template <int K>
 __device__ void delayed_zero(const DelayedSpin<K> &S, int N) {
     float4 *p = reinterpret_cast<float4 *>(S.P);
@@ -1446,7 +1654,7 @@ __device__ __forceinline__ float eff_after(const DelayedSpin<K> &S, int r, int c
     return v;
 }
 
-template <int K, bool kStream, int kThreads>
+template <int K, bool kStream, int kThreads, bool kTC>
 __global__ void __launch_bounds__(kThreads, 512 / kThreads)
 sweep_pipe_kernel(DevModel m, DevBatch b, SweepParams p, int *active_count) {
     const int w = blockIdx.x;
@@ -1483,6 +1691,19 @@ sweep_pipe_kernel(DevModel m, DevBatch b, SweepParams p, int *active_count) {
     short *nbr = reinterpret_cast<short *>(cur); cur += (size_t)2 * m.n_bonds * sizeof(short);
     short *kup = reinterpret_cast<short *>(cur); cur += (size_t)N * sizeof(short);
     short *kdn = reinterpret_cast<short *>(cur);
+    [[maybe_unused]] __shared__ __align__(8) uint64_t tc_mbar;
+    [[maybe_unused]] __shared__ uint32_t tc_tmem_slot;
+    [[maybe_unused]] tc::State tcs{};
+    if constexpr (kTC) {
+        cur = reinterpret_cast<unsigned char *>(kdn + N);
+        cur = reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(cur) + 127) & ~uintptr_t(127));
+        tcs.a_hi = reinterpret_cast<float *>(cur); cur += tc::kTileM * tc::kMaxKK * sizeof(float);
+        tcs.a_lo = reinterpret_cast<float *>(cur); cur += tc::kTileM * tc::kMaxKK * sizeof(float);
+        tcs.b_hi = reinterpret_cast<float *>(cur); cur += tc::kChunkN * tc::kMaxKK * sizeof(float);
+        tcs.b_lo = reinterpret_cast<float *>(cur);
+        tcs.mbar = &tc_mbar;
+        tc::setup(tcs, &tc_tmem_slot);
+    }
 
     if constexpr (!kStream) {
         const int nvec = (int)(wblock / 4);
@@ -1642,7 +1863,10 @@ sweep_pipe_kernel(DevModel m, DevBatch b, SweepParams p, int *active_count) {
         const int state = ctl.state;
         const int mnew = pend ? mm + 1 : mm;
         if (mnew == K) {
-            if constexpr (kStream) {
+            if constexpr (kTC) {
+                delayed_flush_tc<K>(SU, N, kup, &ctl.dev, tcs, &b.status[w]);
+                delayed_flush_tc<K>(SD, N, kdn, &ctl.dev, tcs, &b.status[w]);
+            } else if constexpr (kStream) {
                 delayed_flush_stream<K>(SU, N, kup, &ctl.dev);
                 delayed_flush_stream<K>(SD, N, kdn, &ctl.dev);
             } else {
@@ -1689,7 +1913,10 @@ sweep_pipe_kernel(DevModel m, DevBatch b, SweepParams p, int *active_count) {
         if (state == 2) break;
     }
     if (ctl.m > 0) {
-        if constexpr (kStream) {
+        if constexpr (kTC) {
+            delayed_flush_tc<K>(SU, N, kup, &ctl.dev, tcs, &b.status[w]);
+            delayed_flush_tc<K>(SD, N, kdn, &ctl.dev, tcs, &b.status[w]);
+        } else if constexpr (kStream) {
             delayed_flush_stream<K>(SU, N, kup, &ctl.dev);
             delayed_flush_stream<K>(SD, N, kdn, &ctl.dev);
         } else {
@@ -1698,6 +1925,7 @@ sweep_pipe_kernel(DevModel m, DevBatch b, SweepParams p, int *active_count) {
         }
         __syncthreads();
     }
+    if constexpr (kTC) tc::teardown(tcs);
     if constexpr (!kStream) {
         const int nvec = (int)(wblock / 4);
         const float4 *src = reinterpret_cast<const float4 *>(SU.W);
@@ -1894,14 +2122,14 @@ static cudaError_t launch_delayed_t(const DevModel &m, const DevBatch &b, const 
     return cudaGetLastError();
 }
 
-template <int K, bool kStream, int kThreads>
+template <int K, bool kStream, int kThreads, bool kTC = false>
 static cudaError_t launch_pipe_t(const DevModel &m, const DevBatch &b, const SweepParams &p, int *active,
                                  cudaStream_t stream) {
-    const size_t sm = delayed_smem_bytes(m, K, !kStream);
-    cudaError_t e = cudaFuncSetAttribute(sweep_pipe_kernel<K, kStream, kThreads>,
+    const size_t sm = delayed_smem_bytes(m, K, !kStream) + (kTC ? tc_flush_smem_bytes() : 0);
+    cudaError_t e = cudaFuncSetAttribute(sweep_pipe_kernel<K, kStream, kThreads, kTC>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     if (e != cudaSuccess) return e;
-    sweep_pipe_kernel<K, kStream, kThreads><<<b.n_walkers, kThreads, sm, stream>>>(m, b, p, active);
+    sweep_pipe_kernel<K, kStream, kThreads, kTC><<<b.n_walkers, kThreads, sm, stream>>>(m, b, p, active);
     return cudaGetLastError();
 }
 
@@ -1910,6 +2138,10 @@ static cudaError_t launch_delayed(const DevModel &m, const DevBatch &b, const Sw
                                   cudaStream_t stream) {
     if (p.pipeline) {
         if constexpr (!kStream) return launch_pipe_t<K, false, 512>(m, b, p, active, stream);
+        if (p.tc_flush) {
+            if (p.stream_threads == 128) return launch_pipe_t<K, true, 128, true>(m, b, p, active, stream);
+            return launch_pipe_t<K, true, 256, true>(m, b, p, active, stream);
+        }
         if (p.stream_threads == 128) return launch_pipe_t<K, true, 128>(m, b, p, active, stream);
         return launch_pipe_t<K, true, 256>(m, b, p, active, stream);
     }

@@ -506,3 +506,44 @@ def test_pipelined_scan_chains_match_c_oracle(kv, N, delay_k, placement):
     st = eng.advance(77)
     assert np.all(eng.walker_stats()["accepted"] == ws["accepted"] + 77)
     eng.close()
+
+
+@pytest.mark.parametrize("N,delay_k,threads", [(96, 8, 256), (96, 16, 128), (216, 12, 256), (216, 4, 256),
+                                               (384, 8, 256)])
+def test_tensor_core_flush_chains_match_c_oracle(kv, N, delay_k, threads):
+    """W in HBM with the rank-k flush on the tensor cores (tcgen05, 3xTF32)."""
+    walkers, proposals, seed = 8, 2400, 59
+    ham = ham_for(kv, N)
+    eng = kv.Engine(ham, walkers, precision="mixed", seed=seed, refresh_interval=96, delay_k=delay_k,
+                    w_placement="hbm")
+    eng.set_stream_threads(threads)
+    eng.set_tc_flush(True)
+    eng.init()
+    ku0, kd0, _ = eng.get_state()
+    st = eng.sweep(proposals)
+    ku1, kd1, _ = eng.get_state()
+    ws = eng.walker_stats()
+    m = oracle_c.OracleModel(ham.U_up, ham.U_down, ham.nn)
+    match = 0
+    for w in range(walkers):
+        ch = m.new_chain(ku0[w], kd0[w])
+        ch.run(seed, w, proposals, N // 2, N // 2, 0)
+        if np.array_equal(ch.ku, ku1[w]) and np.array_equal(ch.kd, kd1[w]):
+            match += 1
+            assert ch.c.accepted == ws["accepted"][w]
+            assert abs(ch.c.sum_e - ws["sum_e"][w]) <= 1e-4 * max(1.0, abs(ch.c.sum_e))
+    assert match >= walkers - 1
+    assert st["bad_walkers"] == 0
+    Wu, Wd = eng.get_w()
+    for w in range(walkers):
+        assert close(Wu[w], o.reevaluateW(ham.U_up, ku1[w]), 1e-3)
+        assert close(Wd[w], o.reevaluateW(ham.U_down, kd1[w]), 1e-3)
+    eng.close()
+
+
+def test_tensor_core_flush_refused_off_its_path(kv):
+    ham = ham_for(kv, 96)
+    eng = kv.Engine(ham, 2, precision="mixed", delay_k=8, w_placement="chip")
+    with pytest.raises(kv.KvmcError):
+        eng.set_tc_flush(True)
+    eng.close()
