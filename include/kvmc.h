@@ -281,8 +281,15 @@ KVMC_API int kvmc_kernel_time(kvmc_handle *h, int32_t kind, double *total_ms, in
  *   default; 0 = the two phases one after the other.
  *   KVMC_TUNE_TC_FLUSH: 1 = with W in HBM, the rank-k flush W -= P Q^T runs
  *   on the tensor cores (tcgen05, TF32 operands split in high and low parts,
- *   three products accumulated in FP32 in tensor memory); 0 = FP32 FMA. */
-enum kvmc_tuning { KVMC_TUNE_STREAM_THREADS = 1, KVMC_TUNE_PIPELINE = 2, KVMC_TUNE_TC_FLUSH = 3 };
+ *   three products accumulated in FP32 in tensor memory); 0 = FP32 FMA.
+ *   KVMC_TUNE_REFRESH32: 1 = the periodic refresh of the FP32 W runs as
+ *   iterative refinement on the FP32 pipes (FP32 LU and solves, residual
+ *   with exact products and compensated sums), walkers that do not converge
+ *   falling back to the FP64 refresh; 0 = FP64 LU and solves.  Starts,
+ *   kvmc_set_state and kvmc_refresh always use FP64.  The default is 1 for
+ *   the mixed real form with at most 128 orbitals per spin, else 0. */
+enum kvmc_tuning { KVMC_TUNE_STREAM_THREADS = 1, KVMC_TUNE_PIPELINE = 2, KVMC_TUNE_TC_FLUSH = 3,
+                   KVMC_TUNE_REFRESH32 = 4 };
 KVMC_API int kvmc_set_tuning(kvmc_handle *h, int32_t key, int32_t value);
 
 /* The settings a handle resolved at creation: refresh and measurement

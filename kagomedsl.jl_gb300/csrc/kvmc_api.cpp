@@ -54,6 +54,7 @@ struct kvmc_handle {
     int stream_threads = 256;  // W in HBM: threads per walker
     int pipeline = 1;          // delayed form: pipelined scan / factor-column write
     int tc_flush = 0;          // W in HBM: rank-k flush on the tensor cores
+    int refresh32 = 0;         // mixed real form: periodic refresh by FP32 iterative refinement (default <= 128 orbitals)
     std::string err;
 
     DevModel dm{};
@@ -166,6 +167,14 @@ int upload_kappa(kvmc_handle *h, const int32_t *ku, const int32_t *kd) {
 // The real and the complex kernels behind one call each
 cudaError_t refresh_launch(kvmc_handle *h, int only_due, int track_drift) {
     if (h->cplx) return kvmc::launch_refresh_c(h->dm, h->db, h->mixed, only_due, track_drift, h->stream);
+    if (h->refresh32 && only_due == 1) {
+        // FP32 refresh by iterative refinement; the walkers it gives up on are
+        // rebuilt by the FP64 refresh, then their flag is cleared
+        cudaError_t e = kvmc::launch_refresh32(h->dm, h->db, 1, track_drift, h->stream);
+        if (e == cudaSuccess) e = kvmc::launch_refresh(h->dm, h->db, true, 2, 0, h->stream);
+        if (e == cudaSuccess) e = kvmc::launch_clear_status(h->db, kvmc::kStatusRefine, h->stream);
+        return e;
+    }
     return kvmc::launch_refresh(h->dm, h->db, h->mixed, only_due, track_drift, h->stream);
 }
 
@@ -630,6 +639,28 @@ extern "C" int kvmc_create(const kvmc_model_desc *model, const kvmc_batch_desc *
     cudaMemcpy(dOff, off.data(), (N + 1) * sizeof(int), cudaMemcpyHostToDevice);
     cudaMemcpy(dNbr, nbr.data(), nbr.size() * sizeof(short), cudaMemcpyHostToDevice);
     m.U_up = dUu; m.U_dn = dUd; m.bonds = dB; m.nbr_off = dOff; m.nbr = dNbr;
+    m.U32_up_hi = m.U32_up_lo = m.U32_dn_hi = m.U32_dn_lo = nullptr;
+    if (h->mixed && !h->cplx) {
+        // FP32 (high, low) pairs of U for the FP32 refresh's residual
+        std::vector<float> hu[4];
+        const std::vector<double> *src[2] = {&Uu, &Ud};
+        for (int s2 = 0; s2 < 2; ++s2) {
+            hu[2 * s2].resize(src[s2]->size());
+            hu[2 * s2 + 1].resize(src[s2]->size());
+            for (size_t e = 0; e < src[s2]->size(); ++e) {
+                const double v = (*src[s2])[e];
+                const float hi = (float)v;
+                hu[2 * s2][e] = hi;
+                hu[2 * s2 + 1][e] = (float)(v - (double)hi);
+            }
+        }
+        float *d32[4];
+        for (int q = 0; q < 4; ++q) {
+            if ((rc = h->alloc(&d32[q], hu[q].size()))) return bail(rc);
+            cudaMemcpy(d32[q], hu[q].data(), hu[q].size() * 4, cudaMemcpyHostToDevice);
+        }
+        m.U32_up_hi = d32[0]; m.U32_up_lo = d32[1]; m.U32_dn_hi = d32[2]; m.U32_dn_lo = d32[3];
+    }
     h->U_up_host = std::move(Uu);
     h->U_dn_host = std::move(Ud);
     // thresholds fl(z / n_bonds) for z = 0..n_bonds, with their exact binary form
@@ -702,6 +733,10 @@ extern "C" int kvmc_create(const kvmc_model_desc *model, const kvmc_batch_desc *
     if (place == KVMC_W_ON_CHIP && !fits)
         return bail(h->fail(KVMC_ERR_UNSUPPORTED, "W cannot be kept on chip for this model and precision"));
     h->smem_w = fits && place != KVMC_W_HBM;
+    // the FP32 refresh by iterative refinement is the faster periodic refresh up
+    // to 128 orbitals per spin on GB300 (measured at 48 and 108; at 192 the FP64
+    // refresh is faster), so it is the default there
+    h->refresh32 = (h->mixed && !h->cplx && std::max(nu, nd) <= 128) ? 1 : 0;
     if (h->cplx && batch->delay_k != 0 && batch->delay_k != 1)
         return bail(h->fail(KVMC_ERR_UNSUPPORTED, "complex orbitals use rank-1 updates: delay_k must be 0 or 1 (got %d)",
                             batch->delay_k));
@@ -778,7 +813,10 @@ extern "C" int kvmc_init(kvmc_handle *h, const int32_t *kappa_up, const int32_t 
         std::vector<int> mark(Wk);
         for (int w = 0; w < Wk; ++w) mark[w] = redo[w] ? -1 : 0;
         KV_TRY(h->cuda(cudaMemcpyAsync(h->db.since, mark.data(), Wk * 4, cudaMemcpyHostToDevice, h->stream), "upload"));
-        KV_TRY(h->cuda(refresh_launch(h, 1, 0), "refresh launch"));
+        // FP64 refresh: the start criterion reads the pivot ratio it records
+        KV_TRY(h->cuda(h->cplx ? kvmc::launch_refresh_c(h->dm, h->db, h->mixed, 1, 0, h->stream)
+                               : kvmc::launch_refresh(h->dm, h->db, h->mixed, 1, 0, h->stream),
+                       "refresh launch"));
         KV_TRY(h->cuda(cudaStreamSynchronize(h->stream), "refresh"));
         KV_TRY(h->cuda(cudaMemcpy(ld.data(), h->db.logdet, ld.size() * 8, cudaMemcpyDeviceToHost), "logdet"));
         int left = 0;
@@ -903,6 +941,7 @@ kvmc::SweepParams sweep_params(const kvmc_handle *h) {
     p.stream_threads = h->stream_threads;
     p.pipeline = h->pipeline;
     p.tc_flush = h->tc_flush;
+    p.refresh32 = h->refresh32;
     return p;
 }
 
@@ -1084,7 +1123,8 @@ namespace {
 bool same_params(const kvmc::SweepParams &a, const kvmc::SweepParams &b) {
     return a.seed == b.seed && a.accept_rule == b.accept_rule && a.refresh_every == b.refresh_every &&
            a.measure_every == b.measure_every && a.delay_k == b.delay_k && a.drift_tol == b.drift_tol &&
-           a.stream_threads == b.stream_threads && a.pipeline == b.pipeline && a.tc_flush == b.tc_flush;
+           a.stream_threads == b.stream_threads && a.pipeline == b.pipeline && a.tc_flush == b.tc_flush &&
+           a.refresh32 == b.refresh32;
 }
 
 // Captures one graph: from s0, every handle's stream runs its (sweep,
@@ -1312,6 +1352,19 @@ extern "C" int kvmc_set_tuning(kvmc_handle *h, int32_t key, int32_t value) {
         if (std::max(h->ld_up, h->ld_dn) > 4 * value)
             return h->fail(KVMC_ERR_ARGUMENT, "%d threads cannot flush %d columns", value, std::max(h->ld_up, h->ld_dn));
         h->stream_threads = value;
+        return KVMC_OK;
+    }
+    if (key == KVMC_TUNE_REFRESH32) {
+        if (value != 0 && value != 1) return h->fail(KVMC_ERR_ARGUMENT, "refresh32 must be 0 or 1");
+        if (value == 1) {
+            if (!h->mixed || h->cplx || !kvmc::refresh32_supported(h->dm))
+                return h->fail(KVMC_ERR_UNSUPPORTED,
+                               "the FP32 refresh serves the mixed real form with at most 224 orbitals per spin");
+            if (kvmc::refresh32_smem(h->dm) + 1024 > (size_t)kvmc::max_smem_optin(h->device))
+                return h->fail(KVMC_ERR_UNSUPPORTED, "the FP32 refresh needs %zu B shared memory",
+                               kvmc::refresh32_smem(h->dm));
+        }
+        h->refresh32 = value;
         return KVMC_OK;
     }
     if (key == KVMC_TUNE_TC_FLUSH) {

@@ -28,6 +28,9 @@ struct DevModel {
     const double *U_up;  // row-major [N][n_up]
     const double *U_dn;  // row-major [N][n_dn]
     const ThrEntry *thr_table;  // [n_bonds + 1]
+    // mixed real form: U as FP32 (high, low) pairs, hi = fl32(U), lo = fl32(U - hi),
+    // row-major like U_up / U_dn (the FP32 refresh's residual); null otherwise
+    const float *U32_up_hi, *U32_up_lo, *U32_dn_hi, *U32_dn_lo;
 };
 
 // Device view of the batch state.
@@ -62,6 +65,7 @@ enum : int {
     kStatusSingular = 1,
     kStatusNonFinite = 2,
     kStatusTimeout = 4,   // a bounded wait on the tensor cores gave up
+    kStatusRefine = 8,    // the FP32 refresh did not converge: the FP64 refresh redoes the walker
 };
 
 struct SweepParams {
@@ -74,11 +78,13 @@ struct SweepParams {
     int stream_threads;   // W in HBM: threads per walker's CTA (128 or 256)
     int pipeline;         // delayed form: scan for the next move while the last one's factor column is written
     int tc_flush;         // W in HBM: rank-k flush on the tensor cores (tcgen05, 3xTF32)
+    int refresh32;        // mixed real form: FP32 refresh by iterative refinement
 };
 
 // Launchers.  All enqueue on `stream` and return the launch error.
-// only_due: refresh only walkers whose `since` is negative (marked due by the
-// sweep kernel).  track_drift: record max |W_old - W_new| per walker.
+// only_due: 1 = refresh only walkers whose `since` is negative (marked due
+// by the sweep kernel); 2 = only walkers flagged kStatusRefine.
+// track_drift: record max |W_old - W_new| per walker.
 cudaError_t launch_refresh(const DevModel &m, const DevBatch &b, bool fp32_out,
                            int only_due, int track_drift, cudaStream_t stream);
 // mixed=false: plain FP64 form (W in global memory, refresh every
@@ -103,6 +109,14 @@ size_t mixed_sweep_smem(const DevModel &m);
 // Shared memory of the delayed-update sweep: with W on chip, or with W in
 // HBM (only P, Q and the walker's small state on chip).
 size_t delayed_smem_bytes(const DevModel &m, int K, bool w_on_chip);
+// FP32 refresh by iterative refinement (kvmc_refresh32.cu), mixed real form,
+// at most 224 orbitals per spin.  Walkers it could not converge carry
+// kStatusRefine; launch_refresh with only_due == 2 redoes exactly those.
+size_t refresh32_smem(const DevModel &m);
+bool refresh32_supported(const DevModel &m);
+cudaError_t launch_refresh32(const DevModel &m, const DevBatch &b, int only_due, int track_drift, cudaStream_t stream);
+cudaError_t launch_clear_status(const DevBatch &b, int bits, cudaStream_t stream);
+
 // Extra shared memory of the tensor-core flush (its operand tiles).
 size_t tc_flush_smem_bytes();
 size_t refresh_smem(const DevModel &m);

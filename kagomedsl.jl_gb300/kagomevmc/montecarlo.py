@@ -193,6 +193,10 @@ class Engine:
         """Delayed form: scan for the next move while the last one's factor column is written."""
         self._check(self._lib.kvmc_set_tuning(self.h, 2, int(bool(on))))
 
+    def set_refresh32(self, on: bool = True):
+        """Periodic refresh by FP32 iterative refinement (FP64 fallback per walker)."""
+        self._check(self._lib.kvmc_set_tuning(self.h, 4, int(bool(on))))
+
     def set_tc_flush(self, on: bool = True):
         """W in HBM: rank-k flush on the tensor cores (tcgen05, 3xTF32)."""
         self._check(self._lib.kvmc_set_tuning(self.h, 3, int(bool(on))))

@@ -547,3 +547,31 @@ def test_tensor_core_flush_refused_off_its_path(kv):
     with pytest.raises(kv.KvmcError):
         eng.set_tc_flush(True)
     eng.close()
+
+
+@pytest.mark.parametrize("N,placement", [(96, "hbm"), (216, "hbm"), (216, "chip"), (384, "hbm")])
+def test_fp32_refinement_refresh(kv, N, placement):
+    """The periodic refresh by FP32 iterative refinement: W right after it within
+    5e-6 of the FP64 rebuild (relative to max(1, |W|)), and chains that follow the oracle."""
+    walkers, seed, R = 8, 61, 64
+    ham = ham_for(kv, N)
+    eng = kv.Engine(ham, walkers, precision="mixed", seed=seed, refresh_interval=R, w_placement=placement)
+    eng.set_refresh32(True)
+    eng.set_drift_tolerance(1e9)        # no early refreshes: every walker refreshes exactly every R moves
+    eng.init()
+    ku0, kd0, _ = eng.get_state()
+    st = eng.advance(2 * R)             # ends right after a refresh of every walker
+    assert st["refreshes"] >= 2 * walkers and st["bad_walkers"] == 0
+    ku1, kd1, ct = eng.get_state()
+    Wu, Wd = eng.get_w()
+    for w in range(walkers):
+        assert close(Wu[w], o.reevaluateW(ham.U_up, ku1[w]), 5e-6), w
+        assert close(Wd[w], o.reevaluateW(ham.U_down, kd1[w]), 5e-6), w
+    m = oracle_c.OracleModel(ham.U_up, ham.U_down, ham.nn)
+    match = 0
+    for w in range(walkers):
+        ch = m.new_chain(ku0[w], kd0[w])
+        ch.run(seed, w, int(ct[w]), N // 2, N // 2, 0)
+        match += int(np.array_equal(ch.ku, ku1[w]) and np.array_equal(ch.kd, kd1[w]))
+    assert match >= walkers - 1
+    eng.close()
