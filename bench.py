@@ -59,6 +59,7 @@ def args_():
     p.add_argument("--skip-grad", action="store_true")
     p.add_argument("--skip-uneven", action="store_true")
     p.add_argument("--skip-large", action="store_true")
+    p.add_argument("--skip-field", action="store_true")
     return p.parse_args()
 
 
@@ -335,6 +336,32 @@ def uneven_run(kv, seed, device, moves=512, steps=3):
             "graph_over_sequential": res["graph"]["value"] / res["sequential"]["value"]}
 
 
+def field_run(kv, seed, device, walkers=2048, moves=256):
+    """The field workload of scripts/LL.jl: 8x8 doubled cells (N=192), B =
+    imbalance * pi / S with imbalance 4 (N_up = 98, N_down = 94), complex
+    orbitals; the mixed complex form (delayed updates, W in HBM) against the
+    plain complex FP64 form on the same walkers."""
+    import math
+
+    lat = kv.DoubleKagome(1.0, 8, 8, (True, True), (False, True))
+    H = kv.Hmat(lat, B=4 * math.pi / (64 * 2 * math.sqrt(3)))
+    Uu, Ud = kv.orbitals(H, 98, 94)
+    ham = kv.Hamiltonian(98, 94, Uu, Ud, H, kv.get_nn(H))
+    out = {}
+    for prec, R, mv in (("mixed", 512, moves), ("plain", 0, moves // 4)):
+        eng = kv.Engine(ham, walkers, precision=prec, seed=seed, refresh_interval=R, device=device)
+        eng.init()
+        eng.advance(32)
+        eng.region_start()
+        st = eng.advance(mv)
+        ms = eng.region_stop()
+        out[prec] = {"value": st["accepted"] / (ms * 1e-3), "unit": UNIT, "moves_per_walker": mv,
+                     "delay_k": eng.config()["delay_k"], "walker_refreshes": st["refreshes"]}
+        eng.close()
+    return {"workload": f"kagome VMC in a field, 8x8 doubled cells (N=192), imbalance 4, {walkers} walkers, "
+                        "complex orbitals", **out, "mixed_over_plain": out["mixed"]["value"] / out["plain"]["value"]}
+
+
 def large_run(kv, seed, device, walkers=512, moves=128, steps=2):
     """The large lattice: 12x12 doubled cells (N=864, 432 orbitals per spin),
     512 walkers, W (2 x 864 x 432 FP32 = 2.99 MB per walker, 1.53 GB in all)
@@ -470,6 +497,7 @@ def gpu_arm(a):
     adjoint = None if a.skip_grad else adjoint_run(kv, 4, local)
     uneven = None if a.skip_uneven else uneven_run(kv, a.seed, local)
     large = None if a.skip_large else large_run(kv, a.seed, local)
+    field = None if a.skip_field else field_run(kv, a.seed, local)
 
     # roofline of the dominant kernel
     refreshes = tot["refreshes"]
@@ -530,6 +558,7 @@ def gpu_arm(a):
             "gpu_launches": tot["launches"], "e2e": e2e, "roofline": roof, "cpu_baseline": cpu,
             "plain_fp64": plain, "speedup_vs_plain_fp64": (value / plain["value"]) if plain else None,
             "energy_gate": gate, "adjoint": adjoint, "uneven_batch": uneven, "large_lattice": large,
+            "field_workload": field,
             "drift": drift, "clocks": clk, "peaks_measured": peaks}
     print(json.dumps(line), flush=True)
     if world > 1:

@@ -737,9 +737,20 @@ extern "C" int kvmc_create(const kvmc_model_desc *model, const kvmc_batch_desc *
     // to 128 orbitals per spin on GB300 (measured at 48 and 108; at 192 the FP64
     // refresh is faster), so it is the default there
     h->refresh32 = (h->mixed && !h->cplx && std::max(nu, nd) <= 128) ? 1 : 0;
-    if (h->cplx && batch->delay_k != 0 && batch->delay_k != 1)
-        return bail(h->fail(KVMC_ERR_UNSUPPORTED, "complex orbitals use rank-1 updates: delay_k must be 0 or 1 (got %d)",
-                            batch->delay_k));
+    if (h->cplx) {
+        // complex orbitals: rank-1 (plain form, or delay_k 1) or delayed updates of depth 4 / 8 with W in HBM
+        const int want = batch->delay_k;
+        if (want != 0 && want != 1 && want != 4 && want != 8)
+            return bail(h->fail(KVMC_ERR_UNSUPPORTED, "complex orbitals: delay_k must be 0, 1, 4 or 8 (got %d)", want));
+        h->delay_k = 1;
+        if (h->mixed && want != 1) {
+            const int k = want == 0 ? 8 : want;
+            if (kvmc::complex_delayed_smem(m, k) + 1024 <= (size_t)optin) h->delay_k = k;
+            else if (want != 0)
+                return bail(h->fail(KVMC_ERR_UNSUPPORTED, "complex delay_k=%d needs %zu B shared memory", k,
+                                    kvmc::complex_delayed_smem(m, k)));
+        }
+    }
     // delayed-update depth: 0 = the largest depth whose working set fits on chip
     // (W with P and Q when W is on chip; P and Q alone when W is in HBM)
     const size_t budget = (size_t)optin - 1024;  // leave room for the kernel's static shared memory

@@ -443,6 +443,257 @@ __global__ void __launch_bounds__(256) sweep_c_kernel(DevModel m, DevBatch b, Sw
     }
 }
 
+// ---------------------------------------------------------------------------
+// Mixed complex form with delayed updates (the real delayed kernel's scheme
+// with complex FP32 entries): W stays in HBM, the factors P (N x K) and
+// Q (ld x K) of the last m accepted moves sit in shared memory and
+// W_eff = W - P Q^T; move m (pivot p = W_eff[K,l]) appends
+// P[:,m] = W_eff[:,l] / p and Q[:,m] = W_eff[K,:] - e_l, and every K moves
+// one pass applies W -= P Q^T.
+// ---------------------------------------------------------------------------
+template <int K>
+struct CDelayed {
+    cf *W, *P, *Q;
+    int ld;
+    // W_eff over the first m factor columns
+    __device__ __forceinline__ cf eff(int r, int c, int m) const {
+        cf v = W[(size_t)r * ld + c];
+        const cf *pr = P + (size_t)r * K, *qc = Q + (size_t)c * K;
+#pragma unroll
+        for (int k = 0; k < K; ++k)
+            if (k < m) v = cfms(pr[k], qc[k], v);
+        return v;
+    }
+};
+
+template <int K>
+__device__ void cdelayed_flush(const CDelayed<K> &S, int N) {
+    const int tot = N * S.ld;
+    for (int e = threadIdx.x; e < tot; e += blockDim.x) {
+        const int r = e / S.ld, c = e - r * S.ld;
+        cf v = S.W[e];
+        const cf *pr = S.P + (size_t)r * K, *qc = S.Q + (size_t)c * K;
+#pragma unroll
+        for (int k = 0; k < K; ++k) v = cfms(pr[k], qc[k], v);
+        S.W[e] = v;
+    }
+}
+
+template <int K>
+__device__ void cdelayed_zero(const CDelayed<K> &S, int N) {
+    for (int e = threadIdx.x; e < N * K; e += blockDim.x) S.P[e] = cf{0.f, 0.f};
+    for (int e = threadIdx.x; e < S.ld * K; e += blockDim.x) S.Q[e] = cf{0.f, 0.f};
+}
+
+struct CDelayedCtl {
+    long long t, next_meas;
+    int since, zmu, state, m;
+    int Ku, lu, Kd, ld;
+    cf piv_u, piv_d;
+    Thr thr;
+    double red[33];
+};
+
+template <int K>
+__global__ void __launch_bounds__(256, 2)
+sweep_c_delayed_kernel(DevModel m, DevBatch b, SweepParams p, int *active_count) {
+    const int w = blockIdx.x, N = m.n_sites;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const long long t0 = b.t[w], tend = b.t_end[w];
+    const long long acc_left = b.acc_end[w] - b.accepted[w];
+    if (t0 >= tend || acc_left <= 0) {
+        if (threadIdx.x == 0 && b.since[w] < 0) b.since[w] = 0;
+        return;
+    }
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ CDelayedCtl ctl;
+    const size_t wblock = (size_t)N * (m.ld_up + m.ld_dn);
+    cf *gW = reinterpret_cast<cf *>(b.W32) + (size_t)w * wblock;
+    CDelayed<K> SU, SD;
+    SU.W = gW;
+    SU.ld = m.ld_up;
+    SD.W = gW + (size_t)N * m.ld_up;
+    SD.ld = m.ld_dn;
+    unsigned char *cur = smem;
+    SU.P = reinterpret_cast<cf *>(cur); cur += (size_t)N * K * sizeof(cf);
+    SD.P = reinterpret_cast<cf *>(cur); cur += (size_t)N * K * sizeof(cf);
+    SU.Q = reinterpret_cast<cf *>(cur); cur += (size_t)m.ld_up * K * sizeof(cf);
+    SD.Q = reinterpret_cast<cf *>(cur); cur += (size_t)m.ld_dn * K * sizeof(cf);
+    short *kup = reinterpret_cast<short *>(cur); cur += (size_t)N * sizeof(short);
+    short *kdn = reinterpret_cast<short *>(cur);
+    cdelayed_zero<K>(SU, N);
+    cdelayed_zero<K>(SD, N);
+    for (int s2 = tid; s2 < N; s2 += blockDim.x) {
+        kup[s2] = b.kappa_up[(size_t)w * N + s2];
+        kdn[s2] = b.kappa_dn[(size_t)w * N + s2];
+    }
+    __syncthreads();
+    double zc = 0.0;
+    for (int e = tid; e < m.n_bonds; e += blockDim.x) {
+        const short2 bd = m.bonds[e];
+        zc += ((kup[bd.x] != 0 && kdn[bd.y] != 0) || (kup[bd.y] != 0 && kdn[bd.x] != 0)) ? 1.0 : 0.0;
+    }
+    zc = block_sum(zc, ctl.red);
+    const int R = p.refresh_every, M = p.measure_every;
+    if (tid == 0) {
+        ctl.t = t0;
+        ctl.since = b.since[w] < 0 ? 0 : b.since[w];
+        ctl.zmu = (int)zc;
+        ctl.m = 0;
+        ctl.next_meas = (t0 / M + 1) * M;
+        make_thr(ctl.thr, m.thr_table, ctl.zmu, p.accept_rule);
+    }
+    __syncthreads();
+    long long acc_count = 0, n_meas = 0;
+    double se = 0.0, se2 = 0.0;
+    while (true) {
+        const int mm = ctl.m;
+        if (warp == 0) {
+            long long t = ctl.t;
+            const int since = ctl.since;
+            const long long next_meas = ctl.next_meas;
+            const Thr thr = ctl.thr;
+            int state = 2;
+            while (true) {
+                if (t >= tend || since >= R || acc_count >= acc_left) break;
+                const long long lim = min(tend, next_meas) - t;
+                const int win = lim < 32 ? (int)lim : 32;
+                bool acc = false, bad = false;
+                int Ku = 0, lu = 0, Kd = 0, ld = 0;
+                cf pu{0.f, 0.f}, pd{0.f, 0.f};
+                if (lane < win) {
+                    unsigned long long u53;
+                    int bi;
+                    proposal_bits(p.seed, w, t + lane, m.n_bonds, u53, bi);
+                    const int c = cmp_r_thr(u53, thr);
+                    if (p.accept_rule != 0 || c <= 0) {
+                        const short2 bd = m.bonds[bi];
+                        const int i = bd.x, j = bd.y;
+                        const int kui = kup[i], kuj = kup[j], kdi = kdn[i], kdj = kdn[j];
+                        const bool f1 = kui != 0 && kdj != 0;
+                        const bool f2 = kuj != 0 && kdi != 0;
+                        if (f1 || f2) {
+                            if (f1) { Ku = j; lu = kui - 1; Kd = i; ld = kdj - 1; }
+                            else    { Ku = i; lu = kuj - 1; Kd = j; ld = kdi - 1; }
+                            pu = SU.eff(Ku, lu, mm);
+                            pd = SD.eff(Kd, ld, mm);
+                            acc = decide_c(pu, pd, u53, c, thr, p.accept_rule, bad);
+                        }
+                    }
+                }
+                if (__any_sync(0xffffffffu, bad) && bad) atomicOr(&b.status[w], kStatusNonFinite);
+                const unsigned mask = __ballot_sync(0xffffffffu, acc);
+                if (mask) {
+                    const int f = __ffs(mask) - 1;
+                    if (lane == f) {
+                        ctl.Ku = Ku; ctl.lu = lu; ctl.Kd = Kd; ctl.ld = ld;
+                        ctl.piv_u = pu; ctl.piv_d = pd;
+                    }
+                    t += f + 1;
+                    state = 1;
+                    break;
+                }
+                t += win;
+                if (t == next_meas) { state = 3; break; }
+            }
+            if (lane == 0) { ctl.t = t; ctl.state = state; }
+        }
+        __syncthreads();
+        const int state = ctl.state;
+        if (state == 2) break;
+        if (state == 1) {
+            const int Ku = ctl.Ku, lu = ctl.lu, Kd = ctl.Kd, ld = ctl.ld;
+            const cf ipu = cinv(ctl.piv_u), ipd = cinv(ctl.piv_d);
+            const int tot = 2 * N + m.ld_up + m.ld_dn;
+            for (int e = tid; e < tot; e += blockDim.x) {
+                if (e < N) SU.P[(size_t)e * K + mm] = cmul(SU.eff(e, lu, mm), ipu);
+                else if (e < 2 * N) SD.P[(size_t)(e - N) * K + mm] = cmul(SD.eff(e - N, ld, mm), ipd);
+                else if (e < 2 * N + m.ld_up) {
+                    const int c = e - 2 * N;
+                    cf v = SU.eff(Ku, c, mm);
+                    if (c == lu) v.x -= 1.f;
+                    SU.Q[(size_t)c * K + mm] = v;
+                } else {
+                    const int c = e - 2 * N - m.ld_up;
+                    cf v = SD.eff(Kd, c, mm);
+                    if (c == ld) v.x -= 1.f;
+                    SD.Q[(size_t)c * K + mm] = v;
+                }
+            }
+            if (tid == 0) {
+                // the up spin moves Kd -> Ku, the down spin Ku -> Kd
+                const int before = incident_antiparallel(m, kup, Ku, Kd);
+                kup[Ku] = (short)(lu + 1); kup[Kd] = 0;
+                kdn[Kd] = (short)(ld + 1); kdn[Ku] = 0;
+                const int after = incident_antiparallel(m, kup, Ku, Kd);
+                ctl.zmu += after - before;
+                ctl.since += 1;
+                make_thr(ctl.thr, m.thr_table, ctl.zmu, p.accept_rule);
+            }
+            acc_count += 1;
+            __syncthreads();
+            if (mm + 1 == K) {
+                cdelayed_flush<K>(SU, N);
+                cdelayed_flush<K>(SD, N);
+                __syncthreads();
+                cdelayed_zero<K>(SU, N);
+                cdelayed_zero<K>(SD, N);
+                if (tid == 0) ctl.m = 0;
+            } else if (tid == 0) {
+                ctl.m = mm + 1;
+            }
+            __syncthreads();
+        }
+        const long long t = ctl.t;
+        if (t == ctl.next_meas) {
+            const int mnow = ctl.m;
+            float accE = 0.f;
+            for (int e = tid; e < m.n_bonds; e += blockDim.x) {
+                const short2 bd = m.bonds[e];
+                const int i = bd.x, j = bd.y;
+                const int ui = kup[i], uj = kup[j], di = kdn[i], dj = kdn[j];
+                accE += ((ui != 0) == (uj != 0)) ? 0.25f : -0.25f;
+                if (uj != 0 && di != 0) accE -= 0.5f * cmul(SU.eff(i, uj - 1, mnow), SD.eff(j, di - 1, mnow)).x;
+                if (ui != 0 && dj != 0) accE -= 0.5f * cmul(SU.eff(j, ui - 1, mnow), SD.eff(i, dj - 1, mnow)).x;
+            }
+            const double e = block_sum_f32(accE, ctl.red);
+            if (tid == 0) {
+                se += e;
+                se2 += e * e;
+                n_meas += 1;
+                ctl.next_meas += M;
+            }
+        }
+        __syncthreads();
+    }
+    __syncthreads();
+    if (ctl.m > 0) {
+        // flush only the columns written so far (the rest are zero)
+        cdelayed_flush<K>(SU, N);
+        cdelayed_flush<K>(SD, N);
+        __syncthreads();
+    }
+    for (int s2 = tid; s2 < N; s2 += blockDim.x) {
+        b.kappa_up[(size_t)w * N + s2] = kup[s2];
+        b.kappa_dn[(size_t)w * N + s2] = kdn[s2];
+    }
+    if (tid == 0) {
+        const long long t = ctl.t;
+        b.t[w] = t;
+        b.since[w] = ctl.since >= R ? -1 : ctl.since;
+        b.accepted[w] += acc_count;
+        b.proposals[w] += t - t0;
+        b.sum_e[w] += se;
+        b.sum_e2[w] += se2;
+        b.n_meas[w] += n_meas;
+        if (t < tend && acc_count < acc_left) atomicAdd(active_count, 1);
+    }
+}
+
+size_t complex_delayed_smem(const DevModel &m, int K) {
+    return (size_t)(2 * m.n_sites + m.ld_up + m.ld_dn) * K * sizeof(cf) + (size_t)2 * m.n_sites * 2 + 16;
+}
+
 template <typename C>
 size_t sweep_c_smem(const DevModel &m) {
     return (size_t)(2 * m.n_sites + m.ld_up + m.ld_dn) * sizeof(C) + (size_t)2 * m.n_sites * 2 + 16;
@@ -519,8 +770,20 @@ cudaError_t launch_refresh_c(const DevModel &m, const DevBatch &b, bool fp32_out
     return cudaGetLastError();
 }
 
+template <int K>
+static cudaError_t launch_c_delayed(const DevModel &m, const DevBatch &b, const SweepParams &p, int *active,
+                                    cudaStream_t stream) {
+    const size_t sm = complex_delayed_smem(m, K);
+    cudaError_t e = cudaFuncSetAttribute(sweep_c_delayed_kernel<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    if (e != cudaSuccess) return e;
+    sweep_c_delayed_kernel<K><<<b.n_walkers, 256, sm, stream>>>(m, b, p, active);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_sweep_c(const DevModel &m, const DevBatch &b, const SweepParams &p, bool mixed, int *active,
                            cudaStream_t stream) {
+    if (mixed && p.delay_k == 4) return launch_c_delayed<4>(m, b, p, active, stream);
+    if (mixed && p.delay_k == 8) return launch_c_delayed<8>(m, b, p, active, stream);
     if (mixed) {
         const size_t sm = sweep_c_smem<cf>(m);
         sweep_c_kernel<cf><<<b.n_walkers, 256, sm, stream>>>(m, b, p, 0, active);

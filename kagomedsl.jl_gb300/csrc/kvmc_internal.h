@@ -142,6 +142,7 @@ cudaError_t launch_grad(const DevModel &m, const DevBatch &b, const GradModel &g
 // (re, im) pairs, W64 / W32 at complex FP64 / FP32 pairs, and solve_block
 // counts doubles (two per complex entry).
 int complex_max_orbitals();
+size_t complex_delayed_smem(const DevModel &m, int K);   // mixed complex form, W in HBM
 size_t complex_refresh_smem(const DevModel &m);
 cudaError_t launch_refresh_c(const DevModel &m, const DevBatch &b, bool fp32_out, int only_due, int track_drift,
                              cudaStream_t stream);

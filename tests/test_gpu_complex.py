@@ -95,14 +95,16 @@ def test_complex_ratios_and_local_energy(kv, precision):
     eng.close()
 
 
-@pytest.mark.parametrize("precision", ["plain", "mixed"])
+@pytest.mark.parametrize("precision,delay_k", [("plain", 0), ("mixed", 1), ("mixed", 4), ("mixed", 8)])
 @pytest.mark.parametrize("accept", ["reference", "metropolis"])
-def test_complex_chains_match_c_oracle(kv, precision, accept):
+def test_complex_chains_match_c_oracle(kv, precision, delay_k, accept):
     n1, n2, imbalance = 8, 4, 4
     ham = field_ham(kv, n1, n2, imbalance)
     walkers, proposals, seed = 10, 3000, 19
     eng = kv.Engine(ham, walkers, precision=precision, accept=accept, seed=seed,
-                    refresh_interval=(64 if precision == "mixed" else 0))
+                    refresh_interval=(64 if precision == "mixed" else 0), delay_k=delay_k)
+    if precision == "mixed":
+        assert eng.config()["delay_k"] == delay_k
     eng.init()
     ku0, kd0, _ = eng.get_state()
     for w in range(walkers):   # the seeded starts are the oracle's
@@ -136,7 +138,8 @@ def test_complex_lattice_of_the_field_scan(kv, precision):
     eng = kv.Engine(ham, walkers, precision=precision, seed=seed, refresh_interval=(64 if precision == "mixed" else 0))
     eng.init()
     ku0, kd0, _ = eng.get_state()
-    eng.sweep(proposals)
+    st = eng.sweep(proposals)
+    assert st["bad_walkers"] == 0
     ku1, kd1, _ = eng.get_state()
     ws = eng.walker_stats()
     m = oracle_c.OracleModel(ham.U_up, ham.U_down, ham.nn, "cplx")
@@ -207,10 +210,11 @@ def test_complex_handle_at_zero_field_equals_real_handle(kv):
     np.testing.assert_allclose(wa["sum_e"], wb["sum_e"], rtol=1e-9, atol=1e-9)
 
 
-def test_complex_rejects_delayed_updates(kv):
+def test_complex_delay_depths(kv):
+    """Complex W takes rank-1 or delayed updates of depth 4 or 8 (W in HBM); 8 by default."""
     ham = field_ham(kv, 6, 3, 2)
     with pytest.raises(kv.KvmcError):
-        kv.Engine(ham, 2, precision="mixed", delay_k=8)
+        kv.Engine(ham, 2, precision="mixed", delay_k=12)
     eng = kv.Engine(ham, 2, precision="mixed", delay_k=0)
-    assert eng.config()["delay_k"] == 1 and not eng.config()["w_on_chip"]
+    assert eng.config()["delay_k"] == 8 and not eng.config()["w_on_chip"]
     eng.close()
