@@ -337,6 +337,8 @@ def uneven_run(kv, seed, device, moves=512, steps=3):
 
 
 def field_run(kv, seed, device, walkers=2048, moves=256):
+    # the mixed form runs 4 * moves (two of its refreshes) and the plain form
+    # moves / 4 (it refreshes every 94 proposals)
     """The field workload of scripts/LL.jl: 8x8 doubled cells (N=192), B =
     imbalance * pi / S with imbalance 4 (N_up = 98, N_down = 94), complex
     orbitals; the mixed complex form (delayed updates, W in HBM) against the
@@ -348,7 +350,7 @@ def field_run(kv, seed, device, walkers=2048, moves=256):
     Uu, Ud = kv.orbitals(H, 98, 94)
     ham = kv.Hamiltonian(98, 94, Uu, Ud, H, kv.get_nn(H))
     out = {}
-    for prec, R, mv in (("mixed", 512, moves), ("plain", 0, moves // 4)):
+    for prec, R, mv in (("mixed", 512, 4 * moves), ("plain", 0, moves // 4)):
         eng = kv.Engine(ham, walkers, precision=prec, seed=seed, refresh_interval=R, device=device)
         eng.init()
         eng.advance(32)
@@ -539,9 +541,9 @@ def gpu_arm(a):
     cpu = None
     if not a.skip_cpu:
         threads = cpu_threads()
-        acc, sec = cpu_port_run(ham, threads, 2160, a.seed, threads)
+        acc, sec = cpu_port_run(ham, threads, 64800, a.seed, threads)
         cpu = {"value": acc / sec, "unit": UNIT, "cores": threads, "kind": "port",
-               "sample": f"{threads} chains x 2160 proposals, N=216, complex double (oracle port), "
+               "sample": f"{threads} chains x 64800 proposals, N=216, complex double (oracle port), "
                          f"refresh and E_L every 108 proposals, {sec:.1f} s wall"}
 
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
