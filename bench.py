@@ -476,7 +476,8 @@ def gpu_arm(a):
     d2h = ku.nbytes + kd.nbytes + ct.nbytes + (sum(v.nbytes for v in ws.values()) if e2e_steps else 0)
     e2e = {"value": e2e_acc / (e2e_ms * 1e-3) if e2e_steps else None, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
            "d2h_bytes_per_step": int(d2h), "steps": e2e_steps,
-           "path": "kvmc_set_state (H2D + FP64 rebuild) -> kvmc_sweep -> kvmc_get_state + kvmc_walker_stats (D2H)"}
+           "path": "kvmc_set_state (H2D + W rebuild by FP32 refinement, FP64 per flagged walker) -> kvmc_advance -> "
+                   "kvmc_get_state + kvmc_walker_stats (D2H)"}
     eng.close()
     if rank != 0:
         if world > 1:

@@ -179,8 +179,9 @@ KVMC_API int kvmc_last_error(const kvmc_handle *h, char *buf, size_t len);
  * walker draws a seeded uniformly random configuration, redrawn until
  * tilde_U is regular for both spins (min|pivot|/max|pivot| of its partially
  * pivoted LU above 1e-8); otherwise the given configurations
- * ([n_walkers][n_sites]) are validated and used.  Builds W in FP64 either
- * way.  attempts (may be NULL) receives the draws each walker needed.
+ * ([n_walkers][n_sites]) are validated and used.  Seeded starts build W
+ * in FP64; given configurations are rebuilt like kvmc_set_state.  attempts
+ * (may be NULL) receives the draws each walker needed.
  * Returns KVMC_ERR_SINGULAR if a given configuration is singular. */
 KVMC_API int kvmc_init(kvmc_handle *h, const int32_t *kappa_up, const int32_t *kappa_down,
               int32_t *attempts);
@@ -191,7 +192,7 @@ typedef struct {
     int64_t measurements; /* local-energy samples taken in the call */
     double sum_energy;    /* sum of those samples (FP64) */
     double sum_energy2;   /* sum of their squares */
-    int64_t refreshes;    /* walker W refreshes performed (FP64 LU + solves) */
+    int64_t refreshes;    /* walker W refreshes performed */
     double max_drift;     /* mixed: max |W_fp32 - W_fp64 fresh| seen at a refresh */
     int32_t bad_walkers;  /* walkers whose status word is nonzero */
     int32_t launches;     /* kernels launched by the call */
@@ -236,7 +237,8 @@ KVMC_API int kvmc_refresh(kvmc_handle *h);
  * src/MonteCarlo.jl:715-755): configurations plus the per-walker proposal
  * counter (the position in the Philox stream).  set_state rebuilds W.
  * Any pointer may be NULL to skip that field (set_state: counters NULL
- * keeps the current counters). */
+ * keeps the current counters).  kvmc_set_state rebuilds W: in FP64, or for
+ * the mixed real form with KVMC_TUNE_REFRESH32 by FP32 refinement. */
 KVMC_API int kvmc_get_state(kvmc_handle *h, int32_t *kappa_up, int32_t *kappa_down,
                    int64_t *counters);
 KVMC_API int kvmc_set_state(kvmc_handle *h, const int32_t *kappa_up, const int32_t *kappa_down,
@@ -285,9 +287,11 @@ KVMC_API int kvmc_kernel_time(kvmc_handle *h, int32_t kind, double *total_ms, in
  *   KVMC_TUNE_REFRESH32: 1 = the periodic refresh of the FP32 W runs as
  *   iterative refinement on the FP32 pipes (FP32 LU and solves, residual
  *   with exact products and compensated sums), walkers that do not converge
- *   falling back to the FP64 refresh; 0 = FP64 LU and solves.  Starts,
- *   kvmc_set_state and kvmc_refresh always use FP64.  The default is 1 for
- *   the mixed real form with at most 128 orbitals per spin, else 0. */
+ *   falling back to the FP64 refresh; 0 = FP64 LU and solves.  It also
+ *   rebuilds W in kvmc_set_state and kvmc_init with given configurations
+ *   (log|det| then from the FP32 factors); seeded starts and kvmc_refresh
+ *   always use FP64.  The default is 1 for the mixed real form with at most
+ *   128 orbitals per spin, else 0. */
 enum kvmc_tuning { KVMC_TUNE_STREAM_THREADS = 1, KVMC_TUNE_PIPELINE = 2, KVMC_TUNE_TC_FLUSH = 3,
                    KVMC_TUNE_REFRESH32 = 4 };
 KVMC_API int kvmc_set_tuning(kvmc_handle *h, int32_t key, int32_t value);

@@ -183,9 +183,17 @@ cudaError_t sweep_launch(kvmc_handle *h, const kvmc::SweepParams &p) {
     return kvmc::launch_sweep(h->dm, h->db, p, h->mixed, h->smem_w, h->d_active, h->stream);
 }
 
-int full_refresh(kvmc_handle *h, bool track_drift) {
+// Rebuilds every walker's W.  allow32: with the FP32 refinement refresh
+// enabled, use it (FP64 for the walkers it flags); otherwise FP64 throughout.
+int full_refresh(kvmc_handle *h, bool track_drift, bool allow32 = true) {
     KV_TRY(h->cuda(cudaMemsetAsync(h->db.drift, 0, sizeof(float) * h->n_walkers, h->stream), "memset"));
-    KV_TRY(h->cuda(refresh_launch(h, 0, track_drift ? 1 : 0), "refresh launch"));
+    if (allow32 && h->refresh32 && !h->cplx) {
+        KV_TRY(h->cuda(kvmc::launch_refresh32(h->dm, h->db, 0, track_drift ? 1 : 0, h->stream), "refresh launch"));
+        KV_TRY(h->cuda(kvmc::launch_refresh(h->dm, h->db, true, 2, 0, h->stream), "refresh launch"));
+        KV_TRY(h->cuda(kvmc::launch_clear_status(h->db, kvmc::kStatusRefine, h->stream), "refresh launch"));
+    } else {
+        KV_TRY(h->cuda(refresh_launch(h, 0, track_drift ? 1 : 0), "refresh launch"));
+    }
     KV_TRY(h->cuda(cudaMemsetAsync(h->db.since, 0, sizeof(int) * h->n_walkers, h->stream), "memset"));
     return h->cuda(cudaStreamSynchronize(h->stream), "refresh");
 }
@@ -1293,7 +1301,7 @@ extern "C" int kvmc_refresh(kvmc_handle *h) {
     if (!h) return fail_global(KVMC_ERR_ARGUMENT, "null handle");
     KV_TRY(set_device(h));
     KV_TRY(h->cuda(cudaMemsetAsync(h->db.status, 0, h->n_walkers * 4, h->stream), "memset"));
-    KV_TRY(full_refresh(h, h->mixed));
+    KV_TRY(full_refresh(h, h->mixed, false));   // kvmc_refresh: the FP64 rebuild
     return check_status(h, nullptr);
 }
 

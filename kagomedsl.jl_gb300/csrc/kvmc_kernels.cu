@@ -944,8 +944,11 @@ struct DelayedSpin {
 // come out as exact unit rows (W[R][kappa[R]-1] = 1, zeros elsewhere); their
 // largest deviation, the rounding accumulated since the last FP64 refresh,
 // is folded into *dev (float bits, atomicMax).
+// skip0 / skip1: rows whose configuration entry already describes a move W
+// does not yet hold (their unit-row check is skipped); -1 for none.
 template <int K>
-__device__ void delayed_flush(const DelayedSpin<K> &S, int N, const short *kappa, int *dev) {
+__device__ void delayed_flush(const DelayedSpin<K> &S, int N, const short *kappa, int *dev, int skip0 = -1,
+                              int skip1 = -1) {
     const int qc = S.ld >> 2;
     const int groups = blockDim.x / qc;
     const int t = threadIdx.x;
@@ -993,7 +996,7 @@ __device__ void delayed_flush(const DelayedSpin<K> &S, int N, const short *kappa
             w.x -= a0; w.y -= a1; w.z -= a2; w.w -= a3;
             *wp = w;
             const int c0 = 4 * c4;
-            int l = kappa[r] - 1;
+            int l = (r == skip0 || r == skip1) ? -1 : kappa[r] - 1;
             if (l >= 0) {
                 const float d = fmaxf(fmaxf(fabsf(w.x - (c0 == l ? 1.f : 0.f)), fabsf(w.y - (c0 + 1 == l ? 1.f : 0.f))),
                                       fmaxf(fabsf(w.z - (c0 + 2 == l ? 1.f : 0.f)), fabsf(w.w - (c0 + 3 == l ? 1.f : 0.f))));
@@ -1002,7 +1005,7 @@ __device__ void delayed_flush(const DelayedSpin<K> &S, int N, const short *kappa
             if (two) {
                 w2.x -= b0; w2.y -= b1; w2.z -= b2; w2.w -= b3;
                 *wp2 = w2;
-                l = kappa[r2] - 1;
+                l = (r2 == skip0 || r2 == skip1) ? -1 : kappa[r2] - 1;
                 if (l >= 0) {
                     const float d = fmaxf(fmaxf(fabsf(w2.x - (c0 == l ? 1.f : 0.f)), fabsf(w2.y - (c0 + 1 == l ? 1.f : 0.f))),
                                           fmaxf(fabsf(w2.z - (c0 + 2 == l ? 1.f : 0.f)), fabsf(w2.w - (c0 + 3 == l ? 1.f : 0.f))));
@@ -1019,7 +1022,8 @@ __device__ void delayed_flush(const DelayedSpin<K> &S, int N, const short *kappa
 // loop would otherwise wait one full memory latency per row), and P is read
 // from shared memory per 4-wide k step instead of being held in registers.
 template <int K>
-__device__ void delayed_flush_stream(const DelayedSpin<K> &S, int N, const short *kappa, int *dev) {
+__device__ void delayed_flush_stream(const DelayedSpin<K> &S, int N, const short *kappa, int *dev, int skip0 = -1,
+                                     int skip1 = -1) {
     const int qc = S.ld >> 2;
     const int groups = blockDim.x / qc;
     const int t = threadIdx.x;
@@ -1064,7 +1068,7 @@ __device__ void delayed_flush_stream(const DelayedSpin<K> &S, int N, const short
                 float4 x = w[i];
                 x.x -= a0; x.y -= a1; x.z -= a2; x.w -= a3;
                 reinterpret_cast<float4 *>(S.W + (size_t)r * S.ld)[c4] = x;
-                const int l = kappa[r] - 1;
+                const int l = (r == skip0 || r == skip1) ? -1 : kappa[r] - 1;
                 if (l >= 0) {
                     const float d = fmaxf(fmaxf(fabsf(x.x - (c0 == l ? 1.f : 0.f)), fabsf(x.y - (c0 + 1 == l ? 1.f : 0.f))),
                                           fmaxf(fabsf(x.z - (c0 + 2 == l ? 1.f : 0.f)), fabsf(x.w - (c0 + 3 == l ? 1.f : 0.f))));
@@ -1192,7 +1196,7 @@ __device__ void teardown(const State &st) {
 
 template <int K>
 __device__ void delayed_flush_tc(const DelayedSpin<K> &S, int N, const short *kappa, int *dev, tc::State &st,
-                                 int *status) {
+                                 int *status, int skip0 = -1, int skip1 = -1) {
     constexpr int KK = (K + 7) / 8 * 8;
     static_assert(KK <= tc::kMaxKK, "delay depth beyond the operand tiles");
     const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5, nwarps = nt >> 5;
@@ -1246,7 +1250,7 @@ __device__ void delayed_flush_tc(const DelayedSpin<K> &S, int N, const short *ka
             tc::fence_after();
             // epilogue: row r0 + 32*quarter + lane, this warp's share of the chunk's columns
             const int r = r0 + 32 * quarter + lane;
-            const int l = r < N ? kappa[r] - 1 : -1;
+            const int l = (r < N && r != skip0 && r != skip1) ? kappa[r] - 1 : -1;
             float *wr = S.W + (size_t)(r < N ? r : 0) * S.ld + c0;
             for (int cc = 8 * half; cc < nc; cc += 8 * halves) {
                 float d[8];
@@ -1638,7 +1642,8 @@ struct PendingMove {
 struct PipeCtl {
     long long t, next_meas, acc;
     int since, zmu, m, state, pend, slot, dz;
-    int dev;
+    int state2[2];
+    int dev, dev2[2];
     PendingMove mv[2];
     Thr thr;
     double red[33];
@@ -1740,6 +1745,7 @@ sweep_pipe_kernel(DevModel m, DevBatch b, SweepParams p, int *active_count) {
         ctl.pend = 0;
         ctl.slot = 0;
         ctl.dev = 0;
+        ctl.dev2[0] = ctl.dev2[1] = 0;
         ctl.next_meas = (t0 / M + 1) * M;
         make_thr(ctl.thr, m.thr_table, ctl.zmu, p.accept_rule);
     }
@@ -1747,8 +1753,12 @@ sweep_pipe_kernel(DevModel m, DevBatch b, SweepParams p, int *active_count) {
 
     long long n_meas = 0;
     double se = 0.0, se2 = 0.0;
+    // the loop state below is kept by every thread alike (no broadcast needed):
+    // pend = a move accepted in the previous phase whose factor column this
+    // phase writes, slot = its entry in ctl.mv, mm = complete factor columns,
+    // fp = flushes so far (their parity picks the drift slot)
+    int pend = 0, slot = 0, mm = 0, fp = 0, it = 0;
     while (true) {
-        const int pend = ctl.pend, slot = ctl.slot, mm = ctl.m;
         if (warp == 0) {
             // scan for the next accepted move
             const PendingMove pm = ctl.mv[slot];
@@ -1798,10 +1808,12 @@ sweep_pipe_kernel(DevModel m, DevBatch b, SweepParams p, int *active_count) {
                 t += win;
             }
             if (state == 1) {
+                // apply the move: Z_mu change (configuration before it), then the
+                // configuration, the threshold and the counters.  Nobody else reads
+                // the configuration in this phase; the flush that may follow skips
+                // the unit-row check of the two rows the move changes.
                 __syncwarp();
                 const PendingMove nm = ctl.mv[slot ^ 1];
-                // Z_mu change of the move (configuration before it): the up spin
-                // moves Kd -> Ku, the down spin Ku -> Kd
                 int dz = 0;
                 for (int e = nbr_off[nm.Ku] + lane; e < nbr_off[nm.Ku + 1]; e += 32) {
                     const int k = nbr[e];
@@ -1812,9 +1824,19 @@ sweep_pipe_kernel(DevModel m, DevBatch b, SweepParams p, int *active_count) {
                     if (k != nm.Ku) dz += kup[k] != 0 ? 1 : -1;
                 }
                 dz = __reduce_add_sync(0xffffffffu, dz);
-                if (lane == 0) ctl.dz = dz;
+                __syncwarp();
+                if (lane == 0) {
+                    kup[nm.Ku] = (short)(nm.lu + 1); kup[nm.Kd] = 0;
+                    kdn[nm.Kd] = (short)(nm.ld + 1); kdn[nm.Ku] = 0;
+                    ctl.zmu += dz;
+                    make_thr(ctl.thr, m.thr_table, ctl.zmu, p.accept_rule);
+                    ctl.since += 1;
+                    ctl.acc += 1;
+                }
             }
-            if (lane == 0) { ctl.t = t; ctl.state = state; }
+            // the state word alternates between two slots: a slot is rewritten only
+            // after every thread has passed the barrier that follows its last read
+            if (lane == 0) { ctl.t = t; ctl.state2[it & 1] = state; }
         } else if (pend) {
             // factor column mm of the pending move, over columns [0, mm)
             const PendingMove pm = ctl.mv[slot];
@@ -1862,46 +1884,39 @@ sweep_pipe_kernel(DevModel m, DevBatch b, SweepParams p, int *active_count) {
             }
         }
         __syncthreads();
-        const int state = ctl.state;
+        const int state = ctl.state2[it & 1];
+        ++it;
         const int mnew = pend ? mm + 1 : mm;
         if (mnew == K) {
+            // rows of the move just accepted (not yet in W) skip the unit-row check
+            int s0 = -1, s1 = -1;
+            if (state == 1) { const PendingMove nm = ctl.mv[slot ^ 1]; s0 = nm.Ku; s1 = nm.Kd; }
+            int *dev = &ctl.dev2[fp & 1];
             if constexpr (kTC) {
-                delayed_flush_tc<K>(SU, N, kup, &ctl.dev, tcs, &b.status[w]);
-                delayed_flush_tc<K>(SD, N, kdn, &ctl.dev, tcs, &b.status[w]);
+                delayed_flush_tc<K>(SU, N, kup, dev, tcs, &b.status[w], s0, s1);
+                delayed_flush_tc<K>(SD, N, kdn, dev, tcs, &b.status[w], s0, s1);
             } else if constexpr (kStream) {
-                delayed_flush_stream<K>(SU, N, kup, &ctl.dev);
-                delayed_flush_stream<K>(SD, N, kdn, &ctl.dev);
+                delayed_flush_stream<K>(SU, N, kup, dev, s0, s1);
+                delayed_flush_stream<K>(SD, N, kdn, dev, s0, s1);
             } else {
-                delayed_flush<K>(SU, N, kup, &ctl.dev);
-                delayed_flush<K>(SD, N, kdn, &ctl.dev);
+                delayed_flush<K>(SU, N, kup, dev, s0, s1);
+                delayed_flush<K>(SD, N, kdn, dev, s0, s1);
             }
             __syncthreads();
             delayed_zero<K>(SU, N);
             delayed_zero<K>(SD, N);
-        }
-        if (tid == 0) {
-            int since = ctl.since;
-            ctl.m = mnew == K ? 0 : mnew;
-            if (mnew == K) {
-                // adaptive refresh: rounding past the tolerance ends this walker's run
-                if (__int_as_float(ctl.dev) > p.drift_tol) since = R;
-                ctl.dev = 0;
+            if (tid == 0) {
+                // adaptive refresh: rounding past the tolerance ends this walker's run;
+                // the other drift slot is free again (everybody read it a flush ago)
+                if (__int_as_float(*dev) > p.drift_tol) ctl.since = R;
+                ctl.dev2[(fp & 1) ^ 1] = 0;
             }
-            if (state == 1) {
-                // apply the move just accepted: configuration, Z_mu, threshold
-                const PendingMove nm = ctl.mv[slot ^ 1];
-                kup[nm.Ku] = (short)(nm.lu + 1); kup[nm.Kd] = 0;
-                kdn[nm.Kd] = (short)(nm.ld + 1); kdn[nm.Ku] = 0;
-                ctl.zmu += ctl.dz;
-                make_thr(ctl.thr, m.thr_table, ctl.zmu, p.accept_rule);
-                since += 1;
-                ctl.acc += 1;
-                ctl.slot = slot ^ 1;
-            }
-            ctl.since = since;
-            ctl.pend = state == 1;
+            __syncthreads();
+            ++fp;
         }
-        __syncthreads();
+        mm = mnew == K ? 0 : mnew;
+        if (state == 1) slot ^= 1;
+        pend = state == 1;
         if (state == 3) {
             const double e = delayed_local_energy<K>(m, bonds, kup, kdn, SU, SD, ctl.red);
             if (tid == 0) {
@@ -1910,11 +1925,10 @@ sweep_pipe_kernel(DevModel m, DevBatch b, SweepParams p, int *active_count) {
                 n_meas += 1;
                 ctl.next_meas += M;
             }
-            __syncthreads();
         }
         if (state == 2) break;
     }
-    if (ctl.m > 0) {
+    if (mm > 0) {
         if constexpr (kTC) {
             delayed_flush_tc<K>(SU, N, kup, &ctl.dev, tcs, &b.status[w]);
             delayed_flush_tc<K>(SD, N, kdn, &ctl.dev, tcs, &b.status[w]);

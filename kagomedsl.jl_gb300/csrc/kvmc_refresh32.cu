@@ -228,6 +228,24 @@ refresh32_kernel(DevModel m, DevBatch b, int only_due, int track_drift) {
         if (tid == 0) atomicOr(&b.status[w], kStatusRefine);
         return;
     }
+    {
+        // log|det tilde_U| and log(min|pivot| / max|pivot|) from the FP32 factors
+        __shared__ double red[33];
+        double ldet = 0.0, dmin = INFINITY, dmaxp = 0.0;
+        for (int i = tid; i < n; i += nt) {
+            const float d = fabsf(A[(size_t)i * lda + i]);
+            ldet += (double)logf(d);
+            dmin = fmin(dmin, (double)d);
+            dmaxp = fmax(dmaxp, (double)d);
+        }
+        ldet = block_sum(ldet, red);
+        dmin = -block_sum_max(-dmin, red);
+        dmaxp = block_sum_max(dmaxp, red);
+        if (tid == 0) {
+            b.logdet[4 * w + spin] = ldet;
+            b.logdet[4 * w + 2 + spin] = log(dmin / dmaxp);
+        }
+    }
     // unit rows at occupied sites, zero padding elsewhere
     {
         float dmax = 0.f;
