@@ -60,6 +60,7 @@ def args_():
     p.add_argument("--skip-uneven", action="store_true")
     p.add_argument("--skip-large", action="store_true")
     p.add_argument("--skip-field", action="store_true")
+    p.add_argument("--skip-batched", action="store_true")
     return p.parse_args()
 
 
@@ -336,6 +337,31 @@ def uneven_run(kv, seed, device, moves=512, steps=3):
             "graph_over_sequential": res["graph"]["value"] / res["sequential"]["value"]}
 
 
+def batched_run(kv, seed, device, walkers=4096, moves=1024):
+    """Batched walkers at 4x4 doubled cells (N=96): 4096 chains from seeded
+    random starts, once with the settings the workload names (delayed depth
+    16, FP64-quality refresh every 64 accepted moves) and once with the
+    autotuner's choice for this batch."""
+    from kagomevmc import autotune
+
+    ham = kv.Hamiltonian.build(48, 48, kv.DoubleKagome(1.0, 8, 4, (True, True), (False, True)))
+    named = autotune.Choice(delay_k=16, refresh_interval=64, placement="hbm", threads=128)
+    tuned = autotune.lookup(ham, walkers) or named
+    out = {}
+    for label, ch in (("k16_R64", named), ("tuned", tuned)):
+        eng = autotune.make_engine(ham, walkers, ch, seed=seed, device=device)
+        eng.init()
+        eng.advance(256)
+        eng.region_start()
+        st = eng.advance(moves)
+        ms = eng.region_stop()
+        out[label] = {"value": st["accepted"] / (ms * 1e-3), "unit": UNIT, "delay_k": eng.config()["delay_k"],
+                      "refresh_interval": ch.refresh_interval, "placement": ch.placement, "threads": ch.threads}
+        eng.close()
+    return {"workload": f"kagome VMC, 4x4 doubled cells (N=96), {walkers} walkers, {moves} accepted moves per walker",
+            **out}
+
+
 def field_run(kv, seed, device, walkers=2048, moves=256):
     # the mixed form runs 4 * moves (two of its refreshes) and the plain form
     # moves / 4 (it refreshes every 94 proposals)
@@ -501,6 +527,7 @@ def gpu_arm(a):
     uneven = None if a.skip_uneven else uneven_run(kv, a.seed, local)
     large = None if a.skip_large else large_run(kv, a.seed, local)
     field = None if a.skip_field else field_run(kv, a.seed, local)
+    batched = None if a.skip_batched else batched_run(kv, a.seed, local)
 
     # roofline of the dominant kernel
     refreshes = tot["refreshes"]
@@ -561,7 +588,7 @@ def gpu_arm(a):
             "gpu_launches": tot["launches"], "e2e": e2e, "roofline": roof, "cpu_baseline": cpu,
             "plain_fp64": plain, "speedup_vs_plain_fp64": (value / plain["value"]) if plain else None,
             "energy_gate": gate, "adjoint": adjoint, "uneven_batch": uneven, "large_lattice": large,
-            "field_workload": field,
+            "field_workload": field, "batched_n96": batched,
             "drift": drift, "clocks": clk, "peaks_measured": peaks}
     print(json.dumps(line), flush=True)
     if world > 1:
