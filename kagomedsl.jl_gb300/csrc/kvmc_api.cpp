@@ -633,10 +633,10 @@ extern "C" int kvmc_create(const kvmc_model_desc *model, const kvmc_batch_desc *
         nbr[fill[i]++] = (short)j;
         nbr[fill[j]++] = (short)i;
     }
-    double *dUu, *dUd;
-    short2 *dB;
-    int *dOff;
-    short *dNbr;
+    double *dUu = nullptr, *dUd = nullptr;
+    short2 *dB = nullptr;
+    int *dOff = nullptr;
+    short *dNbr = nullptr;
     int rc = KVMC_OK;
     if ((rc = h->alloc(&dUu, Uu.size())) || (rc = h->alloc(&dUd, Ud.size())) || (rc = h->alloc(&dB, nb)) ||
         (rc = h->alloc(&dOff, N + 1)) || (rc = h->alloc(&dNbr, nbr.size())))
@@ -683,7 +683,7 @@ extern "C" int kvmc_create(const kvmc_model_desc *model, const kvmc_batch_desc *
         e.m = (bits & 0xFFFFFFFFFFFFFull) | (1ull << 52);
         e.k = (int)((bits >> 52) & 0x7ff) - 1075 + 53;
     }
-    kvmc::ThrEntry *dThr;
+    kvmc::ThrEntry *dThr = nullptr;
     if ((rc = h->alloc(&dThr, thr.size()))) return bail(rc);
     cudaMemcpy(dThr, thr.data(), thr.size() * sizeof(kvmc::ThrEntry), cudaMemcpyHostToDevice);
     m.thr_table = dThr;

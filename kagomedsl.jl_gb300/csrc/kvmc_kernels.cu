@@ -1641,7 +1641,7 @@ struct PendingMove {
 
 struct PipeCtl {
     long long t, next_meas, acc;
-    int since, zmu, m, state, pend, slot, dz;
+    int since, zmu;
     int state2[2];
     int dev, dev2[2];
     PendingMove mv[2];
@@ -1741,9 +1741,6 @@ sweep_pipe_kernel(DevModel m, DevBatch b, SweepParams p, int *active_count) {
         ctl.acc = 0;
         ctl.since = b.since[w] < 0 ? 0 : b.since[w];
         ctl.zmu = (int)zc;
-        ctl.m = 0;
-        ctl.pend = 0;
-        ctl.slot = 0;
         ctl.dev = 0;
         ctl.dev2[0] = ctl.dev2[1] = 0;
         ctl.next_meas = (t0 / M + 1) * M;
