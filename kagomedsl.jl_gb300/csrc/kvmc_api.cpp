@@ -1376,12 +1376,14 @@ extern "C" int kvmc_set_tuning(kvmc_handle *h, int32_t key, int32_t value) {
     if (key == KVMC_TUNE_REFRESH32) {
         if (value != 0 && value != 1) return h->fail(KVMC_ERR_ARGUMENT, "refresh32 must be 0 or 1");
         if (value == 1) {
-            if (!h->mixed || h->cplx || !kvmc::refresh32_supported(h->dm))
-                return h->fail(KVMC_ERR_UNSUPPORTED,
-                               "the FP32 refresh serves the mixed real form with at most 224 orbitals per spin");
-            if (kvmc::refresh32_smem(h->dm) + 1024 > (size_t)kvmc::max_smem_optin(h->device))
-                return h->fail(KVMC_ERR_UNSUPPORTED, "the FP32 refresh needs %zu B shared memory",
-                               kvmc::refresh32_smem(h->dm));
+            if (!h->mixed || h->cplx)
+                return h->fail(KVMC_ERR_UNSUPPORTED, "the FP32 refresh serves the mixed real form");
+            const size_t need = kvmc::refresh32_supported(h->dm) ? kvmc::refresh32_smem(h->dm)
+                                                                 : kvmc::refresh_large_smem(h->dm, 4);
+            if (need + 1024 > (size_t)kvmc::max_smem_optin(h->device))
+                return h->fail(KVMC_ERR_UNSUPPORTED, "the FP32 refresh needs %zu B shared memory", need);
+            if (!kvmc::refresh32_supported(h->dm) && !h->db.lu_scratch)
+                return h->fail(KVMC_ERR_UNSUPPORTED, "no LU scratch for the blocked FP32 refresh");
         }
         h->refresh32 = value;
         return KVMC_OK;

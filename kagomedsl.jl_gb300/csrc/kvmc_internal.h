@@ -109,12 +109,16 @@ size_t mixed_sweep_smem(const DevModel &m);
 // Shared memory of the delayed-update sweep: with W on chip, or with W in
 // HBM (only P, Q and the walker's small state on chip).
 size_t delayed_smem_bytes(const DevModel &m, int K, bool w_on_chip);
-// FP32 refresh by iterative refinement (kvmc_refresh32.cu), mixed real form,
-// at most 224 orbitals per spin.  Walkers it could not converge carry
+// FP32 refresh by iterative refinement (kvmc_refresh32.cu), mixed real form:
+// LU in shared memory up to 224 orbitals per spin, blocked in HBM beyond.  Walkers it could not converge carry
 // kStatusRefine; launch_refresh with only_due == 2 redoes exactly those.
 size_t refresh32_smem(const DevModel &m);
 bool refresh32_supported(const DevModel &m);
 cudaError_t launch_refresh32(const DevModel &m, const DevBatch &b, int only_due, int track_drift, cudaStream_t stream);
+// more than 224 orbitals: the same refinement on an FP32 LU blocked in HBM (kvmc_kernels.cu)
+cudaError_t launch_refresh32_large(const DevModel &m, const DevBatch &b, int only_due, int track_drift,
+                                   cudaStream_t stream);
+size_t refresh_large_smem(const DevModel &m, size_t lt_bytes);
 cudaError_t launch_clear_status(const DevBatch &b, int bits, cudaStream_t stream);
 
 // Extra shared memory of the tensor-core flush (its operand tiles).

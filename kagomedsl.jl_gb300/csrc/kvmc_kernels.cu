@@ -17,6 +17,7 @@
 
 #include "kvmc.h"
 #include "kvmc_device.cuh"
+#include "kvmc_refine.cuh"
 #include "kvmc_internal.h"
 
 namespace kvmc {
@@ -344,9 +345,13 @@ refresh_kernel(DevModel m, DevBatch b, int only_due, int track_drift) {
 constexpr int kPanel = 32;
 constexpr int kSmemLuMaxN = 160;
 
-template <typename OutT>
+// LT: the arithmetic of the LU.  double = the FP64 refresh; float = the LU of
+// the FP32 refinement refresh (kvmc_refine.cuh), whose rows are then refined
+// against the exact-product residual (mixed real form, OutT float).
+template <typename LT, typename OutT>
 __global__ void __launch_bounds__(kRefreshThreads)
 refresh_large_kernel(DevModel m, DevBatch b, int only_due, int track_drift) {
+    constexpr bool kF32 = sizeof(LT) == 4;
     const int w = blockIdx.x;
     const int spin = blockIdx.y;
     if (only_due == 1 && b.since[w] >= 0) return;
@@ -360,31 +365,38 @@ refresh_large_kernel(DevModel m, DevBatch b, int only_due, int track_drift) {
     const size_t wblock = (size_t)N * (m.ld_up + m.ld_dn);
     OutT *W = (sizeof(OutT) == 8 ? (OutT *)b.W64 : (OutT *)b.W32) + (size_t)w * wblock +
               (spin == 0 ? 0 : (size_t)N * m.ld_up);
-    double *A = b.lu_scratch + ((size_t)w * 2 + spin) * b.lu_block;  // n x n, row-major, lda = n
+    LT *A = reinterpret_cast<LT *>(b.lu_scratch) + ((size_t)w * 2 + spin) * b.lu_block;  // n x n, lda = n
     double *Y = b.solve_scratch + ((size_t)w * 2 + spin) * b.solve_block;
 
     extern __shared__ __align__(16) unsigned char smem[];
     constexpr int ldp = kPanel + 1;
-    double *Pn = reinterpret_cast<double *>(smem);          // panel [n][ldp]
-    double *Ut = Pn + (size_t)n * ldp;                       // U12 tile [kPanel][64]
-    double *invd = Ut + kPanel * 64;
-    double *red = invd + n;
-    int *perm = reinterpret_cast<int *>(red + 33);
+    double *red = reinterpret_cast<double *>(smem);          // 33 doubles
+    LT *Pn = reinterpret_cast<LT *>(red + 33);               // panel [n][ldp]
+    LT *Ut = Pn + (size_t)n * ldp;                           // U12 tile [kPanel][64]
+    LT *invd = Ut + kPanel * 64;
+    int *perm = reinterpret_cast<int *>(invd + n);
     int *ipiv = perm + n;
     short *rows = reinterpret_cast<short *>(ipiv + n);
+    short *site_of = rows + N;                               // FP32 path: the site holding each label
     __shared__ int s_piv;
-    __shared__ double s_pmax, s_dinv;
+    __shared__ LT s_pmax, s_dinv;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nt = blockDim.x;
 
     // gather tilde_U into A (zeroed first)
-    for (size_t e = tid; e < (size_t)n * n; e += nt) A[e] = 0.0;
+    for (size_t e = tid; e < (size_t)n * n; e += nt) A[e] = LT(0);
     __syncthreads();
+    const float *Uh = spin == 0 ? m.U32_up_hi : m.U32_dn_hi;
     for (int R = warp; R < N; R += nt / 32) {
         const int l = kappa[R];
         if (l >= 1 && l <= n) {
-            const double *src = U + (size_t)R * n;
-            double *dst = A + (size_t)(l - 1) * n;
-            for (int c = lane; c < n; c += 32) dst[c] = src[c];
+            LT *dst = A + (size_t)(l - 1) * n;
+            if constexpr (kF32) {
+                const float *src = Uh + (size_t)R * n;
+                for (int c = lane; c < n; c += 32) dst[c] = src[c];
+            } else {
+                const double *src = U + (size_t)R * n;
+                for (int c = lane; c < n; c += 32) dst[c] = src[c];
+            }
         }
     }
     for (int i = tid; i < n; i += nt) perm[i] = i;
@@ -402,36 +414,36 @@ refresh_large_kernel(DevModel m, DevBatch b, int only_due, int track_drift) {
         __syncthreads();
         for (int k = 0; k < nb; ++k) {
             if (warp == 0) {
-                double best = -1.0;
+                LT best = LT(-1);
                 int bi = rp;
                 for (int i = k + lane; i < rp; i += 32) {
-                    const double v = fabs(Pn[(size_t)i * ldp + k]);
+                    const LT v = fabs(Pn[(size_t)i * ldp + k]);
                     if (v > best) { best = v; bi = i; }
                 }
 #pragma unroll
                 for (int o = 16; o > 0; o >>= 1) {
-                    const double ob = __shfl_xor_sync(0xffffffffu, best, o);
+                    const LT ob = __shfl_xor_sync(0xffffffffu, best, o);
                     const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
                     if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
                 }
                 if (lane == 0) {
                     s_piv = bi;
                     s_pmax = best;
-                    s_dinv = best > 0.0 ? 1.0 / Pn[(size_t)bi * ldp + k] : 0.0;
+                    s_dinv = best > LT(0) ? LT(1) / Pn[(size_t)bi * ldp + k] : LT(0);
                     ipiv[pb + k] = pb + bi;
                 }
             }
             __syncthreads();
-            if (!(s_pmax > 0.0)) { singular = true; break; }
+            if (!(s_pmax > LT(0))) { singular = true; break; }
             const int p = s_piv;
             if (p != k)
                 for (int j = tid; j < nb; j += nt) {
-                    const double a = Pn[(size_t)k * ldp + j];
+                    const LT a = Pn[(size_t)k * ldp + j];
                     Pn[(size_t)k * ldp + j] = Pn[(size_t)p * ldp + j];
                     Pn[(size_t)p * ldp + j] = a;
                 }
             __syncthreads();
-            const double dinv = s_dinv;
+            const LT dinv = s_dinv;
             for (int i = k + 1 + tid; i < rp; i += nt) Pn[(size_t)i * ldp + k] *= dinv;
             __syncthreads();
             for (int e = tid; e < (rp - k - 1) * (nb - k - 1); e += nt) {
@@ -452,7 +464,7 @@ refresh_large_kernel(DevModel m, DevBatch b, int only_due, int track_drift) {
             if (r1 != r2) {
                 for (int c = tid; c < n; c += nt) {
                     if (c >= pb && c < pb + nb) continue;
-                    const double a = A[(size_t)r1 * n + c];
+                    const LT a = A[(size_t)r1 * n + c];
                     A[(size_t)r1 * n + c] = A[(size_t)r2 * n + c];
                     A[(size_t)r2 * n + c] = a;
                 }
@@ -464,13 +476,13 @@ refresh_large_kernel(DevModel m, DevBatch b, int only_due, int track_drift) {
         if (c0 < n) {
             // 3. U12 = L11^{-1} A12, one column per thread
             for (int c = c0 + tid; c < n; c += nt) {
-                double x[kPanel];
+                LT x[kPanel];
 #pragma unroll
-                for (int i = 0; i < kPanel; ++i) x[i] = i < nb ? A[(size_t)(pb + i) * n + c] : 0.0;
+                for (int i = 0; i < kPanel; ++i) x[i] = i < nb ? A[(size_t)(pb + i) * n + c] : LT(0);
 #pragma unroll
                 for (int i = 1; i < kPanel; ++i) {
                     if (i < nb) {
-                        double acc = x[i];
+                        LT acc = x[i];
 #pragma unroll
                         for (int k = 0; k < i; ++k) acc = fma(-Pn[(size_t)i * ldp + k], x[k], acc);
                         x[i] = acc;
@@ -488,21 +500,21 @@ refresh_large_kernel(DevModel m, DevBatch b, int only_due, int track_drift) {
                 const int ncol = min(64, n - cb);
                 for (int e = tid; e < nb * 64; e += nt) {
                     const int k = e >> 6, c = e & 63;
-                    Ut[e] = c < ncol ? A[(size_t)(pb + k) * n + cb + c] : 0.0;
+                    Ut[e] = c < ncol ? A[(size_t)(pb + k) * n + cb + c] : LT(0);
                 }
                 __syncthreads();
                 for (int rb = c0; rb < n; rb += 64) {
-                    double acc[4][4];
+                    LT acc[4][4];
 #pragma unroll
                     for (int a = 0; a < 4; ++a)
 #pragma unroll
-                        for (int q = 0; q < 4; ++q) acc[a][q] = 0.0;
+                        for (int q = 0; q < 4; ++q) acc[a][q] = LT(0);
                     for (int k = 0; k < nb; ++k) {
-                        double lv[4], uv[4];
+                        LT lv[4], uv[4];
 #pragma unroll
                         for (int a = 0; a < 4; ++a) {
                             const int r = rb + 4 * ty + a;
-                            lv[a] = r < n ? Pn[(size_t)(r - pb) * ldp + k] : 0.0;
+                            lv[a] = r < n ? Pn[(size_t)(r - pb) * ldp + k] : LT(0);
                         }
 #pragma unroll
                         for (int q = 0; q < 4; ++q) uv[q] = Ut[k * 64 + 4 * tx + q];
@@ -529,16 +541,20 @@ refresh_large_kernel(DevModel m, DevBatch b, int only_due, int track_drift) {
     }
     if (singular) {
         if (threadIdx.x == 0) {
-            atomicOr(&b.status[w], kStatusSingular);
-            b.logdet[4 * w + spin] = -INFINITY;
-            b.logdet[4 * w + 2 + spin] = -INFINITY;
+            if constexpr (kF32) {
+                atomicOr(&b.status[w], kStatusRefine);  // an exactly zero FP32 pivot: the FP64 refresh decides
+            } else {
+                atomicOr(&b.status[w], kStatusSingular);
+                b.logdet[4 * w + spin] = -INFINITY;
+                b.logdet[4 * w + 2 + spin] = -INFINITY;
+            }
         }
         return;
     }
     double ld = 0.0, dmin = INFINITY, dmaxp = 0.0;
     for (int i = tid; i < n; i += nt) {
-        const double d = A[(size_t)i * n + i];
-        invd[i] = 1.0 / d;
+        const double d = (double)A[(size_t)i * n + i];
+        invd[i] = LT(1) / A[(size_t)i * n + i];
         ld += log(fabs(d));
         dmin = fmin(dmin, fabs(d));
         dmaxp = fmax(dmaxp, fabs(d));
@@ -552,18 +568,47 @@ refresh_large_kernel(DevModel m, DevBatch b, int only_due, int track_drift) {
     }
     const int nrows = collect_empty_rows(kappa, N, rows);
     write_unit_rows(kappa, N, n, W, ldw, track_drift != 0, &b.drift[w]);
-    for (int r0 = 0; r0 < nrows; r0 += blockDim.x) {
-        const int cnt = min((int)blockDim.x, nrows - r0);
-        solve_rows_blocked<OutT>(A, n, invd, perm, U, n, rows + r0, cnt, Y + (size_t)r0 * n, W, ldw, &b.drift[w],
-                                 track_drift != 0);
+    if constexpr (kF32) {
+        for (int i = tid; i < n; i += nt) site_of[i] = -1;
+        __syncthreads();
+        for (int R = tid; R < N; R += nt) {
+            const int l = kappa[R];
+            if (l >= 1 && l <= n) site_of[l - 1] = (short)R;
+        }
+        __syncthreads();
+        const float *Ul = spin == 0 ? m.U32_up_lo : m.U32_dn_lo;
+        float *Yf = reinterpret_cast<float *>(Y);
+        float dmax = 0.f;
+        for (int r0 = 0; r0 < nrows; r0 += blockDim.x) {
+            const int cnt = min((int)blockDim.x, nrows - r0);
+            if (tid < cnt) {
+                const int R = rows[r0 + tid];
+                if (!refine_row(A, n, invd, perm, site_of, Uh, Ul, n, R, Yf + (size_t)r0 * n * 2 + tid, cnt,
+                                reinterpret_cast<float *>(W) + (size_t)R * ldw, track_drift != 0, dmax))
+                    atomicOr(&b.status[w], kStatusRefine);
+            }
+        }
+        if (track_drift) {
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) dmax = fmaxf(dmax, __shfl_xor_sync(0xffffffffu, dmax, o));
+            if (lane == 0 && dmax > 0.f) atomic_max_nonneg(&b.drift[w], dmax);
+        }
+    } else {
+        for (int r0 = 0; r0 < nrows; r0 += blockDim.x) {
+            const int cnt = min((int)blockDim.x, nrows - r0);
+            solve_rows_blocked<OutT>(A, n, invd, perm, U, n, rows + r0, cnt, Y + (size_t)r0 * n, W, ldw, &b.drift[w],
+                                     track_drift != 0);
+        }
     }
 }
 
-size_t refresh_large_smem(const DevModel &m) {
+size_t refresh_large_smem(const DevModel &m, size_t lt_bytes) {
     const int n = m.n_up > m.n_dn ? m.n_up : m.n_dn;
-    return (size_t)n * (kPanel + 1) * 8 + kPanel * 64 * 8 + (size_t)n * 8 + 33 * 8 + (size_t)n * 8 +
-           (size_t)m.n_sites * 2 + 16;
+    return 33 * 8 + ((size_t)n * (kPanel + 1) + kPanel * 64 + (size_t)n) * lt_bytes + (size_t)n * 8 +
+           (size_t)m.n_sites * 2 + (size_t)n * 2 + 16;
 }
+
+size_t refresh_large_smem(const DevModel &m) { return refresh_large_smem(m, 8); }
 
 bool refresh_needs_large(const DevModel &m) { return (m.n_up > m.n_dn ? m.n_up : m.n_dn) > kSmemLuMaxN; }
 
@@ -2079,6 +2124,19 @@ cudaError_t launch_set_tend(const DevBatch &b, long long proposals, long long mo
     return cudaGetLastError();
 }
 
+// The FP32 refinement refresh with the LU blocked in HBM (more orbitals than
+// the shared-memory FP32 LU holds).
+cudaError_t launch_refresh32_large(const DevModel &m, const DevBatch &b, int only_due, int track_drift,
+                                   cudaStream_t stream) {
+    const dim3 grid(b.n_walkers, 2);
+    const size_t sm = refresh_large_smem(m, 4);
+    cudaError_t e = cudaFuncSetAttribute(refresh_large_kernel<float, float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)sm);
+    if (e != cudaSuccess) return e;
+    refresh_large_kernel<float, float><<<grid, kRefreshThreads, sm, stream>>>(m, b, only_due, track_drift);
+    return cudaGetLastError();
+}
+
 int max_smem_optin(int device) {
     int v = 0;
     cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, device);
@@ -2091,13 +2149,15 @@ cudaError_t launch_refresh(const DevModel &m, const DevBatch &b, bool fp32_out, 
     if (refresh_needs_large(m)) {
         const size_t sm = refresh_large_smem(m);
         if (fp32_out) {
-            cudaError_t e = cudaFuncSetAttribute(refresh_large_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+            cudaError_t e = cudaFuncSetAttribute(refresh_large_kernel<double, float>,
+                                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
             if (e != cudaSuccess) return e;
-            refresh_large_kernel<float><<<grid, kRefreshThreads, sm, stream>>>(m, b, only_due, track_drift);
+            refresh_large_kernel<double, float><<<grid, kRefreshThreads, sm, stream>>>(m, b, only_due, track_drift);
         } else {
-            cudaError_t e = cudaFuncSetAttribute(refresh_large_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+            cudaError_t e = cudaFuncSetAttribute(refresh_large_kernel<double, double>,
+                                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
             if (e != cudaSuccess) return e;
-            refresh_large_kernel<double><<<grid, kRefreshThreads, sm, stream>>>(m, b, only_due, track_drift);
+            refresh_large_kernel<double, double><<<grid, kRefreshThreads, sm, stream>>>(m, b, only_due, track_drift);
         }
         return cudaGetLastError();
     }

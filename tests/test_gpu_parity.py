@@ -549,11 +549,11 @@ def test_tensor_core_flush_refused_off_its_path(kv):
     eng.close()
 
 
-@pytest.mark.parametrize("N,placement", [(96, "hbm"), (216, "hbm"), (216, "chip"), (384, "hbm")])
+@pytest.mark.parametrize("N,placement", [(96, "hbm"), (216, "hbm"), (216, "chip"), (384, "hbm"), (864, "hbm")])
 def test_fp32_refinement_refresh(kv, N, placement):
     """The periodic refresh by FP32 iterative refinement: W right after it within
     5e-6 of the FP64 rebuild (relative to max(1, |W|)), and chains that follow the oracle."""
-    walkers, seed, R = 8, 61, 64
+    walkers, seed, R = (8, 61, 64) if N < 864 else (4, 61, 32)
     ham = ham_for(kv, N)
     eng = kv.Engine(ham, walkers, precision="mixed", seed=seed, refresh_interval=R, w_placement=placement)
     eng.set_refresh32(True)
