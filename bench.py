@@ -106,7 +106,7 @@ def reference_arm(a):
         return
     ham = model()
     threads = cpu_threads()
-    proposals = 1080  # ten reference refresh intervals per chain per step
+    proposals = 5400  # fifty reference refresh intervals per chain per step (about a second of host time)
     vals = []
     for s in range(a.warmup + a.steps):
         acc, sec = cpu_port_run(ham, threads, proposals, a.seed + 7919 * s, threads)
