@@ -522,7 +522,10 @@ def gpu_arm(a):
         pe.close()
         plain = {"value": ptot["accepted"] / (pms * 1e-3), "unit": UNIT, "ms": pms,
                  "moves_per_walker": 128, "accepted": ptot["accepted"]}
-    gate = None if a.skip_gate else energy_gate(ham, kv, 256, 8192, choice, a.seed + 1)
+    # long enough for every walker to pass two of the mixed form's periodic refreshes
+    # (acceptance ~0.127 at N=216)
+    gate_props = max(8192, int(2.2 * cfg["refresh_interval"] / 0.12))
+    gate = None if a.skip_gate else energy_gate(ham, kv, 256, gate_props, choice, a.seed + 1)
     adjoint = None if a.skip_grad else adjoint_run(kv, 4, local)
     uneven = None if a.skip_uneven else uneven_run(kv, a.seed, local)
     large = None if a.skip_large else large_run(kv, a.seed, local)

@@ -32,7 +32,7 @@ import numpy as np
 from . import _lib
 
 DELAYS = (1, 4, 8, 12, 16)
-REFRESH = (128, 256, 512, 1024, 2048)
+REFRESH = (128, 256, 512, 1024, 2048, 4096, 8192)
 PLACEMENTS = ("chip", "hbm")
 THREADS = (128, 256)
 DRIFT_BOUND = 1e-2  # on the 99.9th percentile of per-walker relative drift

@@ -21,6 +21,8 @@ from .lattice import DoubleKagome, Hamiltonian
 CELLS = {54: (3, 3), 96: (4, 4), 216: (6, 6), 384: (8, 8), 864: (12, 12)}
 WORKLOADS = [(216, 2048, {}), (96, 4096, {}), (54, 1024, {}), (216, 768, {}), (384, 256, {}),
              (864, 512, dict(delays=(8, 16), refresh=(128, 256), threads=(256,), placements=("hbm",), warmup=128))]
+# Candidates beyond the default refresh list are left out at N=864, where one
+# FP64 refresh of 512 walkers takes ~0.5 s.
 
 
 def model(N):
