@@ -205,9 +205,13 @@ typedef struct {
 KVMC_API int kvmc_sweep(kvmc_handle *h, int64_t proposals_per_walker, kvmc_sweep_stats *stats);
 
 /* Like kvmc_sweep, but every walker runs until it has made
- * moves_per_walker more accepted moves, however many proposals that takes
- * (the measurement and refresh cadences are unchanged).  Equal accepted
- * work per walker keeps the batch's launches balanced. */
+ * moves_per_walker more accepted moves (the measurement and refresh
+ * cadences are unchanged).  Equal accepted work per walker keeps the
+ * batch's launches balanced.  A walker gets at most 65536 proposals per
+ * requested move; one that cannot make its moves within them (a
+ * configuration no proposal leaves) ends the call with KVMC_ERR_NUMERIC,
+ * the other walkers' moves made.  Walkers flagged singular or non-finite
+ * stop at once, and the call reports them. */
 KVMC_API int kvmc_advance(kvmc_handle *h, int64_t moves_per_walker, kvmc_sweep_stats *stats);
 
 /* Local energy of every walker's current state (getOL,

@@ -1,6 +1,6 @@
 """Builds libkvmc.so (CUDA, sm_103a) in-tree under kagomedsl.jl_gb300/_build/.
 
-The two translation units compile in parallel, then link into one shared
+The translation units compile in parallel, then link into one shared
 library that exports the C ABI of include/kvmc.h.  Needs only nvcc; no GPU.
 """
 from __future__ import annotations
@@ -37,7 +37,7 @@ def _stale(out: Path, deps) -> bool:
 
 def build(verbose: bool = False, force: bool = False) -> Path:
     BUILD.mkdir(exist_ok=True)
-    headers = [ROOT / "include" / "kvmc.h", CSRC / "kvmc_internal.h", CSRC / "kvmc_device.cuh"]
+    headers = [ROOT / "include" / "kvmc.h", CSRC / "kvmc_internal.h", CSRC / "kvmc_device.cuh", CSRC / "kvmc_refine.cuh"]
     objs, procs = [], []
     for src in SOURCES:
         s = CSRC / src

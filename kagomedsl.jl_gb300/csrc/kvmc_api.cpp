@@ -969,10 +969,12 @@ struct SweepCall {
     Snapshot before;
     unsigned long long ref0 = 0;
     int launches = 1;
+    int64_t moves = 0;  // kvmc_advance: accepted moves asked of every walker
 };
 
 int sweep_begin(kvmc_handle *h, int64_t proposals_per_walker, int64_t moves_per_walker, bool stats, SweepCall &c) {
     KV_TRY(set_device(h));
+    c.moves = proposals_per_walker > 0 ? 0 : moves_per_walker;
     if (stats) {
         KV_TRY(snapshot(h, c.before));
         KV_TRY(h->cuda(cudaMemcpy(&c.ref0, h->db.refresh_count, 8, cudaMemcpyDeviceToHost), "refresh count"));
@@ -1000,6 +1002,19 @@ int enqueue_pairs(kvmc_handle *h, const kvmc::SweepParams &p, int pairs, bool ti
 int sweep_end(kvmc_handle *h, kvmc_sweep_stats *stats, SweepCall &c) {
     int bad = 0;
     KV_TRY(check_status(h, &bad));
+    if (c.moves > 0) {
+        // a walker that used its proposal allowance without making its moves
+        std::vector<long long> acc(h->n_walkers), want(h->n_walkers);
+        KV_TRY(h->cuda(cudaMemcpy(acc.data(), h->db.accepted, acc.size() * 8, cudaMemcpyDeviceToHost), "accepted"));
+        KV_TRY(h->cuda(cudaMemcpy(want.data(), h->db.acc_end, want.size() * 8, cudaMemcpyDeviceToHost), "acc_end"));
+        int short_n = 0, first = -1;
+        for (int w = 0; w < h->n_walkers; ++w)
+            if (acc[w] < want[w]) { ++short_n; if (first < 0) first = w; }
+        if (short_n)
+            return h->fail(KVMC_ERR_NUMERIC,
+                           "%d walker(s) made fewer than %lld accepted moves within %lld proposals per move "
+                           "(first: walker %d)", short_n, (long long)c.moves, kvmc::kAdvanceProposalsPerMove, first);
+    }
     if (!stats) return KVMC_OK;
     std::memset(stats, 0, sizeof *stats);
     Snapshot after;

@@ -303,9 +303,10 @@ __global__ void __launch_bounds__(256) sweep_c_kernel(DevModel m, DevBatch b, Sw
                                                       int *active_count) {
     const int w = blockIdx.x, N = m.n_sites;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const long long t0 = b.t[w], tend = b.t_end[w];
+    const long long t0 = b.t[w], tend_all = b.t_end[w];
+    const long long tend = min(tend_all, t0 + kLaunchProposals);  // this launch's share
     const long long acc_left = b.acc_end[w] - b.accepted[w];
-    if (t0 >= tend || acc_left <= 0) {
+    if (t0 >= tend || acc_left <= 0 || (b.status[w] & kStatusStop)) {
         if (threadIdx.x == 0 && b.since[w] < 0) b.since[w] = 0;
         return;
     }
@@ -439,7 +440,7 @@ __global__ void __launch_bounds__(256) sweep_c_kernel(DevModel m, DevBatch b, Sw
         b.sum_e[w] += se;
         b.sum_e2[w] += se2;
         b.n_meas[w] += n_meas;
-        if (t < tend && acc_count < acc_left) atomicAdd(active_count, 1);
+        if (t < tend_all && acc_count < acc_left) atomicAdd(active_count, 1);
     }
 }
 
@@ -499,9 +500,10 @@ __global__ void __launch_bounds__(256, 2)
 sweep_c_delayed_kernel(DevModel m, DevBatch b, SweepParams p, int *active_count) {
     const int w = blockIdx.x, N = m.n_sites;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const long long t0 = b.t[w], tend = b.t_end[w];
+    const long long t0 = b.t[w], tend_all = b.t_end[w];
+    const long long tend = min(tend_all, t0 + kLaunchProposals);  // this launch's share
     const long long acc_left = b.acc_end[w] - b.accepted[w];
-    if (t0 >= tend || acc_left <= 0) {
+    if (t0 >= tend || acc_left <= 0 || (b.status[w] & kStatusStop)) {
         if (threadIdx.x == 0 && b.since[w] < 0) b.since[w] = 0;
         return;
     }
@@ -686,7 +688,7 @@ sweep_c_delayed_kernel(DevModel m, DevBatch b, SweepParams p, int *active_count)
         b.sum_e[w] += se;
         b.sum_e2[w] += se2;
         b.n_meas[w] += n_meas;
-        if (t < tend && acc_count < acc_left) atomicAdd(active_count, 1);
+        if (t < tend_all && acc_count < acc_left) atomicAdd(active_count, 1);
     }
 }
 

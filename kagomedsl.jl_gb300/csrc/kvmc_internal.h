@@ -67,6 +67,15 @@ enum : int {
     kStatusTimeout = 4,   // a bounded wait on the tensor cores gave up
     kStatusRefine = 8,    // the FP32 refresh did not converge: the FP64 refresh redoes the walker
 };
+// A walker stops with one of these set: its chain cannot continue.
+constexpr int kStatusStop = kStatusSingular | kStatusNonFinite | kStatusTimeout;
+// Proposals one sweep launch makes per walker at most, so that every launch
+// ends in bounded time, a walker that can no longer accept a move included.
+constexpr long long kLaunchProposals = 1ll << 18;
+// kvmc_advance gives a walker at most this many proposals per requested
+// accepted move (the typical rate is below ten).
+constexpr long long kAdvanceProposalsPerMove = 1ll << 16;
+
 
 struct SweepParams {
     unsigned long long seed;

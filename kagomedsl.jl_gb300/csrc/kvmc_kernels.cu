@@ -729,9 +729,10 @@ __global__ void sweep_kernel(DevModel m, DevBatch b, SweepParams p, int refresh_
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
 
     const long long t0 = b.t[w];
-    const long long tend = b.t_end[w];
+    const long long tend_all = b.t_end[w];
+    const long long tend = min(tend_all, t0 + kLaunchProposals);  // this launch's share
     const long long acc_left = b.acc_end[w] - b.accepted[w];  // accepted moves still wanted
-    if (t0 >= tend || acc_left <= 0) {
+    if (t0 >= tend || acc_left <= 0 || (b.status[w] & kStatusStop)) {
         // nothing to do; a refresh marked due has run since (stream order), clear the mark
         if (threadIdx.x == 0 && b.since[w] < 0) b.since[w] = 0;
         return;
@@ -900,7 +901,7 @@ __global__ void sweep_kernel(DevModel m, DevBatch b, SweepParams p, int refresh_
         b.sum_e[w] += se;
         b.sum_e2[w] += se2;
         b.n_meas[w] += n_meas;
-        if (t < tend && acc_count < acc_left) atomicAdd(active_count, 1);
+        if (t < tend_all && acc_count < acc_left) atomicAdd(active_count, 1);
     }
 }
 
@@ -1383,9 +1384,10 @@ sweep_delayed_kernel(DevModel m, DevBatch b, SweepParams p, int *active_count) {
     const int N = m.n_sites;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const long long t0 = b.t[w];
-    const long long tend = b.t_end[w];
+    const long long tend_all = b.t_end[w];
+    const long long tend = min(tend_all, t0 + kLaunchProposals);  // this launch's share
     const long long acc_left = b.acc_end[w] - b.accepted[w];  // accepted moves still wanted
-    if (t0 >= tend || acc_left <= 0) {
+    if (t0 >= tend || acc_left <= 0 || (b.status[w] & kStatusStop)) {
         // nothing to do; a refresh marked due has run since (stream order), clear the mark
         if (threadIdx.x == 0 && b.since[w] < 0) b.since[w] = 0;
         return;
@@ -1663,7 +1665,7 @@ sweep_delayed_kernel(DevModel m, DevBatch b, SweepParams p, int *active_count) {
         b.sum_e[w] += se;
         b.sum_e2[w] += se2;
         b.n_meas[w] += n_meas;
-        if (t < tend && acc_count < acc_left) atomicAdd(active_count, 1);
+        if (t < tend_all && acc_count < acc_left) atomicAdd(active_count, 1);
     }
 }
 
@@ -1713,9 +1715,10 @@ sweep_pipe_kernel(DevModel m, DevBatch b, SweepParams p, int *active_count) {
     const int N = m.n_sites;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const long long t0 = b.t[w];
-    const long long tend = b.t_end[w];
+    const long long tend_all = b.t_end[w];
+    const long long tend = min(tend_all, t0 + kLaunchProposals);  // this launch's share
     const long long acc_left = b.acc_end[w] - b.accepted[w];
-    if (t0 >= tend || acc_left <= 0) {
+    if (t0 >= tend || acc_left <= 0 || (b.status[w] & kStatusStop)) {
         if (threadIdx.x == 0 && b.since[w] < 0) b.since[w] = 0;
         return;
     }
@@ -2003,7 +2006,7 @@ sweep_pipe_kernel(DevModel m, DevBatch b, SweepParams p, int *active_count) {
         b.sum_e[w] += se;
         b.sum_e2[w] += se2;
         b.n_meas[w] += n_meas;
-        if (t < tend && ctl.acc < acc_left) atomicAdd(active_count, 1);
+        if (t < tend_all && ctl.acc < acc_left) atomicAdd(active_count, 1);
     }
 }
 
@@ -2107,11 +2110,13 @@ __global__ void init_random_kernel(DevModel m, DevBatch b, unsigned long long se
 }
 
 // Targets of one call: kvmc_sweep sets t_end = t + proposals (no accepted
-// target); kvmc_advance sets acc_end = accepted + moves (no proposal limit).
+// target); kvmc_advance sets acc_end = accepted + moves and allows
+// kAdvanceProposalsPerMove proposals per move.
 __global__ void set_tend_kernel(DevBatch b, long long proposals, long long moves) {
     const int w = blockIdx.x * blockDim.x + threadIdx.x;
     if (w < b.n_walkers) {
-        b.t_end[w] = proposals > 0 ? b.t[w] + proposals : 0x3fffffffffffffffll;
+        // moves: a walker that cannot make them stops after its proposal allowance
+        b.t_end[w] = b.t[w] + (proposals > 0 ? proposals : min(moves, 1ll << 40) * kAdvanceProposalsPerMove);
         b.acc_end[w] = moves > 0 ? b.accepted[w] + moves : 0x3fffffffffffffffll;
     }
 }

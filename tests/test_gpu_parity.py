@@ -355,6 +355,27 @@ def test_advance_makes_exactly_the_asked_moves(kv, precision):
 
 
 @pytest.mark.parametrize("precision", ["plain", "mixed"])
+def test_advance_stops_a_walker_that_cannot_move(kv, precision):
+    """Four sites, one bond (0, 1).  Walker 0 holds both up spins on the bond:
+    Z_mu = 0, every proposal is rejected, and kvmc_advance stops it after its
+    allowance of 65536 proposals per requested move with an error; walker 1
+    (opposite spins on the bond) makes its moves."""
+    rng = np.random.default_rng(4)
+    U = rng.normal(size=(4, 2))
+    H = np.zeros((4, 4))
+    H[0, 1] = H[1, 0] = -1.0
+    ham = kv.Hamiltonian(2, 2, U, U.copy(), H, [(0, 1)])
+    eng = kv.Engine(ham, 2, precision=precision, seed=1, refresh_interval=64, measure_interval=64)
+    eng.init(np.array([[1, 2, 0, 0], [1, 0, 2, 0]]), np.array([[0, 0, 1, 2], [0, 1, 0, 2]]))
+    with pytest.raises(kv.KvmcError, match="fewer than 3 accepted moves"):
+        eng.advance(3)
+    ws = eng.walker_stats()
+    assert ws["accepted"][0] == 0 and ws["proposals"][0] == 3 * 65536
+    assert ws["accepted"][1] == 3
+    eng.close()
+
+
+@pytest.mark.parametrize("precision", ["plain", "mixed"])
 def test_unequal_spin_counts(kv, precision):
     """N_up != N_down (src/MonteCarlo.jl:165-185 takes both): two W widths."""
     N, n_up, seed, walkers, proposals = 54, 30, 23, 8, 1500
