@@ -31,7 +31,10 @@ namespace kvmc {
 
 namespace {
 
-constexpr int kThreads32 = 256;
+// 128 threads, four walker-spins per SM: the refinement gives each thread
+// one row of W, and more rows in flight per SM hide its dependent chains.
+constexpr int kThreads32 = 128;
+constexpr int kBlocks32 = 4;
 constexpr int kMaxN32 = 224;
 
 // P A = L Uf in place (float), first maximal |pivot| wins; false when singular.
@@ -87,7 +90,7 @@ __device__ bool lu32(float *A, int lda, int n, int *perm, float *invd) {
     return true;
 }
 
-__global__ void __launch_bounds__(kThreads32, 2)
+__global__ void __launch_bounds__(kThreads32, kBlocks32)
 refresh32_kernel(DevModel m, DevBatch b, int only_due, int track_drift) {
     const int w = blockIdx.x, spin = blockIdx.y;
     if (only_due && b.since[w] >= 0) return;
