@@ -557,6 +557,20 @@ extern "C" int kvmc_create(const kvmc_model_desc *model, const kvmc_batch_desc *
         if (i < 0 || j < 0 || i >= N || j >= N) return fail_global(KVMC_ERR_BOUNDS, "bond %d (%d,%d) out of range", e, i, j);
         if (i == j) return fail_global(KVMC_ERR_ARGUMENT, "bond %d joins site %d to itself", e, i);
     }
+    {
+        // Z_mu counts bonds; the sweep updates it from neighbour counts, which
+        // needs every bond once
+        std::vector<std::pair<int, int>> pairs(nb);
+        for (int e = 0; e < nb; ++e) {
+            const int i = model->bonds[2 * e], j = model->bonds[2 * e + 1];
+            pairs[e] = {std::min(i, j), std::max(i, j)};
+        }
+        std::sort(pairs.begin(), pairs.end());
+        for (int e = 1; e < nb; ++e)
+            if (pairs[e] == pairs[e - 1])
+                return fail_global(KVMC_ERR_ARGUMENT, "bond (%d,%d) appears more than once", pairs[e].first,
+                                   pairs[e].second);
+    }
     if (batch->n_walkers <= 0) return fail_global(KVMC_ERR_ARGUMENT, "n_walkers must be positive");
     if (batch->precision != KVMC_PLAIN_FP64 && batch->precision != KVMC_MIXED_FP32)
         return fail_global(KVMC_ERR_ARGUMENT, "unknown precision %d", batch->precision);

@@ -1748,11 +1748,13 @@ sweep_pipe_kernel(DevModel m, DevBatch b, SweepParams p, int *active_count) {
     short *nbr = reinterpret_cast<short *>(cur); cur += (size_t)2 * m.n_bonds * sizeof(short);
     short *kup = reinterpret_cast<short *>(cur); cur += (size_t)N * sizeof(short);
     short *kdn = reinterpret_cast<short *>(cur);
+    // nu[s] = the number of neighbours of s that hold the up spin
+    int *nu = reinterpret_cast<int *>((reinterpret_cast<uintptr_t>(kdn + N) + 3) & ~uintptr_t(3));
     [[maybe_unused]] __shared__ __align__(8) uint64_t tc_mbar;
     [[maybe_unused]] __shared__ uint32_t tc_tmem_slot;
     [[maybe_unused]] tc::State tcs{};
     if constexpr (kTC) {
-        cur = reinterpret_cast<unsigned char *>(kdn + N);
+        cur = reinterpret_cast<unsigned char *>(nu + N);
         cur = reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(cur) + 127) & ~uintptr_t(127));
         tcs.a_hi = reinterpret_cast<float *>(cur); cur += tc::kTileM * tc::kMaxKK * sizeof(float);
         tcs.a_lo = reinterpret_cast<float *>(cur); cur += tc::kTileM * tc::kMaxKK * sizeof(float);
@@ -1782,6 +1784,11 @@ sweep_pipe_kernel(DevModel m, DevBatch b, SweepParams p, int *active_count) {
     for (int e = tid; e < m.n_bonds; e += blockDim.x) {
         const short2 bd = bonds[e];
         zc += ((kup[bd.x] != 0 && kdn[bd.y] != 0) || (kup[bd.y] != 0 && kdn[bd.x] != 0)) ? 1.0 : 0.0;
+    }
+    for (int s0 = tid; s0 < N; s0 += blockDim.x) {
+        int c = 0;
+        for (int e = nbr_off[s0]; e < nbr_off[s0 + 1]; ++e) c += kup[nbr[e]] != 0 ? 1 : 0;
+        nu[s0] = c;
     }
     zc = block_sum(zc, ctl.red);
     const int R = p.refresh_every;
@@ -1861,17 +1868,17 @@ sweep_pipe_kernel(DevModel m, DevBatch b, SweepParams p, int *active_count) {
                 // the unit-row check of the two rows the move changes.
                 __syncwarp();
                 const PendingMove nm = ctl.mv[slot ^ 1];
-                int dz = 0;
-                for (int e = nbr_off[nm.Ku] + lane; e < nbr_off[nm.Ku + 1]; e += 32) {
-                    const int k = nbr[e];
-                    if (k != nm.Kd) dz += kup[k] == 0 ? 1 : -1;
-                }
-                for (int e = nbr_off[nm.Kd] + lane; e < nbr_off[nm.Kd + 1]; e += 32) {
-                    const int k = nbr[e];
-                    if (k != nm.Ku) dz += kup[k] != 0 ? 1 : -1;
-                }
-                dz = __reduce_add_sync(0xffffffffu, dz);
-                __syncwarp();
+                // the up spin moves Kd -> Ku along their bond (every site holds one
+                // spin, bonds are unique): the bonds from Ku to its other up
+                // neighbours turn parallel and the rest antiparallel, and the other
+                // way round at Kd, so Z_mu changes by
+                //   (deg Ku - 1 - 2 (nu[Ku] - 1)) + (2 nu[Kd] - (deg Kd - 1))
+                const int bu = nbr_off[nm.Ku], du = nbr_off[nm.Ku + 1] - bu;
+                const int bd = nbr_off[nm.Kd], dd = nbr_off[nm.Kd + 1] - bd;
+                const int dz = du - dd + 2 - 2 * nu[nm.Ku] + 2 * nu[nm.Kd];
+                __syncwarp();  // every lane has read nu before it changes
+                for (int e = lane; e < du + dd; e += 32)
+                    atomicAdd(&nu[e < du ? nbr[bu + e] : nbr[bd + e - du]], e < du ? 1 : -1);
                 if (lane == 0) {
                     kup[nm.Ku] = (short)(nm.lu + 1); kup[nm.Kd] = 0;
                     kdn[nm.Kd] = (short)(nm.ld + 1); kdn[nm.Ku] = 0;
@@ -2021,6 +2028,7 @@ size_t delayed_smem_bytes(const DevModel &m, int K, bool w_on_chip) {
     size_t s = w_on_chip ? N * (m.ld_up + m.ld_dn) * 4 : 0;  // W
     s += 2 * N * K * 4 + (size_t)(m.ld_up + m.ld_dn) * K * 4;  // P, Q
     s += (N + 1) * 4 + (size_t)m.n_bonds * 4 + (size_t)2 * m.n_bonds * 2 + 2 * N * 2 + 16;
+    s += N * 4 + 4;  // up-neighbour counts (pipelined kernel)
     return (s + 15) / 16 * 16;
 }
 

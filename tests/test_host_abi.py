@@ -91,6 +91,11 @@ def test_create_validates_before_touching_a_device(built):
     bad = kv.Hamiltonian(12, 12, ham.U_up, ham.U_down, ham.H_mat, [(0, 99)])
     with pytest.raises(kv.BoundsError):
         kv.Engine(bad, 2)
+    # a bond given twice (in either orientation) is refused
+    i, j = ham.nn[0]
+    bad = kv.Hamiltonian(12, 12, ham.U_up, ham.U_down, ham.H_mat, list(ham.nn) + [(j, i)])
+    with pytest.raises(kv.ArgumentError, match="more than once"):
+        kv.Engine(bad, 2)
 
 
 def test_complex_orbitals_beyond_the_limit_are_unsupported(built):
