@@ -1712,7 +1712,7 @@ __device__ __forceinline__ float eff_after(const DelayedSpin<K> &S, int r, int c
 
 template <int K, bool kStream, int kThreads, bool kTC>
 __global__ void __launch_bounds__(kThreads, 512 / kThreads)
-sweep_pipe_kernel(DevModel m, DevBatch b, SweepParams p, int *active_count) {
+sweep_pipe_kernel(DevModel m, DevBatch b, SweepParams p, int *active_count, int thr_in_smem) {
     const int w = blockIdx.x;
     const int N = m.n_sites;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -1750,11 +1750,15 @@ sweep_pipe_kernel(DevModel m, DevBatch b, SweepParams p, int *active_count) {
     short *kdn = reinterpret_cast<short *>(cur);
     // nu[s] = the number of neighbours of s that hold the up spin
     int *nu = reinterpret_cast<int *>((reinterpret_cast<uintptr_t>(kdn + N) + 3) & ~uintptr_t(3));
+    // the acceptance thresholds, on chip when the launch found room for them
+    ThrEntry *thr_s = reinterpret_cast<ThrEntry *>((reinterpret_cast<uintptr_t>(nu + N) + 15) & ~uintptr_t(15));
+    const ThrEntry *thr_tab = thr_in_smem ? thr_s : m.thr_table;
     [[maybe_unused]] __shared__ __align__(8) uint64_t tc_mbar;
     [[maybe_unused]] __shared__ uint32_t tc_tmem_slot;
     [[maybe_unused]] tc::State tcs{};
     if constexpr (kTC) {
-        cur = reinterpret_cast<unsigned char *>(nu + N);
+        cur = thr_in_smem ? reinterpret_cast<unsigned char *>(thr_s + m.n_bonds + 1)
+                          : reinterpret_cast<unsigned char *>(nu + N);
         cur = reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(cur) + 127) & ~uintptr_t(127));
         tcs.a_hi = reinterpret_cast<float *>(cur); cur += tc::kTileM * tc::kMaxKK * sizeof(float);
         tcs.a_lo = reinterpret_cast<float *>(cur); cur += tc::kTileM * tc::kMaxKK * sizeof(float);
@@ -1775,6 +1779,8 @@ sweep_pipe_kernel(DevModel m, DevBatch b, SweepParams p, int *active_count) {
     for (int e = tid; e < m.n_bonds; e += blockDim.x) bonds[e] = m.bonds[e];
     for (int e = tid; e < 2 * m.n_bonds; e += blockDim.x) nbr[e] = m.nbr[e];
     for (int e = tid; e <= N; e += blockDim.x) nbr_off[e] = m.nbr_off[e];
+    if (thr_in_smem)
+        for (int e = tid; e <= m.n_bonds; e += blockDim.x) thr_s[e] = m.thr_table[e];
     for (int s = tid; s < N; s += blockDim.x) {
         kup[s] = b.kappa_up[(size_t)w * N + s];
         kdn[s] = b.kappa_dn[(size_t)w * N + s];
@@ -1822,6 +1828,7 @@ sweep_pipe_kernel(DevModel m, DevBatch b, SweepParams p, int *active_count) {
             const int since = ctl.since;
             const Thr thr = ctl.thr;
             int state = 2;
+            PendingMove nm{};
             while (true) {
                 if (t == next_meas) { state = 3; break; }
                 if (t >= tend || since >= R || acc >= acc_left) break;
@@ -1854,7 +1861,9 @@ sweep_pipe_kernel(DevModel m, DevBatch b, SweepParams p, int *active_count) {
                 const unsigned mask = __ballot_sync(0xffffffffu, accd);
                 if (mask) {
                     const int f = __ffs(mask) - 1;
-                    if (lane == f) ctl.mv[slot ^ 1] = PendingMove{Ku, lu, Kd, ld, pu, pd};
+                    nm = PendingMove{__shfl_sync(0xffffffffu, Ku, f), __shfl_sync(0xffffffffu, lu, f),
+                                     __shfl_sync(0xffffffffu, Kd, f), __shfl_sync(0xffffffffu, ld, f),
+                                     __shfl_sync(0xffffffffu, pu, f), __shfl_sync(0xffffffffu, pd, f)};
                     t += f + 1;
                     state = 1;
                     break;
@@ -1866,8 +1875,6 @@ sweep_pipe_kernel(DevModel m, DevBatch b, SweepParams p, int *active_count) {
                 // configuration, the threshold and the counters.  Nobody else reads
                 // the configuration in this phase; the flush that may follow skips
                 // the unit-row check of the two rows the move changes.
-                __syncwarp();
-                const PendingMove nm = ctl.mv[slot ^ 1];
                 // the up spin moves Kd -> Ku along their bond (every site holds one
                 // spin, bonds are unique): the bonds from Ku to its other up
                 // neighbours turn parallel and the rest antiparallel, and the other
@@ -1880,10 +1887,11 @@ sweep_pipe_kernel(DevModel m, DevBatch b, SweepParams p, int *active_count) {
                 for (int e = lane; e < du + dd; e += 32)
                     atomicAdd(&nu[e < du ? nbr[bu + e] : nbr[bd + e - du]], e < du ? 1 : -1);
                 if (lane == 0) {
+                    ctl.mv[slot ^ 1] = nm;
                     kup[nm.Ku] = (short)(nm.lu + 1); kup[nm.Kd] = 0;
                     kdn[nm.Kd] = (short)(nm.ld + 1); kdn[nm.Ku] = 0;
                     ctl.zmu += dz;
-                    make_thr(ctl.thr, m.thr_table, ctl.zmu, p.accept_rule);
+                    make_thr(ctl.thr, thr_tab, ctl.zmu, p.accept_rule);
                     ctl.since += 1;
                     ctl.acc += 1;
                 }
@@ -2217,11 +2225,18 @@ static cudaError_t launch_delayed_t(const DevModel &m, const DevBatch &b, const 
 template <int K, bool kStream, int kThreads, bool kTC = false>
 static cudaError_t launch_pipe_t(const DevModel &m, const DevBatch &b, const SweepParams &p, int *active,
                                  cudaStream_t stream) {
-    const size_t sm = delayed_smem_bytes(m, K, !kStream) + (kTC ? tc_flush_smem_bytes() : 0);
+    size_t sm = delayed_smem_bytes(m, K, !kStream) + (kTC ? tc_flush_smem_bytes() : 0);
+    // the threshold table joins the CTA's shared memory when the walkers per
+    // SM the launch shape is made for (512 threads per SM) still fit
+    const size_t thr_bytes = 16 + (size_t)(m.n_bonds + 1) * sizeof(ThrEntry);
+    const int per_sm = kStream ? 512 / kThreads : 1;
+    const size_t kSmemPerSM = 228 * 1024, kReserve = 1024 + 2048;  // per-CTA reserve and static shared data
+    const int thr_in_smem = per_sm * (sm + thr_bytes + kReserve) <= kSmemPerSM && sm + thr_bytes <= 227 * 1024;
+    if (thr_in_smem) sm += thr_bytes;
     cudaError_t e = cudaFuncSetAttribute(sweep_pipe_kernel<K, kStream, kThreads, kTC>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     if (e != cudaSuccess) return e;
-    sweep_pipe_kernel<K, kStream, kThreads, kTC><<<b.n_walkers, kThreads, sm, stream>>>(m, b, p, active);
+    sweep_pipe_kernel<K, kStream, kThreads, kTC><<<b.n_walkers, kThreads, sm, stream>>>(m, b, p, active, thr_in_smem);
     return cudaGetLastError();
 }
 
