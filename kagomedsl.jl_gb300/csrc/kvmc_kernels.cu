@@ -1972,9 +1972,16 @@ sweep_pipe_kernel(DevModel m, DevBatch b, SweepParams p, int *active_count, int 
             delayed_zero<K>(SU, N);
             delayed_zero<K>(SD, N);
             if (tid == 0) {
-                // adaptive refresh: rounding past the tolerance ends this walker's run;
-                // the other drift slot is free again (everybody read it a flush ago)
-                if (__int_as_float(*dev) > p.drift_tol) ctl.since = R;
+                // adaptive refresh on rounding past the tolerance: when the moves
+                // this call still asks of the walker are fewer than an interval, at
+                // the end of the call (its counter then reaches R exactly with its
+                // last move, so refreshes stay on call boundaries and no walker stops
+                // mid-call), else now.  The other drift slot is free again
+                // (everybody read it a flush ago).
+                if (__int_as_float(*dev) > p.drift_tol) {
+                    const long long rem = acc_left - ctl.acc;
+                    ctl.since = rem < R ? max(ctl.since, (int)(R - rem)) : R;
+                }
                 ctl.dev2[(fp & 1) ^ 1] = 0;
             }
             __syncthreads();
