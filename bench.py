@@ -363,8 +363,6 @@ def batched_run(kv, seed, device, walkers=4096, moves=1024):
 
 
 def field_run(kv, seed, device, walkers=2048, moves=256):
-    # the mixed form runs 4 * moves (two of its refreshes) and the plain form
-    # moves / 4 (it refreshes every 94 proposals)
     """The field workload of scripts/LL.jl: 8x8 doubled cells (N=192), B =
     imbalance * pi / S with imbalance 4 (N_up = 98, N_down = 94), complex
     orbitals; the mixed complex form (delayed updates, W in HBM) against the
@@ -375,16 +373,26 @@ def field_run(kv, seed, device, walkers=2048, moves=256):
     H = kv.Hmat(lat, B=4 * math.pi / (64 * 2 * math.sqrt(3)))
     Uu, Ud = kv.orbitals(H, 98, 94)
     ham = kv.Hamiltonian(98, 94, Uu, Ud, H, kv.get_nn(H))
+    from kagomevmc import autotune
+
+    # the mixed form with the autotuner's settings for this workload, over two
+    # of its refresh intervals
+    ch = autotune.lookup(ham, walkers) or autotune.Choice(delay_k=8, refresh_interval=512, placement="hbm")
     out = {}
-    for prec, R, mv in (("mixed", 512, 4 * moves), ("plain", 0, moves // 4)):
-        eng = kv.Engine(ham, walkers, precision=prec, seed=seed, refresh_interval=R, device=device)
+    for prec, R, mv in (("mixed", ch.refresh_interval, max(4 * moves, 2 * ch.refresh_interval)),
+                        ("plain", 0, moves // 4)):
+        if prec == "mixed":
+            eng = autotune.make_engine(ham, walkers, ch, seed=seed, device=device)
+        else:
+            eng = kv.Engine(ham, walkers, precision=prec, seed=seed, refresh_interval=R, device=device)
         eng.init()
         eng.advance(32)
         eng.region_start()
         st = eng.advance(mv)
         ms = eng.region_stop()
         out[prec] = {"value": st["accepted"] / (ms * 1e-3), "unit": UNIT, "moves_per_walker": mv,
-                     "delay_k": eng.config()["delay_k"], "walker_refreshes": st["refreshes"]}
+                     "delay_k": eng.config()["delay_k"], "refresh_interval": eng.config()["refresh_interval"],
+                     "walker_refreshes": st["refreshes"]}
         eng.close()
     return {"workload": f"kagome VMC in a field, 8x8 doubled cells (N=192), imbalance 4, {walkers} walkers, "
                         "complex orbitals", **out, "mixed_over_plain": out["mixed"]["value"] / out["plain"]["value"]}

@@ -692,6 +692,292 @@ sweep_c_delayed_kernel(DevModel m, DevBatch b, SweepParams p, int *active_count)
     }
 }
 
+// ---------------------------------------------------------------------------
+// The pipelined form of the complex delayed sweep (the real
+// sweep_pipe_kernel's scheme, kvmc_kernels.cu): warp 0 scans for the next
+// accepted move while the other warps write the factor column of the last
+// one, reading W_eff through that move's Sherman-Morrison correction
+//   W_eff'(r, c) = W_eff(r, c) - W_eff(r, l) (W_eff(K, c) - [c == l]) / pivot
+// over the complete columns only; one barrier per accepted move.  Z_mu
+// changes come from per-site up-neighbour counts, the accepted move reaches
+// the warp by shuffles, the thresholds sit in shared memory when they fit.
+// ---------------------------------------------------------------------------
+template <int K>
+__device__ __forceinline__ cf ceff_after(const CDelayed<K> &S, int r, int c, int mm, bool pend, int Kp, int lp,
+                                         cf ipiv) {
+    cf v = S.eff(r, c, mm);
+    if (pend) {
+        const cf a = S.eff(r, lp, mm);
+        cf q = S.eff(Kp, c, mm);
+        if (c == lp) q.x -= 1.f;
+        v = cfms(cmul(a, ipiv), q, v);
+    }
+    return v;
+}
+
+struct CPipeMove {
+    int Ku, lu, Kd, ld;
+    cf piv_u, piv_d;
+};
+
+struct CPipeCtl {
+    long long t, next_meas, acc;
+    int since, zmu;
+    int state2[2];
+    CPipeMove mv[2];
+    Thr thr;
+    double red[33];
+};
+
+template <int K>
+__global__ void __launch_bounds__(256, 2)
+sweep_c_pipe_kernel(DevModel m, DevBatch b, SweepParams p, int *active_count, int thr_in_smem) {
+    const int w = blockIdx.x, N = m.n_sites;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const long long t0 = b.t[w], tend_all = b.t_end[w];
+    const long long tend = min(tend_all, t0 + kLaunchProposals);  // this launch's share
+    const long long acc_left = b.acc_end[w] - b.accepted[w];
+    if (t0 >= tend || acc_left <= 0 || (b.status[w] & kStatusStop)) {
+        if (threadIdx.x == 0 && b.since[w] < 0) b.since[w] = 0;
+        return;
+    }
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ CPipeCtl ctl;
+    const size_t wblock = (size_t)N * (m.ld_up + m.ld_dn);
+    cf *gW = reinterpret_cast<cf *>(b.W32) + (size_t)w * wblock;
+    CDelayed<K> SU, SD;
+    SU.W = gW;
+    SU.ld = m.ld_up;
+    SD.W = gW + (size_t)N * m.ld_up;
+    SD.ld = m.ld_dn;
+    unsigned char *cur = smem;
+    SU.P = reinterpret_cast<cf *>(cur); cur += (size_t)N * K * sizeof(cf);
+    SD.P = reinterpret_cast<cf *>(cur); cur += (size_t)N * K * sizeof(cf);
+    SU.Q = reinterpret_cast<cf *>(cur); cur += (size_t)m.ld_up * K * sizeof(cf);
+    SD.Q = reinterpret_cast<cf *>(cur); cur += (size_t)m.ld_dn * K * sizeof(cf);
+    int *nbr_off = reinterpret_cast<int *>(cur); cur += (size_t)(N + 1) * sizeof(int);
+    int *nu = reinterpret_cast<int *>(cur); cur += (size_t)N * sizeof(int);
+    short2 *bonds = reinterpret_cast<short2 *>(cur); cur += (size_t)m.n_bonds * sizeof(short2);
+    short *nbr = reinterpret_cast<short *>(cur); cur += (size_t)2 * m.n_bonds * sizeof(short);
+    short *kup = reinterpret_cast<short *>(cur); cur += (size_t)N * sizeof(short);
+    short *kdn = reinterpret_cast<short *>(cur); cur += (size_t)N * sizeof(short);
+    ThrEntry *thr_s = reinterpret_cast<ThrEntry *>((reinterpret_cast<uintptr_t>(cur) + 15) & ~uintptr_t(15));
+    const ThrEntry *thr_tab = thr_in_smem ? thr_s : m.thr_table;
+    cdelayed_zero<K>(SU, N);
+    cdelayed_zero<K>(SD, N);
+    for (int e = tid; e < m.n_bonds; e += blockDim.x) bonds[e] = m.bonds[e];
+    for (int e = tid; e < 2 * m.n_bonds; e += blockDim.x) nbr[e] = m.nbr[e];
+    for (int e = tid; e <= N; e += blockDim.x) nbr_off[e] = m.nbr_off[e];
+    if (thr_in_smem)
+        for (int e = tid; e <= m.n_bonds; e += blockDim.x) thr_s[e] = m.thr_table[e];
+    for (int s2 = tid; s2 < N; s2 += blockDim.x) {
+        kup[s2] = b.kappa_up[(size_t)w * N + s2];
+        kdn[s2] = b.kappa_dn[(size_t)w * N + s2];
+    }
+    __syncthreads();
+    double zc = 0.0;
+    for (int e = tid; e < m.n_bonds; e += blockDim.x) {
+        const short2 bd = bonds[e];
+        zc += ((kup[bd.x] != 0 && kdn[bd.y] != 0) || (kup[bd.y] != 0 && kdn[bd.x] != 0)) ? 1.0 : 0.0;
+    }
+    for (int s2 = tid; s2 < N; s2 += blockDim.x) {
+        int c = 0;
+        for (int e = nbr_off[s2]; e < nbr_off[s2 + 1]; ++e) c += kup[nbr[e]] != 0 ? 1 : 0;
+        nu[s2] = c;
+    }
+    zc = block_sum(zc, ctl.red);
+    const int R = p.refresh_every, M = p.measure_every;
+    if (tid == 0) {
+        ctl.t = t0;
+        ctl.acc = 0;
+        ctl.since = b.since[w] < 0 ? 0 : b.since[w];
+        ctl.zmu = (int)zc;
+        ctl.next_meas = (t0 / M + 1) * M;
+        make_thr(ctl.thr, m.thr_table, ctl.zmu, p.accept_rule);
+    }
+    __syncthreads();
+    long long n_meas = 0;
+    double se = 0.0, se2 = 0.0;
+    // loop state kept by every thread alike: pend = a move accepted in the
+    // previous phase whose factor column this phase writes, slot = its entry
+    // in ctl.mv, mm = complete factor columns
+    int pend = 0, slot = 0, mm = 0, it = 0;
+    while (true) {
+        if (warp == 0) {
+            const CPipeMove pm = ctl.mv[slot];
+            const cf ipu = pend ? cinv(pm.piv_u) : cf{0.f, 0.f}, ipd = pend ? cinv(pm.piv_d) : cf{0.f, 0.f};
+            long long t = ctl.t;
+            const long long acc = ctl.acc, next_meas = ctl.next_meas;
+            const int since = ctl.since;
+            const Thr thr = ctl.thr;
+            int state = 2;
+            CPipeMove nm{};
+            while (true) {
+                if (t == next_meas) { state = 3; break; }
+                if (t >= tend || since >= R || acc >= acc_left) break;
+                const long long lim = min(tend, next_meas) - t;
+                const int win = lim < 32 ? (int)lim : 32;
+                bool accd = false, bad = false;
+                int Ku = 0, lu = 0, Kd = 0, ld = 0;
+                cf pu{0.f, 0.f}, pd{0.f, 0.f};
+                if (lane < win) {
+                    unsigned long long u53;
+                    int bi;
+                    proposal_bits(p.seed, w, t + lane, m.n_bonds, u53, bi);
+                    const short2 bd = bonds[bi];
+                    const int c = cmp_r_thr(u53, thr);
+                    if (p.accept_rule != 0 || c <= 0) {
+                        const int i = bd.x, j = bd.y;
+                        const int kui = kup[i], kuj = kup[j], kdi = kdn[i], kdj = kdn[j];
+                        const bool f1 = kui != 0 && kdj != 0;
+                        const bool f2 = kuj != 0 && kdi != 0;
+                        if (f1 || f2) {
+                            if (f1) { Ku = j; lu = kui - 1; Kd = i; ld = kdj - 1; }
+                            else    { Ku = i; lu = kuj - 1; Kd = j; ld = kdi - 1; }
+                            pu = ceff_after<K>(SU, Ku, lu, mm, pend, pm.Ku, pm.lu, ipu);
+                            pd = ceff_after<K>(SD, Kd, ld, mm, pend, pm.Kd, pm.ld, ipd);
+                            accd = decide_c(pu, pd, u53, c, thr, p.accept_rule, bad);
+                        }
+                    }
+                }
+                if (__any_sync(0xffffffffu, bad) && bad) atomicOr(&b.status[w], kStatusNonFinite);
+                const unsigned mask = __ballot_sync(0xffffffffu, accd);
+                if (mask) {
+                    const int f = __ffs(mask) - 1;
+                    nm.Ku = __shfl_sync(0xffffffffu, Ku, f);
+                    nm.lu = __shfl_sync(0xffffffffu, lu, f);
+                    nm.Kd = __shfl_sync(0xffffffffu, Kd, f);
+                    nm.ld = __shfl_sync(0xffffffffu, ld, f);
+                    nm.piv_u = cf{__shfl_sync(0xffffffffu, pu.x, f), __shfl_sync(0xffffffffu, pu.y, f)};
+                    nm.piv_d = cf{__shfl_sync(0xffffffffu, pd.x, f), __shfl_sync(0xffffffffu, pd.y, f)};
+                    t += f + 1;
+                    state = 1;
+                    break;
+                }
+                t += win;
+            }
+            if (state == 1) {
+                // the up spin moves Kd -> Ku along their bond: Z_mu changes by
+                // (deg Ku - 1 - 2 (nu[Ku] - 1)) + (2 nu[Kd] - (deg Kd - 1))
+                const int bu = nbr_off[nm.Ku], du = nbr_off[nm.Ku + 1] - bu;
+                const int bdn = nbr_off[nm.Kd], dd = nbr_off[nm.Kd + 1] - bdn;
+                const int dz = du - dd + 2 - 2 * nu[nm.Ku] + 2 * nu[nm.Kd];
+                __syncwarp();  // every lane has read nu before it changes
+                for (int e = lane; e < du + dd; e += 32)
+                    atomicAdd(&nu[e < du ? nbr[bu + e] : nbr[bdn + e - du]], e < du ? 1 : -1);
+                if (lane == 0) {
+                    ctl.mv[slot ^ 1] = nm;
+                    kup[nm.Ku] = (short)(nm.lu + 1); kup[nm.Kd] = 0;
+                    kdn[nm.Kd] = (short)(nm.ld + 1); kdn[nm.Ku] = 0;
+                    ctl.zmu += dz;
+                    make_thr(ctl.thr, thr_tab, ctl.zmu, p.accept_rule);
+                    ctl.since += 1;
+                    ctl.acc += 1;
+                }
+            }
+            if (lane == 0) { ctl.t = t; ctl.state2[it & 1] = state; }
+        } else if (pend) {
+            // factor column mm of the pending move, over columns [0, mm)
+            const CPipeMove pm = ctl.mv[slot];
+            const cf ipu = cinv(pm.piv_u), ipd = cinv(pm.piv_d);
+            const int tot = 2 * N + m.ld_up + m.ld_dn;
+            const int nt = blockDim.x - 32, id = tid - 32;
+            for (int e = id; e < tot; e += nt) {
+                if (e < N) SU.P[(size_t)e * K + mm] = cmul(SU.eff(e, pm.lu, mm), ipu);
+                else if (e < 2 * N) SD.P[(size_t)(e - N) * K + mm] = cmul(SD.eff(e - N, pm.ld, mm), ipd);
+                else if (e < 2 * N + m.ld_up) {
+                    const int c = e - 2 * N;
+                    cf v = SU.eff(pm.Ku, c, mm);
+                    if (c == pm.lu) v.x -= 1.f;
+                    SU.Q[(size_t)c * K + mm] = v;
+                } else {
+                    const int c = e - 2 * N - m.ld_up;
+                    cf v = SD.eff(pm.Kd, c, mm);
+                    if (c == pm.ld) v.x -= 1.f;
+                    SD.Q[(size_t)c * K + mm] = v;
+                }
+            }
+        }
+        __syncthreads();
+        const int state = ctl.state2[it & 1];
+        ++it;
+        const int mnew = pend ? mm + 1 : mm;
+        if (mnew == K) {
+            cdelayed_flush<K>(SU, N);
+            cdelayed_flush<K>(SD, N);
+            __syncthreads();
+            cdelayed_zero<K>(SU, N);
+            cdelayed_zero<K>(SD, N);
+            __syncthreads();
+        }
+        mm = mnew == K ? 0 : mnew;
+        if (state == 1) slot ^= 1;
+        pend = state == 1;
+        if (state == 3) {
+            float accE = 0.f;
+            for (int e = tid; e < m.n_bonds; e += blockDim.x) {
+                const short2 bd = bonds[e];
+                const int i = bd.x, j = bd.y;
+                const int ui = kup[i], uj = kup[j], di = kdn[i], dj = kdn[j];
+                accE += ((ui != 0) == (uj != 0)) ? 0.25f : -0.25f;
+                if (uj != 0 && di != 0) accE -= 0.5f * cmul(SU.eff(i, uj - 1, mm), SD.eff(j, di - 1, mm)).x;
+                if (ui != 0 && dj != 0) accE -= 0.5f * cmul(SU.eff(j, ui - 1, mm), SD.eff(i, dj - 1, mm)).x;
+            }
+            const double e = block_sum_f32(accE, ctl.red);
+            if (tid == 0) {
+                se += e;
+                se2 += e * e;
+                n_meas += 1;
+                ctl.next_meas += M;
+            }
+        }
+        __syncthreads();
+        if (state == 2) break;
+    }
+    if (mm > 0) {
+        // columns past mm are zero, so the full flush is exact
+        cdelayed_flush<K>(SU, N);
+        cdelayed_flush<K>(SD, N);
+        __syncthreads();
+    }
+    for (int s2 = tid; s2 < N; s2 += blockDim.x) {
+        b.kappa_up[(size_t)w * N + s2] = kup[s2];
+        b.kappa_dn[(size_t)w * N + s2] = kdn[s2];
+    }
+    if (tid == 0) {
+        const long long t = ctl.t;
+        b.t[w] = t;
+        b.since[w] = ctl.since >= R ? -1 : ctl.since;
+        b.accepted[w] += ctl.acc;
+        b.proposals[w] += t - t0;
+        b.sum_e[w] += se;
+        b.sum_e2[w] += se2;
+        b.n_meas[w] += n_meas;
+        if (t < tend_all && ctl.acc < acc_left) atomicAdd(active_count, 1);
+    }
+}
+
+static size_t complex_pipe_smem(const DevModel &m, int K) {
+    const size_t N = m.n_sites;
+    size_t s = (size_t)(2 * N + m.ld_up + m.ld_dn) * K * sizeof(cf);
+    s += (N + 1) * 4 + N * 4 + (size_t)m.n_bonds * 4 + (size_t)2 * m.n_bonds * 2 + 2 * N * 2;
+    return (s + 15) / 16 * 16 + 16;  // the threshold table starts 16-byte aligned after this
+}
+
+template <int K>
+static cudaError_t launch_c_pipe(const DevModel &m, const DevBatch &b, const SweepParams &p, int *active,
+                                 cudaStream_t stream) {
+    size_t sm = complex_pipe_smem(m, K);
+    const size_t thr_bytes = (size_t)(m.n_bonds + 1) * sizeof(ThrEntry);
+    const size_t kSmemPerSM = 228 * 1024, kReserve = 1024 + 2048;  // per-CTA reserve and static shared data
+    const int thr_in_smem = 2 * (sm + thr_bytes + kReserve) <= kSmemPerSM && sm + thr_bytes <= 227 * 1024;
+    if (thr_in_smem) sm += thr_bytes;
+    cudaError_t e = cudaFuncSetAttribute(sweep_c_pipe_kernel<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    if (e != cudaSuccess) return e;
+    sweep_c_pipe_kernel<K><<<b.n_walkers, 256, sm, stream>>>(m, b, p, active, thr_in_smem);
+    return cudaGetLastError();
+}
+
 size_t complex_delayed_smem(const DevModel &m, int K) {
     return (size_t)(2 * m.n_sites + m.ld_up + m.ld_dn) * K * sizeof(cf) + (size_t)2 * m.n_sites * 2 + 16;
 }
@@ -784,8 +1070,10 @@ static cudaError_t launch_c_delayed(const DevModel &m, const DevBatch &b, const 
 
 cudaError_t launch_sweep_c(const DevModel &m, const DevBatch &b, const SweepParams &p, bool mixed, int *active,
                            cudaStream_t stream) {
-    if (mixed && p.delay_k == 4) return launch_c_delayed<4>(m, b, p, active, stream);
-    if (mixed && p.delay_k == 8) return launch_c_delayed<8>(m, b, p, active, stream);
+    if (mixed && p.delay_k == 4)
+        return p.pipeline ? launch_c_pipe<4>(m, b, p, active, stream) : launch_c_delayed<4>(m, b, p, active, stream);
+    if (mixed && p.delay_k == 8)
+        return p.pipeline ? launch_c_pipe<8>(m, b, p, active, stream) : launch_c_delayed<8>(m, b, p, active, stream);
     if (mixed) {
         const size_t sm = sweep_c_smem<cf>(m);
         sweep_c_kernel<cf><<<b.n_walkers, 256, sm, stream>>>(m, b, p, 0, active);

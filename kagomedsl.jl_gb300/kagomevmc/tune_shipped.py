@@ -8,10 +8,12 @@ acceptance rule):
   N=96  x 4096           batched walkers
   N=54  x 1024, N=216 x 768, N=384 x 256   the classes of the uneven batch
   N=864 x 512            the large lattice (W in HBM)
+  N=192 x 2048, complex  the field workload (8x8 doubled cells, imbalance 4)
 """
 from __future__ import annotations
 
 import json
+import math
 import os
 import sys
 
@@ -30,12 +32,25 @@ def model(N):
     return Hamiltonian.build(N // 2, N // 2, DoubleKagome(1.0, 2 * a, b, (True, True), (False, True)))
 
 
+def field_model():
+    """8x8 doubled cells (N=192) in the field B = 4 pi / S of imbalance 4
+    (N_up = 98, N_down = 94): complex orbitals."""
+    from .lattice import Hmat, get_nn, orbitals
+
+    lat = DoubleKagome(1.0, 8, 8, (True, True), (False, True))
+    H = Hmat(lat, B=4 * math.pi / (64 * 2 * math.sqrt(3)))
+    Uu, Ud = orbitals(H, 98, 94)
+    return Hamiltonian(98, 94, Uu, Ud, H, get_nn(H))
+
+
 def main(argv=None):
     argv = sys.argv[1:] if argv is None else argv
     out = argv[0] if argv else autotune.SHIPPED
     cache = json.load(open(out)) if os.path.exists(out) else {}
-    for N, walkers, kw in WORKLOADS:
-        ham = model(N)
+    jobs = [(model(N), walkers, kw) for N, walkers, kw in WORKLOADS]
+    # complex W: delayed depths 4 and 8, W in HBM
+    jobs.append((field_model(), 2048, dict(delays=(4, 8), placements=("hbm",), threads=(256,))))
+    for ham, walkers, kw in jobs:
         key = autotune.cache_key(ham, walkers, "reference", autotune._device_name(0))
         ch = autotune.tune(ham, walkers, **kw)
         row = dict(delay_k=ch.delay_k, refresh_interval=ch.refresh_interval, placement=ch.placement,

@@ -82,7 +82,7 @@ def test_shipped_table_covers_the_bench_workloads(kv):
     table = json.load(open(autotune.SHIPPED))
     for key in ("N216_nu108_nd108_W2048_reference_r_GB300", "N96_nu48_nd48_W4096_reference_r_GB300",
                 "N54_nu27_nd27_W1024_reference_r_GB300", "N216_nu108_nd108_W768_reference_r_GB300",
-                "N384_nu192_nd192_W256_reference_r_GB300"):
+                "N384_nu192_nd192_W256_reference_r_GB300", "N192_nu98_nd94_W2048_reference_c_GB300"):
         row = table[key]
         assert row["placement"] in ("chip", "hbm") and row["delay_k"] in (1, 4, 8, 12, 16)
         assert row["refresh_interval"] > 0 and row["threads"] in (128, 256)

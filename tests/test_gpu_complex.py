@@ -95,9 +95,12 @@ def test_complex_ratios_and_local_energy(kv, precision):
     eng.close()
 
 
-@pytest.mark.parametrize("precision,delay_k", [("plain", 0), ("mixed", 1), ("mixed", 4), ("mixed", 8)])
+@pytest.mark.parametrize("precision,delay_k,pipeline", [("plain", 0, True), ("mixed", 1, True), ("mixed", 4, True),
+                                                     ("mixed", 8, True), ("mixed", 8, False)])
 @pytest.mark.parametrize("accept", ["reference", "metropolis"])
-def test_complex_chains_match_c_oracle(kv, precision, delay_k, accept):
+def test_complex_chains_match_c_oracle(kv, precision, delay_k, pipeline, accept):
+    """Delayed depths 4 and 8 run the pipelined complex kernel (scan overlapping
+    the factor-column write) unless the pipeline is switched off."""
     n1, n2, imbalance = 8, 4, 4
     ham = field_ham(kv, n1, n2, imbalance)
     walkers, proposals, seed = 10, 3000, 19
@@ -105,6 +108,7 @@ def test_complex_chains_match_c_oracle(kv, precision, delay_k, accept):
                     refresh_interval=(64 if precision == "mixed" else 0), delay_k=delay_k)
     if precision == "mixed":
         assert eng.config()["delay_k"] == delay_k
+        eng.set_pipeline(pipeline)
     eng.init()
     ku0, kd0, _ = eng.get_state()
     for w in range(walkers):   # the seeded starts are the oracle's
