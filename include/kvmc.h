@@ -264,11 +264,14 @@ KVMC_API int kvmc_reset_stats(kvmc_handle *h);
  * the walker was not refreshed).  drift: [n_walkers]. */
 KVMC_API int kvmc_walker_drift(kvmc_handle *h, float *drift);
 
-/* Mixed form with delayed updates: after every flush of the K pending moves
- * the rows of W at occupied sites, which are exact unit rows in exact
- * arithmetic, are compared with their exact values; a walker whose largest
- * deviation exceeds tol is refreshed in FP64 at once instead of waiting for
- * refresh_interval accepted moves.  Default 1e-4. */
+/* Mixed form with delayed updates: after a flush of the K pending moves
+ * (every fourth flush in the pipelined form) the rows of W at occupied
+ * sites, which are exact unit rows in exact arithmetic, are compared with
+ * their exact values; a walker whose largest deviation exceeds tol is
+ * refreshed before its refresh_interval accepted moves are up: at the end of
+ * the kvmc_advance call when the moves it still owes that call are fewer
+ * than refresh_interval (so refreshes stay on call boundaries), otherwise at
+ * once.  Default 1e-4. */
 KVMC_API int kvmc_set_drift_tolerance(kvmc_handle *h, double tol);
 
 /* Device-side timing of the kernels launched by kvmc_sweep, measured with
