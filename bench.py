@@ -231,8 +231,10 @@ def mixed_choice(kv, ham, a):
     return ch
 
 
-def energy_gate(ham, kv, walkers, proposals, choice, seed):
-    """Both forms on identical walkers and proposal streams: |dE/N| over walkers whose chains agree."""
+def energy_gate(ham, kv, walkers, calls, moves, choice, seed):
+    """Both forms on identical walkers and proposal streams, driven the way the
+    bench drives the mixed form (`calls` kvmc_advance calls of `moves`
+    accepted moves per walker): |dE/N| over walkers whose chains agree."""
     import numpy as np
 
     from kagomevmc import autotune
@@ -244,15 +246,18 @@ def energy_gate(ham, kv, walkers, proposals, choice, seed):
         else:
             eng = kv.Engine(ham, walkers, precision="plain", seed=seed)
         eng.init()
-        st = eng.sweep(proposals)
+        drift = 0.0
+        for _ in range(calls):
+            drift = max(drift, eng.advance(moves)["max_drift"])
         ws = eng.walker_stats()
-        res[prec] = (ws["sum_e"], ws["n_meas"], eng.get_state()[0], st["max_drift"])
+        res[prec] = (ws["sum_e"], ws["n_meas"], eng.get_state()[0], drift, ws["proposals"])
         eng.close()
-    (ep, np_, kp, _), (em, nm, km, drift) = res["plain"], res["mixed"]
+    (ep, np_, kp, _, pp), (em, nm, km, drift, pm) = res["plain"], res["mixed"]
     same = np.array([np.array_equal(kp[w], km[w]) for w in range(walkers)])
     dE = abs(ep[same].sum() / np_[same].sum() - em[same].sum() / nm[same].sum()) / N_SITES
-    return {"dE_per_site": float(dE), "walkers": walkers, "proposals_per_walker": proposals,
-            "identical_chains": int(same.sum()), "max_w_drift_at_refresh": float(drift), "pass": bool(dE <= 1e-4)}
+    return {"dE_per_site": float(dE), "walkers": walkers, "calls": calls, "accepted_moves_per_call": moves,
+            "proposals_per_walker": float(np.mean(pm)), "identical_chains": int(same.sum()),
+            "max_w_drift_at_refresh": float(drift), "pass": bool(dE <= 1e-4)}
 
 
 def adjoint_run(kv, seed, device, walkers=1024, sweeps=20):
@@ -532,8 +537,9 @@ def gpu_arm(a):
                  "moves_per_walker": 128, "accepted": ptot["accepted"]}
     # long enough for every walker to pass two of the mixed form's periodic refreshes
     # (acceptance ~0.127 at N=216)
-    gate_props = max(8192, int(2.2 * cfg["refresh_interval"] / 0.12))
-    gate = None if a.skip_gate else energy_gate(ham, kv, 256, gate_props, choice, a.seed + 1)
+    # two of the mixed form's refresh intervals, in calls of the bench's step size
+    gate_calls = max(8, -(-2 * cfg["refresh_interval"] // a.moves))
+    gate = None if a.skip_gate else energy_gate(ham, kv, 256, gate_calls, a.moves, choice, a.seed + 1)
     adjoint = None if a.skip_grad else adjoint_run(kv, 4, local)
     uneven = None if a.skip_uneven else uneven_run(kv, a.seed, local)
     large = None if a.skip_large else large_run(kv, a.seed, local)
