@@ -354,6 +354,38 @@ def test_advance_makes_exactly_the_asked_moves(kv, precision):
     eng.close()
 
 
+def test_drift_triggered_refresh_waits_for_the_end_of_the_call(kv):
+    """A drift tolerance every check exceeds: within a kvmc_advance call whose
+    moves fit in the refresh interval the walkers do not stop, each is
+    refreshed once at the end of the call, the move counts are exact and the
+    chains are still the oracle's."""
+    N, walkers, seed, A = 96, 8, 29, 200
+    ham = ham_for(kv, N)
+    eng = kv.Engine(ham, walkers, precision="mixed", seed=seed, refresh_interval=1024, delay_k=8, w_placement="hbm")
+    eng.set_drift_tolerance(1e-12)
+    eng.init()
+    ku0, kd0, _ = eng.get_state()
+    for call in range(3):
+        st = eng.advance(A)
+        assert st["accepted"] == walkers * A
+        # one refresh per walker (and an FP64 redo of a walker the FP32 refresh
+        # flags, should there be one); a refresh at the trigger would give one
+        # per checked flush, several per call
+        assert walkers <= st["refreshes"] <= walkers + walkers // 4, (call, st["refreshes"])
+    ku1, kd1, ct = eng.get_state()
+    ws = eng.walker_stats()
+    assert np.all(ws["accepted"] == 3 * A)
+    m = oracle_c.OracleModel(ham.U_up, ham.U_down, ham.nn)
+    match = 0
+    for w in range(walkers):
+        ch = m.new_chain(ku0[w], kd0[w])
+        ch.run(seed, w, int(ct[w]), N // 2, N // 2)
+        if np.array_equal(ch.ku, ku1[w]) and np.array_equal(ch.kd, kd1[w]):
+            match += 1
+    assert match >= walkers - 1
+    eng.close()
+
+
 @pytest.mark.parametrize("precision", ["plain", "mixed"])
 def test_advance_stops_a_walker_that_cannot_move(kv, precision):
     """Four sites, one bond (0, 1).  Walker 0 holds both up spins on the bond:
