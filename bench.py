@@ -255,8 +255,13 @@ def energy_gate(ham, kv, walkers, calls, moves, choice, seed):
     (ep, np_, kp, _, pp), (em, nm, km, drift, pm) = res["plain"], res["mixed"]
     same = np.array([np.array_equal(kp[w], km[w]) for w in range(walkers)])
     dE = abs(ep[same].sum() / np_[same].sum() - em[same].sum() / nm[same].sum()) / N_SITES
+    # all walkers: the difference of the two forms' per-walker means, with the
+    # standard error of that difference across walkers (chains share starts
+    # and streams, so the difference is paired)
+    d = (em / nm - ep / np_) / N_SITES
     return {"dE_per_site": float(dE), "walkers": walkers, "calls": calls, "accepted_moves_per_call": moves,
             "proposals_per_walker": float(np.mean(pm)), "identical_chains": int(same.sum()),
+            "dE_per_site_all_walkers": float(abs(d.mean())), "se_dE_all_walkers": float(d.std(ddof=1) / np.sqrt(walkers)),
             "max_w_drift_at_refresh": float(drift), "pass": bool(dE <= 1e-4)}
 
 
