@@ -54,6 +54,9 @@ def args_():
     p.add_argument("--skip-plain", action="store_true")
     p.add_argument("--skip-cpu", action="store_true")
     p.add_argument("--skip-gate", action="store_true")
+    p.add_argument("--gate-walkers", type=int, default=256, help="walkers of the energy gate")
+    p.add_argument("--gate-calls", type=int, default=None,
+                   help="advance calls of the energy gate (default: two refresh intervals, at least 8)")
     p.add_argument("--skip-e2e", action="store_true")
     p.add_argument("--no-peaks", action="store_true")
     p.add_argument("--skip-grad", action="store_true")
@@ -543,8 +546,8 @@ def gpu_arm(a):
     # long enough for every walker to pass two of the mixed form's periodic refreshes
     # (acceptance ~0.127 at N=216)
     # two of the mixed form's refresh intervals, in calls of the bench's step size
-    gate_calls = max(8, -(-2 * cfg["refresh_interval"] // a.moves))
-    gate = None if a.skip_gate else energy_gate(ham, kv, 256, gate_calls, a.moves, choice, a.seed + 1)
+    gate_calls = a.gate_calls or max(8, -(-2 * cfg["refresh_interval"] // a.moves))
+    gate = None if a.skip_gate else energy_gate(ham, kv, a.gate_walkers, gate_calls, a.moves, choice, a.seed + 1)
     adjoint = None if a.skip_grad else adjoint_run(kv, 4, local)
     uneven = None if a.skip_uneven else uneven_run(kv, a.seed, local)
     large = None if a.skip_large else large_run(kv, a.seed, local)
