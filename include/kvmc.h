@@ -270,8 +270,8 @@ KVMC_API int kvmc_walker_drift(kvmc_handle *h, float *drift);
  * their exact values; a walker whose largest deviation exceeds tol is
  * refreshed before its refresh_interval accepted moves are up: at the end of
  * the kvmc_advance call when the moves it still owes that call are fewer
- * than refresh_interval (so refreshes stay on call boundaries), otherwise at
- * once.  Default 1e-4. */
+ * than refresh_interval (so refreshes stay on call boundaries) and the
+ * deviation is below max(100 tol, 1e-2), otherwise at once.  Default 1e-4. */
 KVMC_API int kvmc_set_drift_tolerance(kvmc_handle *h, double tol);
 
 /* Device-side timing of the kernels launched by kvmc_sweep, measured with

@@ -1976,11 +1976,15 @@ sweep_pipe_kernel(DevModel m, DevBatch b, SweepParams p, int *active_count, int 
                 // this call still asks of the walker are fewer than an interval, at
                 // the end of the call (its counter then reaches R exactly with its
                 // last move, so refreshes stay on call boundaries and no walker stops
-                // mid-call), else now.  The other drift slot is free again
+                // mid-call), else now; a deviation past max(100 tolerances, 1e-2)
+                // (W losing its accuracy, as near a singular configuration)
+                // refreshes now in any case.  The other drift slot is free again
                 // (everybody read it a flush ago).
-                if (__int_as_float(*dev) > p.drift_tol) {
+                const float dv = __int_as_float(*dev);
+                if (dv > p.drift_tol) {
                     const long long rem = acc_left - ctl.acc;
-                    ctl.since = rem < R ? max(ctl.since, (int)(R - rem)) : R;
+                    const bool mild = dv <= fmaxf(100.f * p.drift_tol, 1e-2f);
+                    ctl.since = (rem < R && mild) ? max(ctl.since, (int)(R - rem)) : R;
                 }
                 ctl.dev2[(fp & 1) ^ 1] = 0;
             }
