@@ -86,3 +86,30 @@ def test_shipped_table_covers_the_bench_workloads(kv):
         row = table[key]
         assert row["placement"] in ("chip", "hbm") and row["delay_k"] in (1, 4, 8, 12, 16)
         assert row["refresh_interval"] > 0 and row["threads"] in (128, 256)
+
+
+def test_tuner_without_a_candidate_inside_the_bound(kv, monkeypatch):
+    """When every candidate drifts past the bound (as at N=864), the tuner
+    takes the most frequent refresh, and the fastest candidate at it."""
+    from kagomevmc import autotune, montecarlo
+
+    monkeypatch.setattr(montecarlo, "Engine", FakeEngine)
+    ham = kv.Hamiltonian(2, 2, np.eye(4)[:, :2], np.eye(4)[:, 2:], np.zeros((4, 4)), [(0, 1)])
+    ch = autotune.tune(ham, 64, drift_bound=1e-12)
+    assert all(r["max_drift"] > 1e-12 for r in ch.trials)
+    r_min = min(r["refresh_interval"] for r in ch.trials)
+    fastest = max((r for r in ch.trials if r["refresh_interval"] == r_min), key=lambda r: r["moves_per_s"])
+    assert ch.refresh_interval == r_min
+    assert (ch.delay_k, ch.placement, ch.threads) == (fastest["delay_k"], fastest["placement"], fastest["threads"])
+
+
+def test_field_workload_is_in_the_shipped_table(kv):
+    """The complex field workload the bench runs (8x8 doubled cells, imbalance
+    4) resolves to its row of the shipped table."""
+    from kagomevmc import autotune
+    from kagomevmc.tune_shipped import field_model
+
+    ham = field_model()
+    assert np.iscomplexobj(ham.U_up) and ham.U_up.shape == (192, 98) and ham.U_down.shape == (192, 94)
+    ch = autotune.lookup(ham, 2048)
+    assert ch is not None and ch.placement == "hbm" and ch.delay_k in (4, 8) and ch.refresh_interval > 0
