@@ -531,7 +531,7 @@ def gpu_arm(a):
             torch.distributed.destroy_process_group()
         return
 
-    # plain FP64 form on the same walkers (the spec denominator)
+    # plain FP64 form on the same walkers (the denominator of the headline speed-up)
     plain = None
     if not a.skip_plain:
         pe = kv.Engine(ham, a.walkers, precision="plain", seed=a.seed, device=local)

@@ -172,7 +172,7 @@ def test_correlated_finite_differences_agree_with_adjoint(kv, golden):
         e2.close()
 
 
-def test_config4_workload_forms_agree(kv):
+def test_differentiation_workload_forms_agree(kv):
     """N=96, parameters drawn from a seed, 256 chains: the mixed complex FP32
     form and the plain complex FP64 form give the same E and dE/da within
     their statistical errors on identical proposal streams."""
