@@ -313,33 +313,36 @@ KVMC_API int kvmc_get_config(kvmc_handle *h, int32_t *refresh_interval, int32_t 
  * the second call waits for the stream and returns the milliseconds. */
 KVMC_API int kvmc_region_timer(kvmc_handle *h, int32_t start, double *ms);
 
-/* Refresh that allocates nothing.  No counterpart in the reference: it is
- * the reevaluateW! computation (W = U * tilde_U^{-1} in FP64, one
- * configuration per batch item) for callers that cannot allocate device
- * memory -- code whose GPU memory is owned by another allocator (a Julia
- * CUDA.jl pool, a framework's caching allocator) or that must not trigger
- * cudaMalloc's device synchronisation inside its Monte Carlo loop.
+/* Refresh that allocates nothing.  No counterpart in the reference.  It
+ * computes W = U * tilde_U^{-1} in FP64, one configuration per batch item,
+ * for callers that cannot allocate device memory: code whose GPU memory is
+ * owned by another allocator (a Julia CUDA.jl pool, a framework's caching
+ * allocator) or that must not trigger cudaMalloc's device synchronisation
+ * inside its Monte Carlo loop.
  *
  * Inputs and outputs are the caller's device buffers:
  *   U       [n_sites][n_orb] FP64, row-major (row R = orbital amplitudes at site R)
  *   kappa   [batch][n_sites] int32, 0 or 1..n_orb, exactly n_orb nonzero
  *   W       [batch][n_sites][n_orb] FP64 out, row-major
- *   logdet  [batch] FP64 out (may be NULL): log|det tilde_U|, -inf when
- *           tilde_U is singular, NaN when kappa does not have n_orb
- *           occupied sites (W of that item is then left untouched)
+ *   logdet  [batch] FP64 out (may be NULL): log|det tilde_U|; -inf when
+ *           tilde_U is singular (a repeated or out-of-range label makes it
+ *           so), NaN when kappa does not have n_orb occupied sites.  In both
+ *           cases W of that item is left untouched.
  * The rows being solved use a fixed 8 MiB array inside the library, held by
  * every GPU that loads it until the process exits; a call needs
  * batch * n_orb * (n_sites - n_orb) * 8 <= 8 MiB (KVMC_ERR_ARGUMENT
  * otherwise) and n_orb <= 160 (KVMC_ERR_UNSUPPORTED).  No call allocates:
  * no cudaMalloc, cudaFree or allocating library routine.
- * The first call on a device resolves the array's device address and
- * sets the kernel's shared-memory limit; make that first call before any
- * stream capture.  The kernel is enqueued on `stream` (a cudaStream_t,
- * NULL for the legacy default stream) on the current device and the call
- * returns without waiting.  Every call shares the one array: calls that
- * overlap on the GPU (different streams, or the same buffers in flight)
- * race.  The array keeps the last call's contents; nothing in it needs to
- * start at zero, since every element a call reads it first writes. */
+ * A call outside stream capture resolves the array's device address and
+ * the kernel's shared-memory limit for the current device's context; a call
+ * under capture reuses what the last call outside capture on that device
+ * resolved, so make one call on each device before capturing.  The kernel
+ * is enqueued on `stream` (a cudaStream_t, NULL for the legacy default
+ * stream) on the current device and the call returns without waiting.
+ * Every call shares the one array, so calls that overlap on the GPU
+ * (different streams, or the same buffers in flight) race: the caller must
+ * serialise them.  The array keeps the last call's contents; nothing in it
+ * needs to start at zero, since every element a call reads it first writes. */
 KVMC_API int kvmc_refresh_static(int32_t n_sites, int32_t n_orb, int32_t batch, const double *U,
                                  const int32_t *kappa, double *W, double *logdet, void *stream);
 
@@ -397,6 +400,12 @@ KVMC_API int kvmc_walker_logdet(kvmc_handle *h, double *logdet);
 
 /* Library version / build facts: abi version, compiled arch (e.g. 1030). */
 KVMC_API int kvmc_version(int32_t *abi, int32_t *arch);
+
+/* Name of CUDA device `device` (NUL-terminated, truncated to len) and its
+ * SM count (sm_count may be NULL).  No reference counterpart: the tuning
+ * cache is keyed by the chip its settings were measured on.
+ * KVMC_ERR_NO_DEVICE when the device does not exist. */
+KVMC_API int kvmc_device_name(int32_t device, char *buf, size_t len, int32_t *sm_count);
 
 #ifdef __cplusplus
 }

@@ -519,6 +519,20 @@ extern "C" int kvmc_version(int32_t *abi, int32_t *arch) {
     return KVMC_OK;
 }
 
+extern "C" int kvmc_device_name(int32_t device, char *buf, size_t len, int32_t *sm_count) {
+    if (!buf || len == 0) return fail_global(KVMC_ERR_ARGUMENT, "kvmc_device_name: buf must hold at least one byte");
+    buf[0] = 0;
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || device < 0 || device >= n)
+        return fail_global(KVMC_ERR_NO_DEVICE, "kvmc_device_name: no CUDA device %d", device);
+    cudaDeviceProp prop;
+    if (cudaGetDeviceProperties(&prop, device) != cudaSuccess)
+        return fail_global(KVMC_ERR_CUDA, "kvmc_device_name: cudaGetDeviceProperties failed");
+    snprintf(buf, len, "%s", prop.name);
+    if (sm_count) *sm_count = prop.multiProcessorCount;
+    return KVMC_OK;
+}
+
 extern "C" int kvmc_last_error(const kvmc_handle *h, char *buf, size_t len) {
     if (!buf || len == 0) return KVMC_ERR_ARGUMENT;
     const std::string &s = h ? h->err : g_last_error;

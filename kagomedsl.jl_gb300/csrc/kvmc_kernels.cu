@@ -2373,20 +2373,29 @@ constexpr int kMaxDevices = 64;
 void *g_static_scratch_ptr[kMaxDevices] = {};
 std::mutex g_static_setup_mu;
 
-// Once per device, with that device current: the device address of the
-// static array (its host-side name is only a stand-in) and the kernel's
-// shared-memory opt-in.
-cudaError_t static_scratch_setup(int device, void **ptr) {
+// With the caller's device current: the device address of the static array
+// (its host-side name is only a stand-in) and the kernel's shared-memory
+// opt-in.  Both belong to the device's current context, so a call outside
+// stream capture resolves them again (cheap, and right after a device reset
+// or a new primary context); a call under capture, where the runtime must
+// not be asked for them, reuses what the last call outside capture on this
+// device resolved.
+cudaError_t static_scratch_setup(int device, cudaStream_t stream, void **ptr) {
     std::lock_guard<std::mutex> lock(g_static_setup_mu);
-    if (!g_static_scratch_ptr[device]) {
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    cudaError_t e = cudaStreamIsCapturing(stream, &cap);
+    if (e != cudaSuccess) return e;
+    if (cap == cudaStreamCaptureStatusNone) {
         void *p = nullptr;
-        cudaError_t e = cudaGetSymbolAddress(&p, g_static_solve_scratch);
+        e = cudaGetSymbolAddress(&p, g_static_solve_scratch);
         if (e != cudaSuccess) return e;
         // the kernel's own static shared variables count against the opt-in limit
         const int max_dyn = max_smem_optin(device) - 1024;
         e = cudaFuncSetAttribute(refresh_static_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, max_dyn);
         if (e != cudaSuccess) return e;
         g_static_scratch_ptr[device] = p;
+    } else if (!g_static_scratch_ptr[device]) {
+        return cudaErrorStreamCaptureUnsupported;  // never resolved outside capture on this device
     }
     *ptr = g_static_scratch_ptr[device];
     return cudaSuccess;
@@ -2407,7 +2416,7 @@ extern "C" KVMC_API int kvmc_refresh_static(int32_t n_sites, int32_t n_orb, int3
     int device = 0;
     if (cudaGetDevice(&device) != cudaSuccess || device < 0 || device >= kMaxDevices) return KVMC_ERR_NO_DEVICE;
     void *scratch = nullptr;
-    if (static_scratch_setup(device, &scratch) != cudaSuccess) return KVMC_ERR_CUDA;
+    if (static_scratch_setup(device, static_cast<cudaStream_t>(stream), &scratch) != cudaSuccess) return KVMC_ERR_CUDA;
     const size_t sm = (size_t)n_orb * (n_orb + 1) * 8 + (size_t)n_orb * 8 + 33 * 8 + (size_t)n_orb * 4 +
                       (size_t)n_sites * 2 + 16;
     if ((int)sm > max_smem_optin(device) - 1024) return KVMC_ERR_UNSUPPORTED;

@@ -113,6 +113,7 @@ _SIGS = {
     "kvmc_region_timer": [_P, C.c_int32, C.POINTER(C.c_double)],
     "kvmc_get_config": [_P, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(C.c_int32)],
     "kvmc_version": [C.POINTER(C.c_int32), C.POINTER(C.c_int32)],
+    "kvmc_device_name": [C.c_int32, C.c_char_p, C.c_size_t, C.POINTER(C.c_int32)],
     "kvmc_refresh_static": [C.c_int32, C.c_int32, C.c_int32, _P, _P, _P, _P, _P],
     "kvmc_ansatz_hopping": [C.POINTER(LatticeDesc), C.POINTER(Link), C.c_int32, C.POINTER(Link), C.c_int32,
                             C.c_double, _P, _P, _P],

@@ -13,8 +13,8 @@ side of the gradient estimator:
 * ``Ansatz`` -- the model bundle at one parameter point;
 * ``estimate`` -- dE/da and the stochastic-reconfiguration matrix from the
   per-walker sums that ``Engine.measure_grad`` accumulates on the GPU;
-* ``VMCEnergy`` -- the same estimate as a ``torch.autograd.Function``, the
-  counterpart of a ChainRulesCore ``rrule`` on the Julia side.
+  ``julia/KagomeVMCChainRules.jl`` wraps the same estimate as a
+  ChainRulesCore ``rrule`` on the Julia side.
 """
 from __future__ import annotations
 
@@ -156,34 +156,3 @@ def energy_and_gradient(engine, n_sweeps: int, proposals_per_sweep: int | None =
         engine.sweep(nps)
         engine.measure_grad()
     return estimate(engine.grad_sums(), engine.n_params)
-
-
-def _torch_function():
-    import torch
-
-    class VMCEnergy(torch.autograd.Function):
-        """E(alpha) with dE/dalpha from the adjoint estimator.
-
-        forward(alpha, run) -> E: ``run(alpha_numpy)`` must return the dict of
-        ``energy_and_gradient``; the gradient is stored and returned in
-        backward (grad_output * dE/dalpha), as an rrule's pullback would.
-        """
-
-        @staticmethod
-        def forward(ctx, alpha, run):
-            res = run(alpha.detach().cpu().numpy().astype(np.float64))
-            ctx.save_for_backward(torch.as_tensor(res["grad"], dtype=alpha.dtype))
-            return alpha.new_tensor(res["E"])
-
-        @staticmethod
-        def backward(ctx, g):
-            (grad,) = ctx.saved_tensors
-            return g * grad.to(g.device), None
-
-    return VMCEnergy
-
-
-def __getattr__(name):
-    if name == "VMCEnergy":
-        return _torch_function()
-    raise AttributeError(name)

@@ -22,6 +22,7 @@ this module holds the choices measured on a GB300 for the shipped workloads.
 """
 from __future__ import annotations
 
+import ctypes as C
 import json
 import os
 import time
@@ -56,12 +57,14 @@ class Choice:
 
 def _device_name(device: int) -> str:
     """The chip the choice was measured on ("GB300" for any GB300 board)."""
+    buf = C.create_string_buffer(256)
     try:
-        import torch
-
-        name = torch.cuda.get_device_name(device)
-    except Exception:
+        rc = _lib.load().kvmc_device_name(int(device), buf, len(buf), None)
+    except OSError:
         return "GB300"
+    if rc != _lib.KVMC_OK:
+        return "GB300"
+    name = buf.value.decode(errors="replace")
     return "GB300" if "GB300" in name else name
 
 

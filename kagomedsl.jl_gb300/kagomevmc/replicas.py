@@ -3,7 +3,10 @@
 Walker chains are independent, so N GPUs run N replicas of a batch with
 distinct seeds.  The only exchange is a final reduction of a few scalars
 per rank: the slowest rank's elapsed time and the summed counts / energy
-sums.  torch.distributed carries that reduction (NCCL on GPUs, gloo on CPU).
+sums.  The transport is the caller's: ``reduce_run`` takes an ``allreduce``
+callable (bench.py passes one over torch.distributed, NCCL on GPUs and gloo
+on CPU; a Julia host would pass MPI's), so this package needs no
+communication library.
 """
 from __future__ import annotations
 
@@ -21,21 +24,16 @@ def replica_seed(seed: int, rank: int) -> int:
     return (int(seed) + SEED_STRIDE * int(rank)) & 0xFFFFFFFFFFFFFFFF
 
 
-def reduce_run(elapsed_ms: float, sums: dict, device=None) -> tuple:
+def reduce_run(elapsed_ms: float, sums: dict, allreduce=None) -> tuple:
     """Max of elapsed_ms and sum of every entry of `sums` over all ranks.
 
-    Returns (elapsed_ms_max, sums_total).  With no process group (one
-    process) it returns its inputs.
+    allreduce(values, op) -> list of floats, op "max" or "sum", reduces a
+    list of floats over every rank; None (one process) returns the inputs.
+    Returns (elapsed_ms_max, sums_total).
     """
-    import torch
-    import torch.distributed as dist
-
-    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
-        return float(elapsed_ms), {k: float(v) for k, v in sums.items()}
     keys = sorted(sums)
-    dev = device if device is not None else "cpu"
-    t = torch.tensor([float(elapsed_ms)], dtype=torch.float64, device=dev)
-    s = torch.tensor([float(sums[k]) for k in keys], dtype=torch.float64, device=dev)
-    dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    dist.all_reduce(s, op=dist.ReduceOp.SUM)
-    return float(t[0]), {k: float(v) for k, v in zip(keys, s.tolist())}
+    if allreduce is None:
+        return float(elapsed_ms), {k: float(sums[k]) for k in keys}
+    t = allreduce([float(elapsed_ms)], "max")
+    s = allreduce([float(sums[k]) for k in keys], "sum")
+    return float(t[0]), {k: float(v) for k, v in zip(keys, s)}

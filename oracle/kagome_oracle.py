@@ -14,7 +14,7 @@ site and the 1-based orbital label otherwise (src/MonteCarlo.jl:92-115).
 
 Pinning: the functions here are checked against every literal value in the
 reference's own test-suite (test/test-Lattice.jl, test/test-Hamiltonian.jl,
-test/test-MonteCarlo.jl), restated as fixtures in ``tests/golden/reference_pins.json``.
+test/test-MonteCarlo.jl), restated with their literal values in ``tests/test_oracle_pins.py``.
 The Monte Carlo chain itself is parity-unpinned against the reference (its
 RNG stream belongs to the third-party Carlo.jl / StatsBase packages); the
 chain here draws from the Philox4x32-10 counter stream defined below, which

@@ -17,6 +17,12 @@ def _free_port():
     return p
 
 
+def _allreduce(values, op):
+    t = torch.tensor(values, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX if op == "max" else dist.ReduceOp.SUM)
+    return t.tolist()
+
+
 def _worker(rank, world, port, out):
     import sys
     sys.path.insert(0, os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "kagomedsl.jl_gb300"))
@@ -27,7 +33,7 @@ def _worker(rank, world, port, out):
     dist.init_process_group("gloo", rank=rank, world_size=world)
     first, count = replicas.shard(2049, rank, world)
     seed = replicas.replica_seed(7, rank)
-    ms, tot = replicas.reduce_run(10.0 + rank, {"accepted": 100 * (rank + 1), "walkers": count})
+    ms, tot = replicas.reduce_run(10.0 + rank, {"accepted": 100 * (rank + 1), "walkers": count}, _allreduce)
     out[rank] = (first, count, seed, ms, tot["accepted"], tot["walkers"])
     dist.destroy_process_group()
 

@@ -10,8 +10,10 @@ The test drives it through the C ABI.  It makes two calls in a row with
 different configurations, so the second call cannot pass on what the first
 left in the shared array.  Each call is checked against W from the existing
 entry point (kvmc_init with given configurations, then kvmc_get_w, plain FP64
-form) at the tolerance of the other FP64 parity tests: 1e-10 relative to
-max|W|.  This file sorts last so that a run stopping at its first failure has
+form) and against the oracle's reevaluateW, at the tolerance of the other
+FP64 parity tests: 1e-10 relative to max|W|.  Items whose configuration is
+singular or has the wrong number of occupied sites leave their W untouched.
+This file sorts last so that a run stopping at its first failure has
 already run every other test; it also passes on its own in a fresh process.
 """
 import ctypes as C
@@ -82,8 +84,45 @@ def test_static_refresh_matches_existing_entry_on_two_calls(kv, N):
         for w in range(batch):
             tol = 1e-10 * max(1.0, np.abs(want[w]).max())
             assert np.abs(got[w] - want[w]).max() <= tol, (call, w)
+            # and against the oracle's reevaluateW directly
+            exact = o.reevaluateW(ham.U_up, ku[w])
+            assert np.abs(got[w] - exact).max() <= 1e-10 * max(1.0, np.abs(exact).max()), (call, w)
             assert np.isfinite(logdet[w].item())
             assert logdet[w].item() == pytest.approx(o.logabsdet(ham.U_up, ku[w]), abs=1e-9)
+
+
+def test_static_refresh_leaves_bad_items_untouched(kv):
+    """One item with a repeated label (tilde_U then has a zero row: logdet
+    -inf) and one with a site too few occupied (logdet NaN) between two good
+    items: the bad items' W keep their NaN fill, the good ones match the
+    oracle's reevaluateW."""
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("needs a GPU")
+    ham = _ham(kv, 54)
+    N, n = ham.U_up.shape
+    lib = kv.load()
+    dev = torch.device("cuda", 0)
+    ku = np.stack([o.seeded_start(303, w, ham.U_up, ham.U_down)[0] for w in range(4)]).astype(np.int32)
+    occ = np.nonzero(ku[1])[0]
+    ku[1, occ[1]] = ku[1, occ[0]]            # label repeated, another label missing
+    ku[2, np.nonzero(ku[2])[0][0]] = 0        # n - 1 occupied sites
+    U = torch.tensor(np.ascontiguousarray(ham.U_up), dtype=torch.float64, device=dev)
+    kappa = torch.tensor(ku, dtype=torch.int32, device=dev)
+    W = torch.full((4, N, n), float("nan"), dtype=torch.float64, device=dev)
+    logdet = torch.zeros(4, dtype=torch.float64, device=dev)
+    torch.cuda.synchronize()
+    rc = lib.kvmc_refresh_static(N, n, 4, C.c_void_p(U.data_ptr()), C.c_void_p(kappa.data_ptr()),
+                                 C.c_void_p(W.data_ptr()), C.c_void_p(logdet.data_ptr()), None)
+    assert rc == 0
+    torch.cuda.synchronize()
+    got, ld = W.cpu().numpy(), logdet.cpu().numpy()
+    assert ld[1] == -np.inf and np.isnan(ld[2])
+    assert np.all(np.isnan(got[1])) and np.all(np.isnan(got[2]))
+    for w in (0, 3):
+        exact = o.reevaluateW(ham.U_up, ku[w])
+        assert np.abs(got[w] - exact).max() <= 1e-10 * max(1.0, np.abs(exact).max()), w
+        assert ld[w] == pytest.approx(o.logabsdet(ham.U_up, ku[w]), abs=1e-9)
 
 
 def test_static_refresh_rejects_batches_beyond_its_array(kv):
