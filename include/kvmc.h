@@ -298,9 +298,22 @@ KVMC_API int kvmc_kernel_time(kvmc_handle *h, int32_t kind, double *total_ms, in
  *   rebuilds W in kvmc_set_state and kvmc_init with given configurations
  *   (log|det| then from the FP32 factors); seeded starts and kvmc_refresh
  *   always use FP64.  The default is 1 for the mixed real form with at most
- *   128 orbitals per spin, else 0. */
+ *   128 orbitals per spin, else 0.
+ *   KVMC_TUNE_WARP_WALKERS: 0 = one CTA per walker (the kernels above);
+ *   1..14 = one warp per walker, this many walkers per CTA (mixed real form
+ *   with delay_k 4..16).  Each warp keeps only W's non-trivial rows -- the
+ *   rows at the sites of the other spin, indexed by that spin's label --
+ *   so a flush touches half of W; the handle then holds an extra
+ *   n_walkers * 2 * n_up * n_down floats for them.
+ *   KVMC_TUNE_COND_HI, KVMC_TUNE_COND_LO: the one-warp sweep's accuracy
+ *   guard.  FP32 W loses accuracy while it carries large entries (near a
+ *   node of the wave function) and shows it once they shrink again: a walker
+ *   whose largest |W| entry read by its moves has exceeded COND_HI since its
+ *   last refresh is refreshed at once when a move's entries are all below
+ *   COND_LO.  0 turns the guard off (the default). */
 enum kvmc_tuning { KVMC_TUNE_STREAM_THREADS = 1, KVMC_TUNE_PIPELINE = 2, KVMC_TUNE_TC_FLUSH = 3,
-                   KVMC_TUNE_REFRESH32 = 4 };
+                   KVMC_TUNE_REFRESH32 = 4, KVMC_TUNE_WARP_WALKERS = 5, KVMC_TUNE_COND_HI = 6,
+                   KVMC_TUNE_COND_LO = 7 };
 KVMC_API int kvmc_set_tuning(kvmc_handle *h, int32_t key, int32_t value);
 
 /* The settings a handle resolved at creation: refresh and measurement

@@ -55,6 +55,8 @@ struct kvmc_handle {
     int pipeline = 1;          // delayed form: pipelined scan / factor-column write
     int tc_flush = 0;          // W in HBM: rank-k flush on the tensor cores
     int refresh32 = 0;         // mixed real form: periodic refresh by FP32 iterative refinement (default <= 128 orbitals)
+    int warp_walkers = 0;      // mixed real form: > 0 = one warp per walker, walkers per CTA
+    float cond_hi = 0.f, cond_lo = 0.f;  // the warp sweep's accuracy guard (0 = off)
     std::string err;
 
     DevModel dm{};
@@ -195,6 +197,8 @@ int full_refresh(kvmc_handle *h, bool track_drift, bool allow32 = true) {
         KV_TRY(h->cuda(refresh_launch(h, 0, track_drift ? 1 : 0), "refresh launch"));
     }
     KV_TRY(h->cuda(cudaMemsetAsync(h->db.since, 0, sizeof(int) * h->n_walkers, h->stream), "memset"));
+    if (h->db.cond_max)
+        KV_TRY(h->cuda(cudaMemsetAsync(h->db.cond_max, 0, sizeof(float) * h->n_walkers, h->stream), "memset"));
     return h->cuda(cudaStreamSynchronize(h->stream), "refresh");
 }
 
@@ -738,6 +742,11 @@ extern "C" int kvmc_create(const kvmc_model_desc *model, const kvmc_batch_desc *
     if ((rc = h->alloc(&b.solve_scratch, b.solve_block * 2 * (size_t)Wk))) return bail(rc);
     b.lu_block = 0;
     b.lu_scratch = nullptr;
+    b.G32 = nullptr;
+    b.g_block = 0;
+    b.cond_max = nullptr;
+    if (h->mixed && (rc = h->alloc(&b.cond_max, Wk))) return bail(rc);
+    if (b.cond_max) cudaMemset(b.cond_max, 0, Wk * sizeof(float));
     if (!h->cplx && kvmc::refresh_needs_large(m)) {
         const size_t nmax = (size_t)std::max(nu, nd);
         b.lu_block = nmax * nmax;
@@ -989,6 +998,9 @@ kvmc::SweepParams sweep_params(const kvmc_handle *h) {
     p.pipeline = h->pipeline;
     p.tc_flush = h->tc_flush;
     p.refresh32 = h->refresh32;
+    p.warp_walkers = h->warp_walkers;
+    p.cond_hi = h->cond_hi;
+    p.cond_lo = h->cond_lo;
     return p;
 }
 
@@ -1442,6 +1454,31 @@ extern "C" int kvmc_set_tuning(kvmc_handle *h, int32_t key, int32_t value) {
                 return h->fail(KVMC_ERR_UNSUPPORTED, "the tensor-core flush needs %zu B shared memory", need);
         }
         h->tc_flush = value;
+        return KVMC_OK;
+    }
+    if (key == KVMC_TUNE_WARP_WALKERS) {
+        if (value < 0 || value > 14) return h->fail(KVMC_ERR_ARGUMENT, "walkers per CTA must be 0..14");
+        if (value > 0) {
+            if (!h->mixed || h->cplx || h->delay_k < 4)
+                return h->fail(KVMC_ERR_UNSUPPORTED,
+                               "one warp per walker serves the mixed real form with delayed updates (delay_k 4..16)");
+            const size_t need = kvmc::warp_cta_smem(h->dm) + (size_t)value * kvmc::warp_walker_smem(h->dm, h->delay_k);
+            if (need + 1024 > (size_t)kvmc::max_smem_optin(h->device))
+                return h->fail(KVMC_ERR_UNSUPPORTED, "%d walkers per CTA need %zu B shared memory (at most %d walkers)",
+                               value, need,
+                               kvmc::warp_walkers_max(h->dm, h->delay_k, kvmc::max_smem_optin(h->device) - 1024));
+            if (!h->db.G32) {
+                KV_TRY(set_device(h));
+                h->db.g_block = kvmc::warp_compact_block(h->dm);
+                KV_TRY(h->alloc(&h->db.G32, h->db.g_block * (size_t)h->n_walkers));
+            }
+        }
+        h->warp_walkers = value;
+        return KVMC_OK;
+    }
+    if (key == KVMC_TUNE_COND_HI || key == KVMC_TUNE_COND_LO) {
+        if (value < 0) return h->fail(KVMC_ERR_ARGUMENT, "accuracy guard thresholds must be >= 0");
+        (key == KVMC_TUNE_COND_HI ? h->cond_hi : h->cond_lo) = (float)value;
         return KVMC_OK;
     }
     if (key == KVMC_TUNE_PIPELINE) {

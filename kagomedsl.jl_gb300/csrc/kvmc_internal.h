@@ -59,6 +59,11 @@ struct DevBatch {
     size_t solve_block;    // doubles per (walker, spin)
     double *lu_scratch;    // more than 160 orbitals: tilde_U factorised in HBM, [W][2][lu_block]
     size_t lu_block;       // doubles per (walker, spin), 0 when unused
+    // one-warp-per-walker sweep (kvmc_warp.cu): W's non-trivial rows indexed by
+    // the other spin's label, [W][g_block] (null until that sweep is enabled)
+    float *G32;
+    size_t g_block;        // floats per walker: n_dn * ld_up + n_up * ld_dn
+    float *cond_max;       // [W] largest |W| entry the warp sweep saw since the walker's last refresh
 };
 
 enum : int {
@@ -88,6 +93,8 @@ struct SweepParams {
     int pipeline;         // delayed form: scan for the next move while the last one's factor column is written
     int tc_flush;         // W in HBM: rank-k flush on the tensor cores (tcgen05, 3xTF32)
     int refresh32;        // mixed real form: FP32 refresh by iterative refinement
+    int warp_walkers;     // mixed real form: > 0 = one warp per walker, this many walkers per CTA (kvmc_warp.cu)
+    float cond_hi, cond_lo;  // warp sweep's accuracy guard (0 = off), see kvmc_warp.cu
 };
 
 // Launchers.  All enqueue on `stream` and return the launch error.
@@ -129,6 +136,14 @@ cudaError_t launch_refresh32_large(const DevModel &m, const DevBatch &b, int onl
                                    cudaStream_t stream);
 size_t refresh_large_smem(const DevModel &m, size_t lt_bytes);
 cudaError_t launch_clear_status(const DevBatch &b, int bits, cudaStream_t stream);
+
+// One warp per walker with W's non-trivial rows indexed by labels (kvmc_warp.cu).
+size_t warp_cta_smem(const DevModel &m);
+size_t warp_walker_smem(const DevModel &m, int K);
+size_t warp_compact_block(const DevModel &m);
+int warp_walkers_max(const DevModel &m, int K, int optin);
+cudaError_t launch_sweep_warp(const DevModel &m, const DevBatch &b, const SweepParams &p, int *active,
+                              cudaStream_t stream);
 
 // Extra shared memory of the tensor-core flush (its operand tiles).
 size_t tc_flush_smem_bytes();

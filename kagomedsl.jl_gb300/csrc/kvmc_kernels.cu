@@ -2271,6 +2271,7 @@ static cudaError_t launch_delayed(const DevModel &m, const DevBatch &b, const Sw
 cudaError_t launch_sweep(const DevModel &m, const DevBatch &b, const SweepParams &p, bool mixed,
                          bool smem_w, int *active, cudaStream_t stream) {
     if (!mixed) return launch_sweep_impl<double, false>(m, b, p, 1, active, 256, stream);
+    if (p.warp_walkers > 0) return launch_sweep_warp(m, b, p, active, stream);
     if (smem_w && p.delay_k == 4) return launch_delayed<4, false>(m, b, p, active, stream);
     if (smem_w && p.delay_k == 8) return launch_delayed<8, false>(m, b, p, active, stream);
     if (smem_w && p.delay_k == 12) return launch_delayed<12, false>(m, b, p, active, stream);

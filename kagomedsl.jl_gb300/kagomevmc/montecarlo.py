@@ -205,6 +205,17 @@ class Engine:
         """W in HBM: threads per walker's CTA (128 or 256)."""
         self._check(self._lib.kvmc_set_tuning(self.h, 1, int(threads)))
 
+    def set_warp_walkers(self, walkers_per_cta: int):
+        """0 = one CTA per walker; 1..14 = one warp per walker, this many per CTA
+        (W's non-trivial rows indexed by labels; mixed real form, delay_k >= 4)."""
+        self._check(self._lib.kvmc_set_tuning(self.h, 5, int(walkers_per_cta)))
+
+    def set_accuracy_guard(self, hi: int, lo: int):
+        """One-warp sweep: refresh a walker at once when its moves' |W| entries,
+        after exceeding `hi` since its last refresh, are all below `lo` (0 = off)."""
+        self._check(self._lib.kvmc_set_tuning(self.h, 6, int(hi)))
+        self._check(self._lib.kvmc_set_tuning(self.h, 7, int(lo)))
+
     def set_drift_tolerance(self, tol: float):
         self._check(self._lib.kvmc_set_drift_tolerance(self.h, float(tol)))
 
