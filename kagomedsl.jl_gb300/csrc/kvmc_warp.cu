@@ -26,12 +26,10 @@
 // K = 8), so a CTA holds up to 14 walkers, one per warp.  Each warp runs its
 // own serial chain; the SM's other warps fill its latency.  G lives in
 // HBM/L2 (a launch converts the site-indexed W of the handle into G at its
-// start and back at its end).  Within the chain, the latency of global
-// memory is overlapped with other work: the G words of a move's factor
-// columns are loaded before the move is applied to the configuration, the
-// next window's proposals are drawn and their G words loaded before the
-// factor columns are computed, and both G blocks are asked into L2 two
-// moves before a flush.
+// start and back at its end).  The G blocks of the walkers in flight should
+// fit in L2 (7 walkers per SM at N = 216: 99 MB): with more walkers in
+// flight the flushes stream from HBM and each chain slows down more than
+// the extra walkers gain.
 //
 // Accuracy guard: FP32 loses accuracy while W carries large entries (a
 // configuration close to a node of the wave function): rounding at the scale
@@ -76,116 +74,43 @@ struct CSpin {
     __device__ __forceinline__ float eff(int r, int c) const { return G[(size_t)r * ldg + c] - pq(r, c); }
 };
 
-// The factor columns of an accepted move, both spins.  For one spin, with
-// s = the other spin's label whose row is replaced and l = the own label that
-// moves (up: s = b, l = a; down: s = a, l = b):
+// The factor columns of an accepted move for one spin.  s = the other
+// spin's label whose row is replaced, l = the own label that moves (up:
+// s = b, l = a; down: s = a, l = b):
 //   P[r][m] = (G_eff[r][l] + [r == s]) / piv,   Q[c][m] = G_eff[s][c] - [c == l]
-// Entries e of [0, e4): up column, up row, down column, down row.  The G
-// words of up to kCW entries per lane are loaded first (cw_load) and used
-// after the move has been applied to the configuration (cw_compute), so
-// that their latency overlaps that work.  The four entries that read
-// P[s][m] / Q[l][m] themselves (r == s, c == l) are written by the caller
-// after a __syncwarp, so that every dot here sees column m still zero.
-constexpr int kCW = 14;
-
+// The two entries that read P[s][m] / Q[l][m] themselves (r == s, c == l)
+// are written by the caller after a __syncwarp, so that every dot here sees
+// column m still zero.  Four loads per lane are issued before the
+// arithmetic.  Returns the largest |G_eff| entry the lane read.
 template <int K>
-__device__ __forceinline__ void cw_load(const CSpin<K> &SU, const CSpin<K> &SD, int a, int bl, int base, int lane,
-                                        float (&wv)[kCW]) {
-    const int e1 = SU.n_oth, e2 = e1 + SU.n_own, e3 = e2 + SD.n_oth, e4 = e3 + SD.n_own;
-#pragma unroll
-    for (int q = 0; q < kCW; ++q) {
-        const int e = base + 32 * q + lane;
-        float v = 0.f;
-        if (e < e1) v = SU.G[(size_t)e * SU.ldg + a];
-        else if (e < e2) v = SU.G[(size_t)bl * SU.ldg + (e - e1)];
-        else if (e < e3) v = SD.G[(size_t)(e - e2) * SD.ldg + bl];
-        else if (e < e4) v = SD.G[(size_t)a * SD.ldg + (e - e3)];
-        wv[q] = v;
-    }
-}
-
-// Returns the largest |G_eff| entry the lane computed.
-template <int K>
-__device__ __forceinline__ float cw_compute(const CSpin<K> &SU, const CSpin<K> &SD, int a, int bl, int m, float ipu,
-                                           float ipd, int base, int lane, const float (&wv)[kCW]) {
-    const int e1 = SU.n_oth, e2 = e1 + SU.n_own, e3 = e2 + SD.n_oth, e4 = e3 + SD.n_own;
+__device__ __forceinline__ float column_write(const CSpin<K> &S, int s, int l, int m, float ipiv, int lane) {
+    const int tot = S.n_oth + S.n_own;
     float mx = 0.f;
+    for (int base = 0; base < tot; base += 128) {
+        float wv[4];
 #pragma unroll
-    for (int q = 0; q < kCW; ++q) {
-        const int e = base + 32 * q + lane;
-        if (e < e1) {
-            const float v = wv[q] - SU.pq(e, a);
-            mx = fmaxf(mx, fabsf(v));
-            if (e != bl) SU.P[(size_t)e * K + m] = v * ipu;
-        } else if (e < e2) {
-            const int c = e - e1;
-            const float v = wv[q] - SU.pq(bl, c);
-            mx = fmaxf(mx, fabsf(v));
-            if (c != a) SU.Q[(size_t)c * K + m] = v;
-        } else if (e < e3) {
-            const int r = e - e2;
-            const float v = wv[q] - SD.pq(r, bl);
-            mx = fmaxf(mx, fabsf(v));
-            if (r != a) SD.P[(size_t)r * K + m] = v * ipd;
-        } else if (e < e4) {
-            const int c = e - e3;
-            const float v = wv[q] - SD.pq(a, c);
-            mx = fmaxf(mx, fabsf(v));
-            if (c != bl) SD.Q[(size_t)c * K + m] = v;
+        for (int q = 0; q < 4; ++q) {
+            const int e = base + 32 * q + lane;
+            wv[q] = 0.f;
+            if (e < S.n_oth) wv[q] = S.G[(size_t)e * S.ldg + l];
+            else if (e < tot) wv[q] = S.G[(size_t)s * S.ldg + (e - S.n_oth)];
         }
-    }
-    return mx;
-}
-
-// One lane's proposal of a window: drawn (Philox), located on the current
-// configuration and, when it needs a ratio, its two G words loaded.
-struct Proposal {
-    unsigned long long u53;
-    int c;          // sign(r - thr) for the reference rule
-    int a, bl;      // up label and down label that would move
-    int Ku, Kd;     // sites the up and the down spin would move to
-    float gu, gd;   // G_up[bl][a], G_dn[a][bl] before the pending factors
-    bool valid;     // the bond joins opposite spins
-};
-
-template <int K>
-__device__ __forceinline__ bool needs_ratio(const Proposal &pr, int rule) {
-    return pr.valid && (rule != 0 || pr.c <= 0);
-}
-
-template <int K>
-__device__ __forceinline__ void prep_proposal(Proposal &pr, unsigned long long seed, int w, long long tw, int win,
-                                              int nb, const short2 *bonds, const short *lab, const Thr &thr, int rule,
-                                              const CSpin<K> &SU, const CSpin<K> &SD, int lane) {
-    pr.valid = false;
-    pr.c = 1;
-    pr.a = pr.bl = pr.Ku = pr.Kd = 0;
-    pr.gu = pr.gd = 0.f;
-    if (lane < win) {
-        int bi;
-        proposal_bits(seed, w, tw + lane, nb, pr.u53, bi);
-        pr.c = cmp_r_thr(pr.u53, thr);
-        const short2 bd = bonds[bi];
-        const int li = lab[bd.x], lj = lab[bd.y];
-        if ((li > 0) != (lj > 0)) {
-            pr.valid = true;
-            // the up spin at the up site moves to the down site (Ku), the down spin the other way (Kd)
-            if (li > 0) { pr.a = li - 1; pr.bl = -lj - 1; pr.Ku = bd.y; pr.Kd = bd.x; }
-            else        { pr.a = lj - 1; pr.bl = -li - 1; pr.Ku = bd.x; pr.Kd = bd.y; }
-            if (needs_ratio<K>(pr, rule)) {
-                pr.gu = SU.G[(size_t)pr.bl * SU.ldg + pr.a];
-                pr.gd = SD.G[(size_t)pr.a * SD.ldg + pr.bl];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const int e = base + 32 * q + lane;
+            if (e < S.n_oth) {
+                const float v = wv[q] - S.pq(e, l);
+                mx = fmaxf(mx, fabsf(v));
+                if (e != s) S.P[(size_t)e * K + m] = v * ipiv;
+            } else if (e < tot) {
+                const int c = e - S.n_oth;
+                const float v = wv[q] - S.pq(s, c);
+                mx = fmaxf(mx, fabsf(v));
+                if (c != l) S.Q[(size_t)c * K + m] = v;
             }
         }
     }
-}
-
-// Asks the copy engine to bring a spin's G block into L2 (one instruction,
-// no completion to wait for): the flush then reads its rows at L2 latency.
-template <int K>
-__device__ __forceinline__ void prefetch_l2(const CSpin<K> &S) {
-    const unsigned bytes = (unsigned)((size_t)S.n_oth * S.ldg * sizeof(float));  // a multiple of 16
-    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(S.G), "r"(bytes) : "memory");
+    return mx;
 }
 
 // G -= P Q^T.  Lane = a group of four columns (Q of those columns held in
@@ -384,9 +309,6 @@ sweep_warp_kernel(DevModel m, DevBatch b, SweepParams p, int *active_count, size
     int mm = 0;
     bool bad_walker = false;
 
-    Proposal pr;
-    long long prep_t = -1;
-    int prep_win = -1;
     while (true) {
         if (t == next_meas) {
             // local energy (getOL): SzSz over the bonds, -1/2 ratio per antiparallel bond
@@ -410,20 +332,29 @@ sweep_warp_kernel(DevModel m, DevBatch b, SweepParams p, int *active_count, size
             next_meas += M;
             continue;
         }
-        if (t >= tend || since >= R || acc >= acc_left) break;
+        if (t >= tend || since >= R || acc >= acc_left || bad_walker) break;
         const long long lim = min(tend, next_meas) - t;
         const int win = lim < 32 ? (int)lim : 32;
-        if (prep_t != t || prep_win != win) {
-            prep_proposal<K>(pr, p.seed, w, t, win, nb, bonds, lab, thr, p.accept_rule, SU, SD, lane);
-            prep_t = t;
-            prep_win = win;
-        }
         bool accd = false, bad = false;
+        int a = 0, bl = 0, Ku = 0, Kd = 0;
         float pu = 0.f, pd = 0.f;
-        if (needs_ratio<K>(pr, p.accept_rule)) {
-            pu = pr.gu - SU.pq(pr.bl, pr.a);
-            pd = pr.gd - SD.pq(pr.a, pr.bl);
-            accd = decide(pu, pd, pr.u53, pr.c, thr, p.accept_rule, bad);
+        if (lane < win) {
+            unsigned long long u53;
+            int bi;
+            proposal_bits(p.seed, w, t + lane, nb, u53, bi);
+            const int c = cmp_r_thr(u53, thr);
+            if (p.accept_rule != 0 || c <= 0) {
+                const short2 bd = bonds[bi];
+                const int li = lab[bd.x], lj = lab[bd.y];
+                if ((li > 0) != (lj > 0)) {
+                    // the up spin at the up site moves to the down site (Ku), the down spin the other way (Kd)
+                    if (li > 0) { a = li - 1; bl = -lj - 1; Ku = bd.y; Kd = bd.x; }
+                    else        { a = lj - 1; bl = -li - 1; Ku = bd.x; Kd = bd.y; }
+                    pu = SU.eff(bl, a);
+                    pd = SD.eff(a, bl);
+                    accd = decide(pu, pd, u53, c, thr, p.accept_rule, bad);
+                }
+            }
         }
         if (__any_sync(0xffffffffu, bad)) {
             // a non-finite ratio: the walker stops here and the call reports it
@@ -437,23 +368,27 @@ sweep_warp_kernel(DevModel m, DevBatch b, SweepParams p, int *active_count, size
             continue;
         }
         const int f = __ffs(mask) - 1;
-        const int a = __shfl_sync(0xffffffffu, pr.a, f);
-        const int bl = __shfl_sync(0xffffffffu, pr.bl, f);
-        const int Ku = __shfl_sync(0xffffffffu, pr.Ku, f);
-        const int Kd = __shfl_sync(0xffffffffu, pr.Kd, f);
+        a = __shfl_sync(0xffffffffu, a, f);
+        bl = __shfl_sync(0xffffffffu, bl, f);
+        Ku = __shfl_sync(0xffffffffu, Ku, f);
+        Kd = __shfl_sync(0xffffffffu, Kd, f);
         pu = __shfl_sync(0xffffffffu, pu, f);
         pd = __shfl_sync(0xffffffffu, pd, f);
         t += f + 1;
-        // 1. the G words of the factor columns (G does not change before the flush)
-        float wv[kCW];
-        cw_load<K>(SU, SD, a, bl, 0, lane, wv);
-        // 2. the move on the configuration: the Z_mu change from the
-        // up-neighbour counts (before the move), labels, counts, threshold
+        // factor columns mm of both spins (from the configuration before the move)
+        const float ipu = 1.f / pu, ipd = 1.f / pd;
+        float mx = column_write<K>(SU, bl, a, mm, ipu, lane);
+        mx = fmaxf(mx, column_write<K>(SD, a, bl, mm, ipd, lane));
+        // Z_mu change from the up-neighbour counts (configuration before the move)
         const int bu = nbr_off[Ku], du = nbr_off[Ku + 1] - bu;
         const int bd0 = nbr_off[Kd], dd = nbr_off[Kd + 1] - bd0;
         const int dz = du - dd + 2 - 2 * nup[Ku] + 2 * nup[Kd];
-        __syncwarp();  // every count read is done
+        __syncwarp();  // every dot of the column write and every count read is done
         if (lane == 0) {
+            SU.P[(size_t)bl * K + mm] = (pu + 1.f) * ipu;
+            SU.Q[(size_t)a * K + mm] = pu - 1.f;
+            SD.P[(size_t)a * K + mm] = (pd + 1.f) * ipd;
+            SD.Q[(size_t)bl * K + mm] = pd - 1.f;
             lab[Ku] = (short)(a + 1);
             lab[Kd] = (short)(-(bl + 1));
         }
@@ -463,36 +398,11 @@ sweep_warp_kernel(DevModel m, DevBatch b, SweepParams p, int *active_count, size
         make_thr(thr, m.thr_table, zmu, p.accept_rule);
         since += 1;
         acc += 1;
-        __syncwarp();  // the new labels are visible
-        // 3. the next window's proposals on the new configuration
-        {
-            const long long lim2 = min(tend, next_meas) - t;
-            prep_win = lim2 < 32 ? (int)max(lim2, 0ll) : 32;
-            prep_t = t;
-            prep_proposal<K>(pr, p.seed, w, t, prep_win, nb, bonds, lab, thr, p.accept_rule, SU, SD, lane);
-        }
-        // 4. the factor columns
-        const float ipu = 1.f / pu, ipd = 1.f / pd;
-        float mx = cw_compute<K>(SU, SD, a, bl, mm, ipu, ipd, 0, lane, wv);
-        const int e4 = 2 * (SU.n_oth + SU.n_own);
-        for (int base = 32 * kCW; base < e4; base += 32 * kCW) {
-            cw_load<K>(SU, SD, a, bl, base, lane, wv);
-            mx = fmaxf(mx, cw_compute<K>(SU, SD, a, bl, mm, ipu, ipd, base, lane, wv));
-        }
-        __syncwarp();  // every dot of the column write is done
-        if (lane == 0) {
-            SU.P[(size_t)bl * K + mm] = (pu + 1.f) * ipu;
-            SU.Q[(size_t)a * K + mm] = pu - 1.f;
-            SD.P[(size_t)a * K + mm] = (pd + 1.f) * ipd;
-            SD.Q[(size_t)bl * K + mm] = pd - 1.f;
-        }
         mm += 1;
         // accuracy guard
         mx = warp_max_nonneg(mx);
         cmax = fmaxf(cmax, mx);
         if (p.cond_hi > 0.f && cmax > p.cond_hi && mx < p.cond_lo) since = max(since, R);
-        // two moves before the flush: both G blocks into L2
-        if (mm == K - 2 && lane == 0) { prefetch_l2<K>(SU); prefetch_l2<K>(SD); }
         __syncwarp();
         if (mm == K) {
             warp_flush<K>(SU, lane);
@@ -502,11 +412,6 @@ sweep_warp_kernel(DevModel m, DevBatch b, SweepParams p, int *active_count, size
             zero_factors<K>(SD, lane);
             __syncwarp();
             mm = 0;
-            // the next window's G words changed with the flush
-            if (needs_ratio<K>(pr, p.accept_rule)) {
-                pr.gu = SU.G[(size_t)pr.bl * SU.ldg + pr.a];
-                pr.gd = SD.G[(size_t)pr.a * SD.ldg + pr.bl];
-            }
         }
     }
     if (mm > 0) {
