@@ -309,11 +309,16 @@ KVMC_API int kvmc_kernel_time(kvmc_handle *h, int32_t kind, double *total_ms, in
  *   guard.  FP32 W loses accuracy while it carries large entries (near a
  *   node of the wave function) and shows it once they shrink again: a walker
  *   whose largest |W| entry read by its moves has exceeded COND_HI since its
- *   last refresh is refreshed at once when a move's entries are all below
- *   COND_LO.  0 turns the guard off (the default). */
+ *   last refresh is refreshed when a move's entries are all below COND_LO --
+ *   at the end of the kvmc_advance call (or of its segment) when the moves it
+ *   still owes are fewer than refresh_interval, else at once.  0 turns the
+ *   guard off (the default).
+ *   KVMC_TUNE_SEGMENT: one-warp mode: kvmc_advance runs its moves in
+ *   segments of this many accepted moves per walker, so a refresh the guard
+ *   asks for waits at most one segment; 0 = the whole call (the default). */
 enum kvmc_tuning { KVMC_TUNE_STREAM_THREADS = 1, KVMC_TUNE_PIPELINE = 2, KVMC_TUNE_TC_FLUSH = 3,
                    KVMC_TUNE_REFRESH32 = 4, KVMC_TUNE_WARP_WALKERS = 5, KVMC_TUNE_COND_HI = 6,
-                   KVMC_TUNE_COND_LO = 7 };
+                   KVMC_TUNE_COND_LO = 7, KVMC_TUNE_SEGMENT = 8 };
 KVMC_API int kvmc_set_tuning(kvmc_handle *h, int32_t key, int32_t value);
 
 /* The settings a handle resolved at creation: refresh and measurement

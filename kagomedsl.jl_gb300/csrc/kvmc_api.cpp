@@ -57,6 +57,7 @@ struct kvmc_handle {
     int refresh32 = 0;         // mixed real form: periodic refresh by FP32 iterative refinement (default <= 128 orbitals)
     int warp_walkers = 0;      // mixed real form: > 0 = one warp per walker, walkers per CTA
     float cond_hi = 0.f, cond_lo = 0.f;  // the warp sweep's accuracy guard (0 = off)
+    int64_t segment = 0;       // one-warp mode: kvmc_advance in segments of this many moves (0 = whole call)
     std::string err;
 
     DevModel dm{};
@@ -188,6 +189,7 @@ cudaError_t sweep_launch(kvmc_handle *h, const kvmc::SweepParams &p) {
 // Rebuilds every walker's W.  allow32: with the FP32 refinement refresh
 // enabled, use it (FP64 for the walkers it flags); otherwise FP64 throughout.
 int full_refresh(kvmc_handle *h, bool track_drift, bool allow32 = true) {
+    h->db.compact = 0;  // outside a sweep call W32 is the state
     KV_TRY(h->cuda(cudaMemsetAsync(h->db.drift, 0, sizeof(float) * h->n_walkers, h->stream), "memset"));
     if (allow32 && h->refresh32 && !h->cplx) {
         KV_TRY(h->cuda(kvmc::launch_refresh32(h->dm, h->db, 0, track_drift ? 1 : 0, h->stream), "refresh launch"));
@@ -1079,15 +1081,26 @@ int sweep_end(kvmc_handle *h, kvmc_sweep_stats *stats, SweepCall &c) {
     return KVMC_OK;
 }
 
-int run_sweep(kvmc_handle *h, int64_t proposals_per_walker, int64_t moves_per_walker, kvmc_sweep_stats *stats) {
-    SweepCall c;
-    if (proposals_per_walker == 0 && moves_per_walker == 0) {
-        KV_TRY(set_device(h));
-        if (stats) std::memset(stats, 0, sizeof *stats);
-        return KVMC_OK;
-    }
-    KV_TRY(sweep_begin(h, proposals_per_walker, moves_per_walker, stats != nullptr, c));
-    const kvmc::SweepParams p = sweep_params(h);
+bool warp_mode(const kvmc_handle *h) { return h->mixed && !h->cplx && h->warp_walkers > 0; }
+
+// One-warp mode: the sweep and the refreshes of a call work on the
+// label-indexed blocks; W32 is converted to them at the start of the call
+// and back at its end (the refreshes write the blocks while db.compact is set).
+int compact_begin(kvmc_handle *h) {
+    if (!warp_mode(h)) return KVMC_OK;
+    KV_TRY(h->cuda(kvmc::launch_warp_convert(h->dm, h->db, true, h->stream), "to label-indexed W"));
+    h->db.compact = 1;
+    return KVMC_OK;
+}
+
+int compact_end(kvmc_handle *h) {
+    if (!h->db.compact) return KVMC_OK;
+    h->db.compact = 0;
+    return h->cuda(kvmc::launch_warp_convert(h->dm, h->db, false, h->stream), "to site-indexed W");
+}
+
+// Runs (sweep, refresh) pairs until every walker has reached its target.
+int run_pairs(kvmc_handle *h, const kvmc::SweepParams &p, SweepCall &c) {
     // Between host checks the loop issues a group of (sweep, refresh) pairs.
     const int group = h->mixed ? 4 : 8;
     for (int iter = 0;; iter += group) {
@@ -1100,6 +1113,34 @@ int run_sweep(kvmc_handle *h, int64_t proposals_per_walker, int64_t moves_per_wa
         if (active == 0) break;
         if (iter > 100000000) return h->fail(KVMC_ERR_NUMERIC, "sweep made no progress");
     }
+    return KVMC_OK;
+}
+
+int run_sweep(kvmc_handle *h, int64_t proposals_per_walker, int64_t moves_per_walker, kvmc_sweep_stats *stats) {
+    SweepCall c;
+    if (proposals_per_walker == 0 && moves_per_walker == 0) {
+        KV_TRY(set_device(h));
+        if (stats) std::memset(stats, 0, sizeof *stats);
+        return KVMC_OK;
+    }
+    KV_TRY(sweep_begin(h, proposals_per_walker, moves_per_walker, stats != nullptr, c));
+    const kvmc::SweepParams p = sweep_params(h);
+    KV_TRY(compact_begin(h));
+    int rc = KVMC_OK;
+    if (moves_per_walker > 0 && warp_mode(h) && h->segment > 0 && h->segment < moves_per_walker) {
+        // in segments of `segment` accepted moves per walker: a refresh the
+        // accuracy guard asks for waits at most until the segment's end
+        for (int64_t done = 0; done < moves_per_walker && rc == KVMC_OK; done += h->segment) {
+            const int64_t seg = std::min<int64_t>(h->segment, moves_per_walker - done);
+            rc = h->cuda(kvmc::launch_set_tend(h->db, 0, seg, h->stream), "set t_end");
+            if (rc == KVMC_OK) rc = run_pairs(h, p, c);
+        }
+    } else {
+        rc = run_pairs(h, p, c);
+    }
+    const int rc2 = compact_end(h);
+    if (rc != KVMC_OK) return rc;
+    KV_TRY(rc2);
     return sweep_end(h, stats, c);
 }
 
@@ -1198,7 +1239,8 @@ bool same_params(const kvmc::SweepParams &a, const kvmc::SweepParams &b) {
     return a.seed == b.seed && a.accept_rule == b.accept_rule && a.refresh_every == b.refresh_every &&
            a.measure_every == b.measure_every && a.delay_k == b.delay_k && a.drift_tol == b.drift_tol &&
            a.stream_threads == b.stream_threads && a.pipeline == b.pipeline && a.tc_flush == b.tc_flush &&
-           a.refresh32 == b.refresh32;
+           a.refresh32 == b.refresh32 && a.warp_walkers == b.warp_walkers && a.cond_hi == b.cond_hi &&
+           a.cond_lo == b.cond_lo;
 }
 
 // Captures one graph: from s0, every handle's stream runs its (sweep,
@@ -1252,6 +1294,8 @@ extern "C" int kvmc_group_advance(kvmc_group *g, int64_t moves_per_walker, kvmc_
     for (size_t i = 0; i < n; ++i) {
         kvmc_handle *h = g->hs[i];
         if (int rc = sweep_begin(h, 0, moves_per_walker, stats != nullptr, calls[i])) { g->err = h->err; return rc; }
+        // one-warp handles: the graph's refreshes are captured writing the label-indexed blocks
+        if (int rc = compact_begin(h)) { g->err = h->err; return rc; }
         // enough pairs for every walker to reach its target in one graph launch when no early refresh intervenes
         const int R = h->mixed ? std::max(h->refresh_every, 1) : 1;
         pairs[i] = h->mixed ? (int)std::min<int64_t>(64, moves_per_walker / R + 2) : 8;
@@ -1284,6 +1328,8 @@ extern "C" int kvmc_group_advance(kvmc_group *g, int64_t moves_per_walker, kvmc_
         KV_TRY(g->cuda(cudaEventElapsedTime(&t, g->t0, g->t1), "event time"));
         *ms = t;
     }
+    for (size_t i = 0; i < n; ++i)
+        if (int rc = compact_end(g->hs[i])) { g->err = g->hs[i]->err; return rc; }
     for (size_t i = 0; i < n; ++i) {
         kvmc_handle *h = g->hs[i];
         calls[i].launches = launches;
@@ -1474,6 +1520,11 @@ extern "C" int kvmc_set_tuning(kvmc_handle *h, int32_t key, int32_t value) {
             }
         }
         h->warp_walkers = value;
+        return KVMC_OK;
+    }
+    if (key == KVMC_TUNE_SEGMENT) {
+        if (value < 0) return h->fail(KVMC_ERR_ARGUMENT, "segment must be >= 0");
+        h->segment = value;
         return KVMC_OK;
     }
     if (key == KVMC_TUNE_COND_HI || key == KVMC_TUNE_COND_LO) {

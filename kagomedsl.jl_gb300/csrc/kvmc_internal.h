@@ -64,6 +64,7 @@ struct DevBatch {
     float *G32;
     size_t g_block;        // floats per walker: n_dn * ld_up + n_up * ld_dn
     float *cond_max;       // [W] largest |W| entry the warp sweep saw since the walker's last refresh
+    int compact;           // 1 while a one-warp sweep call runs: FP32 refreshes write G32, not W32
 };
 
 enum : int {
@@ -142,6 +143,8 @@ size_t warp_cta_smem(const DevModel &m);
 size_t warp_walker_smem(const DevModel &m, int K);
 size_t warp_compact_block(const DevModel &m);
 int warp_walkers_max(const DevModel &m, int K, int optin);
+// W32 -> G32 (to_compact) or back, every walker; kvmc_warp.cu
+cudaError_t launch_warp_convert(const DevModel &m, const DevBatch &b, bool to_compact, cudaStream_t stream);
 cudaError_t launch_sweep_warp(const DevModel &m, const DevBatch &b, const SweepParams &p, int *active,
                               cudaStream_t stream);
 

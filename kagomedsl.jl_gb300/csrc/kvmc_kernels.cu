@@ -46,7 +46,7 @@ constexpr int kSolveB = 16;
 template <typename OutT>
 __device__ void solve_rows_blocked(const double *A, int lda, const double *invd, const int *perm, const double *U,
                                    int n, const short *rows, int n_rows, double *Y, OutT *Wout, int ldw,
-                                   float *drift_slot, bool track_drift) {
+                                   float *drift_slot, bool track_drift, const short *krow = nullptr) {
     const int r = threadIdx.x;
     float dmax = 0.f;
     if (r < n_rows) {
@@ -128,7 +128,9 @@ __device__ void solve_rows_blocked(const double *A, int lda, const double *invd,
                     if (t < cnt) Y[(size_t)(i0 + t) * ld + r] = acc[t];
             }
         }
-        OutT *wr = Wout + (size_t)R * ldw;
+        // krow: the label-indexed blocks of the one-warp sweep (row = the other
+        // spin's label at site R); null: site-indexed W
+        OutT *wr = Wout + (size_t)(krow ? krow[R] - 1 : R) * ldw;
         for (int i = 0; i < n; ++i) {
             const OutT nv = (OutT)Y[(size_t)i * ld + r];
             if (track_drift) {
@@ -296,8 +298,12 @@ refresh_kernel(DevModel m, DevBatch b, int only_due, int track_drift) {
     const double *U = spin == 0 ? m.U_up : m.U_dn;
     const short *kappa = (spin == 0 ? b.kappa_up : b.kappa_dn) + (size_t)w * N;
     const size_t wblock = (size_t)N * (m.ld_up + m.ld_dn);
-    OutT *W = (sizeof(OutT) == 8 ? (OutT *)b.W64 : (OutT *)b.W32) + (size_t)w * wblock +
-              (spin == 0 ? 0 : (size_t)N * m.ld_up);
+    // during a one-warp sweep call the FP32 rows go to the label-indexed blocks
+    const bool cpt = sizeof(OutT) == 4 && b.compact;
+    OutT *W = cpt ? (OutT *)(b.G32 + (size_t)w * b.g_block + (spin == 0 ? 0 : (size_t)m.n_dn * m.ld_up))
+                  : (sizeof(OutT) == 8 ? (OutT *)b.W64 : (OutT *)b.W32) + (size_t)w * wblock +
+                        (spin == 0 ? 0 : (size_t)N * m.ld_up);
+    const short *krow = cpt ? (spin == 0 ? b.kappa_dn : b.kappa_up) + (size_t)w * N : nullptr;
 
     extern __shared__ __align__(16) unsigned char smem[];
     const int lda = n + 1;  // odd stride: column reads hit distinct banks
@@ -324,11 +330,11 @@ refresh_kernel(DevModel m, DevBatch b, int only_due, int track_drift) {
         b.logdet[4 * w + 2 + spin] = log_ratio;
     }
     const int nrows = collect_empty_rows(kappa, N, rows);
-    write_unit_rows(kappa, N, n, W, ldw, track_drift != 0, &b.drift[w]);
+    if (!cpt) write_unit_rows(kappa, N, n, W, ldw, track_drift != 0, &b.drift[w]);
     for (int r0 = 0; r0 < nrows; r0 += blockDim.x) {
         const int cnt = min((int)blockDim.x, nrows - r0);
         solve_rows_blocked<OutT>(A, lda, invd, perm, U, n, rows + r0, cnt, Y + (size_t)r0 * n, W, ldw, &b.drift[w],
-                                 track_drift != 0);
+                                 track_drift != 0, krow);
     }
 }
 
@@ -363,8 +369,11 @@ refresh_large_kernel(DevModel m, DevBatch b, int only_due, int track_drift) {
     const double *U = spin == 0 ? m.U_up : m.U_dn;
     const short *kappa = (spin == 0 ? b.kappa_up : b.kappa_dn) + (size_t)w * N;
     const size_t wblock = (size_t)N * (m.ld_up + m.ld_dn);
-    OutT *W = (sizeof(OutT) == 8 ? (OutT *)b.W64 : (OutT *)b.W32) + (size_t)w * wblock +
-              (spin == 0 ? 0 : (size_t)N * m.ld_up);
+    const bool cpt = sizeof(OutT) == 4 && b.compact;
+    OutT *W = cpt ? (OutT *)(b.G32 + (size_t)w * b.g_block + (spin == 0 ? 0 : (size_t)m.n_dn * m.ld_up))
+                  : (sizeof(OutT) == 8 ? (OutT *)b.W64 : (OutT *)b.W32) + (size_t)w * wblock +
+                        (spin == 0 ? 0 : (size_t)N * m.ld_up);
+    const short *krow = cpt ? (spin == 0 ? b.kappa_dn : b.kappa_up) + (size_t)w * N : nullptr;
     LT *A = reinterpret_cast<LT *>(b.lu_scratch) + ((size_t)w * 2 + spin) * b.lu_block;  // n x n, lda = n
     double *Y = b.solve_scratch + ((size_t)w * 2 + spin) * b.solve_block;
 
@@ -567,7 +576,7 @@ refresh_large_kernel(DevModel m, DevBatch b, int only_due, int track_drift) {
         b.logdet[4 * w + 2 + spin] = log(dmin / dmaxp);
     }
     const int nrows = collect_empty_rows(kappa, N, rows);
-    write_unit_rows(kappa, N, n, W, ldw, track_drift != 0, &b.drift[w]);
+    if (!cpt) write_unit_rows(kappa, N, n, W, ldw, track_drift != 0, &b.drift[w]);
     if constexpr (kF32) {
         for (int i = tid; i < n; i += nt) site_of[i] = -1;
         __syncthreads();
@@ -584,7 +593,8 @@ refresh_large_kernel(DevModel m, DevBatch b, int only_due, int track_drift) {
             if (tid < cnt) {
                 const int R = rows[r0 + tid];
                 if (!refine_row(A, n, invd, perm, site_of, Uh, Ul, n, R, Yf + (size_t)r0 * n * 2 + tid, cnt,
-                                reinterpret_cast<float *>(W) + (size_t)R * ldw, track_drift != 0, dmax))
+                                reinterpret_cast<float *>(W) + (size_t)(krow ? krow[R] - 1 : R) * ldw,
+                                track_drift != 0, dmax))
                     atomicOr(&b.status[w], kStatusRefine);
             }
         }
@@ -597,7 +607,7 @@ refresh_large_kernel(DevModel m, DevBatch b, int only_due, int track_drift) {
         for (int r0 = 0; r0 < nrows; r0 += blockDim.x) {
             const int cnt = min((int)blockDim.x, nrows - r0);
             solve_rows_blocked<OutT>(A, n, invd, perm, U, n, rows + r0, cnt, Y + (size_t)r0 * n, W, ldw, &b.drift[w],
-                                     track_drift != 0);
+                                     track_drift != 0, krow);
         }
     }
 }

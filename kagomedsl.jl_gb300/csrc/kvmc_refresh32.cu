@@ -102,7 +102,11 @@ refresh32_kernel(DevModel m, DevBatch b, int only_due, int track_drift) {
     const float *Ul = spin == 0 ? m.U32_up_lo : m.U32_dn_lo;
     const short *kappa = (spin == 0 ? b.kappa_up : b.kappa_dn) + (size_t)w * N;
     const size_t wblock = (size_t)N * (m.ld_up + m.ld_dn);
-    float *W = b.W32 + (size_t)w * wblock + (spin == 0 ? 0 : (size_t)N * m.ld_up);
+    // during a one-warp sweep call the rows go to the label-indexed blocks
+    const bool cpt = b.compact != 0;
+    float *W = cpt ? b.G32 + (size_t)w * b.g_block + (spin == 0 ? 0 : (size_t)m.n_dn * m.ld_up)
+                   : b.W32 + (size_t)w * wblock + (spin == 0 ? 0 : (size_t)N * m.ld_up);
+    const short *krow = cpt ? (spin == 0 ? b.kappa_dn : b.kappa_up) + (size_t)w * N : nullptr;
 
     extern __shared__ __align__(16) unsigned char smem[];
     const int lda = n + 1;
@@ -158,8 +162,8 @@ refresh32_kernel(DevModel m, DevBatch b, int only_due, int track_drift) {
             b.logdet[4 * w + 2 + spin] = log(dmin / dmaxp);
         }
     }
-    // unit rows at occupied sites, zero padding elsewhere
-    {
+    // unit rows at occupied sites, zero padding elsewhere (site-indexed W only)
+    if (!cpt) {
         float dmax = 0.f;
         for (int R = warp; R < N; R += nt / 32) {
             const int l = kappa[R];
@@ -191,7 +195,7 @@ refresh32_kernel(DevModel m, DevBatch b, int only_due, int track_drift) {
         if (r < cnt) {
             const int R = rows[r0 + r];
             if (!refine_row(A, lda, invd, perm, site_of, Uh, Ul, n, R, Y + (size_t)r0 * n * 2 + r, cnt,
-                            W + (size_t)R * ldw, track_drift != 0, dmax))
+                            W + (size_t)(krow ? krow[R] - 1 : R) * ldw, track_drift != 0, dmax))
                 atomicOr(&b.status[w], kStatusRefine);
         }
     }

@@ -25,8 +25,8 @@
 // configuration live in shared memory (about 15 KB per walker at N = 216,
 // K = 8), so a CTA holds up to 14 walkers, one per warp.  Each warp runs its
 // own serial chain; the SM's other warps fill its latency.  G lives in
-// HBM/L2 (a launch converts the site-indexed W of the handle into G at its
-// start and back at its end).  The G blocks of the walkers in flight should
+// HBM/L2; a sweep call converts the handle's site-indexed W into G at its
+// start and back at its end, and the refreshes in between write G.  The G blocks of the walkers in flight should
 // fit in L2 (7 walkers per SM at N = 216: 99 MB): with more walkers in
 // flight the flushes stream from HBM and each chain slows down more than
 // the extra walkers gain.
@@ -243,9 +243,6 @@ sweep_warp_kernel(DevModel m, DevBatch b, SweepParams p, int *active_count, size
     SD.ldg = m.ld_dn; SD.n_oth = nu_; SD.n_own = nd_;
     SU.G = b.G32 + (size_t)w * b.g_block;
     SD.G = SU.G + (size_t)nd_ * m.ld_up;
-    const size_t wblock = (size_t)N * (m.ld_up + m.ld_dn);
-    float *Wu = b.W32 + (size_t)w * wblock;
-    float *Wd = Wu + (size_t)N * m.ld_up;
 
     // configuration: +a for up label a, -b for down label b
     for (int s = lane; s < N; s += 32) {
@@ -255,34 +252,6 @@ sweep_warp_kernel(DevModel m, DevBatch b, SweepParams p, int *active_count, size
     zero_factors<K>(SU, lane);
     zero_factors<K>(SD, lane);
     __syncwarp();
-    // site-indexed W -> label-indexed G (the rows at the sites of the other spin)
-    {
-        const int qu = m.ld_up >> 2, qd = m.ld_dn >> 2, qm = max(qu, qd);
-        const int tot = N * qm;
-        const int dn_off = (int)(((size_t)nd_ * m.ld_up) / 4);
-        for (int e0 = 0; e0 < tot; e0 += 128) {
-            float4 v[4];
-            int dst[4];
-#pragma unroll
-            for (int q = 0; q < 4; ++q) {
-                const int e = e0 + 32 * q + lane;
-                dst[q] = -1;
-                if (e < tot) {
-                    const int s = e / qm, c4 = e - s * qm, l = lab[s];
-                    if (l < 0 && c4 < qu) {
-                        v[q] = reinterpret_cast<const float4 *>(Wu + (size_t)s * m.ld_up)[c4];
-                        dst[q] = (-l - 1) * qu + c4;
-                    } else if (l > 0 && c4 < qd) {
-                        v[q] = reinterpret_cast<const float4 *>(Wd + (size_t)s * m.ld_dn)[c4];
-                        dst[q] = dn_off + (l - 1) * qd + c4;
-                    }
-                }
-            }
-#pragma unroll
-            for (int q = 0; q < 4; ++q)
-                if (dst[q] >= 0) reinterpret_cast<float4 *>(SU.G)[dst[q]] = v[q];
-        }
-    }
     // Z_mu and the up-neighbour counts
     int zl = 0;
     for (int e = lane; e < nb; e += 32) {
@@ -402,7 +371,13 @@ sweep_warp_kernel(DevModel m, DevBatch b, SweepParams p, int *active_count, size
         // accuracy guard
         mx = warp_max_nonneg(mx);
         cmax = fmaxf(cmax, mx);
-        if (p.cond_hi > 0.f && cmax > p.cond_hi && mx < p.cond_lo) since = max(since, R);
+        if (p.cond_hi > 0.f && cmax > p.cond_hi && mx < p.cond_lo) {
+            // refresh when the moves this launch still owes are done (the end of
+            // the call, or of its segment) if they are fewer than an interval,
+            // so that refreshes stay on launch boundaries; else at once
+            const long long rem = acc_left - acc;
+            since = rem < R ? max(since, R - (int)rem) : R;
+        }
         __syncwarp();
         if (mm == K) {
             warp_flush<K>(SU, lane);
@@ -419,44 +394,6 @@ sweep_warp_kernel(DevModel m, DevBatch b, SweepParams p, int *active_count, size
         warp_flush<K>(SD, lane);
     }
     __syncwarp();
-    // label-indexed G -> site-indexed W (unit rows at the sites of each spin)
-    {
-        const int qu = m.ld_up >> 2, qd = m.ld_dn >> 2, qm = max(qu, qd);
-        const int tot = N * qm;
-        const float4 *Gv = reinterpret_cast<const float4 *>(SU.G);
-        const int dn_off = (int)(((size_t)nd_ * m.ld_up) / 4);
-        for (int e0 = 0; e0 < tot; e0 += 128) {
-            float4 vu[4], vd[4];
-            int s_[4], c_[4];
-#pragma unroll
-            for (int q = 0; q < 4; ++q) {
-                const int e = e0 + 32 * q + lane;
-                s_[q] = -1;
-                c_[q] = 0;
-                const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
-                vu[q] = z;
-                vd[q] = z;
-                if (e < tot) {
-                    const int s = e / qm, c4 = e - s * qm, l = lab[s];
-                    s_[q] = s;
-                    c_[q] = c4;
-                    if (l < 0) {
-                        if (c4 < qu) vu[q] = Gv[(-l - 1) * qu + c4];
-                        if (c4 < qd) vd[q] = unit4(-l - 1 - 4 * c4);
-                    } else {
-                        if (c4 < qd) vd[q] = Gv[dn_off + (l - 1) * qd + c4];
-                        if (c4 < qu) vu[q] = unit4(l - 1 - 4 * c4);
-                    }
-                }
-            }
-#pragma unroll
-            for (int q = 0; q < 4; ++q) {
-                if (s_[q] < 0) continue;
-                if (c_[q] < qu) reinterpret_cast<float4 *>(Wu + (size_t)s_[q] * m.ld_up)[c_[q]] = vu[q];
-                if (c_[q] < qd) reinterpret_cast<float4 *>(Wd + (size_t)s_[q] * m.ld_dn)[c_[q]] = vd[q];
-            }
-        }
-    }
     for (int s = lane; s < N; s += 32) {
         const int l = lab[s];
         b.kappa_up[(size_t)w * N + s] = (short)(l > 0 ? l : 0);
@@ -473,6 +410,102 @@ sweep_warp_kernel(DevModel m, DevBatch b, SweepParams p, int *active_count, size
         b.n_meas[w] += n_meas;
         if (t < tend_all && acc < acc_left && !bad_walker) atomicAdd(active_count, 1);
     }
+}
+
+// Site-indexed W -> the label-indexed blocks (and back), one warp per walker.
+// A sweep call of a handle in one-warp mode converts at its start and end;
+// the sweep and the refreshes in between work on the blocks.
+__global__ void __launch_bounds__(128)
+warp_to_compact_kernel(DevModel m, DevBatch b) {
+    const int lane = threadIdx.x & 31, w = blockIdx.x * 4 + (threadIdx.x >> 5);
+    if (w >= b.n_walkers) return;
+    const int N = m.n_sites, nd_ = m.n_dn;
+    const short *ku = b.kappa_up + (size_t)w * N, *kd = b.kappa_dn + (size_t)w * N;
+    const size_t wblock = (size_t)N * (m.ld_up + m.ld_dn);
+    const float *Wu = b.W32 + (size_t)w * wblock;
+    const float *Wd = Wu + (size_t)N * m.ld_up;
+    float *G = b.G32 + (size_t)w * b.g_block;
+    const int qu = m.ld_up >> 2, qd = m.ld_dn >> 2, qm = max(qu, qd);
+    const int tot = N * qm;
+    const int dn_off = (int)(((size_t)nd_ * m.ld_up) / 4);
+    for (int e0 = 0; e0 < tot; e0 += 128) {
+        float4 v[4];
+        int dst[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const int e = e0 + 32 * q + lane;
+            dst[q] = -1;
+            if (e < tot) {
+                const int s = e / qm, c4 = e - s * qm;
+                const int lu = ku[s], ld = kd[s];
+                if (lu == 0 && ld > 0 && c4 < qu) {
+                    v[q] = reinterpret_cast<const float4 *>(Wu + (size_t)s * m.ld_up)[c4];
+                    dst[q] = (ld - 1) * qu + c4;
+                } else if (lu > 0 && c4 < qd) {
+                    v[q] = reinterpret_cast<const float4 *>(Wd + (size_t)s * m.ld_dn)[c4];
+                    dst[q] = dn_off + (lu - 1) * qd + c4;
+                }
+            }
+        }
+#pragma unroll
+        for (int q = 0; q < 4; ++q)
+            if (dst[q] >= 0) reinterpret_cast<float4 *>(G)[dst[q]] = v[q];
+    }
+}
+
+__global__ void __launch_bounds__(128)
+warp_from_compact_kernel(DevModel m, DevBatch b) {
+    const int lane = threadIdx.x & 31, w = blockIdx.x * 4 + (threadIdx.x >> 5);
+    if (w >= b.n_walkers) return;
+    const int N = m.n_sites, nd_ = m.n_dn;
+    const short *ku = b.kappa_up + (size_t)w * N, *kd = b.kappa_dn + (size_t)w * N;
+    const size_t wblock = (size_t)N * (m.ld_up + m.ld_dn);
+    float *Wu = b.W32 + (size_t)w * wblock;
+    float *Wd = Wu + (size_t)N * m.ld_up;
+    const float4 *Gv = reinterpret_cast<const float4 *>(b.G32 + (size_t)w * b.g_block);
+    const int qu = m.ld_up >> 2, qd = m.ld_dn >> 2, qm = max(qu, qd);
+    const int tot = N * qm;
+    const int dn_off = (int)(((size_t)nd_ * m.ld_up) / 4);
+    for (int e0 = 0; e0 < tot; e0 += 128) {
+        float4 vu[4], vd[4];
+        int s_[4], c_[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const int e = e0 + 32 * q + lane;
+            s_[q] = -1;
+            c_[q] = 0;
+            const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
+            vu[q] = z;
+            vd[q] = z;
+            if (e < tot) {
+                const int s = e / qm, c4 = e - s * qm;
+                const int lu = ku[s], ld = kd[s];
+                s_[q] = s;
+                c_[q] = c4;
+                if (lu == 0) {
+                    if (c4 < qu && ld > 0) vu[q] = Gv[(ld - 1) * qu + c4];
+                    if (c4 < qd) vd[q] = unit4(ld - 1 - 4 * c4);
+                } else {
+                    if (c4 < qd) vd[q] = Gv[dn_off + (lu - 1) * qd + c4];
+                    if (c4 < qu) vu[q] = unit4(lu - 1 - 4 * c4);
+                }
+            }
+        }
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            if (s_[q] < 0) continue;
+            if (c_[q] < qu) reinterpret_cast<float4 *>(Wu + (size_t)s_[q] * m.ld_up)[c_[q]] = vu[q];
+            if (c_[q] < qd) reinterpret_cast<float4 *>(Wd + (size_t)s_[q] * m.ld_dn)[c_[q]] = vd[q];
+        }
+    }
+}
+
+cudaError_t launch_warp_convert(const DevModel &m, const DevBatch &b, bool to_compact, cudaStream_t stream) {
+    if (!b.G32) return cudaErrorInvalidValue;
+    const int grid = (b.n_walkers + 3) / 4;
+    if (to_compact) warp_to_compact_kernel<<<grid, 128, 0, stream>>>(m, b);
+    else warp_from_compact_kernel<<<grid, 128, 0, stream>>>(m, b);
+    return cudaGetLastError();
 }
 
 int warp_walkers_max(const DevModel &m, int K, int optin) {

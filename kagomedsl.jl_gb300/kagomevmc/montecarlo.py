@@ -211,10 +211,16 @@ class Engine:
         self._check(self._lib.kvmc_set_tuning(self.h, 5, int(walkers_per_cta)))
 
     def set_accuracy_guard(self, hi: int, lo: int):
-        """One-warp sweep: refresh a walker at once when its moves' |W| entries,
-        after exceeding `hi` since its last refresh, are all below `lo` (0 = off)."""
+        """One-warp sweep: refresh a walker when its moves' |W| entries, after
+        exceeding `hi` since its last refresh, are all below `lo` (0 = off); the
+        refresh waits for the end of the call or segment when that is nearer
+        than the refresh interval."""
         self._check(self._lib.kvmc_set_tuning(self.h, 6, int(hi)))
         self._check(self._lib.kvmc_set_tuning(self.h, 7, int(lo)))
+
+    def set_segment(self, moves: int):
+        """One-warp mode: advance in segments of this many accepted moves (0 = whole call)."""
+        self._check(self._lib.kvmc_set_tuning(self.h, 8, int(moves)))
 
     def set_drift_tolerance(self, tol: float):
         self._check(self._lib.kvmc_set_drift_tolerance(self.h, float(tol)))

@@ -131,22 +131,27 @@ def test_warp_matches_cta_kernel_walker_by_walker(kv):
         assert abs(e0[w] - e1[w]) <= 1e-4 * max(1.0, abs(e0[w]))
 
 
-def test_warp_accuracy_guard_refreshes_and_keeps_chains(kv):
+@pytest.mark.parametrize("segment", [0, 16])
+def test_warp_accuracy_guard_refreshes_and_keeps_chains(kv, segment):
     """A guard every walker trips at almost every move (hi 1, lo 1000: some
     entry above 1 has always been seen, and a move's entries stay below
-    1000): far more refreshes than the interval alone gives, exact move
-    counts, chains still the oracle's."""
+    1000).  The refresh it asks for waits for the end of the call, or of its
+    segment of 16 moves: one refresh per walker per call or segment, exact
+    move counts, chains still the oracle's, W at the end the oracle's."""
     N, walkers, seed, A = 96, 8, 43, 300
     ham = ham_for(kv, N)
     eng = kv.Engine(ham, walkers, precision="mixed", seed=seed, refresh_interval=4096, delay_k=8,
                     w_placement="hbm")
     eng.set_warp_walkers(8)
     eng.set_accuracy_guard(1, 1000)
+    eng.set_segment(segment)
     eng.init()
     ku0, kd0, _ = eng.get_state()
     st = eng.advance(A)
     assert st["accepted"] == walkers * A
-    assert st["refreshes"] >= walkers * A // 4, st["refreshes"]
+    per_walker = 1 if segment == 0 else -(-A // segment)
+    # an FP32 refresh that does not converge is redone in FP64 (counted once more)
+    assert walkers * per_walker <= st["refreshes"] <= walkers * per_walker + walkers, st["refreshes"]
     ku1, kd1, ct = eng.get_state()
     m = oracle_c.OracleModel(ham.U_up, ham.U_down, ham.nn)
     match = 0
@@ -155,6 +160,11 @@ def test_warp_accuracy_guard_refreshes_and_keeps_chains(kv):
         ch.run(seed, w, int(ct[w]), N // 2, N // 2)
         match += int(np.array_equal(ch.ku, ku1[w]) and np.array_equal(ch.kd, kd1[w]))
     assert match >= walkers - 1
+    Wu, Wd = eng.get_w()
+    for w in range(walkers):
+        # right after the refresh at the end of the call
+        assert close(Wu[w], o.reevaluateW(ham.U_up, ku1[w]), 1e-5), w
+        assert close(Wd[w], o.reevaluateW(ham.U_down, kd1[w]), 1e-5), w
     eng.close()
 
 
