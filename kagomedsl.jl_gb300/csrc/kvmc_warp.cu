@@ -226,7 +226,12 @@ sweep_warp_kernel(DevModel m, DevBatch b, SweepParams p, int *active_count, size
     const long long acc_left = b.acc_end[w] - b.accepted[w];
     const int since0 = b.since[w];
     if (t0 >= tend || acc_left <= 0 || (b.status[w] & kStatusStop)) {
-        if (lane == 0 && since0 < 0) b.since[w] = 0;
+        // nothing to do; a refresh marked due has run since (stream order): clear
+        // the mark and the guard's record of the W it replaced
+        if (lane == 0 && since0 < 0) {
+            b.since[w] = 0;
+            b.cond_max[w] = 0.f;
+        }
         return;
     }
 
