@@ -22,7 +22,8 @@ from .lattice import DoubleKagome, Hamiltonian
 
 CELLS = {54: (3, 3), 96: (4, 4), 216: (6, 6), 384: (8, 8), 864: (12, 12)}
 WORKLOADS = [(216, 2048, {}), (96, 4096, {}), (54, 1024, {}), (216, 768, {}), (384, 256, {}),
-             (864, 512, dict(delays=(8, 16), refresh=(128, 256), threads=(256,), placements=("hbm",), warmup=128))]
+             (864, 512, dict(delays=(8, 16), refresh=(128, 256), threads=(256,), placements=("hbm",), warps=(2,),
+                             warmup=128))]
 # Candidates beyond the default refresh list are left out at N=864, where one
 # FP64 refresh of 512 walkers takes ~0.5 s.
 
@@ -45,16 +46,23 @@ def field_model():
 
 def main(argv=None):
     argv = sys.argv[1:] if argv is None else argv
+    only = None
+    if "--only" in argv:
+        i = argv.index("--only")
+        only = {int(x) for x in argv[i + 1].split(",")}
+        argv = argv[:i] + argv[i + 2:]
     out = argv[0] if argv else autotune.SHIPPED
     cache = json.load(open(out)) if os.path.exists(out) else {}
-    jobs = [(model(N), walkers, kw) for N, walkers, kw in WORKLOADS]
+    jobs = [(model(N), walkers, kw) for N, walkers, kw in WORKLOADS if only is None or N in only]
     # complex W: delayed depths 4 and 8, W in HBM
-    jobs.append((field_model(), 2048, dict(delays=(4, 8), placements=("hbm",), threads=(256,))))
+    if only is None or 192 in only:
+        jobs.append((field_model(), 2048, dict(delays=(4, 8), placements=("hbm",), threads=(256,), warps=())))
     for ham, walkers, kw in jobs:
         key = autotune.cache_key(ham, walkers, "reference", autotune._device_name(0))
         ch = autotune.tune(ham, walkers, **kw)
         row = dict(delay_k=ch.delay_k, refresh_interval=ch.refresh_interval, placement=ch.placement,
-                   threads=ch.threads, moves_per_s=ch.moves_per_s, max_drift=ch.max_drift, trials=ch.trials)
+                   threads=ch.threads, moves_per_s=ch.moves_per_s, max_drift=ch.max_drift, trials=ch.trials,
+                   warp=ch.warp, guard_hi=ch.guard_hi, guard_lo=ch.guard_lo)
         cache[key] = row
         print(key, {k: v for k, v in row.items() if k != "trials"}, flush=True)
         with open(out, "w") as f:

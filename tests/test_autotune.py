@@ -26,9 +26,16 @@ class FakeEngine:
         if w_placement == "chip" and delay_k == 16:
             raise kagomevmc.KvmcError(7, "does not fit")
         self.k, self.R, self.place, self.walkers, self.threads = delay_k, refresh_interval, w_placement, walkers, 256
+        self.warp = 0
 
     def set_stream_threads(self, th):
         self.threads = th
+
+    def set_warp_walkers(self, wp):
+        self.warp = wp
+
+    def set_accuracy_guard(self, hi, lo):
+        self.guard = (hi, lo)
 
     def config(self):
         return dict(delay_k=self.k, refresh_interval=self.R, measure_interval=1, w_on_chip=self.place == "chip")
@@ -44,6 +51,7 @@ class FakeEngine:
 
     def region_stop(self):
         speed = 1.0 + 0.1 * self.k + (0.5 if self.place == "hbm" else 0.0) + (0.2 if self.threads == 128 else 0.0)
+        speed += 0.05 * self.warp
         speed *= 1.0 + np.log2(self.R) / 10
         return 1000.0 / speed
 
@@ -66,8 +74,9 @@ def test_tuner_picks_fastest_within_drift_bound(kv, monkeypatch, tmp_path):
         assert not (row["placement"] == "chip" and row["delay_k"] == 16)
     ok = [r for r in ch.trials if r["max_drift"] <= 5e-3]
     best = max(ok, key=lambda r: r["moves_per_s"])
-    assert (ch.delay_k, ch.refresh_interval, ch.placement, ch.threads) == (best["delay_k"], best["refresh_interval"],
-                                                                          best["placement"], best["threads"])
+    assert (ch.delay_k, ch.refresh_interval, ch.placement, ch.threads, ch.warp) == (
+        best["delay_k"], best["refresh_interval"], best["placement"], best["threads"], best["warp"])
+    assert ch.warp == 14 and (ch.guard_hi, ch.guard_lo) == autotune.GUARD   # the fastest shape of the stand-in
     assert ch.max_drift <= 5e-3
     # cached: a second call returns the same choice without trials
     ch2 = autotune.tune(ham, 64, cache_path=cache)
@@ -86,6 +95,7 @@ def test_shipped_table_covers_the_bench_workloads(kv):
         row = table[key]
         assert row["placement"] in ("chip", "hbm") and row["delay_k"] in (1, 4, 8, 12, 16)
         assert row["refresh_interval"] > 0 and row["threads"] in (128, 256)
+        assert row.get("warp", 0) in (0, 2, 4, 7, 10, 14)
 
 
 def test_tuner_without_a_candidate_inside_the_bound(kv, monkeypatch):
