@@ -9,8 +9,9 @@ every 108 proposals), with W refreshed in FP64 every R accepted moves (mixed
 form) or every 108 proposals (plain FP64 form).  The mixed form's settings
 (where W lives, delayed-update depth k, R, threads per walker) are the
 autotuner's choice for this workload on a GB300 (kagomevmc/tuned.json);
-flags override them.  The walkers' FP32 W state (2048 x 186.6 KB = 382 MB)
-is larger than L2, so no flush is needed between steps.
+flags override them.  The walkers' FP32 W state (2048 x 186.6 KB = 382 MB,
+and 191 MB for the non-trivial rows the one-warp sweep works on during a
+call) is larger than L2, so no flush is needed between steps.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
@@ -50,6 +51,8 @@ def args_():
     p.add_argument("--delay-k", type=int, default=None)
     p.add_argument("--placement", default=None, choices=["auto", "chip", "hbm"])
     p.add_argument("--threads", type=int, default=None, help="threads per walker with W in HBM")
+    p.add_argument("--warp", type=int, default=None, help="walkers per CTA with one warp per walker (0: one CTA each)")
+    p.add_argument("--guard", default=None, help="accuracy guard hi,lo of the one-warp sweep (0,0: off)")
     p.add_argument("--seed", type=int, default=2024)
     p.add_argument("--skip-plain", action="store_true")
     p.add_argument("--skip-cpu", action="store_true")
@@ -64,6 +67,7 @@ def args_():
     p.add_argument("--skip-large", action="store_true")
     p.add_argument("--skip-field", action="store_true")
     p.add_argument("--skip-batched", action="store_true")
+    p.add_argument("--skip-plugin", action="store_true")
     return p.parse_args()
 
 
@@ -241,6 +245,10 @@ def mixed_choice(kv, ham, a):
         ch.placement = a.placement
     if a.threads is not None:
         ch.threads = a.threads
+    if a.warp is not None:
+        ch.warp = a.warp
+    if a.guard is not None:
+        ch.guard_hi, ch.guard_lo = (int(x) for x in a.guard.split(","))
     ch.trials = []
     return ch
 
@@ -316,6 +324,46 @@ def adjoint_run(kv, seed, device, walkers=1024, sweeps=20):
             "adjoint_over_sweep": k2 / (k0 + k1) if k0 + k1 > 0 else None, "target_ratio": 2.0,
             "wall_ms": wall, "E_per_site": res["E"] / 96, "grad_per_site": (res["grad"] / 96).tolist(),
             "se_grad_per_site": (np.asarray(res["se_grad"]) / 96).tolist(), "S": res["S"].tolist()}
+
+
+def plugin_run(kv, seed, device, walkers=2048, sweeps=200, warm=20):
+    """The reference-shaped plugin surface end to end: MC / init_ / sweep_ /
+    measure_ (the Carlo.jl callbacks, kagomevmc/montecarlo.py) at the headline
+    workload, one fused sweep_ of min(N_up, N_down) = 108 proposals per walker
+    per Carlo sweep (the reference's refresh and measurement interval), the
+    autotuner's settings, host buffers: every call returns its statistics to
+    the host, and measure_ pushes the batch mean of the call's E_L samples.
+    Host wall clock around `sweeps` calls."""
+    params = dict(n1=2 * CELLS[0], n2=CELLS[1], PBC=(True, True), antiPBC=(False, True), N_up=N_SITES // 2,
+                  N_down=N_SITES // 2, walkers=walkers, precision="mixed", proposals_per_sweep=N_SITES // 2,
+                  seed=seed, device=device, tuned=True)
+    mc = kv.MC(params)
+    ctx = kv.MCContext()
+    kv.init_(mc, ctx, params)
+    for _ in range(warm):
+        kv.sweep_(mc, ctx)
+        ctx.sweeps += 1
+        kv.measure_(mc, ctx)
+    acc = 0
+    t0 = time.perf_counter()
+    for _ in range(sweeps):
+        kv.sweep_(mc, ctx)
+        ctx.sweeps += 1
+        kv.measure_(mc, ctx)
+        acc += mc.last_stats["accepted"]
+    sec = time.perf_counter() - t0
+    ev = kv.Evaluator()
+    kv.register_evaluables(kv.MC, ev, params)
+    energy = ev.run({"OL": ctx.observables["OL"][warm:]})["energy"]
+    cfg = mc.engine.config()
+    mc.engine.close()
+    # per call: the per-walker counters and sums read before and after (5 x 8 B
+    # each), the status words and drift (4 B each), two refresh counters
+    d2h = walkers * (2 * 5 * 8 + 4 + 4) + 16
+    return {"value": acc / sec, "unit": UNIT, "sweeps": sweeps, "proposals_per_sweep": N_SITES // 2,
+            "accepted_per_sweep": acc / sweeps, "ms_per_sweep": 1e3 * sec / sweeps, "h2d_bytes_per_step": 0,
+            "d2h_bytes_per_step": d2h, "energy_per_site": float(energy), "delay_k": cfg["delay_k"],
+            "path": "MC -> init_ -> (sweep_ -> measure_) x sweeps: kvmc_sweep(h, 108) per Carlo sweep, host wall clock"}
 
 
 def uneven_run(kv, seed, device, moves=512, steps=3):
@@ -573,14 +621,21 @@ def gpu_arm(a):
     large = None if a.skip_large else large_run(kv, a.seed, local)
     field = None if a.skip_field else field_run(kv, a.seed, local)
     batched = None if a.skip_batched else batched_run(kv, a.seed, local)
+    plugin = None if a.skip_plugin else plugin_run(kv, a.seed, local, walkers=a.walkers)
 
     # roofline of the dominant kernel
     refreshes = tot["refreshes"]
     f_refresh = 2 * ((2.0 / 3.0) * n ** 3 + 2.0 * (N_SITES - n) * n ** 2)   # FP64 flop per walker refresh
     f_move = 2.0 * N_SITES * N_SITES                                        # FP32 flop per accepted move
+    warp = getattr(choice, "warp", 0)
     kern = {
         "sweep_mixed": {"ms": sweep_ms, "launches": sweep_n, "flop": tot["accepted"] * f_move,
-                        "unit_work": "2*N^2 FP32 flop per accepted move (both spins' rank-1 update)"},
+                        "unit_work": "2*N^2 FP32 flop per accepted move (both spins' rank-1 update of N x n W)",
+                        **({"kernel": "sweep_warp_kernel (one warp per walker)",
+                            "executed_flop_per_move": N_SITES * N_SITES,
+                            "executed_note": "the label-indexed blocks hold W's non-trivial rows only: "
+                                             "2 spins x 2 flop x n_up x n_down = N^2 per accepted move"}
+                           if warp else {})},
         "refresh": {"ms": ref_ms, "launches": ref_n, "flop": refreshes * f_refresh,
                     "unit_work": "2*((2/3)n^3 + 2(N-n)n^2) flop per walker refresh (the FP64 algorithm's count)",
                     "arithmetic": ("FP32 iterative refinement (FP32 LU and solves, exact-product compensated "
@@ -599,8 +654,13 @@ def gpu_arm(a):
     if os.path.exists(tfile):
         tj = json.load(open(tfile))
         if dom == "sweep_mixed" and kern[dom]["launches"]:
-            key = "sweep_mixed" if cfg["w_on_chip"] else "sweep_mixed_hbm"
-            traffic = tj[key]["bytes_per_walker_launch"] * a.walkers * a.steps / kern[dom]["launches"]
+            key = "sweep_warp" if warp else ("sweep_mixed" if cfg["w_on_chip"] else "sweep_mixed_hbm")
+            if key in tj:
+                # bytes per accepted move of the captured launch, times this run's moves per launch
+                if "bytes_per_accepted_move" in tj[key]:
+                    traffic = tj[key]["bytes_per_accepted_move"] * tot["accepted"] / kern[dom]["launches"]
+                else:
+                    traffic = tj[key]["bytes_per_walker_launch"] * a.walkers * a.steps / kern[dom]["launches"]
         elif dom == "refresh" and kern[dom]["launches"]:
             traffic = tj["refresh_fp64"]["bytes_per_walker_spin"] * 2 * refreshes / kern[dom]["launches"]
     ach = kern[dom]["achieved_tflops"]
@@ -626,7 +686,10 @@ def gpu_arm(a):
                        "walkers_per_gpu": a.walkers, "accepted_moves_per_walker_per_step": a.moves,
                        "refresh_every_accepted": cfg["refresh_interval"], "measure_every_proposals": n,
                        "delay_k": cfg["delay_k"], "w_on_chip": cfg["w_on_chip"],
-                       "threads_per_walker": (choice.threads if not cfg["w_on_chip"] else 512),
+                       "threads_per_walker": (32 if warp else choice.threads if not cfg["w_on_chip"] else 512),
+                       **({"kernel": "one warp per walker, W's non-trivial rows indexed by labels",
+                           "walkers_per_cta": warp, "accuracy_guard": [choice.guard_hi, choice.guard_lo]}
+                          if warp else {}),
                        "settings_from": "autotuner cache kagomevmc/tuned.json (GB300), flags override",
                        "parallelism": f"replicas x{world}", "l2": "inputs larger than L2 (W state 382 MB per GPU)",
                        # the accuracy gate of the metric, as flat keys next to the workload it qualifies
@@ -638,7 +701,7 @@ def gpu_arm(a):
             "gpu_launches": tot["launches"], "e2e": e2e, "roofline": roof, "cpu_baseline": cpu,
             "plain_fp64": plain, "speedup_vs_plain_fp64": (value / plain["value"]) if plain else None,
             "energy_gate": gate, "adjoint": adjoint, "uneven_batch": uneven, "large_lattice": large,
-            "field_workload": field, "batched_n96": batched,
+            "field_workload": field, "batched_n96": batched, "plugin_e2e": plugin,
             "drift": drift, "clocks": clk, "peaks_measured": peaks}
     print(json.dumps(line), flush=True)
     if world > 1:

@@ -331,7 +331,9 @@ class MC:
     ``walkers``, ``precision`` ("plain" | "mixed"), ``accept``
     ("reference" | "metropolis"), ``refresh_interval``,
     ``measure_interval``, ``proposals_per_sweep``, ``seed``, ``device``,
-    ``init`` ("qr" | "random"; default "qr" for one walker, else "random").
+    ``init`` ("qr" | "random"; default "qr" for one walker, else "random"),
+    ``tuned`` (True: the mixed form with the autotuner's settings for this
+    model and batch size from the shipped GB300 table, when it has them).
     """
 
     def __init__(self, params: dict):
@@ -346,11 +348,23 @@ class MC:
         self.ns = n1 * n2 * 3
         self.walkers = int(params.get("walkers", 1))
         self.proposals_per_sweep = int(params.get("proposals_per_sweep", 1))
-        self.engine = Engine(self.Ham, self.walkers, params.get("precision", "plain"),
-                             params.get("accept", "reference"), params.get("refresh_interval", 0),
-                             params.get("measure_interval", 0), params.get("seed", 0), params.get("device", 0),
-                             params.get("delay_k", 0))
+        choice = None
+        if params.get("tuned", False):
+            from . import autotune
+
+            choice = autotune.lookup(self.Ham, self.walkers, params.get("accept", "reference"))
+        if choice is not None:
+            from . import autotune
+
+            self.engine = autotune.make_engine(self.Ham, self.walkers, choice, accept=params.get("accept", "reference"),
+                                               seed=params.get("seed", 0), device=params.get("device", 0))
+        else:
+            self.engine = Engine(self.Ham, self.walkers, params.get("precision", "plain"),
+                                 params.get("accept", "reference"), params.get("refresh_interval", 0),
+                                 params.get("measure_interval", 0), params.get("seed", 0), params.get("device", 0),
+                                 params.get("delay_k", 0))
         self.n_occupied = min(self.Ham.N_up, self.Ham.N_down)
+        self.last_stats = None   # the statistics of the last sweep_ call
 
     @property
     def kappa_up(self):
@@ -396,13 +410,21 @@ def sweep_(mc: MC, ctx: MCContext):
     Records the batch acceptance fraction as ``acc`` (the reference records
     0.0 / 1.0 per call, :548-589)."""
     st = mc.engine.sweep(mc.proposals_per_sweep)
+    mc.last_stats = st
     ctx.measure("acc", st["accepted"] / max(st["proposals"], 1))
 
 
 def measure_(mc: MC, ctx: MCContext):
-    """Carlo.measure! (src/MonteCarlo.jl:628-634): batch mean of the local energy when
+    """Carlo.measure! (src/MonteCarlo.jl:628-634): batch mean of the local energy.
+
+    With a fused sweep (proposals_per_sweep of at least min(N_up, N_down)),
+    the mean of the samples the last sweep_ took inside the library at the
+    reference's cadence; otherwise a measurement of the current state when
     ctx.sweeps * proposals_per_sweep is a multiple of min(N_up, N_down)."""
-    if (ctx.sweeps * mc.proposals_per_sweep) % mc.n_occupied == 0:
+    st = mc.last_stats
+    if st is not None and st["measurements"] > 0:
+        ctx.measure("OL", st["sum_energy"] / st["measurements"])
+    elif (ctx.sweeps * mc.proposals_per_sweep) % mc.n_occupied == 0:
         ctx.measure("OL", float(np.mean(mc.engine.measure())))
 
 
