@@ -336,54 +336,62 @@ extern "C" int kvmc_hopping_matrix(const kvmc_lattice_desc *lat, const kvmc_link
                 auto it = lin.find({(s1 - 1) % 6 + 1, (s2 - 1) % 6 + 1});
                 if (it != lin.end()) at(s1, s2) = it->second * peierls(B, g.site(s1), g.site(s2));
             }
-    // inter-cell (src/Hamiltonian.jl:333-343 with :99-153, :177-207)
-    const double det = g.a1.x * g.a2.y - g.a1.y * g.a2.x;
-    struct Shift { int dx, dy; double sign; };
-    std::vector<Shift> shifts;
-    for (int c1 = 1; c1 <= ncell; ++c1)
-        for (int c2 = 1; c2 <= ncell; ++c2) {
-            if (c1 == c2) continue;
-            for (int s1 = (c1 - 1) * 6 + 1; s1 <= c1 * 6; ++s1)
-                for (int s2 = (c2 - 1) * 6 + 1; s2 <= c2 * 6; ++s2) {
-                    if (s1 >= s2) continue;
-                    const int l1 = (s1 - 1) % 6 + 1, l2 = (s2 - 1) % 6 + 1;
-                    const Vec2 u1 = g.uc(s1), u2 = g.uc(s2);
-                    const double ddx = u2.x - u1.x, ddy = u2.y - u1.y;
-                    const int dx = (int)std::nearbyint((g.a2.y * ddx - g.a2.x * ddy) / det);
-                    const int dy = (int)std::nearbyint((-g.a1.y * ddx + g.a1.x * ddy) / det);
-                    shifts.clear();
-                    shifts.push_back({dx, dy, 1.0});
-                    if (g.pbc1 || g.pbc2) {
-                        const int sx[3] = {-g.n1h, 0, g.n1h}, sy[3] = {-g.n2, 0, g.n2};
-                        for (int ix = 0; ix < 3; ++ix) {
-                            if (!g.pbc1 && ix != 1) continue;
-                            for (int iy = 0; iy < 3; ++iy) {
-                                if (!g.pbc2 && iy != 1) continue;
-                                if (ix == 1 && iy == 1) continue;
-                                double sign = 1.0;
-                                if (g.anti1 && sx[ix] != 0) sign *= -1.0;
-                                if (g.anti2 && sy[iy] != 0) sign *= -1.0;
-                                const Shift cand{dx + sx[ix], dy + sy[iy], sign};
-                                bool dup = false;
-                                for (const auto &q : shifts)
-                                    if (q.dx == cand.dx && q.dy == cand.dy && q.sign == cand.sign) { dup = true; break; }
-                                if (!dup) shifts.push_back(cand);
-                            }
-                        }
+    // Inter-cell (src/Hamiltonian.jl:333-343 with :99-153, :177-207).  The
+    // reference visits every cell pair and, per site pair, every image shift
+    // (O(N^2)); here every (cell, inter-cell link, image) triple names its one
+    // partner cell directly (O(N)).  For a pair (s1 < s2) in cells (c1, c2),
+    // the reference tries the plain cell offset d first and then d + image
+    // for the images (ix, iy) in order; a link key (l1, l2, dx, dy) matches
+    // when that candidate equals (dx, dy), i.e. when c2 = c1 + (dx, dy) - image.
+    // Each entry's contributions are summed in the reference's candidate
+    // order, from the same floating-point expressions, so T is bit-identical.
+    {
+        struct Contrib { size_t entry; int pos; std::complex<double> v; };
+        std::vector<Contrib> contrib;
+        const int sx[3] = {-g.n1h, 0, g.n1h}, sy[3] = {-g.n2, 0, g.n2};
+        for (int c1 = 1; c1 <= ncell; ++c1) {
+            const int k1 = (c1 - 1) % g.n1h, k2 = (c1 - 1) / g.n1h;
+            for (const auto &kv : linter) {
+                const int l1 = std::get<0>(kv.first), l2 = std::get<1>(kv.first);
+                const int qdx = std::get<2>(kv.first), qdy = std::get<3>(kv.first);
+                // candidate positions: 0 = the plain offset, then the images in (ix, iy) order
+                int pos = 0;
+                for (int img = -1; img < 9; ++img) {
+                    int ix = 1, iy = 1;
+                    double sign = 1.0;
+                    if (img >= 0) {
+                        ix = img / 3;
+                        iy = img % 3;
+                        if (!(g.pbc1 || g.pbc2)) break;
+                        if (!g.pbc1 && ix != 1) continue;
+                        if (!g.pbc2 && iy != 1) continue;
+                        if (ix == 1 && iy == 1) continue;
+                        ++pos;
+                        if (g.anti1 && sx[ix] != 0) sign *= -1.0;
+                        if (g.anti2 && sy[iy] != 0) sign *= -1.0;
                     }
+                    const int k1b = k1 + qdx - sx[ix], k2b = k2 + qdy - sy[iy];
+                    if (k1b < 0 || k1b >= g.n1h || k2b < 0 || k2b >= g.n2) continue;
+                    const int c2 = k2b * g.n1h + k1b + 1;
+                    if (c2 <= c1) continue;  // s1 < s2 in different cells means c1 < c2
+                    const int s1 = (c1 - 1) * 6 + l1, s2 = (c2 - 1) * 6 + l2;
+                    const Vec2 u1 = g.uc(s1), u2 = g.uc(s2);
                     const Vec2 r1 = g.site(s1);
                     const Vec2 s2c = g.site(s2);
                     const Vec2 dr2 = {s2c.x - u2.x, s2c.y - u2.y};
-                    for (const auto &q : shifts) {
-                        auto it = linter.find(std::make_tuple(l1, l2, q.dx, q.dy));
-                        if (it == linter.end()) continue;
-                        Vec2 ruc2 = {u1.x + q.dx * g.a1.x, u1.y + q.dx * g.a1.y};
-                        ruc2 = {ruc2.x + q.dy * g.a2.x, ruc2.y + q.dy * g.a2.y};
-                        const Vec2 r2 = {ruc2.x + dr2.x, ruc2.y + dr2.y};
-                        at(s1, s2) += (q.sign * it->second) * peierls(B, r1, r2);
-                    }
+                    Vec2 ruc2 = {u1.x + qdx * g.a1.x, u1.y + qdx * g.a1.y};
+                    ruc2 = {ruc2.x + qdy * g.a2.x, ruc2.y + qdy * g.a2.y};
+                    const Vec2 r2 = {ruc2.x + dr2.x, ruc2.y + dr2.y};
+                    contrib.push_back({(size_t)(s1 - 1) + (size_t)(s2 - 1) * N, img < 0 ? 0 : pos,
+                                       (sign * kv.second) * peierls(B, r1, r2)});
                 }
+            }
         }
+        std::stable_sort(contrib.begin(), contrib.end(), [](const Contrib &x, const Contrib &y) {
+            return x.entry != y.entry ? x.entry < y.entry : x.pos < y.pos;
+        });
+        for (const auto &c : contrib) T[c.entry] += c.v;
+    }
     // H = -(T + T^dagger), column-major interleaved
     for (int j = 0; j < N; ++j)
         for (int i = 0; i < N; ++i) {

@@ -63,6 +63,38 @@ def test_custom_links_zero_flux_shape(built):
     assert np.array_equal(kv.Hmat(L, lin, lint), o.hmat(Lo, lin, lint))
 
 
+@pytest.mark.parametrize("n1,n2,pbc,anti,B", [(6, 3, (True, True), (True, True), 0.2),
+                                              (8, 2, (True, False), (True, False), 0.05),
+                                              (4, 4, (False, True), (False, True), 0.0)])
+def test_hopping_builder_with_wide_and_wrapping_links(built, n1, n2, pbc, anti, B):
+    """Inter-cell keys two cells away and keys that only an image reaches: the
+    builder that visits (cell, link, image) triples gives the oracle's
+    cell-pair loop (src/Hamiltonian.jl:333-343) bit for bit, accumulation
+    order included."""
+    import kagomevmc as kv
+
+    lint = dict(kv.PI_LINK_INTER)
+    lint.update({(1, 2, 2, 0): 0.5, (4, 3, -2, 1): -0.25, (6, 1, 1, 2): 0.75, (2, 5, 0, -3): 0.3})
+    L = kv.DoubleKagome(1.0, n1, n2, pbc, anti)
+    Lo = o.double_kagome(1.0, n1, n2, pbc, anti)
+    assert np.array_equal(kv.Hmat(L, kv.PI_LINK_IN, lint, B=B), o.hmat(Lo, kv.PI_LINK_IN, lint, B=B))
+
+
+def test_hopping_builder_scales_linearly(built):
+    """12 x 12 doubled cells (N=864): the couplings take O(N) work, so the
+    whole dense build (an N x N output) takes well under a second."""
+    import time
+
+    import kagomevmc as kv
+
+    L = kv.DoubleKagome(1.0, 24, 12, (True, True), (False, True))
+    t0 = time.perf_counter()
+    H = kv.Hmat(L)
+    assert time.perf_counter() - t0 < 1.0
+    # 4-regular, |t| = 1: 2N bonds
+    assert len(kv.get_nn(H)) == 2 * 864 and np.allclose(np.abs(H[np.abs(H) > 0]), 1.0)
+
+
 def test_lattice_errors(built):
     import kagomevmc as kv
 
