@@ -253,10 +253,13 @@ def mixed_choice(kv, ham, a):
     return ch
 
 
-def energy_gate(ham, kv, walkers, calls, moves, choice, seed):
+def energy_gate(ham, kv, walkers, calls, moves, choice, seed, therm=1):
     """Both forms on identical walkers and proposal streams, driven the way the
-    bench drives the mixed form (`calls` kvmc_advance calls of `moves`
-    accepted moves per walker): |dE/N| over walkers whose chains agree."""
+    bench drives the mixed form: `therm` kvmc_advance calls of `moves`
+    accepted moves per walker to leave the random starts behind (their
+    samples are discarded, as the bench's warm-up steps are), then `calls`
+    calls whose local energies are compared.  The worst relative W drift
+    seen at a refresh is reported for both phases."""
     import numpy as np
 
     from kagomevmc import autotune
@@ -268,13 +271,17 @@ def energy_gate(ham, kv, walkers, calls, moves, choice, seed):
         else:
             eng = kv.Engine(ham, walkers, precision="plain", seed=seed)
         eng.init()
+        drift_therm = 0.0
+        for _ in range(therm):
+            drift_therm = max(drift_therm, eng.advance(moves)["max_drift"])
+        eng.reset_stats()
         drift = 0.0
         for _ in range(calls):
             drift = max(drift, eng.advance(moves)["max_drift"])
         ws = eng.walker_stats()
-        res[prec] = (ws["sum_e"], ws["n_meas"], eng.get_state()[0], drift, ws["proposals"])
+        res[prec] = (ws["sum_e"], ws["n_meas"], eng.get_state()[0], (drift, drift_therm), ws["proposals"])
         eng.close()
-    (ep, np_, kp, _, pp), (em, nm, km, drift, pm) = res["plain"], res["mixed"]
+    (ep, np_, kp, _, pp), (em, nm, km, (drift, drift_therm), pm) = res["plain"], res["mixed"]
     same = np.array([np.array_equal(kp[w], km[w]) for w in range(walkers)])
     dE_same = abs(ep[same].sum() / np_[same].sum() - em[same].sum() / nm[same].sum()) / N_SITES
     # all walkers: the difference of the two forms' per-walker means, with the
@@ -288,7 +295,8 @@ def energy_gate(ham, kv, walkers, calls, moves, choice, seed):
             "accepted_moves_per_call": moves, "proposals_per_walker": float(np.mean(pm)),
             "identical_chains": int(same.sum()), "dE_per_site_identical_chains": float(dE_same),
             "worst_walker_dE_per_site": float(np.abs(d).max()),
-            "max_w_drift_at_refresh": float(drift), "pass": bool(dE + 2 * se <= 1e-4)}
+            "thermalization_calls": therm, "max_w_drift_at_refresh": float(drift),
+            "max_w_drift_at_refresh_thermalization": float(drift_therm), "pass": bool(dE + 2 * se <= 1e-4)}
 
 
 def adjoint_run(kv, seed, device, walkers=1024, sweeps=20):
