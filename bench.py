@@ -57,7 +57,7 @@ def args_():
     p.add_argument("--skip-plain", action="store_true")
     p.add_argument("--skip-cpu", action="store_true")
     p.add_argument("--skip-gate", action="store_true")
-    p.add_argument("--gate-walkers", type=int, default=256, help="walkers of the energy gate")
+    p.add_argument("--gate-walkers", type=int, default=512, help="walkers of the energy gate")
     p.add_argument("--gate-calls", type=int, default=None,
                    help="advance calls of the energy gate (default: two refresh intervals, at least 8)")
     p.add_argument("--skip-e2e", action="store_true")
