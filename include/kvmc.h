@@ -33,7 +33,7 @@ extern "C" {
 #define KVMC_API
 #endif
 
-#define KVMC_ABI_VERSION 3
+#define KVMC_ABI_VERSION 4
 
 enum kvmc_status {
     KVMC_OK = 0,
@@ -196,6 +196,7 @@ typedef struct {
     double max_drift;     /* mixed: max |W_fp32 - W_fp64 fresh| seen at a refresh */
     int32_t bad_walkers;  /* walkers whose status word is nonzero */
     int32_t launches;     /* kernels launched by the call */
+    int64_t fp64_redos;   /* refreshes the FP32 refinement handed to the FP64 refresh */
 } kvmc_sweep_stats;
 
 /* Replaces Carlo.sweep! (src/MonteCarlo.jl:538-607) plus the cadenced
@@ -294,7 +295,10 @@ KVMC_API int kvmc_kernel_time(kvmc_handle *h, int32_t kind, double *total_ms, in
  *   KVMC_TUNE_REFRESH32: 1 = the periodic refresh of the FP32 W runs as
  *   iterative refinement on the FP32 pipes (FP32 LU and solves, residual
  *   with exact products and compensated sums), walkers that do not converge
- *   falling back to the FP64 refresh; 0 = FP64 LU and solves.  It also
+ *   falling back to the FP64 refresh; 2 = the same refinement with the
+ *   solves and the residual in tiles of 32 rows, one CTA per walker and
+ *   spin (the faster form from about 200 orbitals per spin); 0 = FP64 LU
+ *   and solves.  It also
  *   rebuilds W in kvmc_set_state and kvmc_init with given configurations
  *   (log|det| then from the FP32 factors); seeded starts and kvmc_refresh
  *   always use FP64.  The default is 1 for the mixed real form with at most

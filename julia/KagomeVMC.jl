@@ -98,6 +98,7 @@ struct SweepStats
     max_drift::Float64
     bad_walkers::Int32
     launches::Int32
+    fp64_redos::Int64
 end
 
 SweepStats() = SweepStats(0, 0, 0, 0.0, 0.0, 0, 0.0, 0, 0)

@@ -54,7 +54,7 @@ struct kvmc_handle {
     int stream_threads = 256;  // W in HBM: threads per walker
     int pipeline = 1;          // delayed form: pipelined scan / factor-column write
     int tc_flush = 0;          // W in HBM: rank-k flush on the tensor cores
-    int refresh32 = 0;         // mixed real form: periodic refresh by FP32 iterative refinement (default <= 128 orbitals)
+    int refresh32 = 0;         // mixed real form: periodic refresh by FP32 iterative refinement, 1 per row, 2 tiled (default <= 128 orbitals)
     int warp_walkers = 0;      // mixed real form: > 0 = one warp per walker, walkers per CTA
     float cond_hi = 0.f, cond_lo = 0.f;  // the warp sweep's accuracy guard (0 = off)
     int64_t segment = 0;       // one-warp mode: kvmc_advance in segments of this many moves (0 = whole call)
@@ -167,13 +167,19 @@ int upload_kappa(kvmc_handle *h, const int32_t *ku, const int32_t *kd) {
     return h->cuda(cudaStreamSynchronize(h->stream), "upload kappa");
 }
 
+// The FP32 refresh by iterative refinement: one thread per row (1) or tiled (2)
+cudaError_t refresh32_launch(kvmc_handle *h, int only_due, int track_drift) {
+    return h->refresh32 == 2 ? kvmc::launch_refresh_tile(h->dm, h->db, only_due, track_drift, h->stream)
+                             : kvmc::launch_refresh32(h->dm, h->db, only_due, track_drift, h->stream);
+}
+
 // The real and the complex kernels behind one call each
 cudaError_t refresh_launch(kvmc_handle *h, int only_due, int track_drift) {
     if (h->cplx) return kvmc::launch_refresh_c(h->dm, h->db, h->mixed, only_due, track_drift, h->stream);
     if (h->refresh32 && only_due == 1) {
         // FP32 refresh by iterative refinement; the walkers it gives up on are
         // rebuilt by the FP64 refresh, then their flag is cleared
-        cudaError_t e = kvmc::launch_refresh32(h->dm, h->db, 1, track_drift, h->stream);
+        cudaError_t e = refresh32_launch(h, 1, track_drift);
         if (e == cudaSuccess) e = kvmc::launch_refresh(h->dm, h->db, true, 2, 0, h->stream);
         if (e == cudaSuccess) e = kvmc::launch_clear_status(h->db, kvmc::kStatusRefine, h->stream);
         return e;
@@ -192,7 +198,7 @@ int full_refresh(kvmc_handle *h, bool track_drift, bool allow32 = true) {
     h->db.compact = 0;  // outside a sweep call W32 is the state
     KV_TRY(h->cuda(cudaMemsetAsync(h->db.drift, 0, sizeof(float) * h->n_walkers, h->stream), "memset"));
     if (allow32 && h->refresh32 && !h->cplx) {
-        KV_TRY(h->cuda(kvmc::launch_refresh32(h->dm, h->db, 0, track_drift ? 1 : 0, h->stream), "refresh launch"));
+        KV_TRY(h->cuda(refresh32_launch(h, 0, track_drift ? 1 : 0), "refresh launch"));
         KV_TRY(h->cuda(kvmc::launch_refresh(h->dm, h->db, true, 2, 0, h->stream), "refresh launch"));
         KV_TRY(h->cuda(kvmc::launch_clear_status(h->db, kvmc::kStatusRefine, h->stream), "refresh launch"));
     } else {
@@ -745,7 +751,7 @@ extern "C" int kvmc_create(const kvmc_model_desc *model, const kvmc_batch_desc *
         (rc = h->alloc(&b.sum_e, Wk)) || (rc = h->alloc(&b.sum_e2, Wk)) || (rc = h->alloc(&b.n_meas, Wk)) ||
         (rc = h->alloc(&b.accepted, Wk)) || (rc = h->alloc(&b.proposals, Wk)) || (rc = h->alloc(&b.status, Wk)) ||
         (rc = h->alloc(&b.logdet, 4 * (size_t)Wk)) || (rc = h->alloc(&b.drift, Wk)) ||
-        (rc = h->alloc(&b.energy_out, Wk)) || (rc = h->alloc(&b.refresh_count, 1)) || (rc = h->alloc(&h->d_active, 1)) ||
+        (rc = h->alloc(&b.energy_out, Wk)) || (rc = h->alloc(&b.refresh_count, 2)) || (rc = h->alloc(&h->d_active, 1)) ||
         (rc = h->alloc(&h->d_attempt, Wk)) || (rc = h->alloc(&h->d_redo, Wk)))
         return bail(rc);
     b.solve_block = kvmc::refresh_scratch_block(m) * cw;
@@ -772,7 +778,7 @@ extern "C" int kvmc_create(const kvmc_model_desc *model, const kvmc_batch_desc *
     cudaMemset(b.since, 0, Wk * 4);
     cudaMemset(b.status, 0, Wk * 4);
     cudaMemset(b.drift, 0, Wk * 4);
-    cudaMemset(b.refresh_count, 0, 8);
+    cudaMemset(b.refresh_count, 0, 16);
     if (int e = kvmc_reset_stats(h)) return bail(e);
     // shared-memory capacity decides whether the FP32 W can be staged on chip
     const int optin = kvmc::max_smem_optin(h->device);
@@ -1017,7 +1023,7 @@ kvmc::SweepParams sweep_params(const kvmc_handle *h) {
 // The accounting around one kvmc_sweep / kvmc_advance call.
 struct SweepCall {
     Snapshot before;
-    unsigned long long ref0 = 0;
+    unsigned long long ref0[2] = {0, 0};
     int launches = 1;
     int64_t moves = 0;  // kvmc_advance: accepted moves asked of every walker
 };
@@ -1027,7 +1033,7 @@ int sweep_begin(kvmc_handle *h, int64_t proposals_per_walker, int64_t moves_per_
     c.moves = proposals_per_walker > 0 ? 0 : moves_per_walker;
     if (stats) {
         KV_TRY(snapshot(h, c.before));
-        KV_TRY(h->cuda(cudaMemcpy(&c.ref0, h->db.refresh_count, 8, cudaMemcpyDeviceToHost), "refresh count"));
+        KV_TRY(h->cuda(cudaMemcpy(c.ref0, h->db.refresh_count, 16, cudaMemcpyDeviceToHost), "refresh count"));
     }
     KV_TRY(h->cuda(kvmc::launch_set_tend(h->db, proposals_per_walker, moves_per_walker, h->stream), "set t_end"));
     return h->cuda(cudaMemsetAsync(h->db.drift, 0, sizeof(float) * h->n_walkers, h->stream), "memset");
@@ -1083,9 +1089,10 @@ int sweep_end(kvmc_handle *h, kvmc_sweep_stats *stats, SweepCall &c) {
     stats->max_drift = md;
     stats->bad_walkers = bad;
     stats->launches = c.launches;
-    unsigned long long ref1 = 0;
-    KV_TRY(h->cuda(cudaMemcpy(&ref1, h->db.refresh_count, 8, cudaMemcpyDeviceToHost), "refresh count"));
-    stats->refreshes = (int64_t)(ref1 - c.ref0);
+    unsigned long long ref1[2] = {0, 0};
+    KV_TRY(h->cuda(cudaMemcpy(ref1, h->db.refresh_count, 16, cudaMemcpyDeviceToHost), "refresh count"));
+    stats->refreshes = (int64_t)(ref1[0] - c.ref0[0]);
+    stats->fp64_redos = (int64_t)(ref1[1] - c.ref0[1]);
     return KVMC_OK;
 }
 
@@ -1483,7 +1490,14 @@ extern "C" int kvmc_set_tuning(kvmc_handle *h, int32_t key, int32_t value) {
         return KVMC_OK;
     }
     if (key == KVMC_TUNE_REFRESH32) {
-        if (value != 0 && value != 1) return h->fail(KVMC_ERR_ARGUMENT, "refresh32 must be 0 or 1");
+        if (value < 0 || value > 2) return h->fail(KVMC_ERR_ARGUMENT, "refresh32 must be 0, 1 or 2");
+        if (value == 2) {
+            if (!h->mixed || h->cplx)
+                return h->fail(KVMC_ERR_UNSUPPORTED, "the FP32 refresh serves the mixed real form");
+            const size_t need = kvmc::refresh_tile_smem(h->dm);
+            if (need + 1024 > (size_t)kvmc::max_smem_optin(h->device))
+                return h->fail(KVMC_ERR_UNSUPPORTED, "the tiled FP32 refresh needs %zu B shared memory", need);
+        }
         if (value == 1) {
             if (!h->mixed || h->cplx)
                 return h->fail(KVMC_ERR_UNSUPPORTED, "the FP32 refresh serves the mixed real form");

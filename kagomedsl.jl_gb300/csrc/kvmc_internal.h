@@ -54,7 +54,7 @@ struct DevBatch {
                            // log(min|pivot|/max|pivot|) up, down
     float *drift;          // [W] max |W32_old - W64_new| at the last refresh
     double *energy_out;    // [W] scratch for kvmc_measure
-    unsigned long long *refresh_count;  // walker refreshes performed (one counter)
+    unsigned long long *refresh_count;  // [2] walker refreshes performed; FP32 refreshes redone in FP64
     double *solve_scratch; // FP64 rows being solved by the refresh: [W][2][solve_block]
     size_t solve_block;    // doubles per (walker, spin)
     double *lu_scratch;    // more than 160 orbitals: tilde_U factorised in HBM, [W][2][lu_block]
@@ -93,7 +93,7 @@ struct SweepParams {
     int stream_threads;   // W in HBM: threads per walker's CTA (128 or 256)
     int pipeline;         // delayed form: scan for the next move while the last one's factor column is written
     int tc_flush;         // W in HBM: rank-k flush on the tensor cores (tcgen05, 3xTF32)
-    int refresh32;        // mixed real form: FP32 refresh by iterative refinement
+    int refresh32;        // mixed real form: FP32 refresh by iterative refinement (1 per row, 2 tiled)
     int warp_walkers;     // mixed real form: > 0 = one warp per walker, this many walkers per CTA (kvmc_warp.cu)
     float cond_hi, cond_lo;  // warp sweep's accuracy guard (0 = off), see kvmc_warp.cu
 };
@@ -136,6 +136,11 @@ cudaError_t launch_refresh32(const DevModel &m, const DevBatch &b, int only_due,
 cudaError_t launch_refresh32_large(const DevModel &m, const DevBatch &b, int only_due, int track_drift,
                                    cudaStream_t stream);
 size_t refresh_large_smem(const DevModel &m, size_t lt_bytes);
+// The same refinement with tiled solves and residual, one CTA per walker-spin
+// (kvmc_refresh_tile.cu): only_due 0 or 1 as for launch_refresh32.
+size_t refresh_tile_smem(const DevModel &m);
+cudaError_t launch_refresh_tile(const DevModel &m, const DevBatch &b, int only_due, int track_drift,
+                                cudaStream_t stream);
 cudaError_t launch_clear_status(const DevBatch &b, int bits, cudaStream_t stream);
 
 // One warp per walker with W's non-trivial rows indexed by labels (kvmc_warp.cu).

@@ -291,7 +291,7 @@ refresh_kernel(DevModel m, DevBatch b, int only_due, int track_drift) {
     if (only_due == 1 && b.since[w] >= 0) return;  // a negative `since` marks a refresh as due
     if (only_due == 2 && !(b.status[w] & kStatusRefine)) return;  // the FP32 refresh gave this walker up
 
-    if (spin == 0 && threadIdx.x == 0 && only_due != 2) atomicAdd(b.refresh_count, 1ull);
+    if (spin == 0 && threadIdx.x == 0) atomicAdd(b.refresh_count + (only_due == 2 ? 1 : 0), 1ull);
     const int N = m.n_sites;
     const int n = spin == 0 ? m.n_up : m.n_dn;
     const int ldw = spin == 0 ? m.ld_up : m.ld_dn;
@@ -362,7 +362,7 @@ refresh_large_kernel(DevModel m, DevBatch b, int only_due, int track_drift) {
     const int spin = blockIdx.y;
     if (only_due == 1 && b.since[w] >= 0) return;
     if (only_due == 2 && !(b.status[w] & kStatusRefine)) return;
-    if (spin == 0 && threadIdx.x == 0 && only_due != 2) atomicAdd(b.refresh_count, 1ull);
+    if (spin == 0 && threadIdx.x == 0) atomicAdd(b.refresh_count + (only_due == 2 ? 1 : 0), 1ull);
     const int N = m.n_sites;
     const int n = spin == 0 ? m.n_up : m.n_dn;
     const int ldw = spin == 0 ? m.ld_up : m.ld_dn;

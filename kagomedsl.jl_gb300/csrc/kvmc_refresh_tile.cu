@@ -1,0 +1,581 @@
+// The periodic refresh of the mixed real form with tiled triangular solves
+// (kvmc.h: KVMC_TUNE_REFRESH32 = 2).
+//
+// Reference counterpart: reevaluateW! with tilde_U (KagomeDSL.jl
+// src/MonteCarlo.jl:55-115): W = U tilde_U^{-1}.  Only the rows of W at the
+// sites of the other spin are computed (the rest are unit rows); stacked as
+// the n_oth x n matrix X (row b = the site holding the other spin's label
+// b+1) they solve X tilde_U = B, B the rows of U at those sites.
+//
+// One CTA per (walker, spin), everything in FP32 (no FP64 operation but the
+// log|det| sum):
+//   1. tilde_U (FP32 high parts of U) gathered into an n x n block in HBM and
+//      factorised there by a blocked right-looking LU with partial pivoting,
+//      rows never moved (the pivot order is an index, perm): 32-column panels
+//      in shared memory, the trailing update as 4 x 4 register tiles.
+//      P tilde_U = L Uf with row i of P tilde_U = tilde_U[perm[i]].
+//   2. X in tiles of 32 rows held in shared memory.  V L Uf = B is solved as
+//      Z Uf = B (column blocks of 32 ascending: a GEMM update from the
+//      finished columns against the staged block column of Uf, then the
+//      32 x 32 triangle, one lane per column and the rows interleaved), then
+//      V L = Z (descending, unit lower L); X[:, perm[i]] = V[:, i].
+//   3. Iterative refinement: R = B - V (P tilde_U) with U as FP32 (high, low)
+//      pairs, every product exact (fmaf two-product) and the sums compensated
+//      (TwoSum), solved the same way for the correction D.  With d_k the
+//      largest |D| of pass k relative to its row's largest entry, the error
+//      left is about d_k^2 / d_{k-1} (the error contracts by a factor near
+//      cond(tilde_U) 2^-24 per pass, d_0 = 1); passes run until that is below
+//      1e-6, at most 4.  A tile left above 1e-5 (or whose correction grew)
+//      flags the walker (kStatusRefine) and the FP64 refresh redoes it.
+// Against one thread per row (kvmc_refresh32.cu) the O(n^2 (N - n)) solves
+// and residual run as tiles that reuse every operand staged in shared memory.
+// Each warp owns 4 rows of the tile, so the solves need no barrier beyond the
+// staging of the block column.
+#include <algorithm>
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "kvmc.h"
+#include "kvmc_device.cuh"
+#include "kvmc_internal.h"
+#include "kvmc_refine.cuh"
+
+namespace kvmc {
+
+namespace {
+
+constexpr int kTT = 256;       // threads per CTA (8 warps)
+constexpr int kPB = 32;        // LU panel width, column block of the solves and the residual
+constexpr int kRT = 32;        // rows per tile of X: 4 per warp
+constexpr int kLdc = kPB + 1;  // leading dimension of the staged block columns
+constexpr int kMaxPasses = 4; // refinement passes per tile at most
+
+__host__ __device__ inline int round4(int n) { return (n + 3) & ~3; }
+__host__ __device__ inline int ld_tile(int n) { return round4(n) + 4; }
+
+// Copies `rows` rows of up to 32 columns into shared memory: dst[k * ld + c]
+// = src(k)[c] for c < nc, zero where src(k) is null or nc <= c < wc; columns
+// from wc on are not written.  Each thread issues up to 8 global loads
+// before its first store, so that their latencies overlap.
+template <typename Src>
+__device__ __forceinline__ void stage_rows32(float *dst, int ld, int rows, int nc, int wc, Src src) {
+    constexpr int kB = 8;
+    const int tid = threadIdx.x, nt = blockDim.x;
+    const int total = rows * 32;
+    for (int e0 = tid; e0 < total; e0 += nt * kB) {
+        float v[kB];
+#pragma unroll
+        for (int q = 0; q < kB; ++q) {
+            const int e = e0 + q * nt;
+            const int k = e >> 5, c = e & 31;
+            const float *p = (e < total && c < nc) ? src(k) : nullptr;
+            v[q] = p ? p[c] : 0.f;
+        }
+#pragma unroll
+        for (int q = 0; q < kB; ++q) {
+            const int e = e0 + q * nt;
+            if (e < total && (e & 31) < wc) dst[(e >> 5) * ld + (e & 31)] = v[q];
+        }
+    }
+}
+
+// Shared-memory layout (byte offsets, each a multiple of 16).
+struct TileSmem {
+    size_t z, r, pn, ut, uc, invd, perm, srow, site_of, site_oth, total;
+};
+
+__host__ __device__ inline TileSmem tile_smem_layout(int n, int n_oth) {
+    auto al = [](size_t x) { return (x + 15) / 16 * 16; };
+    TileSmem s{};
+    const size_t tile = al((size_t)kRT * ld_tile(n) * 4);
+    const size_t lu = al((size_t)n * kLdc * 4) + (size_t)kPB * 64 * 4;
+    s.z = 0;
+    s.r = tile;
+    s.pn = 0;  // the LU's panel lives where the tiles will be
+    s.ut = al((size_t)n * kLdc * 4);
+    size_t o = 2 * tile > lu ? 2 * tile : lu;
+    s.uc = o; o = al(o + (size_t)round4(n) * kLdc * 4);
+    s.invd = o; o = al(o + (size_t)n * 4);
+    s.perm = o; o = al(o + (size_t)n * 4);
+    s.srow = o; o = al(o + (size_t)n * 4);
+    s.site_of = o; o = al(o + (size_t)n * 2);
+    s.site_oth = o; o = al(o + (size_t)n_oth * 2);
+    s.total = o;
+    return s;
+}
+
+// P A = L Uf of A (n x n, row-major, lda = n, global memory) in FP32 with
+// partial pivoting (first maximal |pivot| wins).  Rows stay where they are:
+// row i of the factors is A[perm[i]].  Returns false on an exactly zero
+// pivot (every thread sees the same answer).
+__device__ __forceinline__ bool lu_blocked(float *A, int n, float *Pn, float *Ut, float *invd, int *perm) {
+    __shared__ int s_piv;
+    __shared__ float s_pmax, s_dinv;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nt = blockDim.x;
+    for (int i = tid; i < n; i += nt) perm[i] = i;
+    __syncthreads();
+    for (int pb = 0; pb < n; pb += kPB) {
+        const int nb = min(kPB, n - pb);
+        const int rp = n - pb;
+        stage_rows32(Pn, kLdc, rp, nb, 32, [&](int r) -> const float * { return A + (size_t)perm[pb + r] * n + pb; });
+        __syncthreads();
+        for (int k = 0; k < nb; ++k) {
+            if (warp == 0) {
+                float best = -1.f;
+                int bi = rp;
+                for (int i = k + lane; i < rp; i += 32) {
+                    const float v = fabsf(Pn[(size_t)i * kLdc + k]);
+                    if (v > best) { best = v; bi = i; }
+                }
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) {
+                    const float ob = __shfl_xor_sync(0xffffffffu, best, o);
+                    const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+                    if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
+                }
+                if (lane == 0) {
+                    s_piv = bi;
+                    s_pmax = best;
+                    s_dinv = best > 0.f ? 1.f / Pn[(size_t)bi * kLdc + k] : 0.f;
+                }
+            }
+            __syncthreads();
+            if (!(s_pmax > 0.f)) return false;
+            const int p = s_piv;
+            if (p != k) {
+                for (int j = tid; j < kPB; j += nt) {
+                    const float a = Pn[(size_t)k * kLdc + j];
+                    Pn[(size_t)k * kLdc + j] = Pn[(size_t)p * kLdc + j];
+                    Pn[(size_t)p * kLdc + j] = a;
+                }
+                if (tid == 0) { const int t = perm[pb + k]; perm[pb + k] = perm[pb + p]; perm[pb + p] = t; }
+            }
+            __syncthreads();
+            const float dinv = s_dinv;
+            for (int i = k + 1 + tid; i < rp; i += nt) {
+                const float l = Pn[(size_t)i * kLdc + k] * dinv;
+                Pn[(size_t)i * kLdc + k] = l;
+                for (int j = k + 1; j < nb; ++j)
+                    Pn[(size_t)i * kLdc + j] = fmaf(-l, Pn[(size_t)k * kLdc + j], Pn[(size_t)i * kLdc + j]);
+            }
+            __syncthreads();
+        }
+        for (int e = tid; e < rp * kPB; e += nt) {
+            const int r = e >> 5, c = e & 31;
+            if (c < nb) A[(size_t)perm[pb + r] * n + pb + c] = Pn[(size_t)r * kLdc + c];
+        }
+        const int c0 = pb + nb;
+        if (c0 < n) {
+            // U12 = L11^{-1} A12, one column per thread (rows perm[pb .. pb + nb))
+            for (int c = c0 + tid; c < n; c += nt) {
+                float x[kPB];
+#pragma unroll
+                for (int i = 0; i < kPB; ++i) x[i] = i < nb ? A[(size_t)perm[pb + i] * n + c] : 0.f;
+#pragma unroll
+                for (int i = 1; i < kPB; ++i) {
+                    float acc = x[i];
+#pragma unroll
+                    for (int k = 0; k < i; ++k) acc = fmaf(-Pn[(size_t)i * kLdc + k], x[k], acc);
+                    x[i] = acc;
+                }
+#pragma unroll
+                for (int i = 0; i < kPB; ++i)
+                    if (i < nb) A[(size_t)perm[pb + i] * n + c] = x[i];
+            }
+            __syncthreads();
+            // A22 -= L21 U12: 64-column tiles of U12 in shared memory, 4 x 4 per thread
+            const int tx = tid & 15, ty = tid >> 4;
+            for (int cb = c0; cb < n; cb += 64) {
+                const int ncol = min(64, n - cb);
+                for (int h = 0; h < 2; ++h)
+                    stage_rows32(Ut + 32 * h, 64, kPB, ncol - 32 * h, 32, [&](int k) -> const float * {
+                        return k < nb ? A + (size_t)perm[pb + k] * n + cb + 32 * h : nullptr;
+                    });
+                __syncthreads();
+                for (int rb = c0; rb < n; rb += 64) {
+                    // the A22 entries first, so that their loads overlap the products
+                    float acc[4][4] = {}, old[4][4];
+                    int rr[4];
+#pragma unroll
+                    for (int a = 0; a < 4; ++a) {
+                        rr[a] = min(rb + 4 * ty + a, n - 1);
+                        const float *Ar = A + (size_t)perm[rr[a]] * n;
+#pragma unroll
+                        for (int q = 0; q < 4; ++q) old[a][q] = Ar[min(cb + 4 * tx + q, n - 1)];
+                    }
+                    for (int k = 0; k < nb; ++k) {
+                        float lv[4];
+#pragma unroll
+                        for (int a = 0; a < 4; ++a) lv[a] = Pn[(size_t)(rr[a] - pb) * kLdc + k];
+                        const float4 uv = *reinterpret_cast<const float4 *>(Ut + k * 64 + 4 * tx);
+#pragma unroll
+                        for (int a = 0; a < 4; ++a) {
+                            acc[a][0] = fmaf(lv[a], uv.x, acc[a][0]);
+                            acc[a][1] = fmaf(lv[a], uv.y, acc[a][1]);
+                            acc[a][2] = fmaf(lv[a], uv.z, acc[a][2]);
+                            acc[a][3] = fmaf(lv[a], uv.w, acc[a][3]);
+                        }
+                    }
+#pragma unroll
+                    for (int a = 0; a < 4; ++a) {
+                        const int r = rb + 4 * ty + a;
+                        if (r >= n) continue;
+                        float *Ar = A + (size_t)perm[r] * n;
+#pragma unroll
+                        for (int q = 0; q < 4; ++q) {
+                            const int c = cb + 4 * tx + q;
+                            if (c < n) Ar[c] = old[a][q] - acc[a][q];
+                        }
+                    }
+                }
+                __syncthreads();
+            }
+        }
+        __syncthreads();
+    }
+    for (int i = tid; i < n; i += nt) invd[i] = 1.f / A[(size_t)perm[i] * n + i];
+    __syncthreads();
+    return true;
+}
+
+// Z := Z (L Uf)^{-1} for the tile (rows x n, leading dimension ldz): forward
+// with Uf, backward with the unit lower L, in pivot order.  Warp g owns rows
+// g, g + 8, g + 16, g + 24; lane = column within the block.  Uc stages one
+// block column of the factors.  Columns n .. round4(n) of Z are zero.
+__device__ __forceinline__ void tile_solve(const float *A, const int *perm, int n, const float *invd, float *Z, int ldz, int rows,
+                           float *Uc) {
+    const int tid = threadIdx.x, lane = tid & 31, g = tid >> 5, nt = blockDim.x;
+    const int n4 = round4(n);
+    for (int jb = 0; jb < n; jb += kPB) {
+        const int nb = min(kPB, n - jb);
+        const int kr = jb + nb;
+        __syncthreads();
+        stage_rows32(Uc, kLdc, kr, nb, 32, [&](int k) -> const float * { return A + (size_t)perm[k] * n + jb; });
+        __syncthreads();
+        float acc[4] = {0.f, 0.f, 0.f, 0.f};
+        for (int k = 0; k < jb; k += 4) {
+            const float u0 = Uc[(k + 0) * kLdc + lane], u1 = Uc[(k + 1) * kLdc + lane];
+            const float u2 = Uc[(k + 2) * kLdc + lane], u3 = Uc[(k + 3) * kLdc + lane];
+#pragma unroll
+            for (int a = 0; a < 4; ++a) {
+                const float4 z = *reinterpret_cast<const float4 *>(Z + (size_t)(g + 8 * a) * ldz + k);
+                acc[a] = fmaf(z.x, u0, acc[a]);
+                acc[a] = fmaf(z.y, u1, acc[a]);
+                acc[a] = fmaf(z.z, u2, acc[a]);
+                acc[a] = fmaf(z.w, u3, acc[a]);
+            }
+        }
+        float x[4];
+#pragma unroll
+        for (int a = 0; a < 4; ++a) {
+            const int r = g + 8 * a;
+            x[a] = (r < rows && lane < nb) ? Z[(size_t)r * ldz + jb + lane] - acc[a] : 0.f;
+        }
+        for (int j = 0; j < nb; ++j) {
+            const float uj = Uc[(jb + j) * kLdc + lane];
+            const float dj = invd[jb + j];
+#pragma unroll
+            for (int a = 0; a < 4; ++a) {
+                const float xj = __shfl_sync(0xffffffffu, x[a], j) * dj;
+                x[a] = lane == j ? xj : (lane > j ? fmaf(-xj, uj, x[a]) : x[a]);
+            }
+        }
+#pragma unroll
+        for (int a = 0; a < 4; ++a) {
+            const int r = g + 8 * a;
+            if (r < rows && lane < nb) Z[(size_t)r * ldz + jb + lane] = x[a];
+        }
+    }
+    const int last = ((n - 1) / kPB) * kPB;
+    for (int jb = last; jb >= 0; jb -= kPB) {
+        const int nb = min(kPB, n - jb);
+        const int kr = n4 - jb;
+        __syncthreads();
+        stage_rows32(Uc, kLdc, kr, nb, 32, [&](int k) -> const float * {
+            return jb + k < n ? A + (size_t)perm[jb + k] * n + jb : nullptr;
+        });
+        __syncthreads();
+        float acc[4] = {0.f, 0.f, 0.f, 0.f};
+        for (int k = jb + kPB; k < n4; k += 4) {
+            const float *u = Uc + (size_t)(k - jb) * kLdc + lane;
+            const float u0 = u[0], u1 = u[kLdc], u2 = u[2 * kLdc], u3 = u[3 * kLdc];
+#pragma unroll
+            for (int a = 0; a < 4; ++a) {
+                const float4 z = *reinterpret_cast<const float4 *>(Z + (size_t)(g + 8 * a) * ldz + k);
+                acc[a] = fmaf(z.x, u0, acc[a]);
+                acc[a] = fmaf(z.y, u1, acc[a]);
+                acc[a] = fmaf(z.z, u2, acc[a]);
+                acc[a] = fmaf(z.w, u3, acc[a]);
+            }
+        }
+        float x[4];
+#pragma unroll
+        for (int a = 0; a < 4; ++a) {
+            const int r = g + 8 * a;
+            x[a] = (r < rows && lane < nb) ? Z[(size_t)r * ldz + jb + lane] - acc[a] : 0.f;
+        }
+        for (int j = nb - 1; j > 0; --j) {
+            const float lj = Uc[j * kLdc + lane];
+#pragma unroll
+            for (int a = 0; a < 4; ++a) {
+                const float vj = __shfl_sync(0xffffffffu, x[a], j);
+                if (lane < j) x[a] = fmaf(-vj, lj, x[a]);
+            }
+        }
+#pragma unroll
+        for (int a = 0; a < 4; ++a) {
+            const int r = g + 8 * a;
+            if (r < rows && lane < nb) Z[(size_t)r * ldz + jb + lane] = x[a];
+        }
+    }
+    __syncthreads();
+}
+
+// R = B - V (P tilde_U) for the tile: row k of P tilde_U is U at site
+// srow[k], row r of B is U at site site_oth[b0 + r].  U enters as FP32
+// (high, low) pairs.  Per column block the high parts are staged and summed
+// with exact products and compensated sums; then the low parts (2^-24 of
+// the high ones) are staged and summed by plain FMA into the low word.
+__device__ __forceinline__ void tile_residual(const float *Uh, const float *Ul, int n, const int *srow, const short *site_oth, int b0,
+                              int rows, const float *V, float *R, int ldz, float *Uc) {
+    const int tid = threadIdx.x, lane = tid & 31, g = tid >> 5, nt = blockDim.x;
+    const int n4 = round4(n);
+    for (int cb = 0; cb < n; cb += kPB) {
+        const int nc = min(kPB, n - cb);
+        float hi[4] = {0.f, 0.f, 0.f, 0.f}, lo[4] = {0.f, 0.f, 0.f, 0.f};
+        for (int part = 0; part < 2; ++part) {
+            const float *Up = part == 0 ? Uh : Ul;
+            __syncthreads();
+            stage_rows32(Uc, kLdc, n4, nc, 32, [&](int k) -> const float * {
+                return k < n ? Up + (size_t)srow[k] * n + cb : nullptr;
+            });
+            __syncthreads();
+            if (part == 0) {
+                for (int k = 0; k < n4; k += 4) {
+                    const float u0 = Uc[(k + 0) * kLdc + lane], u1 = Uc[(k + 1) * kLdc + lane];
+                    const float u2 = Uc[(k + 2) * kLdc + lane], u3 = Uc[(k + 3) * kLdc + lane];
+#pragma unroll
+                    for (int a = 0; a < 4; ++a) {
+                        const float4 v = *reinterpret_cast<const float4 *>(V + (size_t)(g + 8 * a) * ldz + k);
+                        df_fma(v.x, u0, hi[a], lo[a]);
+                        df_fma(v.y, u1, hi[a], lo[a]);
+                        df_fma(v.z, u2, hi[a], lo[a]);
+                        df_fma(v.w, u3, hi[a], lo[a]);
+                    }
+                }
+            } else {
+                for (int k = 0; k < n4; k += 4) {
+                    const float u0 = Uc[(k + 0) * kLdc + lane], u1 = Uc[(k + 1) * kLdc + lane];
+                    const float u2 = Uc[(k + 2) * kLdc + lane], u3 = Uc[(k + 3) * kLdc + lane];
+#pragma unroll
+                    for (int a = 0; a < 4; ++a) {
+                        const float4 v = *reinterpret_cast<const float4 *>(V + (size_t)(g + 8 * a) * ldz + k);
+                        lo[a] = fmaf(v.x, u0, lo[a]);
+                        lo[a] = fmaf(v.y, u1, lo[a]);
+                        lo[a] = fmaf(v.z, u2, lo[a]);
+                        lo[a] = fmaf(v.w, u3, lo[a]);
+                    }
+                }
+            }
+        }
+#pragma unroll
+        for (int a = 0; a < 4; ++a) {
+            const int r = g + 8 * a;
+            if (r < rows && lane < nc) {
+                const size_t src = (size_t)site_oth[b0 + r] * n + cb + lane;
+                R[(size_t)r * ldz + cb + lane] = ((Uh[src] - hi[a]) - lo[a]) + Ul[src];
+            }
+        }
+    }
+    __syncthreads();
+}
+
+__global__ void __launch_bounds__(kTT) refresh_tile_kernel(DevModel m, DevBatch b, int only_due, int track_drift) {
+    const int w = blockIdx.x, spin = blockIdx.y;
+    if (only_due && b.since[w] >= 0) return;
+    if (spin == 0 && threadIdx.x == 0) atomicAdd(b.refresh_count, 1ull);
+    const int N = m.n_sites;
+    const int n = spin == 0 ? m.n_up : m.n_dn;
+    const int n_oth = N - n;
+    const int ldw = spin == 0 ? m.ld_up : m.ld_dn;
+    const float *Uh = spin == 0 ? m.U32_up_hi : m.U32_dn_hi;
+    const float *Ul = spin == 0 ? m.U32_up_lo : m.U32_dn_lo;
+    const short *kown = (spin == 0 ? b.kappa_up : b.kappa_dn) + (size_t)w * N;
+    const short *koth = (spin == 0 ? b.kappa_dn : b.kappa_up) + (size_t)w * N;
+    // during a one-warp sweep call the rows go to the label-indexed blocks
+    const bool cpt = b.compact != 0;
+    float *Wout = cpt ? b.G32 + (size_t)w * b.g_block + (spin == 0 ? 0 : (size_t)m.n_dn * m.ld_up)
+                      : b.W32 + (size_t)w * N * (m.ld_up + m.ld_dn) + (spin == 0 ? 0 : (size_t)N * m.ld_up);
+    // tilde_U and its factors: the FP64 refresh's row scratch (n x rows doubles >= n x n floats)
+    float *A = reinterpret_cast<float *>(b.solve_scratch + ((size_t)w * 2 + spin) * b.solve_block);
+
+    extern __shared__ __align__(16) unsigned char smem[];
+    const TileSmem L = tile_smem_layout(n, n_oth);
+    float *Z = reinterpret_cast<float *>(smem + L.z);
+    float *Rt = reinterpret_cast<float *>(smem + L.r);
+    float *Pn = reinterpret_cast<float *>(smem + L.pn);
+    float *Ut = reinterpret_cast<float *>(smem + L.ut);
+    float *Uc = reinterpret_cast<float *>(smem + L.uc);
+    float *invd = reinterpret_cast<float *>(smem + L.invd);
+    int *perm = reinterpret_cast<int *>(smem + L.perm);
+    int *srow = reinterpret_cast<int *>(smem + L.srow);
+    short *site_of = reinterpret_cast<short *>(smem + L.site_of);
+    short *site_oth = reinterpret_cast<short *>(smem + L.site_oth);
+    __shared__ int s_bad;
+    __shared__ double red[33];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nt = blockDim.x, nw = nt / 32;
+
+    // the sites holding each label of both spins
+    for (int i = tid; i < n; i += nt) site_of[i] = -1;
+    for (int i = tid; i < n_oth; i += nt) site_oth[i] = -1;
+    if (tid == 0) s_bad = 0;
+    __syncthreads();
+    for (int s = tid; s < N; s += nt) {
+        const int lw = kown[s], lt = koth[s];
+        if (lw >= 1 && lw <= n) site_of[lw - 1] = (short)s;
+        else if (lt >= 1 && lt <= n_oth) site_oth[lt - 1] = (short)s;
+    }
+    __syncthreads();
+    for (int i = tid; i < n; i += nt)
+        if (site_of[i] < 0) s_bad = 1;
+    for (int i = tid; i < n_oth; i += nt)
+        if (site_oth[i] < 0) s_bad = 1;
+    __syncthreads();
+    if (s_bad) {  // not a complete configuration: the FP64 refresh decides
+        if (tid == 0) atomicOr(&b.status[w], kStatusRefine);
+        return;
+    }
+    // tilde_U (high parts): row l = U at the site holding label l + 1
+    for (int l = warp; l < n; l += nw) {
+        const float *src = Uh + (size_t)site_of[l] * n;
+        float *dst = A + (size_t)l * n;
+        for (int c = lane; c < n; c += 32) dst[c] = src[c];
+    }
+    __syncthreads();
+    if (!lu_blocked(A, n, Pn, Ut, invd, perm)) {
+        if (tid == 0) atomicOr(&b.status[w], kStatusRefine);  // an exactly zero FP32 pivot
+        return;
+    }
+    for (int i = tid; i < n; i += nt) srow[i] = site_of[perm[i]];
+    {
+        // log|det tilde_U| and log(min|pivot| / max|pivot|) from the FP32 factors
+        double ldet = 0.0, dmin = INFINITY, dmaxp = 0.0;
+        for (int i = tid; i < n; i += nt) {
+            const float d = fabsf(A[(size_t)perm[i] * n + i]);
+            ldet += (double)logf(d);
+            dmin = fmin(dmin, (double)d);
+            dmaxp = fmax(dmaxp, (double)d);
+        }
+        ldet = block_sum(ldet, red);
+        dmin = -block_sum_max(-dmin, red);
+        dmaxp = block_sum_max(dmaxp, red);
+        if (tid == 0) {
+            b.logdet[4 * w + spin] = ldet;
+            b.logdet[4 * w + 2 + spin] = log(dmin / dmaxp);
+        }
+    }
+    const int ldz = ld_tile(n);
+    // the pad columns n .. ldz of both tiles stay zero
+    for (int e = tid; e < kRT * (ldz - n); e += nt) {
+        const int r = e / (ldz - n), c = n + e % (ldz - n);
+        Z[(size_t)r * ldz + c] = 0.f;
+        Rt[(size_t)r * ldz + c] = 0.f;
+    }
+    float dmax = 0.f;
+    bool converged = true;
+    for (int b0 = 0; b0 < n_oth; b0 += kRT) {
+        const int rows = min(kRT, n_oth - b0);
+        __syncthreads();
+        for (int cb = 0; cb < n; cb += 32)
+            stage_rows32(Z + cb, ldz, kRT, min(32, n - cb), min(32, n - cb), [&](int r) -> const float * {
+                return r < rows ? Uh + (size_t)site_oth[b0 + r] * n + cb : nullptr;
+            });
+        tile_solve(A, perm, n, invd, Z, ldz, rows, Uc);
+        // passes until the error left, estimated as d_k^2 / d_{k-1} from the
+        // relative corrections d_k (d_0 = 1: the error contracts by about
+        // the size of the first correction), is below 1e-6; at most 4
+        float est = 1.f, dprev = 1.f;
+        for (int pass = 0; pass < kMaxPasses; ++pass) {
+            tile_residual(Uh, Ul, n, srow, site_oth, b0, rows, Z, Rt, ldz, Uc);
+            tile_solve(A, perm, n, invd, Rt, ldz, rows, Uc);
+            // V += D; the largest correction relative to the row's largest entry
+            float rmax = 0.f;
+#pragma unroll
+            for (int a = 0; a < 4; ++a) {
+                const int r = warp + 8 * a;
+                if (r >= rows) continue;  // warp-uniform
+                float dm = 0.f, vm = 0.f;
+                for (int c = lane; c < n; c += 32) {
+                    const float d = Rt[(size_t)r * ldz + c];
+                    const float v = Z[(size_t)r * ldz + c] + d;
+                    Z[(size_t)r * ldz + c] = v;
+                    dm = fmaxf(dm, isfinite(v) ? fabsf(d) : INFINITY);
+                    vm = fmaxf(vm, fabsf(v));
+                }
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) {
+                    dm = fmaxf(dm, __shfl_xor_sync(0xffffffffu, dm, o));
+                    vm = fmaxf(vm, __shfl_xor_sync(0xffffffffu, vm, o));
+                }
+                // a non-finite row (fmaxf drops NaN) counts as not converged
+                const float q = dm / fmaxf(vm, 1e-30f);
+                rmax = isnan(q) ? INFINITY : fmaxf(rmax, q);
+            }
+            const float d = (float)block_sum_max((double)rmax, red);
+            est = d < dprev ? d * d / dprev : INFINITY;  // a correction that grows: diverging
+            dprev = d;
+            if (!(est > 1e-6f)) break;
+        }
+        if (!(est <= 1e-5f)) converged = false;
+        // the tile's rows out, in label order: X[:, perm[i]] = V[:, i]
+#pragma unroll
+        for (int a = 0; a < 4; ++a) {
+            const int r = warp + 8 * a;
+            if (r >= rows) continue;
+            float *wr = Wout + (size_t)(cpt ? b0 + r : site_oth[b0 + r]) * ldw;
+            for (int i = lane; i < n; i += 32) {
+                const float nv = Z[(size_t)r * ldz + i];
+                if (track_drift) dmax = fmaxf(dmax, fabsf(wr[perm[i]] - nv) / (1.f + fabsf(nv)));
+                wr[perm[i]] = nv;
+            }
+            if (!cpt)
+                for (int c = n + lane; c < ldw; c += 32) wr[c] = 0.f;
+        }
+    }
+    // unit rows at the sites holding this spin (site-indexed W only)
+    if (!cpt) {
+        for (int l = warp; l < n; l += nw) {
+            float *wr = Wout + (size_t)site_of[l] * ldw;
+            for (int c = lane; c < ldw; c += 32) {
+                const float nv = c == l ? 1.f : 0.f;
+                if (track_drift) dmax = fmaxf(dmax, fabsf(wr[c] - nv) / (1.f + fabsf(nv)));
+                wr[c] = nv;
+            }
+        }
+    }
+    if (track_drift) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) dmax = fmaxf(dmax, __shfl_xor_sync(0xffffffffu, dmax, o));
+        if (lane == 0 && dmax > 0.f) atomic_max_nonneg(&b.drift[w], dmax);
+    }
+    if (!converged && tid == 0) atomicOr(&b.status[w], kStatusRefine);
+}
+
+}  // namespace
+
+size_t refresh_tile_smem(const DevModel &m) {
+    const TileSmem a = tile_smem_layout(m.n_up, m.n_dn), c = tile_smem_layout(m.n_dn, m.n_up);
+    return std::max(a.total, c.total) + 64;
+}
+
+cudaError_t launch_refresh_tile(const DevModel &m, const DevBatch &b, int only_due, int track_drift,
+                                cudaStream_t stream) {
+    if (!m.U32_up_hi || !b.solve_scratch) return cudaErrorInvalidValue;
+    const size_t sm = refresh_tile_smem(m);
+    cudaError_t e = cudaFuncSetAttribute(refresh_tile_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    if (e != cudaSuccess) return e;
+    refresh_tile_kernel<<<dim3(b.n_walkers, 2), kTT, sm, stream>>>(m, b, only_due, track_drift);
+    return cudaGetLastError();
+}
+
+}  // namespace kvmc

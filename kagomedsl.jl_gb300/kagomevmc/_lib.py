@@ -81,7 +81,8 @@ class BatchDesc(C.Structure):
 class SweepStats(C.Structure):
     _fields_ = [("proposals", C.c_int64), ("accepted", C.c_int64), ("measurements", C.c_int64),
                 ("sum_energy", C.c_double), ("sum_energy2", C.c_double), ("refreshes", C.c_int64),
-                ("max_drift", C.c_double), ("bad_walkers", C.c_int32), ("launches", C.c_int32)]
+                ("max_drift", C.c_double), ("bad_walkers", C.c_int32), ("launches", C.c_int32),
+                ("fp64_redos", C.c_int64)]
 
 
 # name -> argtypes (all return c_int)

@@ -193,9 +193,12 @@ class Engine:
         """Delayed form: scan for the next move while the last one's factor column is written."""
         self._check(self._lib.kvmc_set_tuning(self.h, 2, int(bool(on))))
 
-    def set_refresh32(self, on: bool = True):
-        """Periodic refresh by FP32 iterative refinement (FP64 fallback per walker)."""
-        self._check(self._lib.kvmc_set_tuning(self.h, 4, int(bool(on))))
+    def set_refresh32(self, mode=True):
+        """Periodic refresh by FP32 iterative refinement (FP64 fallback per
+        walker): True / 1 = one thread per row, 2 or "tiled" = tiles of 32 rows
+        per CTA (faster from about 200 orbitals per spin), False / 0 = FP64."""
+        value = 2 if mode in (2, "tiled") else int(bool(mode))
+        self._check(self._lib.kvmc_set_tuning(self.h, 4, value))
 
     def set_tc_flush(self, on: bool = True):
         """W in HBM: rank-k flush on the tensor cores (tcgen05, 3xTF32)."""

@@ -604,14 +604,16 @@ def test_tensor_core_flush_refused_off_its_path(kv):
     eng.close()
 
 
+@pytest.mark.parametrize("mode", [1, 2])
 @pytest.mark.parametrize("N,placement", [(96, "hbm"), (216, "hbm"), (216, "chip"), (384, "hbm"), (864, "hbm")])
-def test_fp32_refinement_refresh(kv, N, placement):
-    """The periodic refresh by FP32 iterative refinement: W right after it within
-    5e-6 of the FP64 rebuild (relative to max(1, |W|)), and chains that follow the oracle."""
+def test_fp32_refinement_refresh(kv, N, placement, mode):
+    """The periodic refresh by FP32 iterative refinement, one thread per row (1)
+    or in tiles of 32 rows (2): W right after it within 5e-6 of the FP64
+    rebuild (relative to max(1, |W|)), and chains that follow the oracle."""
     walkers, seed, R = (8, 61, 64) if N < 864 else (4, 61, 32)
     ham = ham_for(kv, N)
     eng = kv.Engine(ham, walkers, precision="mixed", seed=seed, refresh_interval=R, w_placement=placement)
-    eng.set_refresh32(True)
+    eng.set_refresh32(mode)
     eng.set_drift_tolerance(1e9)        # no early refreshes: every walker refreshes exactly every R moves
     eng.init()
     ku0, kd0, _ = eng.get_state()
@@ -627,6 +629,40 @@ def test_fp32_refinement_refresh(kv, N, placement):
     for w in range(walkers):
         ch = m.new_chain(ku0[w], kd0[w])
         ch.run(seed, w, int(ct[w]), N // 2, N // 2, 0)
+        match += int(np.array_equal(ch.ku, ku1[w]) and np.array_equal(ch.kd, kd1[w]))
+    assert match >= walkers - 1
+    eng.close()
+
+
+@pytest.mark.parametrize("n1,n2,n_up", [(10, 5, 75), (10, 5, 77), (6, 3, 30), (4, 2, 12)])
+def test_tiled_refresh_ragged_sizes(kv, n1, n2, n_up):
+    """The tiled FP32 refresh where neither spin's orbital count nor the other
+    spin's row count is a multiple of 4 or 32 (N = 150 with 75 + 75 and
+    77 + 73 orbitals, N = 54 with 30 + 24, N = 24): W after a refresh of every
+    walker against the FP64 rebuild, and the chains against the oracle."""
+    lat = kv.DoubleKagome(1.0, n1, n2, (True, True), (False, True))
+    H = kv.Hmat(lat)
+    N = H.shape[0]
+    Uu, Ud = kv.orbitals(H, n_up, N - n_up)
+    ham = kv.Hamiltonian(n_up, N - n_up, Uu, Ud, H, kv.get_nn(H))
+    walkers, seed, R = 6, 17, 48
+    eng = kv.Engine(ham, walkers, precision="mixed", seed=seed, refresh_interval=R, w_placement="hbm")
+    eng.set_refresh32("tiled")
+    eng.set_drift_tolerance(1e9)
+    eng.init()
+    ku0, kd0, _ = eng.get_state()
+    st = eng.advance(2 * R)
+    assert st["refreshes"] >= 2 * walkers and st["bad_walkers"] == 0
+    ku1, kd1, ct = eng.get_state()
+    Wu, Wd = eng.get_w()
+    for w in range(walkers):
+        assert close(Wu[w], o.reevaluateW(Uu, ku1[w]), 5e-6), w
+        assert close(Wd[w], o.reevaluateW(Ud, kd1[w]), 5e-6), w
+    m = oracle_c.OracleModel(Uu, Ud, ham.nn)
+    match = 0
+    for w in range(walkers):
+        ch = m.new_chain(ku0[w], kd0[w])
+        ch.run(seed, w, int(ct[w]), min(n_up, N - n_up), min(n_up, N - n_up), 0)
         match += int(np.array_equal(ch.ku, ku1[w]) and np.array_equal(ch.kd, kd1[w]))
     assert match >= walkers - 1
     eng.close()

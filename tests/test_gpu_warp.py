@@ -131,17 +131,20 @@ def test_warp_matches_cta_kernel_walker_by_walker(kv):
         assert abs(e0[w] - e1[w]) <= 1e-4 * max(1.0, abs(e0[w]))
 
 
-@pytest.mark.parametrize("segment", [0, 16])
-def test_warp_accuracy_guard_refreshes_and_keeps_chains(kv, segment):
+@pytest.mark.parametrize("segment,refresh32", [(0, 1), (16, 1), (16, 2)])
+def test_warp_accuracy_guard_refreshes_and_keeps_chains(kv, segment, refresh32):
     """A guard every walker trips at almost every move (hi 1, lo 1000: some
     entry above 1 has always been seen, and a move's entries stay below
     1000).  The refresh it asks for waits for the end of the call, or of its
     segment of 16 moves: one refresh per walker per call or segment, exact
-    move counts, chains still the oracle's, W at the end the oracle's."""
+    move counts, chains still the oracle's, W at the end the oracle's.  The
+    refreshes inside the call write the label-indexed rows, by the FP32
+    refresh one thread per row (1) or in tiles (2)."""
     N, walkers, seed, A = 96, 8, 43, 300
     ham = ham_for(kv, N)
     eng = kv.Engine(ham, walkers, precision="mixed", seed=seed, refresh_interval=4096, delay_k=8,
                     w_placement="hbm")
+    eng.set_refresh32(refresh32)
     eng.set_warp_walkers(8)
     eng.set_accuracy_guard(1, 1000)
     eng.set_segment(segment)

@@ -34,7 +34,7 @@ def test_version(built):
 
     abi, arch = C.c_int32(), C.c_int32()
     assert kv.load().kvmc_version(C.byref(abi), C.byref(arch)) == 0
-    assert abi.value == 3 and arch.value == 1030
+    assert abi.value == 4 and arch.value == 1030
 
 
 @pytest.mark.parametrize("n1,n2,pbc,anti,B", [
