@@ -13,24 +13,26 @@
 //      factorised there by a blocked right-looking LU with partial pivoting,
 //      rows never moved (the pivot order is an index, perm): 32-column panels
 //      in shared memory, the trailing update as 4 x 4 register tiles.
-//      P tilde_U = L Uf with row i of P tilde_U = tilde_U[perm[i]].
-//   2. X in tiles of 32 rows held in shared memory.  V L Uf = B is solved as
-//      Z Uf = B (column blocks of 32 ascending: a GEMM update from the
+//      M = P tilde_U = L Uf with row i of M = tilde_U[perm[i]].
+//   2. G = M^{-1} (n x n, HBM) from identity rows in tiles of 32: forward
+//      with Uf (column blocks of 32 ascending: a GEMM update from the
 //      finished columns against the staged block column of Uf, then the
-//      32 x 32 triangle, one lane per column and the rows interleaved), then
-//      V L = Z (descending, unit lower L); X[:, perm[i]] = V[:, i].
-//   3. Iterative refinement: R = B - V (P tilde_U) with U as FP32 (high, low)
-//      pairs, every product exact (fmaf two-product) and the sums compensated
-//      (TwoSum), solved the same way for the correction D.  With d_k the
-//      largest |D| of pass k relative to its row's largest entry, the error
-//      left is about d_k^2 / d_{k-1} (the error contracts by a factor near
-//      cond(tilde_U) 2^-24 per pass, d_0 = 1); passes run until that is below
-//      1e-6, at most 4.  A tile left above 1e-5 (or whose correction grew)
-//      flags the walker (kStatusRefine) and the FP64 refresh redoes it.
-// Against one thread per row (kvmc_refresh32.cu) the O(n^2 (N - n)) solves
-// and residual run as tiles that reuse every operand staged in shared memory.
-// Each warp owns 4 rows of the tile, so the solves need no barrier beyond the
-// staging of the block column.
+//      32 x 32 triangle, one lane per column and the rows interleaved; the
+//      blocks left of the tile's diagonal are zero and skipped), then
+//      backward with the unit lower L.
+//   3. X in tiles of 32 rows held in shared memory: V = B G, then iterative
+//      refinement V += (B - V M) G, X[:, perm[i]] = V[:, i].  The residual
+//      B - V M takes U as FP32 (high, low) pairs and sums the high-part
+//      products without rounding error on a fixed grid (tile_residual).
+//      With d_k the largest correction of pass k relative to its row's
+//      largest entry, the error left is about d_k^2 / d_{k-1} (it contracts
+//      by a factor near cond(tilde_U) 2^-24 per pass, d_0 = 1); passes run
+//      until that is below 1e-6, at most 4.  A tile left above 1e-5 (or
+//      whose correction grew) flags the walker (kStatusRefine) and the FP64
+//      refresh redoes it.
+// Every pass is then two GEMM-shaped loops over 64 x 64 chunks of G or of
+// tilde_U, staged by cp.async into a double buffer while the previous chunk
+// is multiplied: 2 rows x 4 columns per thread, no serial dependency.
 #include <algorithm>
 #include <cstdint>
 #include <cuda_runtime.h>
@@ -44,14 +46,18 @@ namespace kvmc {
 
 namespace {
 
-constexpr int kTT = 256;       // threads per CTA (8 warps)
+constexpr int kTT = 256;                // threads per CTA
+constexpr int kNW = kTT / 32;           // warps per CTA
 constexpr int kPB = 32;        // LU panel width, column block of the solves and the residual
-constexpr int kRT = 32;        // rows per tile of X: 4 per warp
+constexpr int kRT = 32;        // rows per tile of X
+constexpr int kRW = kRT / kNW;  // rows of the tile each warp owns
 constexpr int kLdc = kPB + 1;  // leading dimension of the staged block columns
 constexpr int kMaxPasses = 4; // refinement passes per tile at most
+constexpr int kCB = 64;        // columns per block of the GEMM-shaped loops
+constexpr int kKC = 64;        // rows of G / tilde_U per staged chunk
 
 __host__ __device__ inline int round4(int n) { return (n + 3) & ~3; }
-__host__ __device__ inline int ld_tile(int n) { return round4(n) + 4; }
+__host__ __device__ inline int ld_tile(int n) { return round4(n); }
 
 // Copies `rows` rows of up to 32 columns into shared memory: dst[k * ld + c]
 // = src(k)[c] for c < nc, zero where src(k) is null or nc <= c < wc; columns
@@ -81,7 +87,7 @@ __device__ __forceinline__ void stage_rows32(float *dst, int ld, int rows, int n
 
 // Shared-memory layout (byte offsets, each a multiple of 16).
 struct TileSmem {
-    size_t z, r, pn, ut, uc, invd, perm, srow, site_of, site_oth, total;
+    size_t z, r, pn, ut, st, invd, perm, srow, site_of, site_oth, total;
 };
 
 __host__ __device__ inline TileSmem tile_smem_layout(int n, int n_oth) {
@@ -94,7 +100,10 @@ __host__ __device__ inline TileSmem tile_smem_layout(int n, int n_oth) {
     s.pn = 0;  // the LU's panel lives where the tiles will be
     s.ut = al((size_t)n * kLdc * 4);
     size_t o = 2 * tile > lu ? 2 * tile : lu;
-    s.uc = o; o = al(o + (size_t)round4(n) * kLdc * 4);
+    // the chunk double buffer (two buffers of high and low planes), or the
+    // block column of tile_solve
+    const size_t chunks = (size_t)2 * 2 * kKC * kCB * 4, bcol = (size_t)round4(n) * kLdc * 4;
+    s.st = o; o = al(o + (chunks > bcol ? chunks : bcol));
     s.invd = o; o = al(o + (size_t)n * 4);
     s.perm = o; o = al(o + (size_t)n * 4);
     s.srow = o; o = al(o + (size_t)n * 4);
@@ -192,7 +201,7 @@ __device__ __forceinline__ bool lu_blocked(float *A, int n, float *Pn, float *Ut
                         return k < nb ? A + (size_t)perm[pb + k] * n + cb + 32 * h : nullptr;
                     });
                 __syncthreads();
-                for (int rb = c0; rb < n; rb += 64) {
+                for (int rb = c0; rb < n; rb += 4 * (kTT / 16)) {
                     // the A22 entries first, so that their loads overlap the products
                     float acc[4][4] = {}, old[4][4];
                     int rr[4];
@@ -240,49 +249,51 @@ __device__ __forceinline__ bool lu_blocked(float *A, int n, float *Pn, float *Ut
 
 // Z := Z (L Uf)^{-1} for the tile (rows x n, leading dimension ldz): forward
 // with Uf, backward with the unit lower L, in pivot order.  Warp g owns rows
-// g, g + 8, g + 16, g + 24; lane = column within the block.  Uc stages one
-// block column of the factors.  Columns n .. round4(n) of Z are zero.
-__device__ __forceinline__ void tile_solve(const float *A, const int *perm, int n, const float *invd, float *Z, int ldz, int rows,
-                           float *Uc) {
-    const int tid = threadIdx.x, lane = tid & 31, g = tid >> 5, nt = blockDim.x;
+// g, g + kNW, ...; lane = column within the block.  Uc stages one
+// block column of the factors.  Columns n .. round4(n) of Z are zero, and
+// so are its columns left of j0 (a multiple of 32), which the forward
+// sweep then skips.
+__device__ __forceinline__ void tile_solve(const float *A, const int *perm, int n, const float *invd, float *Z, int ldz,
+                                           int rows, float *Uc, int j0) {
+    const int lane = threadIdx.x & 31, g = threadIdx.x >> 5;
     const int n4 = round4(n);
-    for (int jb = 0; jb < n; jb += kPB) {
+    for (int jb = j0; jb < n; jb += kPB) {
         const int nb = min(kPB, n - jb);
         const int kr = jb + nb;
         __syncthreads();
         stage_rows32(Uc, kLdc, kr, nb, 32, [&](int k) -> const float * { return A + (size_t)perm[k] * n + jb; });
         __syncthreads();
-        float acc[4] = {0.f, 0.f, 0.f, 0.f};
-        for (int k = 0; k < jb; k += 4) {
+        float acc[kRW] = {};
+        for (int k = j0; k < jb; k += 4) {
             const float u0 = Uc[(k + 0) * kLdc + lane], u1 = Uc[(k + 1) * kLdc + lane];
             const float u2 = Uc[(k + 2) * kLdc + lane], u3 = Uc[(k + 3) * kLdc + lane];
 #pragma unroll
-            for (int a = 0; a < 4; ++a) {
-                const float4 z = *reinterpret_cast<const float4 *>(Z + (size_t)(g + 8 * a) * ldz + k);
+            for (int a = 0; a < kRW; ++a) {
+                const float4 z = *reinterpret_cast<const float4 *>(Z + (size_t)(g + kNW * a) * ldz + k);
                 acc[a] = fmaf(z.x, u0, acc[a]);
                 acc[a] = fmaf(z.y, u1, acc[a]);
                 acc[a] = fmaf(z.z, u2, acc[a]);
                 acc[a] = fmaf(z.w, u3, acc[a]);
             }
         }
-        float x[4];
+        float x[kRW];
 #pragma unroll
-        for (int a = 0; a < 4; ++a) {
-            const int r = g + 8 * a;
+        for (int a = 0; a < kRW; ++a) {
+            const int r = g + kNW * a;
             x[a] = (r < rows && lane < nb) ? Z[(size_t)r * ldz + jb + lane] - acc[a] : 0.f;
         }
         for (int j = 0; j < nb; ++j) {
             const float uj = Uc[(jb + j) * kLdc + lane];
             const float dj = invd[jb + j];
 #pragma unroll
-            for (int a = 0; a < 4; ++a) {
+            for (int a = 0; a < kRW; ++a) {
                 const float xj = __shfl_sync(0xffffffffu, x[a], j) * dj;
                 x[a] = lane == j ? xj : (lane > j ? fmaf(-xj, uj, x[a]) : x[a]);
             }
         }
 #pragma unroll
-        for (int a = 0; a < 4; ++a) {
-            const int r = g + 8 * a;
+        for (int a = 0; a < kRW; ++a) {
+            const int r = g + kNW * a;
             if (r < rows && lane < nb) Z[(size_t)r * ldz + jb + lane] = x[a];
         }
     }
@@ -295,99 +306,262 @@ __device__ __forceinline__ void tile_solve(const float *A, const int *perm, int 
             return jb + k < n ? A + (size_t)perm[jb + k] * n + jb : nullptr;
         });
         __syncthreads();
-        float acc[4] = {0.f, 0.f, 0.f, 0.f};
+        float acc[kRW] = {};
         for (int k = jb + kPB; k < n4; k += 4) {
             const float *u = Uc + (size_t)(k - jb) * kLdc + lane;
             const float u0 = u[0], u1 = u[kLdc], u2 = u[2 * kLdc], u3 = u[3 * kLdc];
 #pragma unroll
-            for (int a = 0; a < 4; ++a) {
-                const float4 z = *reinterpret_cast<const float4 *>(Z + (size_t)(g + 8 * a) * ldz + k);
+            for (int a = 0; a < kRW; ++a) {
+                const float4 z = *reinterpret_cast<const float4 *>(Z + (size_t)(g + kNW * a) * ldz + k);
                 acc[a] = fmaf(z.x, u0, acc[a]);
                 acc[a] = fmaf(z.y, u1, acc[a]);
                 acc[a] = fmaf(z.z, u2, acc[a]);
                 acc[a] = fmaf(z.w, u3, acc[a]);
             }
         }
-        float x[4];
+        float x[kRW];
 #pragma unroll
-        for (int a = 0; a < 4; ++a) {
-            const int r = g + 8 * a;
+        for (int a = 0; a < kRW; ++a) {
+            const int r = g + kNW * a;
             x[a] = (r < rows && lane < nb) ? Z[(size_t)r * ldz + jb + lane] - acc[a] : 0.f;
         }
         for (int j = nb - 1; j > 0; --j) {
             const float lj = Uc[j * kLdc + lane];
 #pragma unroll
-            for (int a = 0; a < 4; ++a) {
+            for (int a = 0; a < kRW; ++a) {
                 const float vj = __shfl_sync(0xffffffffu, x[a], j);
                 if (lane < j) x[a] = fmaf(-vj, lj, x[a]);
             }
         }
 #pragma unroll
-        for (int a = 0; a < 4; ++a) {
-            const int r = g + 8 * a;
+        for (int a = 0; a < kRW; ++a) {
+            const int r = g + kNW * a;
             if (r < rows && lane < nb) Z[(size_t)r * ldz + jb + lane] = x[a];
         }
     }
     __syncthreads();
 }
 
-// R = B - V (P tilde_U) for the tile: row k of P tilde_U is U at site
-// srow[k], row r of B is U at site site_oth[b0 + r].  U enters as FP32
-// (high, low) pairs.  Per column block the high parts are staged and summed
-// with exact products and compensated sums; then the low parts (2^-24 of
-// the high ones) are staged and summed by plain FMA into the low word.
-__device__ __forceinline__ void tile_residual(const float *Uh, const float *Ul, int n, const int *srow, const short *site_oth, int b0,
-                              int rows, const float *V, float *R, int ldz, float *Uc) {
-    const int tid = threadIdx.x, lane = tid & 31, g = tid >> 5, nt = blockDim.x;
-    const int n4 = round4(n);
-    for (int cb = 0; cb < n; cb += kPB) {
-        const int nc = min(kPB, n - cb);
-        float hi[4] = {0.f, 0.f, 0.f, 0.f}, lo[4] = {0.f, 0.f, 0.f, 0.f};
-        for (int part = 0; part < 2; ++part) {
-            const float *Up = part == 0 ? Uh : Ul;
-            __syncthreads();
-            stage_rows32(Uc, kLdc, n4, nc, 32, [&](int k) -> const float * {
-                return k < n ? Up + (size_t)srow[k] * n + cb : nullptr;
-            });
-            __syncthreads();
-            if (part == 0) {
-                for (int k = 0; k < n4; k += 4) {
-                    const float u0 = Uc[(k + 0) * kLdc + lane], u1 = Uc[(k + 1) * kLdc + lane];
-                    const float u2 = Uc[(k + 2) * kLdc + lane], u3 = Uc[(k + 3) * kLdc + lane];
-#pragma unroll
-                    for (int a = 0; a < 4; ++a) {
-                        const float4 v = *reinterpret_cast<const float4 *>(V + (size_t)(g + 8 * a) * ldz + k);
-                        df_fma(v.x, u0, hi[a], lo[a]);
-                        df_fma(v.y, u1, hi[a], lo[a]);
-                        df_fma(v.z, u2, hi[a], lo[a]);
-                        df_fma(v.w, u3, hi[a], lo[a]);
-                    }
-                }
-            } else {
-                for (int k = 0; k < n4; k += 4) {
-                    const float u0 = Uc[(k + 0) * kLdc + lane], u1 = Uc[(k + 1) * kLdc + lane];
-                    const float u2 = Uc[(k + 2) * kLdc + lane], u3 = Uc[(k + 3) * kLdc + lane];
-#pragma unroll
-                    for (int a = 0; a < 4; ++a) {
-                        const float4 v = *reinterpret_cast<const float4 *>(V + (size_t)(g + 8 * a) * ldz + k);
-                        lo[a] = fmaf(v.x, u0, lo[a]);
-                        lo[a] = fmaf(v.y, u1, lo[a]);
-                        lo[a] = fmaf(v.z, u2, lo[a]);
-                        lo[a] = fmaf(v.w, u3, lo[a]);
-                    }
-                }
-            }
-        }
-#pragma unroll
-        for (int a = 0; a < 4; ++a) {
-            const int r = g + 8 * a;
-            if (r < rows && lane < nc) {
-                const size_t src = (size_t)site_oth[b0 + r] * n + cb + lane;
-                R[(size_t)r * ldz + cb + lane] = ((Uh[src] - hi[a]) - lo[a]) + Ul[src];
-            }
-        }
+// 4-byte asynchronous copy global -> shared; ok = false writes a zero.
+__device__ __forceinline__ void cp_async4(float *dst, const float *src, bool ok) {
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" ::"r"(d), "l"(src), "r"(ok ? 4 : 0) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
+
+// Chunk (k0 .. k0 + kKC) x (c0 .. c0 + kCB) of a matrix whose row k is
+// row(k) (n columns), into buf (row stride kCB); zero outside n x n.
+template <typename Row>
+__device__ __forceinline__ void stage_chunk(float *buf, int n, int k0, int c0, Row row) {
+    for (int e = threadIdx.x; e < kKC * kCB; e += kTT) {
+        const int k = k0 + (e >> 6), c = c0 + (e & 63);
+        const bool ok = k < n && c < n;
+        const float *src = row(ok ? k : 0);
+        cp_async4(buf + e, ok ? src + c : src, ok);
     }
-    __syncthreads();
+}
+
+// The loop both GEMM-shaped phases share: for each 64-column block, the
+// k-chunks of the right operand are staged by cp.async into one half of
+// the double buffer while the other half is multiplied.  body(buf, kc, kn)
+// multiplies one staged chunk (kn rows); begin(cb) / end(cb) open and close
+// a column block.  Thread (rg = tid / 16, cg = tid % 16) owns tile rows rg
+// and rg + 16 and columns 4 cg .. 4 cg + 3 of the block.
+template <int kPlanes, typename Stage, typename Begin, typename Body, typename End>
+__device__ __forceinline__ void chunk_loop(int n, float *st, Stage stage, Begin begin, Body body, End end) {
+    const int n4 = round4(n);
+    const int ncb = (n + kCB - 1) / kCB, nkc = (n4 + kKC - 1) / kKC, S = ncb * nkc;
+    constexpr int kBuf = kPlanes * kKC * kCB;
+    __syncthreads();  // the buffer's previous users are done
+    stage(st, 0, 0);
+    cp_async_commit();
+    for (int s = 0; s < S; ++s) {
+        const int cbi = s / nkc, kci = s - cbi * nkc;
+        if (s + 1 < S) {
+            const int cn = (s + 1) / nkc, kn = (s + 1) - cn * nkc;
+            stage(st + ((s + 1) & 1) * kBuf, kn * kKC, cn * kCB);
+            cp_async_commit();
+            cp_async_wait<1>();
+        } else {
+            cp_async_wait<0>();
+        }
+        __syncthreads();
+        if (kci == 0) begin(cbi * kCB);
+        body(st + (s & 1) * kBuf, kci * kKC, min(kKC, n4 - kci * kKC));
+        if (kci == nkc - 1) end(cbi * kCB);
+        __syncthreads();  // this half is free for the chunk after next
+    }
+}
+
+// Out = In G (mode 0) or Out += In G (mode 1) for the tile; G (n x n,
+// row-major) in HBM.  Mode 1 returns, for the tile's first `rows` rows, the
+// largest |In G| relative to the row's largest |Out| (infinite when a row
+// is not finite); In and Out have leading dimension ldz.
+__device__ __forceinline__ float tile_gemm(const float *G, int n, const float *In, float *Out, int ldz, int rows,
+                                           int mode, float *st, double *red) {
+    const int tid = threadIdx.x, rg = tid >> 4, cg = tid & 15;
+    float acc[2][4];
+    float dm[2] = {0.f, 0.f}, vm[2] = {0.f, 0.f};
+    chunk_loop<1>(
+        n, st,
+        [&](float *buf, int k0, int c0) { stage_chunk(buf, n, k0, c0, [&](int k) { return G + (size_t)k * n; }); },
+        [&](int) {
+#pragma unroll
+            for (int i = 0; i < 2; ++i)
+#pragma unroll
+                for (int j = 0; j < 4; ++j) acc[i][j] = 0.f;
+        },
+        [&](const float *buf, int kc, int kn) {
+            const float *a0 = In + (size_t)rg * ldz + kc, *a1 = In + (size_t)(rg + 16) * ldz + kc;
+            for (int kk = 0; kk < kn; kk += 4) {
+                const float4 x0 = *reinterpret_cast<const float4 *>(a0 + kk);
+                const float4 x1 = *reinterpret_cast<const float4 *>(a1 + kk);
+                const float v0[4] = {x0.x, x0.y, x0.z, x0.w}, v1[4] = {x1.x, x1.y, x1.z, x1.w};
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    const float4 u = *reinterpret_cast<const float4 *>(buf + (kk + q) * kCB + 4 * cg);
+                    acc[0][0] = fmaf(v0[q], u.x, acc[0][0]);
+                    acc[0][1] = fmaf(v0[q], u.y, acc[0][1]);
+                    acc[0][2] = fmaf(v0[q], u.z, acc[0][2]);
+                    acc[0][3] = fmaf(v0[q], u.w, acc[0][3]);
+                    acc[1][0] = fmaf(v1[q], u.x, acc[1][0]);
+                    acc[1][1] = fmaf(v1[q], u.y, acc[1][1]);
+                    acc[1][2] = fmaf(v1[q], u.z, acc[1][2]);
+                    acc[1][3] = fmaf(v1[q], u.w, acc[1][3]);
+                }
+            }
+        },
+        [&](int cb) {
+#pragma unroll
+            for (int i = 0; i < 2; ++i) {
+                const int r = rg + 16 * i;
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    const int c = cb + 4 * cg + j;
+                    if (c >= n) continue;
+                    float *o = Out + (size_t)r * ldz + c;
+                    if (mode == 0) {
+                        *o = acc[i][j];
+                    } else {
+                        const float nv = *o + acc[i][j];
+                        *o = nv;
+                        if (r < rows) {
+                            dm[i] = fmaxf(dm[i], isfinite(nv) ? fabsf(acc[i][j]) : INFINITY);
+                            vm[i] = fmaxf(vm[i], fabsf(nv));
+                        }
+                    }
+                }
+            }
+        });
+    if (mode == 0) return 0.f;
+    // per row over its 16 threads (lanes of one half-warp), then over the rows
+    float q = 0.f;
+#pragma unroll
+    for (int i = 0; i < 2; ++i) {
+#pragma unroll
+        for (int o = 8; o > 0; o >>= 1) {
+            dm[i] = fmaxf(dm[i], __shfl_xor_sync(0xffffffffu, dm[i], o));
+            vm[i] = fmaxf(vm[i], __shfl_xor_sync(0xffffffffu, vm[i], o));
+        }
+        const float qi = dm[i] / fmaxf(vm[i], 1e-30f);
+        q = isnan(qi) ? INFINITY : fmaxf(q, qi);
+    }
+    return (float)block_sum_max((double)q, red);
+}
+
+// R = B - V M for the tile: row k of M is U at site srow[k], row r of B is U
+// at site site_oth[b0 + r] (rows from `rows` on are zero).  U enters as FP32
+// (high, low) pairs.
+//
+// The high-part products are summed without rounding error by splitting
+// each on a fixed grid (the extraction step of Rump, Ogita and Oishi's
+// accurate summation): for row r, sigma_r is a power of two with
+// sum_k |v_k u_kc| <= sigma_r / 4, which 4 ||v_r||_2 max_c ||u_:c||_2
+// bounds (cmax = the largest column norm of tilde_U).  Then t = fl(v u +
+// sigma) lies in [3/4, 5/4] sigma, q = t - sigma is exact and a multiple
+// of 2^-24 sigma, and every partial sum of the q stays below sigma / 2, so
+// hi = sum q is exact.  The remainders fl(v u - q) (at most 2^-24 sigma)
+// and the products with the low parts (2^-24 of the high ones) are summed
+// in lo.  Six FP32 operations per product.
+__device__ __forceinline__ void tile_residual(const float *Uh, const float *Ul, int n, const int *srow,
+                                              const short *site_oth, int b0, int rows, const float *V, float *R,
+                                              int ldz, float *st, float cmax) {
+    const int tid = threadIdx.x, rg = tid >> 4, cg = tid & 15;
+    float sg[2];
+#pragma unroll
+    for (int i = 0; i < 2; ++i) {
+        const float *vr = V + (size_t)(rg + 16 * i) * ldz;
+        float ss = 0.f;
+        for (int c = cg; c < n; c += 16) ss = fmaf(vr[c], vr[c], ss);
+#pragma unroll
+        for (int o = 8; o > 0; o >>= 1) ss += __shfl_xor_sync(0xffffffffu, ss, o);
+        const float x = 4.f * sqrtf(ss) * cmax * 1.0001f;
+        int e = 0;
+        frexpf(x, &e);                               // x = m 2^e, m in [1/2, 1)
+        sg[i] = x < INFINITY ? ldexpf(1.f, e) : x;   // a power of two >= x (0 for a zero row)
+    }
+    float hi[2][4], lo[2][4], bh[2][4], bl[2][4];
+    constexpr int kPlane = kKC * kCB;
+    chunk_loop<2>(
+        n, st,
+        [&](float *buf, int k0, int c0) {
+            stage_chunk(buf, n, k0, c0, [&](int k) { return Uh + (size_t)srow[k] * n; });
+            stage_chunk(buf + kPlane, n, k0, c0, [&](int k) { return Ul + (size_t)srow[k] * n; });
+        },
+        [&](int cb) {
+            // this block's entries of B, loaded now so that they arrive during the block
+#pragma unroll
+            for (int i = 0; i < 2; ++i) {
+                const int r = rg + 16 * i;
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    const int c = cb + 4 * cg + j;
+                    const bool ok = r < rows && c < n;
+                    const size_t src = ok ? (size_t)site_oth[b0 + r] * n + c : 0;
+                    bh[i][j] = ok ? Uh[src] : 0.f;
+                    bl[i][j] = ok ? Ul[src] : 0.f;
+                    hi[i][j] = 0.f;
+                    lo[i][j] = 0.f;
+                }
+            }
+        },
+        [&](const float *buf, int kc, int kn) {
+            const float *a0 = V + (size_t)rg * ldz + kc, *a1 = V + (size_t)(rg + 16) * ldz + kc;
+            for (int kk = 0; kk < kn; kk += 4) {
+                const float4 x0 = *reinterpret_cast<const float4 *>(a0 + kk);
+                const float4 x1 = *reinterpret_cast<const float4 *>(a1 + kk);
+                const float v[2][4] = {{x0.x, x0.y, x0.z, x0.w}, {x1.x, x1.y, x1.z, x1.w}};
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    const float4 uh4 = *reinterpret_cast<const float4 *>(buf + (kk + q) * kCB + 4 * cg);
+                    const float4 ul4 = *reinterpret_cast<const float4 *>(buf + kPlane + (kk + q) * kCB + 4 * cg);
+                    const float uh[4] = {uh4.x, uh4.y, uh4.z, uh4.w}, ul[4] = {ul4.x, ul4.y, ul4.z, ul4.w};
+#pragma unroll
+                    for (int i = 0; i < 2; ++i)
+#pragma unroll
+                        for (int j = 0; j < 4; ++j) {
+                            const float t = fmaf(v[i][q], uh[j], sg[i]);
+                            const float qq = t - sg[i];
+                            hi[i][j] += qq;
+                            lo[i][j] += fmaf(v[i][q], uh[j], -qq);
+                            lo[i][j] = fmaf(v[i][q], ul[j], lo[i][j]);
+                        }
+                }
+            }
+        },
+        [&](int cb) {
+#pragma unroll
+            for (int i = 0; i < 2; ++i) {
+                const int r = rg + 16 * i;
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    const int c = cb + 4 * cg + j;
+                    if (c < n) R[(size_t)r * ldz + c] = r < rows ? ((bh[i][j] - hi[i][j]) - lo[i][j]) + bl[i][j] : 0.f;
+                }
+            }
+        });
 }
 
 __global__ void __launch_bounds__(kTT) refresh_tile_kernel(DevModel m, DevBatch b, int only_due, int track_drift) {
@@ -406,7 +580,7 @@ __global__ void __launch_bounds__(kTT) refresh_tile_kernel(DevModel m, DevBatch 
     const bool cpt = b.compact != 0;
     float *Wout = cpt ? b.G32 + (size_t)w * b.g_block + (spin == 0 ? 0 : (size_t)m.n_dn * m.ld_up)
                       : b.W32 + (size_t)w * N * (m.ld_up + m.ld_dn) + (spin == 0 ? 0 : (size_t)N * m.ld_up);
-    // tilde_U and its factors: the FP64 refresh's row scratch (n x rows doubles >= n x n floats)
+    // tilde_U's factors and G: the FP64 refresh's row scratch (n x rows doubles >= 2 n x n floats)
     float *A = reinterpret_cast<float *>(b.solve_scratch + ((size_t)w * 2 + spin) * b.solve_block);
 
     extern __shared__ __align__(16) unsigned char smem[];
@@ -415,7 +589,7 @@ __global__ void __launch_bounds__(kTT) refresh_tile_kernel(DevModel m, DevBatch 
     float *Rt = reinterpret_cast<float *>(smem + L.r);
     float *Pn = reinterpret_cast<float *>(smem + L.pn);
     float *Ut = reinterpret_cast<float *>(smem + L.ut);
-    float *Uc = reinterpret_cast<float *>(smem + L.uc);
+    float *St = reinterpret_cast<float *>(smem + L.st);
     float *invd = reinterpret_cast<float *>(smem + L.invd);
     int *perm = reinterpret_cast<int *>(smem + L.perm);
     int *srow = reinterpret_cast<int *>(smem + L.srow);
@@ -457,6 +631,24 @@ __global__ void __launch_bounds__(kTT) refresh_tile_kernel(DevModel m, DevBatch 
         return;
     }
     for (int i = tid; i < n; i += nt) srow[i] = site_of[perm[i]];
+    // the largest column norm of tilde_U, for the residual's summation grid
+    __shared__ float s_cmax;
+    {
+        float cm = 0.f;
+        for (int c = tid; c < n; c += nt) {
+            float ss = 0.f;
+#pragma unroll 8
+            for (int l = 0; l < n; ++l) {
+                const float u = Uh[(size_t)site_of[l] * n + c];
+                ss = fmaf(u, u, ss);
+            }
+            cm = fmaxf(cm, ss);
+        }
+        const float cm2 = (float)block_sum_max((double)cm, red);
+        if (tid == 0) s_cmax = sqrtf(cm2);
+        __syncthreads();
+    }
+    const float cmax = s_cmax;
     {
         // log|det tilde_U| and log(min|pivot| / max|pivot|) from the FP32 factors
         double ldet = 0.0, dmin = INFINITY, dmaxp = 0.0;
@@ -475,10 +667,21 @@ __global__ void __launch_bounds__(kTT) refresh_tile_kernel(DevModel m, DevBatch 
         }
     }
     const int ldz = ld_tile(n);
-    // the pad columns n .. ldz of both tiles stay zero
+    // G = M^{-1}, 32 identity rows at a time (pad columns n .. ldz stay zero)
+    float *G = A + (size_t)n * n;
+    for (int t0 = 0; t0 < n; t0 += kRT) {
+        const int rows = min(kRT, n - t0);
+        __syncthreads();
+        for (int e = tid; e < kRT * ldz; e += nt) {
+            const int r = e / ldz, c = e - r * ldz;
+            Z[e] = (r < rows && c == t0 + r) ? 1.f : 0.f;
+        }
+        tile_solve(A, perm, n, invd, Z, ldz, rows, St, t0);
+        for (int r = warp; r < rows; r += nw)
+            for (int c = lane; c < n; c += 32) G[(size_t)(t0 + r) * n + c] = Z[(size_t)r * ldz + c];
+    }
     for (int e = tid; e < kRT * (ldz - n); e += nt) {
         const int r = e / (ldz - n), c = n + e % (ldz - n);
-        Z[(size_t)r * ldz + c] = 0.f;
         Rt[(size_t)r * ldz + c] = 0.f;
     }
     float dmax = 0.f;
@@ -486,52 +689,25 @@ __global__ void __launch_bounds__(kTT) refresh_tile_kernel(DevModel m, DevBatch 
     for (int b0 = 0; b0 < n_oth; b0 += kRT) {
         const int rows = min(kRT, n_oth - b0);
         __syncthreads();
+        // B (high parts) into the residual tile, then V = B G
         for (int cb = 0; cb < n; cb += 32)
-            stage_rows32(Z + cb, ldz, kRT, min(32, n - cb), min(32, n - cb), [&](int r) -> const float * {
+            stage_rows32(Rt + cb, ldz, kRT, min(32, n - cb), min(32, n - cb), [&](int r) -> const float * {
                 return r < rows ? Uh + (size_t)site_oth[b0 + r] * n + cb : nullptr;
             });
-        tile_solve(A, perm, n, invd, Z, ldz, rows, Uc);
+        tile_gemm(G, n, Rt, Z, ldz, rows, 0, St, red);
         // passes until the error left, estimated as d_k^2 / d_{k-1} from the
-        // relative corrections d_k (d_0 = 1: the error contracts by about
-        // the size of the first correction), is below 1e-6; at most 4
+        // relative corrections d_k, is below 1e-6; at most kMaxPasses
         float est = 1.f, dprev = 1.f;
         for (int pass = 0; pass < kMaxPasses; ++pass) {
-            tile_residual(Uh, Ul, n, srow, site_oth, b0, rows, Z, Rt, ldz, Uc);
-            tile_solve(A, perm, n, invd, Rt, ldz, rows, Uc);
-            // V += D; the largest correction relative to the row's largest entry
-            float rmax = 0.f;
-#pragma unroll
-            for (int a = 0; a < 4; ++a) {
-                const int r = warp + 8 * a;
-                if (r >= rows) continue;  // warp-uniform
-                float dm = 0.f, vm = 0.f;
-                for (int c = lane; c < n; c += 32) {
-                    const float d = Rt[(size_t)r * ldz + c];
-                    const float v = Z[(size_t)r * ldz + c] + d;
-                    Z[(size_t)r * ldz + c] = v;
-                    dm = fmaxf(dm, isfinite(v) ? fabsf(d) : INFINITY);
-                    vm = fmaxf(vm, fabsf(v));
-                }
-#pragma unroll
-                for (int o = 16; o > 0; o >>= 1) {
-                    dm = fmaxf(dm, __shfl_xor_sync(0xffffffffu, dm, o));
-                    vm = fmaxf(vm, __shfl_xor_sync(0xffffffffu, vm, o));
-                }
-                // a non-finite row (fmaxf drops NaN) counts as not converged
-                const float q = dm / fmaxf(vm, 1e-30f);
-                rmax = isnan(q) ? INFINITY : fmaxf(rmax, q);
-            }
-            const float d = (float)block_sum_max((double)rmax, red);
+            tile_residual(Uh, Ul, n, srow, site_oth, b0, rows, Z, Rt, ldz, St, cmax);
+            const float d = tile_gemm(G, n, Rt, Z, ldz, rows, 1, St, red);  // V += R G
             est = d < dprev ? d * d / dprev : INFINITY;  // a correction that grows: diverging
             dprev = d;
             if (!(est > 1e-6f)) break;
         }
         if (!(est <= 1e-5f)) converged = false;
         // the tile's rows out, in label order: X[:, perm[i]] = V[:, i]
-#pragma unroll
-        for (int a = 0; a < 4; ++a) {
-            const int r = warp + 8 * a;
-            if (r >= rows) continue;
+        for (int r = warp; r < rows; r += nw) {
             float *wr = Wout + (size_t)(cpt ? b0 + r : site_oth[b0 + r]) * ldw;
             for (int i = lane; i < n; i += 32) {
                 const float nv = Z[(size_t)r * ldz + i];
