@@ -301,8 +301,9 @@ KVMC_API int kvmc_kernel_time(kvmc_handle *h, int32_t kind, double *total_ms, in
  *   and solves.  It also
  *   rebuilds W in kvmc_set_state and kvmc_init with given configurations
  *   (log|det| then from the FP32 factors); seeded starts and kvmc_refresh
- *   always use FP64.  The default is 1 for the mixed real form with at most
- *   128 orbitals per spin, else 0.
+ *   always use FP64.  The default for the mixed real form is 1 below 96
+ *   orbitals per spin and 2 from 96 on (while the tiles fit in shared
+ *   memory, up to about 540 orbitals); 0 for the other forms.
  *   KVMC_TUNE_WARP_WALKERS: 0 = one CTA per walker (the kernels above);
  *   1..14 = one warp per walker, this many walkers per CTA (mixed real form
  *   with delay_k 4..16).  Each warp keeps only W's non-trivial rows -- the

@@ -794,10 +794,18 @@ extern "C" int kvmc_create(const kvmc_model_desc *model, const kvmc_batch_desc *
     if (place == KVMC_W_ON_CHIP && !fits)
         return bail(h->fail(KVMC_ERR_UNSUPPORTED, "W cannot be kept on chip for this model and precision"));
     h->smem_w = fits && place != KVMC_W_HBM;
-    // the FP32 refresh by iterative refinement is the faster periodic refresh up
-    // to 128 orbitals per spin on GB300 (measured at 48 and 108; at 192 the FP64
-    // refresh is faster), so it is the default there
-    h->refresh32 = (h->mixed && !h->cplx && std::max(nu, nd) <= 128) ? 1 : 0;
+    // the FP32 refresh by iterative refinement is the faster periodic refresh of
+    // the mixed real form on GB300: one thread per row below 96 orbitals per spin
+    // (measured at 27 and 48), in tiles of 32 rows from 96 on (measured at 108,
+    // 192 and 432: 1.4x, 3.5x and 2.1x the FP64 refresh) while its tiles fit in
+    // shared memory, else the FP64 refresh
+    if (h->mixed && !h->cplx) {
+        const int nmax = std::max(nu, nd);
+        if (nmax < 96) h->refresh32 = kvmc::refresh32_supported(m) ? 1 : 0;
+        else h->refresh32 = kvmc::refresh_tile_smem(m) + 1024 <= (size_t)optin ? 2 : 0;
+    } else {
+        h->refresh32 = 0;
+    }
     if (h->cplx) {
         // complex orbitals: rank-1 (plain form, or delay_k 1) or delayed updates of depth 4 / 8 with W in HBM
         const int want = batch->delay_k;

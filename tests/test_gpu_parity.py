@@ -267,7 +267,7 @@ def test_qr_start_singular_message(kv):
 @pytest.mark.parametrize("precision", ["plain", "mixed"])
 @pytest.mark.parametrize("accept,key", [("reference", "E_per_site_reference_rule"), ("metropolis", "E_per_site_psi2")])
 def test_energy_matches_exact_enumeration(kv, golden, precision, accept, key):
-    """N=24: E/N within 3 standard errors of the exact value for the rule's stationary law."""
+    """N=24: E/N within 2 standard errors of the exact value for the rule's stationary law."""
     ham = ham_for(kv, 24)
     walkers = 2048
     eng = kv.Engine(ham, walkers, precision=precision, accept=accept, seed=99)
@@ -280,7 +280,7 @@ def test_energy_matches_exact_enumeration(kv, golden, precision, accept, key):
     e = m.mean() / 24
     se = m.std(ddof=1) / np.sqrt(walkers) / 24
     exact = golden["enum_N24"][key]
-    assert abs(e - exact) <= 3 * se + 1e-5, (e, exact, se)
+    assert abs(e - exact) <= 2 * se, (e, exact, se)
     eng.close()
 
 
