@@ -426,6 +426,8 @@ def batched_run(kv, seed, device, walkers=4096, moves=1024):
     random starts, once with the settings the workload names (delayed depth
     16, FP64-quality refresh every 64 accepted moves) and once with the
     autotuner's choice for this batch."""
+    import numpy as np
+
     from kagomevmc import autotune
 
     ham = kv.Hamiltonian.build(48, 48, kv.DoubleKagome(1.0, 8, 4, (True, True), (False, True)))
@@ -442,8 +444,40 @@ def batched_run(kv, seed, device, walkers=4096, moves=1024):
         out[label] = {"value": st["accepted"] / (ms * 1e-3), "unit": UNIT, "delay_k": eng.config()["delay_k"],
                       "refresh_interval": ch.refresh_interval, "placement": ch.placement, "threads": ch.threads}
         eng.close()
+    # as the workload is written: 500 warm-up and 2000 measured sweeps (one
+    # proposal each) per chain, E/N of the FMA and the 3xTF32 flush against
+    # the plain FP64 form on the same starts and proposal streams
+    energies, rates = {}, {}
+    for label in ("plain", "fma", "3xtf32"):
+        if label == "plain":
+            eng = kv.Engine(ham, walkers, precision="plain", seed=seed, device=device)
+        else:
+            eng = kv.Engine(ham, walkers, precision="mixed", seed=seed, device=device, delay_k=16,
+                            refresh_interval=64, w_placement="hbm")
+            eng.set_stream_threads(128)
+            eng.set_tc_flush(label == "3xtf32")
+        eng.init()
+        eng.sweep(500)
+        eng.reset_stats()
+        eng.region_start()
+        st = eng.sweep(2000)
+        ms = eng.region_stop()
+        ws = eng.walker_stats()
+        energies[label] = ws["sum_e"] / ws["n_meas"] / 96
+        rates[label] = st["accepted"] / (ms * 1e-3)
+        eng.close()
+    sweeps = {}
+    for label, e in energies.items():
+        row = {"E_per_site": float(e.mean()), "se": float(e.std(ddof=1) / np.sqrt(walkers)),
+               "accepted_moves_per_s": rates[label]}
+        if label != "plain":
+            d = e - energies["plain"]
+            row["dE_per_site_vs_plain"] = float(d.mean())
+            row["se_dE"] = float(d.std(ddof=1) / np.sqrt(walkers))
+            row["gate_pass"] = bool(abs(d.mean()) + 2 * row["se_dE"] <= 1e-4)
+        sweeps[label] = row
     return {"workload": f"kagome VMC, 4x4 doubled cells (N=96), {walkers} walkers, {moves} accepted moves per walker",
-            **out}
+            **out, "as_written_500_2000_sweeps": sweeps}
 
 
 def field_run(kv, seed, device, walkers=2048, moves=256):
