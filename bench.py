@@ -695,8 +695,10 @@ def gpu_arm(a):
                            if warp else {})},
         "refresh": {"ms": ref_ms, "launches": ref_n, "flop": refreshes * f_refresh,
                     "unit_work": "2*((2/3)n^3 + 2(N-n)n^2) flop per walker refresh (the FP64 algorithm's count)",
-                    "arithmetic": ("FP32 iterative refinement (FP32 LU and solves, exact-product compensated "
-                                   "residual), FP64 fallback per walker" if n <= 128 else "FP64 LU and solves")},
+                    "arithmetic": ("FP32 iterative refinement, one thread per row (FP32 LU and solves, "
+                                   "exact-product compensated residual), FP64 fallback per walker" if n < 96 else
+                                   "tiled FP32 iterative refinement (FP32 LU, explicit inverse, GEMM-shaped solves, "
+                                   "residual summed exactly on a fixed grid), FP64 fallback per walker")},
     }
     for k in kern.values():
         k["achieved_tflops"] = k["flop"] / (k["ms"] * 1e-3) / 1e12 if k["ms"] > 0 else None
