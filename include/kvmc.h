@@ -139,9 +139,10 @@ typedef struct {
     const double *U_down;  /* column-major n_sites x n_down */
     /* Imaginary parts, same layout; both NULL for real orbitals (B = 0).  A
      * non-NULL pointer makes the handle complex, as the reference's
-     * ComplexF64 W for B != 0 (src/Hamiltonian.jl:201-204, :325-327); a
-     * complex handle supports at most 112 orbitals per spin and rank-1
-     * updates (delay_k 0 or 1). */
+     * ComplexF64 W for B != 0 (src/Hamiltonian.jl:201-204, :325-327).  A
+     * complex handle refreshes W in FP64, tilde_U factorised in shared
+     * memory up to 112 orbitals per spin and blocked in HBM beyond; its
+     * mixed form takes delay_k 1 (rank-1), 4 or 8 (W in HBM). */
     const double *U_up_imag;
     const double *U_down_imag;
 } kvmc_model_desc;

@@ -614,9 +614,6 @@ extern "C" int kvmc_create(const kvmc_model_desc *model, const kvmc_batch_desc *
         return fail_global(KVMC_ERR_ARGUMENT, "intervals must be >= 0");
     if (std::max(nu, nd) > 2048)
         return fail_global(KVMC_ERR_UNSUPPORTED, "more than 2048 orbitals per spin is not supported by this build");
-    if ((model->U_up_imag || model->U_down_imag) && std::max(nu, nd) > kvmc::complex_max_orbitals())
-        return fail_global(KVMC_ERR_UNSUPPORTED, "complex orbitals: at most %d per spin (got %d)",
-                           kvmc::complex_max_orbitals(), std::max(nu, nd));
 
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
@@ -766,6 +763,11 @@ extern "C" int kvmc_create(const kvmc_model_desc *model, const kvmc_batch_desc *
     if (!h->cplx && kvmc::refresh_needs_large(m)) {
         const size_t nmax = (size_t)std::max(nu, nd);
         b.lu_block = nmax * nmax;
+        if ((rc = h->alloc(&b.lu_scratch, b.lu_block * 2 * (size_t)Wk))) return bail(rc);
+    } else if (h->cplx && kvmc::complex_refresh_needs_large(m)) {
+        // complex tilde_U factorised in HBM: n x n complex = 2 n^2 doubles per walker-spin
+        const size_t nmax = (size_t)std::max(nu, nd);
+        b.lu_block = 2 * nmax * nmax;
         if ((rc = h->alloc(&b.lu_scratch, b.lu_block * 2 * (size_t)Wk))) return bail(rc);
     }
     if (h->mixed) cudaMemset(b.W32, 0, wblock * Wk * sizeof(float));

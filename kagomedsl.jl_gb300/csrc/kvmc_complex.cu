@@ -27,8 +27,9 @@ template <> __device__ __forceinline__ cf to_out<cf>(cd v) { return cf{(float)v.
 // ---------------------------------------------------------------------------
 // Refresh: W = U * tilde_U^{-1}, complex FP64.  One CTA per (walker, spin);
 // tilde_U is LU-factorised with partial pivoting in shared memory (n <= 112
-// orbitals per spin fit), the rows at sites not holding this spin are solved
-// one thread per row from a column-major FP64 scratch block.
+// orbitals per spin fit; refresh_c_large_kernel below takes larger n), the
+// rows at sites not holding this spin are solved one thread per row from a
+// column-major FP64 scratch block.
 // ---------------------------------------------------------------------------
 constexpr int kThreadsC = 256;
 constexpr int kMaxComplexOrbitals = 112;
@@ -205,6 +206,273 @@ refresh_c_kernel(DevModel m, DevBatch b, int only_due, int track_drift) {
 size_t refresh_c_smem(const DevModel &m) {
     const int n = m.n_up > m.n_dn ? m.n_up : m.n_dn;
     return (size_t)n * (n + 1) * 16 + (size_t)n * 16 + 33 * 8 + (size_t)n * 4 + (size_t)m.n_sites * 2 + 32;
+}
+
+// ---------------------------------------------------------------------------
+// Refresh beyond 112 orbitals per spin: the same W = U tilde_U^{-1} with
+// tilde_U factorised in HBM (lu_scratch, n x n complex per walker-spin) by
+// a blocked right-looking LU with partial pivoting whose rows never move
+// (row i of the factors is A[perm[i]]): 16-column panels in shared memory,
+// the trailing update A22 -= L21 U12 in 2 x 2 complex register tiles
+// against 32-column slices of U12 staged in shared memory.  The rows at
+// sites not holding this spin are then solved one thread per row as in
+// refresh_c_kernel, reading the factors through perm.
+// ---------------------------------------------------------------------------
+constexpr int kPanelC = 16;
+constexpr int kPanelLd = kPanelC + 1;
+
+__device__ __forceinline__ bool lu_c_blocked(cd *A, int n, cd *Pn, cd *Ut, int *perm) {
+    __shared__ int s_piv;
+    __shared__ double s_pmax;
+    __shared__ cd s_dinv;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nt = blockDim.x;
+    for (int i = tid; i < n; i += nt) perm[i] = i;
+    __syncthreads();
+    for (int pb = 0; pb < n; pb += kPanelC) {
+        const int nb = min(kPanelC, n - pb);
+        const int rp = n - pb;
+        for (int e = tid; e < rp * kPanelC; e += nt) {
+            const int r = e / kPanelC, c = e - r * kPanelC;
+            Pn[(size_t)r * kPanelLd + c] = c < nb ? A[(size_t)perm[pb + r] * n + pb + c] : cd{0.0, 0.0};
+        }
+        __syncthreads();
+        for (int k = 0; k < nb; ++k) {
+            if (warp == 0) {
+                double best = -1.0;
+                int bi = rp;
+                for (int i = k + lane; i < rp; i += 32) {
+                    const double v = cabs1(Pn[(size_t)i * kPanelLd + k]);
+                    if (v > best) { best = v; bi = i; }
+                }
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) {
+                    const double ob = __shfl_xor_sync(0xffffffffu, best, o);
+                    const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+                    if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
+                }
+                if (lane == 0) {
+                    s_piv = bi;
+                    s_pmax = best;
+                    s_dinv = best > 0.0 ? cinv(Pn[(size_t)bi * kPanelLd + k]) : cd{0.0, 0.0};
+                }
+            }
+            __syncthreads();
+            if (!(s_pmax > 0.0)) return false;
+            const int p = s_piv;
+            if (p != k) {
+                for (int j = tid; j < kPanelC; j += nt) {
+                    const cd a = Pn[(size_t)k * kPanelLd + j];
+                    Pn[(size_t)k * kPanelLd + j] = Pn[(size_t)p * kPanelLd + j];
+                    Pn[(size_t)p * kPanelLd + j] = a;
+                }
+                if (tid == 0) { const int t = perm[pb + k]; perm[pb + k] = perm[pb + p]; perm[pb + p] = t; }
+            }
+            __syncthreads();
+            const cd dinv = s_dinv;
+            for (int i = k + 1 + tid; i < rp; i += nt) {
+                const cd l = cmul(Pn[(size_t)i * kPanelLd + k], dinv);
+                Pn[(size_t)i * kPanelLd + k] = l;
+                for (int j = k + 1; j < nb; ++j)
+                    Pn[(size_t)i * kPanelLd + j] = cfms(l, Pn[(size_t)k * kPanelLd + j], Pn[(size_t)i * kPanelLd + j]);
+            }
+            __syncthreads();
+        }
+        for (int e = tid; e < rp * kPanelC; e += nt) {
+            const int r = e / kPanelC, c = e - r * kPanelC;
+            if (c < nb) A[(size_t)perm[pb + r] * n + pb + c] = Pn[(size_t)r * kPanelLd + c];
+        }
+        const int c0 = pb + nb;
+        if (c0 < n) {
+            // U12 = L11^{-1} A12, one column per thread (nb = kPanelC here);
+            // each row is finished in place before the next reads it
+            for (int c = c0 + tid; c < n; c += nt) {
+                for (int i = 1; i < kPanelC; ++i) {
+                    cd *xi = A + (size_t)perm[pb + i] * n + c;
+                    cd acc = *xi;
+                    for (int k = 0; k < i; ++k)
+                        acc = cfms(Pn[(size_t)i * kPanelLd + k], A[(size_t)perm[pb + k] * n + c], acc);
+                    *xi = acc;
+                }
+            }
+            __syncthreads();
+            // A22 -= L21 U12: 32-column slices of U12, 2 x 2 complex per thread
+            const int tx = tid & 15, ty = tid >> 4, rstep = 2 * (nt >> 4);
+            for (int cb = c0; cb < n; cb += 32) {
+                const int ncol = min(32, n - cb);
+                for (int e = tid; e < kPanelC * 32; e += nt) {
+                    const int k = e >> 5, c = e & 31;
+                    Ut[e] = c < ncol ? A[(size_t)perm[pb + k] * n + cb + c] : cd{0.0, 0.0};
+                }
+                __syncthreads();
+                for (int rb = c0; rb < n; rb += rstep) {
+                    cd acc[2][2] = {};
+                    int rr[2];
+#pragma unroll
+                    for (int a = 0; a < 2; ++a) rr[a] = min(rb + 2 * ty + a, n - 1);
+#pragma unroll 4
+                    for (int k = 0; k < kPanelC; ++k) {
+                        const cd l0 = Pn[(size_t)(rr[0] - pb) * kPanelLd + k], l1 = Pn[(size_t)(rr[1] - pb) * kPanelLd + k];
+                        const cd u0 = Ut[k * 32 + 2 * tx], u1 = Ut[k * 32 + 2 * tx + 1];
+                        acc[0][0] = cfma(l0, u0, acc[0][0]);
+                        acc[0][1] = cfma(l0, u1, acc[0][1]);
+                        acc[1][0] = cfma(l1, u0, acc[1][0]);
+                        acc[1][1] = cfma(l1, u1, acc[1][1]);
+                    }
+#pragma unroll
+                    for (int a = 0; a < 2; ++a) {
+                        const int r = rb + 2 * ty + a;
+                        if (r >= n) continue;
+                        cd *Ar = A + (size_t)perm[r] * n;
+#pragma unroll
+                        for (int q = 0; q < 2; ++q) {
+                            const int c = cb + 2 * tx + q;
+                            if (c < n) {
+                                const cd o = Ar[c];
+                                Ar[c] = cd{o.x - acc[a][q].x, o.y - acc[a][q].y};
+                            }
+                        }
+                    }
+                }
+                __syncthreads();
+            }
+        }
+        __syncthreads();
+    }
+    return true;
+}
+
+template <typename OutC>
+__global__ void __launch_bounds__(kThreadsC)
+refresh_c_large_kernel(DevModel m, DevBatch b, int only_due, int track_drift) {
+    const int w = blockIdx.x, spin = blockIdx.y;
+    if (only_due && b.since[w] >= 0) return;
+    if (spin == 0 && threadIdx.x == 0) atomicAdd(b.refresh_count, 1ull);
+    const int N = m.n_sites;
+    const int n = spin == 0 ? m.n_up : m.n_dn;
+    const int ldw = spin == 0 ? m.ld_up : m.ld_dn;
+    const cd *U = reinterpret_cast<const cd *>(spin == 0 ? m.U_up : m.U_dn);
+    const short *kappa = (spin == 0 ? b.kappa_up : b.kappa_dn) + (size_t)w * N;
+    const size_t wblock = (size_t)N * (m.ld_up + m.ld_dn);
+    OutC *W = (sizeof(OutC) == 16 ? reinterpret_cast<OutC *>(b.W64) : reinterpret_cast<OutC *>(b.W32)) +
+              (size_t)w * wblock + (spin == 0 ? 0 : (size_t)N * m.ld_up);
+    cd *Y = reinterpret_cast<cd *>(b.solve_scratch) + ((size_t)w * 2 + spin) * (b.solve_block / 2);
+    cd *A = reinterpret_cast<cd *>(b.lu_scratch + ((size_t)w * 2 + spin) * b.lu_block);
+
+    extern __shared__ __align__(16) unsigned char smem[];
+    cd *Pn = reinterpret_cast<cd *>(smem);
+    cd *Ut = Pn + (size_t)n * kPanelLd;
+    cd *invd = Ut + kPanelC * 32;
+    double *red = reinterpret_cast<double *>(invd + n);
+    int *perm = reinterpret_cast<int *>(red + 33);
+    short *rows = reinterpret_cast<short *>(perm + n);
+    __shared__ int s_nrows;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nt = blockDim.x;
+
+    // tilde_U: row l = U at the site holding label l + 1 (rows of labels no
+    // site holds stay zero: an exactly singular tilde_U)
+    for (int e = tid; e < n * n; e += nt) A[e] = cd{0.0, 0.0};
+    __syncthreads();
+    for (int R = warp; R < N; R += nt / 32) {
+        const int l = kappa[R];
+        if (l >= 1 && l <= n)
+            for (int c = lane; c < n; c += 32) A[(size_t)(l - 1) * n + c] = U[(size_t)R * n + c];
+    }
+    __syncthreads();
+    if (!lu_c_blocked(A, n, Pn, Ut, perm)) {
+        if (tid == 0) {
+            atomicOr(&b.status[w], kStatusSingular);
+            b.logdet[4 * w + spin] = -INFINITY;
+            b.logdet[4 * w + 2 + spin] = -INFINITY;
+        }
+        return;
+    }
+    double ld = 0.0, dmin = INFINITY, dmaxp = 0.0;
+    for (int i = tid; i < n; i += nt) {
+        const cd d = A[(size_t)perm[i] * n + i];
+        invd[i] = cinv(d);
+        const double mag = hypot(d.x, d.y);
+        ld += log(mag);
+        dmin = fmin(dmin, mag);
+        dmaxp = fmax(dmaxp, mag);
+    }
+    ld = block_sum(ld, red);
+    dmin = -block_sum_max(-dmin, red);
+    dmaxp = block_sum_max(dmaxp, red);
+    if (tid == 0) {
+        b.logdet[4 * w + spin] = ld;
+        b.logdet[4 * w + 2 + spin] = log(dmin / dmaxp);
+        s_nrows = 0;
+    }
+    // sites not holding this spin, in site order
+    if (warp == 0) {
+        int base = 0;
+        for (int R0 = 0; R0 < N; R0 += 32) {
+            const int R = R0 + lane;
+            const bool un = R < N && kappa[R] == 0;
+            const unsigned bal = __ballot_sync(0xffffffffu, un);
+            if (un) rows[base + __popc(bal & ((1u << lane) - 1u))] = (short)R;
+            base += __popc(bal);
+        }
+        if (lane == 0) s_nrows = base;
+    }
+    // unit rows at occupied sites, zero padding
+    float dmax = 0.f;
+    for (int R = warp; R < N; R += nt / 32) {
+        const int l = kappa[R];
+        OutC *wr = W + (size_t)R * ldw;
+        if (l != 0) {
+            for (int c = lane; c < ldw; c += 32) {
+                const cd nv = cd{c == l - 1 ? 1.0 : 0.0, 0.0};
+                if (track_drift) {
+                    const OutC o = wr[c];
+                    dmax = fmaxf(dmax, (float)(hypot((double)o.x - nv.x, (double)o.y) / (1.0 + hypot(nv.x, nv.y))));
+                }
+                wr[c] = to_out<OutC>(nv);
+            }
+        } else {
+            for (int c = n + lane; c < ldw; c += 32) wr[c] = to_out<OutC>(cd{0.0, 0.0});
+        }
+    }
+    __syncthreads();
+    const int nrows = s_nrows;
+    // w * tilde_U = u: forward with Uf, backward with unit L (row i of the
+    // factors at A[perm[i]]), then w[perm[i]] = v[i]
+    for (int r = tid; r < nrows; r += nt) {
+        const int R = rows[r];
+        cd *y = Y + r;  // column-major: y[j * nrows]
+        for (int j = 0; j < n; ++j) y[(size_t)j * nrows] = U[(size_t)R * n + j];
+        for (int i = 0; i < n; ++i) {
+            const cd yi = cmul(y[(size_t)i * nrows], invd[i]);
+            y[(size_t)i * nrows] = yi;
+            const cd *Ai = A + (size_t)perm[i] * n;
+            for (int j = i + 1; j < n; ++j) y[(size_t)j * nrows] = cfms(yi, Ai[j], y[(size_t)j * nrows]);
+        }
+        for (int j = n - 1; j > 0; --j) {
+            const cd vj = y[(size_t)j * nrows];
+            const cd *Aj = A + (size_t)perm[j] * n;
+            for (int i = 0; i < j; ++i) y[(size_t)i * nrows] = cfms(vj, Aj[i], y[(size_t)i * nrows]);
+        }
+        OutC *wr = W + (size_t)R * ldw;
+        for (int i = 0; i < n; ++i) {
+            const cd nv = y[(size_t)i * nrows];
+            if (track_drift) {
+                const OutC o = wr[perm[i]];
+                dmax = fmaxf(dmax, (float)(hypot((double)o.x - nv.x, (double)o.y - nv.y) / (1.0 + hypot(nv.x, nv.y))));
+            }
+            wr[perm[i]] = to_out<OutC>(nv);
+        }
+    }
+    if (track_drift) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) dmax = fmaxf(dmax, __shfl_xor_sync(0xffffffffu, dmax, o));
+        if (lane == 0 && dmax > 0.f) atomic_max_nonneg(&b.drift[w], dmax);
+    }
+}
+
+size_t refresh_c_large_smem(const DevModel &m) {
+    const int n = m.n_up > m.n_dn ? m.n_up : m.n_dn;
+    return (size_t)n * kPanelLd * 16 + (size_t)kPanelC * 32 * 16 + (size_t)n * 16 + 33 * 8 + (size_t)n * 4 +
+           (size_t)m.n_sites * 2 + 32;
 }
 
 // ---------------------------------------------------------------------------
@@ -1040,12 +1308,34 @@ __global__ void apply_moves_c_kernel(DevModel m, DevBatch b, const int *moves) {
 // ---- launchers ----------------------------------------------------------------
 int complex_max_orbitals() { return kMaxComplexOrbitals; }
 
-size_t complex_refresh_smem(const DevModel &m) { return refresh_c_smem(m); }
+bool complex_refresh_needs_large(const DevModel &m) {
+    return (m.n_up > m.n_dn ? m.n_up : m.n_dn) > kMaxComplexOrbitals;
+}
+
+size_t complex_refresh_smem(const DevModel &m) {
+    return complex_refresh_needs_large(m) ? refresh_c_large_smem(m) : refresh_c_smem(m);
+}
 
 cudaError_t launch_refresh_c(const DevModel &m, const DevBatch &b, bool fp32_out, int only_due, int track_drift,
                              cudaStream_t stream) {
-    const size_t sm = refresh_c_smem(m);
     const dim3 grid(b.n_walkers, 2);
+    if (complex_refresh_needs_large(m)) {
+        if (!b.lu_scratch) return cudaErrorInvalidValue;
+        const size_t sm = refresh_c_large_smem(m);
+        if (fp32_out) {
+            cudaError_t e = cudaFuncSetAttribute(refresh_c_large_kernel<cf>,
+                                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+            if (e != cudaSuccess) return e;
+            refresh_c_large_kernel<cf><<<grid, kThreadsC, sm, stream>>>(m, b, only_due, track_drift);
+        } else {
+            cudaError_t e = cudaFuncSetAttribute(refresh_c_large_kernel<cd>,
+                                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+            if (e != cudaSuccess) return e;
+            refresh_c_large_kernel<cd><<<grid, kThreadsC, sm, stream>>>(m, b, only_due, track_drift);
+        }
+        return cudaGetLastError();
+    }
+    const size_t sm = refresh_c_smem(m);
     if (fp32_out) {
         cudaError_t e = cudaFuncSetAttribute(refresh_c_kernel<cf>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
         if (e != cudaSuccess) return e;

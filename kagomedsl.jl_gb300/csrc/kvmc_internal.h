@@ -177,7 +177,8 @@ cudaError_t launch_grad(const DevModel &m, const DevBatch &b, const GradModel &g
 // Complex orbitals (kvmc_complex.cu).  U_up / U_dn then point at interleaved
 // (re, im) pairs, W64 / W32 at complex FP64 / FP32 pairs, and solve_block
 // counts doubles (two per complex entry).
-int complex_max_orbitals();
+int complex_max_orbitals();   // the shared-memory complex refresh's limit
+bool complex_refresh_needs_large(const DevModel &m);   // beyond it: tilde_U factorised in HBM (lu_scratch)
 size_t complex_delayed_smem(const DevModel &m, int K);   // mixed complex form, W in HBM
 size_t complex_refresh_smem(const DevModel &m);
 cudaError_t launch_refresh_c(const DevModel &m, const DevBatch &b, bool fp32_out, int only_due, int track_drift,

@@ -47,9 +47,10 @@ def close(a, b, rel):
 
 
 @pytest.mark.parametrize("precision", ["plain", "mixed"])
-@pytest.mark.parametrize("cells", [(6, 3, 2), (8, 4, 4), (8, 8, 4)])
+@pytest.mark.parametrize("cells", [(6, 3, 2), (8, 4, 4), (8, 8, 4), (8, 10, 4), (12, 10, 2)])
 def test_complex_refresh_matches_oracle(kv, cells, precision):
-    """W = U tilde_U^{-1} in complex FP64 (N = 54, 96, 192)."""
+    """W = U tilde_U^{-1} in complex FP64 (N = 54, 96, 192; and N = 240, 360
+    with 122 and 181 orbitals, where tilde_U is factorised in HBM)."""
     ham = field_ham(kv, *cells)
     nw = 4
     starts = [o.seeded_start(13, w, ham.U_up, ham.U_down)[:2] for w in range(nw)]
@@ -221,4 +222,40 @@ def test_complex_delay_depths(kv):
         kv.Engine(ham, 2, precision="mixed", delay_k=12)
     eng = kv.Engine(ham, 2, precision="mixed", delay_k=0)
     assert eng.config()["delay_k"] == 8 and not eng.config()["w_on_chip"]
+    eng.close()
+
+
+@pytest.mark.parametrize("precision,delay_k", [("plain", 0), ("mixed", 4)])
+def test_complex_chains_beyond_the_shared_memory_refresh(kv, precision, delay_k):
+    """N = 240 in a field (122 + 118 orbitals, more than the 112 the
+    shared-memory complex refresh holds): chains against the complex C
+    oracle, with the blocked HBM refresh every 64 accepted moves (mixed) or
+    every n proposals (plain)."""
+    ham = field_ham(kv, 8, 10, 4)
+    walkers, proposals, seed = 6, 1500, 29
+    eng = kv.Engine(ham, walkers, precision=precision, seed=seed,
+                    refresh_interval=(64 if precision == "mixed" else 0), delay_k=delay_k)
+    eng.init()
+    ku0, kd0, _ = eng.get_state()
+    st = eng.sweep(proposals)
+    ku1, kd1, _ = eng.get_state()
+    ws = eng.walker_stats()
+    m = oracle_c.OracleModel(ham.U_up, ham.U_down, ham.nn, "cplx")
+    n_occ = min(ham.N_up, ham.N_down)
+    match = 0
+    for w in range(walkers):
+        ch = m.new_chain(ku0[w], kd0[w])
+        ch.run(seed, w, proposals, n_occ, n_occ, 0)
+        if np.array_equal(ch.ku, ku1[w]) and np.array_equal(ch.kd, kd1[w]):
+            match += 1
+            assert ch.c.accepted == ws["accepted"][w]
+            tol = 1e-8 if precision == "plain" else 1e-4
+            assert abs(ch.c.sum_e - ws["sum_e"][w]) <= tol * max(1.0, abs(ch.c.sum_e))
+    assert match >= walkers - (0 if precision == "plain" else 1)
+    assert st["bad_walkers"] == 0 and st["accepted"] > 0
+    Wu, Wd = eng.get_w()
+    tol = 1e-8 if precision == "plain" else 1e-3
+    for w in range(walkers):
+        assert close(Wu[w], o.reevaluateW(ham.U_up, ku1[w]), tol), w
+        assert close(Wd[w], o.reevaluateW(ham.U_down, kd1[w]), tol), w
     eng.close()
