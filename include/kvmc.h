@@ -321,10 +321,21 @@ KVMC_API int kvmc_kernel_time(kvmc_handle *h, int32_t kind, double *total_ms, in
  *   guard off (the default).
  *   KVMC_TUNE_SEGMENT: one-warp mode: kvmc_advance runs its moves in
  *   segments of this many accepted moves per walker, so a refresh the guard
- *   asks for waits at most one segment; 0 = the whole call (the default). */
+ *   asks for waits at most one segment; 0 = the whole call (the default).
+ *   KVMC_TUNE_DRIFT_SEVERE: one CTA per walker with delayed updates: a
+ *   unit-row deviation past the drift tolerance refreshes the walker at the
+ *   end of the kvmc_advance call when its remaining moves fit in an
+ *   interval, unless it is past the severe threshold, which refreshes at
+ *   once.  value > 0 sets that threshold to value tolerances; 0 (the
+ *   default) to max(100 tolerances, 1e-2).
+ *   KVMC_TUNE_CLUSTER: 0 (the default) or 2 / 4 = the mixed real form with
+ *   rank-1 updates (delay_k 1) keeps W on chip split over a thread-block
+ *   cluster of that many CTAs per walker (rows by site blocks in each CTA's
+ *   shared memory, read by the others over distributed shared memory). */
 enum kvmc_tuning { KVMC_TUNE_STREAM_THREADS = 1, KVMC_TUNE_PIPELINE = 2, KVMC_TUNE_TC_FLUSH = 3,
                    KVMC_TUNE_REFRESH32 = 4, KVMC_TUNE_WARP_WALKERS = 5, KVMC_TUNE_COND_HI = 6,
-                   KVMC_TUNE_COND_LO = 7, KVMC_TUNE_SEGMENT = 8 };
+                   KVMC_TUNE_COND_LO = 7, KVMC_TUNE_SEGMENT = 8, KVMC_TUNE_DRIFT_SEVERE = 9,
+                   KVMC_TUNE_CLUSTER = 10 };
 KVMC_API int kvmc_set_tuning(kvmc_handle *h, int32_t key, int32_t value);
 
 /* The settings a handle resolved at creation: refresh and measurement

@@ -45,6 +45,9 @@ const KVMC_W_HBM = Int32(2)
 const KVMC_TUNE_WARP_WALKERS = Int32(5)
 const KVMC_TUNE_COND_HI = Int32(6)
 const KVMC_TUNE_COND_LO = Int32(7)
+const KVMC_TUNE_REFRESH32 = Int32(4)
+const KVMC_TUNE_DRIFT_SEVERE = Int32(9)
+const KVMC_TUNE_CLUSTER = Int32(10)
 
 # the C structs, field for field (kvmc_lattice_desc, kvmc_link, kvmc_model_desc,
 # kvmc_batch_desc, kvmc_sweep_stats)

@@ -18,7 +18,7 @@ LIB = BUILD / "libkvmc.so"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-fvisibility=hidden", "-I", str(ROOT / "include"), "-I", str(CSRC)]
-SOURCES = ["kvmc_kernels.cu", "kvmc_warp.cu", "kvmc_complex.cu", "kvmc_grad.cu", "kvmc_refresh32.cu", "kvmc_refresh_tile.cu", "kvmc_api.cpp"]
+SOURCES = ["kvmc_kernels.cu", "kvmc_warp.cu", "kvmc_complex.cu", "kvmc_grad.cu", "kvmc_refresh32.cu", "kvmc_refresh_tile.cu", "kvmc_cluster.cu", "kvmc_api.cpp"]
 
 
 def nvcc() -> str:

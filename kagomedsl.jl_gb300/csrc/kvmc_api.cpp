@@ -51,6 +51,8 @@ struct kvmc_handle {
     int measure_every = 0;
     int delay_k = 1;  // mixed form: 1 = rank-1 updates, 4/8/12/16 = delayed-update depth
     float drift_tol = 1e-4f;  // delayed form: early refresh past this unit-row deviation
+    int drift_severe = 0;     // > 0: immediate refresh past this many tolerances; 0: max(100 tol, 1e-2)
+    int cluster = 0;          // mixed real form, rank-1: W split over a cluster of 2 or 4 CTAs
     int stream_threads = 256;  // W in HBM: threads per walker
     int pipeline = 1;          // delayed form: pipelined scan / factor-column write
     int tc_flush = 0;          // W in HBM: rank-k flush on the tensor cores
@@ -1020,6 +1022,8 @@ kvmc::SweepParams sweep_params(const kvmc_handle *h) {
     p.measure_every = h->measure_every;
     p.delay_k = h->delay_k;
     p.drift_tol = h->drift_tol;
+    p.cluster = h->cluster;
+    p.drift_severe = h->drift_severe > 0 ? (float)h->drift_severe * h->drift_tol : std::max(100.f * h->drift_tol, 1e-2f);
     p.stream_threads = h->stream_threads;
     p.pipeline = h->pipeline;
     p.tc_flush = h->tc_flush;
@@ -1262,7 +1266,7 @@ namespace {
 
 bool same_params(const kvmc::SweepParams &a, const kvmc::SweepParams &b) {
     return a.seed == b.seed && a.accept_rule == b.accept_rule && a.refresh_every == b.refresh_every &&
-           a.measure_every == b.measure_every && a.delay_k == b.delay_k && a.drift_tol == b.drift_tol &&
+           a.measure_every == b.measure_every && a.delay_k == b.delay_k && a.drift_tol == b.drift_tol && a.drift_severe == b.drift_severe && a.cluster == b.cluster &&
            a.stream_threads == b.stream_threads && a.pipeline == b.pipeline && a.tc_flush == b.tc_flush &&
            a.refresh32 == b.refresh32 && a.warp_walkers == b.warp_walkers && a.cond_hi == b.cond_hi &&
            a.cond_lo == b.cond_lo;
@@ -1497,6 +1501,25 @@ extern "C" int kvmc_set_tuning(kvmc_handle *h, int32_t key, int32_t value) {
         if (std::max(h->ld_up, h->ld_dn) > 4 * value)
             return h->fail(KVMC_ERR_ARGUMENT, "%d threads cannot flush %d columns", value, std::max(h->ld_up, h->ld_dn));
         h->stream_threads = value;
+        return KVMC_OK;
+    }
+    if (key == KVMC_TUNE_CLUSTER) {
+        if (value != 0 && value != 2 && value != 4) return h->fail(KVMC_ERR_ARGUMENT, "cluster size must be 0, 2 or 4");
+        if (value > 0) {
+            if (!h->mixed || h->cplx || h->delay_k != 1 || h->warp_walkers > 0)
+                return h->fail(KVMC_ERR_UNSUPPORTED,
+                               "the cluster sweep serves the mixed real form with rank-1 updates (delay_k 1)");
+            const size_t need = kvmc::sweep_cluster_smem(h->dm, value);
+            if (need + 1024 > (size_t)kvmc::max_smem_optin(h->device))
+                return h->fail(KVMC_ERR_UNSUPPORTED, "a cluster of %d CTAs needs %zu B shared memory per CTA", value,
+                               need);
+        }
+        h->cluster = value;
+        return KVMC_OK;
+    }
+    if (key == KVMC_TUNE_DRIFT_SEVERE) {
+        if (value < 0) return h->fail(KVMC_ERR_ARGUMENT, "the severe-drift factor must be >= 0");
+        h->drift_severe = value;
         return KVMC_OK;
     }
     if (key == KVMC_TUNE_REFRESH32) {

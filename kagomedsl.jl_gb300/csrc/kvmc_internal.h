@@ -90,12 +90,14 @@ struct SweepParams {
     int measure_every;    // proposals between energy samples
     int delay_k;          // mixed form: delayed-update depth (4, 8, 12, 16), else rank-1
     float drift_tol;      // delayed form: unit-row deviation that triggers an early refresh
+    float drift_severe;   // delayed form: a deviation past this refreshes at once even within a call
     int stream_threads;   // W in HBM: threads per walker's CTA (128 or 256)
     int pipeline;         // delayed form: scan for the next move while the last one's factor column is written
     int tc_flush;         // W in HBM: rank-k flush on the tensor cores (tcgen05, 3xTF32)
     int refresh32;        // mixed real form: FP32 refresh by iterative refinement (1 per row, 2 tiled)
     int warp_walkers;     // mixed real form: > 0 = one warp per walker, this many walkers per CTA (kvmc_warp.cu)
     float cond_hi, cond_lo;  // warp sweep's accuracy guard (0 = off), see kvmc_warp.cu
+    int cluster;          // mixed real form, rank-1: W split over a cluster of this many CTAs (0 = off)
 };
 
 // Launchers.  All enqueue on `stream` and return the launch error.
@@ -152,6 +154,10 @@ int warp_walkers_max(const DevModel &m, int K, int optin);
 cudaError_t launch_warp_convert(const DevModel &m, const DevBatch &b, bool to_compact, cudaStream_t stream);
 cudaError_t launch_sweep_warp(const DevModel &m, const DevBatch &b, const SweepParams &p, int *active,
                               cudaStream_t stream);
+// W's rows split over a thread-block cluster in distributed shared memory (kvmc_cluster.cu)
+size_t sweep_cluster_smem(const DevModel &m, int cluster);
+cudaError_t launch_sweep_cluster(const DevModel &m, const DevBatch &b, const SweepParams &p, int *active,
+                                 cudaStream_t stream);
 
 // Extra shared memory of the tensor-core flush (its operand tiles).
 size_t tc_flush_smem_bytes();

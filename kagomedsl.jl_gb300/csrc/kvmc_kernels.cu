@@ -1986,14 +1986,14 @@ sweep_pipe_kernel(DevModel m, DevBatch b, SweepParams p, int *active_count, int 
                 // this call still asks of the walker are fewer than an interval, at
                 // the end of the call (its counter then reaches R exactly with its
                 // last move, so refreshes stay on call boundaries and no walker stops
-                // mid-call), else now; a deviation past max(100 tolerances, 1e-2)
-                // (W losing its accuracy, as near a singular configuration)
-                // refreshes now in any case.  The other drift slot is free again
+                // mid-call), else now; a deviation past drift_severe (by default
+                // max(100 tolerances, 1e-2): W losing its accuracy, as near a
+                // singular configuration) refreshes now in any case.  The other drift slot is free again
                 // (everybody read it a flush ago).
                 const float dv = __int_as_float(*dev);
                 if (dv > p.drift_tol) {
                     const long long rem = acc_left - ctl.acc;
-                    const bool mild = dv <= fmaxf(100.f * p.drift_tol, 1e-2f);
+                    const bool mild = dv <= p.drift_severe;
                     ctl.since = (rem < R && mild) ? max(ctl.since, (int)(R - rem)) : R;
                 }
                 ctl.dev2[(fp & 1) ^ 1] = 0;
@@ -2281,6 +2281,7 @@ static cudaError_t launch_delayed(const DevModel &m, const DevBatch &b, const Sw
 cudaError_t launch_sweep(const DevModel &m, const DevBatch &b, const SweepParams &p, bool mixed,
                          bool smem_w, int *active, cudaStream_t stream) {
     if (!mixed) return launch_sweep_impl<double, false>(m, b, p, 1, active, 256, stream);
+    if (p.cluster > 0) return launch_sweep_cluster(m, b, p, active, stream);
     if (p.warp_walkers > 0) return launch_sweep_warp(m, b, p, active, stream);
     if (smem_w && p.delay_k == 4) return launch_delayed<4, false>(m, b, p, active, stream);
     if (smem_w && p.delay_k == 8) return launch_delayed<8, false>(m, b, p, active, stream);

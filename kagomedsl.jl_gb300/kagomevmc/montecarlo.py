@@ -200,6 +200,17 @@ class Engine:
         value = 2 if mode in (2, "tiled") else int(bool(mode))
         self._check(self._lib.kvmc_set_tuning(self.h, 4, value))
 
+    def set_cluster(self, ctas: int):
+        """Mixed real form with rank-1 updates (delay_k 1): W split over a
+        thread-block cluster of 2 or 4 CTAs per walker (0 = off)."""
+        self._check(self._lib.kvmc_set_tuning(self.h, 10, int(ctas)))
+
+    def set_drift_severe(self, factor: int):
+        """One CTA per walker, delayed form: a drift past `factor` tolerances
+        refreshes at once inside a call (0 = the default max(100 tol, 1e-2));
+        milder drift waits for the end of the call."""
+        self._check(self._lib.kvmc_set_tuning(self.h, 9, int(factor)))
+
     def set_tc_flush(self, on: bool = True):
         """W in HBM: rank-k flush on the tensor cores (tcgen05, 3xTF32)."""
         self._check(self._lib.kvmc_set_tuning(self.h, 3, int(bool(on))))

@@ -356,6 +356,37 @@ def test_advance_makes_exactly_the_asked_moves(kv, precision):
     eng.close()
 
 
+def test_severe_drift_refreshes_at_once_within_the_call(kv):
+    """The severe branch of the drift trigger: with the severe threshold set
+    to the tolerance itself, every check past the tolerance refreshes the
+    walker at once, so each walker is refreshed several times inside one
+    call; the move counts stay exact and the chains stay the oracle's."""
+    N, walkers, seed, A = 96, 8, 29, 200
+    ham = ham_for(kv, N)
+    eng = kv.Engine(ham, walkers, precision="mixed", seed=seed, refresh_interval=1024, delay_k=8, w_placement="hbm")
+    eng.set_drift_tolerance(1e-12)
+    eng.set_drift_severe(1)
+    eng.init()
+    ku0, kd0, _ = eng.get_state()
+    st = eng.advance(A)
+    assert st["accepted"] == walkers * A
+    # checks on every fourth flush of 8 moves: about A / 32 per walker
+    assert st["refreshes"] >= 3 * walkers, st["refreshes"]
+    ku1, kd1, ct = eng.get_state()
+    ws = eng.walker_stats()
+    assert np.all(ws["accepted"] == A)
+    m = oracle_c.OracleModel(ham.U_up, ham.U_down, ham.nn)
+    match = 0
+    for w in range(walkers):
+        ch = m.new_chain(ku0[w], kd0[w])
+        ch.run(seed, w, int(ct[w]), N // 2, N // 2)
+        match += int(np.array_equal(ch.ku, ku1[w]) and np.array_equal(ch.kd, kd1[w]))
+    assert match >= walkers - 1
+    with pytest.raises(kv.KvmcError):
+        eng.set_drift_severe(-1)
+    eng.close()
+
+
 def test_drift_triggered_refresh_waits_for_the_end_of_the_call(kv):
     """A drift tolerance every check exceeds: within a kvmc_advance call whose
     moves fit in the refresh interval the walkers do not stop, each is
@@ -665,4 +696,55 @@ def test_tiled_refresh_ragged_sizes(kv, n1, n2, n_up):
         ch.run(seed, w, int(ct[w]), min(n_up, N - n_up), min(n_up, N - n_up), 0)
         match += int(np.array_equal(ch.ku, ku1[w]) and np.array_equal(ch.kd, kd1[w]))
     assert match >= walkers - 1
+    eng.close()
+
+
+@pytest.mark.parametrize("N,ctas", [(96, 2), (216, 2), (216, 4), (384, 4)])
+def test_cluster_sweep_matches_oracle_and_the_one_cta_kernel(kv, N, ctas):
+    """W split over a thread-block cluster (rows by site blocks in each CTA's
+    shared memory, read by the others over DSMEM), rank-1 updates: chains
+    against the oracle, and against the one-CTA rank-1 kernel on the same
+    walkers, which does the same FP32 operations (identical chains, energy
+    sums within 1e-5: only the order of the energy reduction differs)."""
+    walkers, proposals, seed = 8, 2000, 37
+    ham = ham_for(kv, N)
+    out = []
+    for ct in (0, ctas):
+        eng = kv.Engine(ham, walkers, precision="mixed", seed=seed, refresh_interval=96, delay_k=1,
+                        w_placement="hbm")
+        if ct:
+            eng.set_cluster(ct)
+        eng.init()
+        ku0, kd0, _ = eng.get_state()
+        st = eng.sweep(proposals)
+        assert st["bad_walkers"] == 0
+        ku1, kd1, ct_ = eng.get_state()
+        ws = eng.walker_stats()
+        Wu, Wd = eng.get_w()
+        out.append((ku0, kd0, ku1, kd1, ws["sum_e"].copy(), ws["accepted"].copy(), Wu, Wd))
+        eng.close()
+    (a0, b0, a1, b1, e0, n0, _, _), (c0, d0, c1, d1, e1, n1, Wu, Wd) = out
+    assert np.array_equal(a1, c1) and np.array_equal(b1, d1) and np.array_equal(n0, n1)
+    assert np.all(np.abs(e0 - e1) <= 1e-5 * np.maximum(1.0, np.abs(e0)))
+    m = oracle_c.OracleModel(ham.U_up, ham.U_down, ham.nn)
+    match = 0
+    for w in range(walkers):
+        ch = m.new_chain(c0[w], d0[w])
+        ch.run(seed, w, proposals, N // 2, N // 2, 0)
+        match += int(np.array_equal(ch.ku, c1[w]) and np.array_equal(ch.kd, d1[w]))
+    assert match >= walkers - 1
+    for w in range(walkers):
+        assert close(Wu[w], o.reevaluateW(ham.U_up, c1[w]), 1e-3), w
+        assert close(Wd[w], o.reevaluateW(ham.U_down, d1[w]), 1e-3), w
+
+
+def test_cluster_sweep_refused_off_its_path(kv):
+    ham = ham_for(kv, 96)
+    eng = kv.Engine(ham, 2, precision="mixed", delay_k=8, w_placement="hbm")
+    with pytest.raises(kv.KvmcError):
+        eng.set_cluster(4)
+    eng.close()
+    eng = kv.Engine(ham, 2, precision="mixed", delay_k=1, w_placement="hbm")
+    with pytest.raises(kv.KvmcError):
+        eng.set_cluster(3)
     eng.close()

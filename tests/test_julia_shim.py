@@ -149,3 +149,13 @@ def test_carlo_callbacks_and_fused_sweep():
     assert "kvmc_sweep(mc.h, mc.proposals_per_sweep)" in body
     # the default cadence is min(N_up, N_down) proposals per sweep! call
     assert 'get(params, :proposals_per_sweep, nocc)' in src and "nocc = min(params[:N_up], params[:N_down])" in src
+
+
+def test_constants_match_the_header():
+    """Every KVMC_* constant the Julia module defines has the header's value."""
+    hdr = open(os.path.join(ROOT, "include", "kvmc.h")).read()
+    consts = re.findall(r"const (KVMC_\w+) = Int32\((-?\d+)\)", open(JULIA[0]).read())
+    assert len(consts) >= 10
+    for name, val in consts:
+        m = re.search(r"\b" + name + r"\s*=\s*(-?\d+)", hdr) or re.search(r"#define\s+" + name + r"\s+(-?\d+)", hdr)
+        assert m and int(m.group(1)) == int(val), (name, val)
