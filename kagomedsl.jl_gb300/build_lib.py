@@ -18,7 +18,7 @@ LIB = BUILD / "libkvmc.so"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-fvisibility=hidden", "-I", str(ROOT / "include"), "-I", str(CSRC)]
-SOURCES = ["kvmc_kernels.cu", "kvmc_warp.cu", "kvmc_complex.cu", "kvmc_grad.cu", "kvmc_refresh32.cu", "kvmc_refresh_tile.cu", "kvmc_cluster.cu", "kvmc_api.cpp"]
+SOURCES = ["kvmc_kernels.cu", "kvmc_warp.cu", "kvmc_complex.cu", "kvmc_grad.cu", "kvmc_refresh32.cu", "kvmc_refresh_tile.cu", "kvmc_cluster.cu", "kvmc_refresh_oz.cu", "kvmc_api.cpp"]
 
 
 def nvcc() -> str:
@@ -37,7 +37,7 @@ def _stale(out: Path, deps) -> bool:
 
 def build(verbose: bool = False, force: bool = False) -> Path:
     BUILD.mkdir(exist_ok=True)
-    headers = [ROOT / "include" / "kvmc.h", CSRC / "kvmc_internal.h", CSRC / "kvmc_device.cuh", CSRC / "kvmc_refine.cuh"]
+    headers = [ROOT / "include" / "kvmc.h", CSRC / "kvmc_internal.h", CSRC / "kvmc_device.cuh", CSRC / "kvmc_refine.cuh", CSRC / "kvmc_tile.cuh"]
     objs, procs = [], []
     for src in SOURCES:
         s = CSRC / src

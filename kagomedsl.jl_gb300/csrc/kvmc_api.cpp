@@ -56,7 +56,9 @@ struct kvmc_handle {
     int stream_threads = 256;  // W in HBM: threads per walker
     int pipeline = 1;          // delayed form: pipelined scan / factor-column write
     int tc_flush = 0;          // W in HBM: rank-k flush on the tensor cores
-    int refresh32 = 0;         // mixed real form: periodic refresh by FP32 iterative refinement, 1 per row, 2 tiled (default <= 128 orbitals)
+    int refresh32 = 0;         // mixed real form: periodic refresh by FP32 iterative refinement, 1 per row, 2 tiled, 3 tiled with the residual on the tensor cores
+    kvmc::OzRefresh oz{};      // buffers of refresh32 = 3 (allocated when it is first chosen)
+    bool oz_ready = false;
     int warp_walkers = 0;      // mixed real form: > 0 = one warp per walker, walkers per CTA
     float cond_hi = 0.f, cond_lo = 0.f;  // the warp sweep's accuracy guard (0 = off)
     int64_t segment = 0;       // one-warp mode: kvmc_advance in segments of this many moves (0 = whole call)
@@ -171,8 +173,41 @@ int upload_kappa(kvmc_handle *h, const int32_t *ku, const int32_t *kd) {
 
 // The FP32 refresh by iterative refinement: one thread per row (1) or tiled (2)
 cudaError_t refresh32_launch(kvmc_handle *h, int only_due, int track_drift) {
+    if (h->refresh32 == 3) return kvmc::launch_refresh_oz(h->dm, h->db, h->oz, only_due, track_drift, h->stream);
     return h->refresh32 == 2 ? kvmc::launch_refresh_tile(h->dm, h->db, only_due, track_drift, h->stream)
                              : kvmc::launch_refresh32(h->dm, h->db, only_due, track_drift, h->stream);
+}
+
+// The buffers of the refresh with its residual on the tensor cores: U's digit
+// planes for both spins (computed here from the host copy of U) and the
+// per-walker planes, matrices and tile states, zeroed once.
+int oz_prepare(kvmc_handle *h) {
+    if (h->oz_ready) return KVMC_OK;
+    KV_TRY(set_device(h));
+    const int N = h->n_sites;
+    const int ns[2] = {h->n_up, h->n_dn};
+    const std::vector<double> *U[2] = {&h->U_up_host, &h->U_dn_host};
+    for (int s = 0; s < 2; ++s) {
+        if (U[s]->size() != (size_t)N * ns[s]) return h->fail(KVMC_ERR_UNSUPPORTED, "no host copy of the orbitals");
+        std::vector<uint16_t> ud((size_t)kvmc::kOzUDigits * N * ns[s]);
+        std::vector<int> fe(ns[s]);
+        kvmc::oz_digits_host(U[s]->data(), N, ns[s], ud.data(), fe.data());
+        uint16_t *d_ud = nullptr;
+        int *d_fe = nullptr;
+        KV_TRY(h->alloc(&d_ud, ud.size()));
+        KV_TRY(h->alloc(&d_fe, fe.size()));
+        KV_TRY(h->cuda(cudaMemcpy(d_ud, ud.data(), ud.size() * 2, cudaMemcpyHostToDevice), "upload U digits"));
+        KV_TRY(h->cuda(cudaMemcpy(d_fe, fe.data(), fe.size() * 4, cudaMemcpyHostToDevice), "upload U digits"));
+        h->oz.ud[s] = d_ud;
+        h->oz.fexp[s] = d_fe;
+    }
+    const size_t bytes = kvmc::oz_scratch_bytes(h->dm, h->n_walkers);
+    unsigned char *scr = nullptr;
+    KV_TRY(h->alloc(&scr, bytes));
+    KV_TRY(h->cuda(cudaMemset(scr, 0, bytes), "clear refresh buffers"));
+    KV_TRY(h->cuda(kvmc::oz_setup(h->dm, h->n_walkers, scr, h->oz), "tensor maps of the refresh"));
+    h->oz_ready = true;
+    return KVMC_OK;
 }
 
 // The real and the complex kernels behind one call each
@@ -1523,7 +1558,15 @@ extern "C" int kvmc_set_tuning(kvmc_handle *h, int32_t key, int32_t value) {
         return KVMC_OK;
     }
     if (key == KVMC_TUNE_REFRESH32) {
-        if (value < 0 || value > 2) return h->fail(KVMC_ERR_ARGUMENT, "refresh32 must be 0, 1 or 2");
+        if (value < 0 || value > 3) return h->fail(KVMC_ERR_ARGUMENT, "refresh32 must be 0, 1, 2 or 3");
+        if (value == 3) {
+            if (!h->mixed || h->cplx)
+                return h->fail(KVMC_ERR_UNSUPPORTED, "the FP32 refresh serves the mixed real form");
+            if (!kvmc::oz_supported(h->dm, kvmc::max_smem_optin(h->device)))
+                return h->fail(KVMC_ERR_UNSUPPORTED,
+                               "the tensor-core residual serves fewer than 1024 orbitals per spin");
+            KV_TRY(oz_prepare(h));
+        }
         if (value == 2) {
             if (!h->mixed || h->cplx)
                 return h->fail(KVMC_ERR_UNSUPPORTED, "the FP32 refresh serves the mixed real form");

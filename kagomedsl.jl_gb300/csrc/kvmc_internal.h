@@ -145,6 +145,42 @@ cudaError_t launch_refresh_tile(const DevModel &m, const DevBatch &b, int only_d
                                 cudaStream_t stream);
 cudaError_t launch_clear_status(const DevBatch &b, int bits, cudaStream_t stream);
 
+// The tiled refresh with its residual B - V M on the tensor cores
+// (kvmc_refresh_oz.cu, KVMC_TUNE_REFRESH32 = 3).  U is split once per model
+// into seven bf16 digit planes on a per-column fixed-point grid, V into four
+// per row at every pass; the digit products are exact integer sums in FP32
+// TMEM accumulators, one per weight class.  The buffers belong to the handle.
+constexpr int kOzUDigits = 7;   // digit planes of U (48 bits below its column's scale)
+constexpr int kOzVDigits = 4;   // digit planes of V (27 bits below its row's scale)
+struct OzRefresh {
+    int n_max, oth_max;          // max over the spins of n and of N - n
+    int ldz;                     // row stride of V and R (floats): round4(n_max)
+    int kp;                      // K (orbitals) padded to a multiple of 32
+    int rows_v, rows_m;          // rows of the V planes (multiple of 128) and of M^T (multiple of 64)
+    int tiles;                   // 32-row tiles of X per (walker, spin): ceil(oth_max / 32)
+    const uint16_t *ud[2];       // per spin: U's digits, [kOzUDigits][N][n] bf16 bits, row-major by site
+    const int *fexp[2];          // per spin: column scale exponents, [n]
+    float *V, *R;                // [W*2][rows_v][ldz]
+    uint16_t *vd;                // [W*2][kOzVDigits][kp/8][rows_v][8] bf16 bits
+    uint16_t *mt;                // [W*2][kOzUDigits][kp/8][rows_m][8] bf16 bits: M^T's digits
+    int *vexp;                   // [W*2][rows_v] row scale exponents of V
+    int *perm, *srow;            // [W*2][n_max] pivot order and the site of M's row i
+    short *site_oth;             // [W*2][oth_max]
+    float *est, *dprev;          // [W*2][tiles] refinement state per tile
+    int *done, *active;          // [W*2][tiles], [W*2]
+    alignas(64) unsigned char tmap_v[128], tmap_m[128];   // CUtensorMap of vd and mt
+};
+size_t oz_scratch_bytes(const DevModel &m, int n_walkers);
+bool oz_supported(const DevModel &m, int optin);
+// U's digits for one spin on the host: `ud` receives kOzUDigits planes of
+// N x n bf16 bits, `fexp` the n column exponents.
+void oz_digits_host(const double *U, int N, int n, uint16_t *ud, int *fexp);
+// Lays out the per-walker buffers in `scratch` (oz_scratch_bytes, zeroed by
+// the caller) and encodes the tensor maps; ud / fexp must be set already.
+cudaError_t oz_setup(const DevModel &m, int n_walkers, void *scratch, OzRefresh &oz);
+cudaError_t launch_refresh_oz(const DevModel &m, const DevBatch &b, const OzRefresh &oz, int only_due,
+                              int track_drift, cudaStream_t stream);
+
 // One warp per walker with W's non-trivial rows indexed by labels (kvmc_warp.cu).
 size_t warp_cta_smem(const DevModel &m);
 size_t warp_walker_smem(const DevModel &m, int K);

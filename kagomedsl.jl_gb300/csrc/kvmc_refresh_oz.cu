@@ -1,0 +1,750 @@
+// The periodic refresh of the mixed real form with the residual of its
+// iterative refinement on the tensor cores (kvmc.h: KVMC_TUNE_REFRESH32 = 3).
+//
+// Reference counterpart: reevaluateW! with tilde_U (KagomeDSL.jl
+// src/MonteCarlo.jl:55-115): W = U tilde_U^{-1}.  The algorithm is the tiled
+// FP32 refinement of kvmc_refresh_tile.cu -- X tilde_U = B for the n_oth rows
+// at the other spin's sites, V = B G with G = M^{-1} (M = P tilde_U), then
+// passes of V += (B - V M) G -- split into batched kernels so that the
+// residual B - V M, where the refinement needs more than FP32, runs as a
+// tensor-core GEMM over every walker and spin at once:
+//   oz_prep_kernel      one CTA per (walker, spin): site tables, the FP32 LU,
+//                       G and V = B G as in the tiled refresh; V, the pivot
+//                       order and the site tables to HBM; unit rows of W.
+//   oz_gather_kernel    the digit planes of M^T for this configuration.
+//   per pass (at most 4):
+//   oz_slice_kernel     V's rows split into four digit planes.
+//   oz_residual_kernel  R = B - V M from the digit planes (tcgen05, TMA).
+//   oz_correct_kernel   V += R G per 32-row tile on the CUDA cores, the
+//                       tile's convergence test (as in the tiled refresh),
+//                       and the tile's rows out to W once it has converged
+//                       or the passes are spent.
+//
+// Error-free products (the splitting of Ozaki, Ogita, Oishi and Rump,
+// "Error-free transformations of matrix multiplication by using fast
+// routines of matrix multiplication and its applications", Numer.
+// Algorithms 59, 2012).  Every column j of U gets a scale 2^f_j above its
+// largest entry over all sites, every row i of V a scale 2^e_i above its
+// largest entry; the scaled values are written as signed digits d_0, d_1,
+// ... with |d| <= 64 and weights 2^-6, 2^-13, 2^-20, ... (round to nearest
+// at each step, so every digit fits 7 bits and is exact in bf16): seven
+// digits for U (48 bits below its column's scale), four for V (27 bits).
+// A digit product is an integer of at most 2^12; the digit pairs (s, t)
+// with the same s + t = c share one FP32 accumulator in tensor memory
+// (weight 2^-7c), at most four pairs per class, so a sum over k < n stays
+// below 2^24 for n < 1024 and the accumulation is exact.  Pairs with
+// s + t > 6 weigh at most 2^-49 of class 0 per product and are left out.
+// The classes are combined by TwoSum in FP32, scaled by 2^(e_i + f_j - 12)
+// and subtracted from B (U's FP32 high and low parts): R to the accuracy of
+// the tiled refresh's fixed-grid residual, with 22 bf16 MMAs per k-step of
+// 16 in place of six FP32 operations per product.
+#include <cuda.h>
+#include <cuda_bf16.h>
+
+#include <cmath>
+#include <cstring>
+
+#include "kvmc_tile.cuh"
+
+namespace kvmc {
+
+namespace {
+
+namespace oz {
+
+constexpr int kBM = 128;  // rows of V per residual tile (TMEM lanes)
+constexpr int kBN = 64;   // columns of R per residual tile (TMEM columns per class)
+constexpr int kKS = 32;   // k per pipeline stage: two MMA k-steps of 16
+constexpr int kStages = 3;
+constexpr int kClasses = 7;  // weight classes c = s + t, 0..6
+constexpr int kABytes = kOzVDigits * kBM * kKS * 2;   // V's planes of one stage
+constexpr int kBBytes = kOzUDigits * kBN * kKS * 2;   // M^T's planes of one stage
+constexpr int kStageBytes = kABytes + kBBytes;
+constexpr int kSmem = kStages * kStageBytes + 1024;   // + alignment slack
+constexpr uint32_t kTmemCols = 512;                   // kClasses * kBN = 448, rounded to a power of two
+constexpr uint32_t kWaitLimit = 1u << 22;
+// Operand tiles in shared memory: plane p, k-group g (8 k), row r at byte
+// ((p * (kKS / 8) + g) * rows + r) * 16: every 8 rows x 16 bytes is one
+// core matrix of the no-swizzle K-major layout, adjacent along the rows 128
+// bytes apart (stride offset), adjacent along k rows * 16 bytes apart
+// (leading offset).  The TMA boxes below land in exactly this order.
+constexpr uint32_t kLboA = kBM * 16, kLboB = kBN * 16, kSbo = 128;
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ uint64_t sdesc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+    uint64_t d = (uint64_t)((addr >> 4) & 0x3FFF);
+    d |= (uint64_t)((lbo >> 4) & 0x3FFF) << 16;
+    d |= (uint64_t)((sbo >> 4) & 0x3FFF) << 32;
+    d |= (uint64_t)1 << 46;  // descriptor version; no swizzle, base offset 0
+    return d;
+}
+
+// kind::f16 with bf16 A and B (both K-major), FP32 accumulator, M x N
+__host__ __device__ constexpr uint32_t idesc_bf16(int m, int n) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(m >> 4) << 24);
+}
+
+__device__ __forceinline__ void mma(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t idesc, uint32_t accumulate) {
+    asm volatile("{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+                 "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}"
+                 :: "r"(d_tmem), "l"(a), "l"(b), "r"(idesc), "r"(accumulate));
+}
+
+__device__ __forceinline__ void commit(uint64_t *bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" :: "r"(smem_u32(bar))
+                 : "memory");
+}
+
+__device__ __forceinline__ void bar_init(uint64_t *bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(smem_u32(bar)), "r"(count));
+}
+
+__device__ __forceinline__ void expect_tx(uint64_t *bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" :: "r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+
+// bounded wait for the completion of the barrier's phase with this parity
+__device__ __forceinline__ bool wait(uint64_t *bar, uint32_t parity) {
+    uint32_t done = 0;
+    for (uint32_t it = 0; it < kWaitLimit && !done; ++it)
+        asm volatile("{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}"
+                     : "=r"(done) : "r"(smem_u32(bar)), "r"(parity) : "memory");
+    return done != 0;
+}
+
+// 5-d tiled TMA load into shared memory, completing on `bar`
+__device__ __forceinline__ void tma_load5(void *dst, const CUtensorMap *map, int c0, int c1, int c2, int c3, int c4,
+                                          uint64_t *bar) {
+    asm volatile("cp.async.bulk.tensor.5d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+                 " [%0], [%1, {%2, %3, %4, %5, %6}], [%7];"
+                 :: "r"(smem_u32(dst)), "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(c3),
+                    "r"(c4), "r"(smem_u32(bar))
+                 : "memory");
+}
+
+__device__ __forceinline__ void ld8(uint32_t taddr, float (&v)[8]) {
+    uint32_t r[8];
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+                 : "r"(taddr));
+#pragma unroll
+    for (int j = 0; j < 8; ++j) v[j] = __uint_as_float(r[j]);
+}
+
+__device__ __forceinline__ void fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+// 2^e as a float for the exponents the scales take; ldexpf outside the normal range
+__device__ __forceinline__ float pow2(int e) {
+    return (e >= -126 && e <= 127) ? __int_as_float((e + 127) << 23) : ldexpf(1.f, e);
+}
+
+__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
+    s = a + b;
+    const float bb = s - a;
+    e = (a - (s - bb)) + (b - bb);
+}
+
+}  // namespace oz
+
+// Device view of the per-walker buffers (kvmc_internal.h: OzRefresh).
+struct OzView {
+    int n_max, oth_max, ldz, kp, rows_v, rows_m, tiles;
+    const uint16_t *ud0, *ud1;
+    const int *fexp0, *fexp1;
+    float *V, *R;
+    uint16_t *vd, *mt;
+    int *vexp, *perm, *srow;
+    short *site_oth;
+    float *est, *dprev;
+    int *done, *active;
+};
+
+OzView view_of(const OzRefresh &o) {
+    OzView v;
+    v.n_max = o.n_max; v.oth_max = o.oth_max; v.ldz = o.ldz; v.kp = o.kp;
+    v.rows_v = o.rows_v; v.rows_m = o.rows_m; v.tiles = o.tiles;
+    v.ud0 = o.ud[0]; v.ud1 = o.ud[1]; v.fexp0 = o.fexp[0]; v.fexp1 = o.fexp[1];
+    v.V = o.V; v.R = o.R; v.vd = o.vd; v.mt = o.mt; v.vexp = o.vexp; v.perm = o.perm; v.srow = o.srow;
+    v.site_oth = o.site_oth; v.est = o.est; v.dprev = o.dprev; v.done = o.done; v.active = o.active;
+    return v;
+}
+
+// Steps 1 and 2 of the tiled refresh, then V = B G per 32-row tile into HBM.
+__global__ void __launch_bounds__(kTT) oz_prep_kernel(DevModel m, DevBatch b, OzView v, int only_due, int track_drift) {
+    const int w = blockIdx.x, spin = blockIdx.y, ws = 2 * w + spin;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nt = blockDim.x, nw = nt / 32;
+    if (only_due && b.since[w] >= 0) {
+        if (tid == 0) v.active[ws] = 0;
+        return;
+    }
+    if (spin == 0 && tid == 0) atomicAdd(b.refresh_count, 1ull);
+    const int N = m.n_sites;
+    const int n = spin == 0 ? m.n_up : m.n_dn;
+    const int n_oth = N - n;
+    const int ldw = spin == 0 ? m.ld_up : m.ld_dn;
+    const float *Uh = spin == 0 ? m.U32_up_hi : m.U32_dn_hi;
+    const bool cpt = b.compact != 0;
+    float *Wout = cpt ? b.G32 + (size_t)w * b.g_block + (spin == 0 ? 0 : (size_t)m.n_dn * m.ld_up)
+                      : b.W32 + (size_t)w * N * (m.ld_up + m.ld_dn) + (spin == 0 ? 0 : (size_t)N * m.ld_up);
+    float *A = reinterpret_cast<float *>(b.solve_scratch + ((size_t)w * 2 + spin) * b.solve_block);
+
+    extern __shared__ __align__(16) unsigned char smem[];
+    const TileSmem L = tile_smem_layout(n, n_oth);
+    float *Z = reinterpret_cast<float *>(smem + L.z);
+    float *Rt = reinterpret_cast<float *>(smem + L.r);
+    float *Pn = reinterpret_cast<float *>(smem + L.pn);
+    float *Ut = reinterpret_cast<float *>(smem + L.ut);
+    float *St = reinterpret_cast<float *>(smem + L.st);
+    float *invd = reinterpret_cast<float *>(smem + L.invd);
+    int *perm = reinterpret_cast<int *>(smem + L.perm);
+    int *srow = reinterpret_cast<int *>(smem + L.srow);
+    short *site_of = reinterpret_cast<short *>(smem + L.site_of);
+    short *site_oth = reinterpret_cast<short *>(smem + L.site_oth);
+    __shared__ double red[33];
+
+    if (!tile_factor(m, b, w, spin, A, Z, Pn, Ut, St, invd, perm, srow, site_of, site_oth, red)) {
+        if (tid == 0) v.active[ws] = 0;
+        return;
+    }
+    const int ldz = ld_tile(n);   // the tile functions' stride; V and R in HBM use v.ldz >= ldz
+    const float *G = A + (size_t)n * n;
+    for (int i = tid; i < n; i += nt) {
+        v.perm[(size_t)ws * v.n_max + i] = perm[i];
+        v.srow[(size_t)ws * v.n_max + i] = srow[i];
+    }
+    for (int i = tid; i < n_oth; i += nt) v.site_oth[(size_t)ws * v.oth_max + i] = site_oth[i];
+    for (int t = tid; t < v.tiles; t += nt) {
+        v.est[(size_t)ws * v.tiles + t] = 1.f;
+        v.dprev[(size_t)ws * v.tiles + t] = 1.f;
+        v.done[(size_t)ws * v.tiles + t] = t * kRT < n_oth ? 0 : 1;
+    }
+    for (int e = tid; e < kRT * (ldz - n); e += nt) {
+        const int r = e / (ldz - n), c = n + e % (ldz - n);
+        Rt[(size_t)r * ldz + c] = 0.f;
+    }
+    float *Vw = v.V + (size_t)ws * v.rows_v * v.ldz;
+    for (int b0 = 0; b0 < n_oth; b0 += kRT) {
+        const int rows = min(kRT, n_oth - b0);
+        __syncthreads();
+        for (int cb = 0; cb < n; cb += 32)
+            stage_rows32(Rt + cb, ldz, kRT, min(32, n - cb), min(32, n - cb), [&](int r) -> const float * {
+                return r < rows ? Uh + (size_t)site_oth[b0 + r] * n + cb : nullptr;
+            });
+        tile_gemm(G, n, Rt, Z, ldz, rows, 0, St, red);
+        __syncthreads();
+        for (int r = warp; r < rows; r += nw)
+            for (int c = lane; c < n; c += 32) Vw[(size_t)(b0 + r) * v.ldz + c] = Z[(size_t)r * ldz + c];
+    }
+    // unit rows at the sites holding this spin (site-indexed W only)
+    float dmax = 0.f;
+    if (!cpt) {
+        for (int l = warp; l < n; l += nw) {
+            float *wr = Wout + (size_t)site_of[l] * ldw;
+            for (int c = lane; c < ldw; c += 32) {
+                const float nv = c == l ? 1.f : 0.f;
+                if (track_drift) dmax = fmaxf(dmax, fabsf(wr[c] - nv) / (1.f + fabsf(nv)));
+                wr[c] = nv;
+            }
+        }
+    }
+    if (track_drift) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) dmax = fmaxf(dmax, __shfl_xor_sync(0xffffffffu, dmax, o));
+        if (lane == 0 && dmax > 0.f) atomic_max_nonneg(&b.drift[w], dmax);
+    }
+    if (tid == 0) v.active[ws] = 1;
+}
+
+// M^T's digit planes: plane t, k-group g, row j holds digit t of
+// U[srow[8 g + q]][j] for q = 0..7 (zero beyond n, where nothing writes).
+__global__ void __launch_bounds__(256) oz_gather_kernel(DevModel m, OzView v) {
+    const int w = blockIdx.x, spin = blockIdx.y, t = blockIdx.z, ws = 2 * w + spin;
+    if (!v.active[ws]) return;
+    const int N = m.n_sites;
+    const int n = spin == 0 ? m.n_up : m.n_dn;
+    __shared__ int srow[1024];
+    for (int i = threadIdx.x; i < n; i += blockDim.x) srow[i] = v.srow[(size_t)ws * v.n_max + i];
+    __syncthreads();
+    const uint16_t *ud = (spin == 0 ? v.ud0 : v.ud1) + (size_t)t * N * n;
+    uint16_t *dst = v.mt + ((size_t)ws * kOzUDigits + t) * (size_t)(v.kp / 8) * v.rows_m * 8;
+    const int groups = (n + 7) / 8;
+    for (int e = threadIdx.x; e < groups * n; e += blockDim.x) {
+        const int g = e / n, j = e - g * n;
+        uint16_t d[8];
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+            const int k = 8 * g + q;
+            d[q] = k < n ? ud[(size_t)srow[k] * n + j] : (uint16_t)0;
+        }
+        uint4 pk;
+        pk.x = d[0] | ((uint32_t)d[1] << 16);
+        pk.y = d[2] | ((uint32_t)d[3] << 16);
+        pk.z = d[4] | ((uint32_t)d[5] << 16);
+        pk.w = d[6] | ((uint32_t)d[7] << 16);
+        *reinterpret_cast<uint4 *>(dst + ((size_t)g * v.rows_m + j) * 8) = pk;
+    }
+}
+
+// V's digit planes for the 32-row tiles still refining: row i is scaled by
+// 2^-e_i (2^e_i above its largest entry), then split into kOzVDigits digits.
+__global__ void __launch_bounds__(256) oz_slice_kernel(DevModel m, OzView v) {
+    const int w = blockIdx.x, spin = blockIdx.y, tt = blockIdx.z, ws = 2 * w + spin;
+    const int n = spin == 0 ? m.n_up : m.n_dn;
+    const int n_oth = m.n_sites - n;
+    const int b0 = tt * kRT;
+    if (!v.active[ws] || b0 >= n_oth || v.done[(size_t)ws * v.tiles + tt]) return;
+    const int rows = min(kRT, n_oth - b0);
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    __shared__ int s_e[kRT];
+    const float *Vw = v.V + ((size_t)ws * v.rows_v + b0) * v.ldz;
+    for (int r = warp; r < kRT; r += 8) {
+        float mx = 0.f;
+        if (r < rows)
+            for (int c = lane; c < n; c += 32) mx = fmaxf(mx, fabsf(Vw[(size_t)r * v.ldz + c]));
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+        if (lane == 0) {
+            int e = 0;
+            if (mx > 0.f && mx < INFINITY) frexpf(mx, &e);   // mx < 2^e
+            s_e[r] = e;
+            if (r < rows) v.vexp[(size_t)ws * v.rows_v + b0 + r] = e;
+        }
+    }
+    __syncthreads();
+    const int groups = (n + 7) / 8;
+    const size_t plane = (size_t)(v.kp / 8) * v.rows_v * 8;
+    uint16_t *dst = v.vd + (size_t)ws * kOzVDigits * plane;
+    for (int e = tid; e < groups * kRT; e += blockDim.x) {
+        const int r = e & (kRT - 1), g = e / kRT;
+        if (r >= rows) continue;
+        const float sc = oz::pow2(6 - s_e[r]);
+        float y[8];
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+            const int k = 8 * g + q;
+            y[q] = k < n ? Vw[(size_t)r * v.ldz + k] * sc : 0.f;   // |y| < 64, exact
+        }
+#pragma unroll
+        for (int s = 0; s < kOzVDigits; ++s) {
+            uint32_t h[8];
+#pragma unroll
+            for (int q = 0; q < 8; ++q) {
+                const float d = rintf(y[q]);                   // |d| <= 64
+                h[q] = __float_as_uint(d) >> 16;               // exact in bf16
+                y[q] = (y[q] - d) * 128.f;                     // exact; |y| <= 64
+            }
+            uint4 pk;
+            pk.x = h[0] | (h[1] << 16);
+            pk.y = h[2] | (h[3] << 16);
+            pk.z = h[4] | (h[5] << 16);
+            pk.w = h[6] | (h[7] << 16);
+            *reinterpret_cast<uint4 *>(dst + s * plane + ((size_t)g * v.rows_v + b0 + r) * 8) = pk;
+        }
+    }
+}
+
+// R = B - V M for one 128 x 64 tile of one (walker, spin).  Warp 0's first
+// lane loads the digit planes stage by stage with TMA, warp 1's first lane
+// issues the 22 MMAs of each k-step into the seven class accumulators, and
+// all four warps then read their 32 rows of the classes from tensor memory,
+// combine them and subtract them from B.  Every wait is bounded; one that
+// gives up marks the walker kStatusTimeout and the tile is left unwritten.
+__global__ void __launch_bounds__(128, 1)
+oz_residual_kernel(DevModel m, DevBatch b, OzView v, const __grid_constant__ CUtensorMap tmv,
+                   const __grid_constant__ CUtensorMap tmm) {
+    using namespace oz;
+    const int ws = blockIdx.z, w = ws >> 1, spin = ws & 1;
+    if (!v.active[ws]) return;
+    const int n = spin == 0 ? m.n_up : m.n_dn;
+    const int n_oth = m.n_sites - n;
+    const int r0 = blockIdx.x * kBM, c0 = blockIdx.y * kBN;
+    if (r0 >= n_oth || c0 >= n) return;
+    bool any = false;
+    for (int q = 0; q < kBM / kRT; ++q) {
+        const int tt = r0 / kRT + q;
+        if (tt * kRT < n_oth && !v.done[(size_t)ws * v.tiles + tt]) any = true;
+    }
+    if (!any) return;
+
+    extern __shared__ unsigned char smem_raw[];
+    unsigned char *sm = reinterpret_cast<unsigned char *>(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    __shared__ __align__(8) uint64_t full[kStages], empty[kStages], done_bar;
+    __shared__ uint32_t tmem_slot;
+    __shared__ int s_fail, s_issued;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    if (tid == 0) {
+        for (int s = 0; s < kStages; ++s) {
+            bar_init(&full[s], 1);
+            bar_init(&empty[s], 1);
+        }
+        bar_init(&done_bar, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        s_fail = 0;
+        s_issued = 0;
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
+                     :: "r"(smem_u32(&tmem_slot)), "r"(kTmemCols));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    fence_before();
+    __syncthreads();
+    fence_after();
+    const uint32_t tmem = tmem_slot;
+    const int nch = (n + kKS - 1) / kKS;
+
+    if (warp == 0) {
+        if (lane == 0) {
+            int ch = 0;
+            for (; ch < nch; ++ch) {
+                const int s = ch % kStages;
+                if (ch >= kStages && !wait(&empty[s], ((ch / kStages) - 1) & 1)) {
+                    s_fail = 1;
+                    break;
+                }
+                expect_tx(&full[s], kStageBytes);
+                unsigned char *st = sm + (size_t)s * kStageBytes;
+                tma_load5(st, &tmv, 0, r0, ch * (kKS / 8), 0, ws, &full[s]);
+                tma_load5(st + kABytes, &tmm, 0, c0, ch * (kKS / 8), 0, ws, &full[s]);
+            }
+            s_issued = ch;
+        }
+        __syncwarp();
+    } else if (warp == 1) {
+        if (lane == 0) {
+            constexpr uint32_t idesc = idesc_bf16(kBM, kBN);
+            bool ok = true;
+            for (int ch = 0; ch < nch; ++ch) {
+                const int s = ch % kStages;
+                if (!wait(&full[s], (ch / kStages) & 1)) {
+                    ok = false;
+                    break;
+                }
+                fence_after();
+                const uint32_t a0 = smem_u32(sm + (size_t)s * kStageBytes), b0 = a0 + kABytes;
+#pragma unroll
+                for (int q = 0; q < kKS / 16; ++q) {
+#pragma unroll
+                    for (int c = 0; c < kClasses; ++c) {
+#pragma unroll
+                        for (int sa = 0; sa < kOzVDigits; ++sa) {
+                            const int tb = c - sa;
+                            if (tb < 0 || tb >= kOzUDigits) continue;
+                            const uint64_t ad = sdesc(a0 + sa * (kBM * kKS * 2) + q * 2 * kLboA, kLboA, kSbo);
+                            const uint64_t bd = sdesc(b0 + tb * (kBN * kKS * 2) + q * 2 * kLboB, kLboB, kSbo);
+                            mma(tmem + (uint32_t)(c * kBN), ad, bd, idesc, (ch > 0 || q > 0 || sa > 0) ? 1u : 0u);
+                        }
+                    }
+                }
+                commit(&empty[s]);   // the stage is free once these MMAs have read it
+            }
+            if (!ok) s_fail = 1;
+            commit(&done_bar);       // arrives once every MMA issued above has completed
+        }
+        __syncwarp();
+    }
+    __syncthreads();
+    const bool ok = wait(&done_bar, 0) && !s_fail;
+    fence_after();
+
+    // epilogue: row i of the tile is TMEM lane i; warp g reads lanes 32 g ..
+    const int i = r0 + 32 * warp + lane;
+    const bool row_ok = ok && i < n_oth && !v.done[(size_t)ws * v.tiles + i / kRT];
+    const int *fexp = spin == 0 ? v.fexp0 : v.fexp1;
+    const float *Uh = spin == 0 ? m.U32_up_hi : m.U32_dn_hi;
+    const float *Ul = spin == 0 ? m.U32_up_lo : m.U32_dn_lo;
+    const int site = row_ok ? v.site_oth[(size_t)ws * v.oth_max + i] : 0;
+    const float sc_i = row_ok ? pow2(v.vexp[(size_t)ws * v.rows_v + i] - 12) : 0.f;
+    const float *bh = Uh + (size_t)site * n, *bl = Ul + (size_t)site * n;
+    float *Rrow = v.R + ((size_t)ws * v.rows_v + (row_ok ? i : 0)) * v.ldz;
+    const uint32_t tl = tmem + ((uint32_t)(32 * warp) << 16);
+    for (int cc = 0; cc < kBN; cc += 8) {
+        float d[kClasses][8];
+#pragma unroll
+        for (int c = 0; c < kClasses; ++c) ld8(tl + (uint32_t)(c * kBN + cc), d[c]);
+        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+        if (!row_ok) continue;
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+            const int j = c0 + cc + q;
+            if (j >= n) break;
+            float h1, e1, h2, e2;
+            two_sum(d[0][q], d[1][q] * 0x1p-7f, h1, e1);
+            two_sum(h1, d[2][q] * 0x1p-14f, h2, e2);
+            const float t = fmaf(d[6][q], 0x1p-42f, fmaf(d[5][q], 0x1p-35f, fmaf(d[4][q], 0x1p-28f, d[3][q] * 0x1p-21f)));
+            const float lo = (e1 + e2) + t;
+            const float s = sc_i * pow2(fexp[j]);
+            Rrow[j] = ((bh[j] - h2 * s) - lo * s) + bl[j];
+        }
+    }
+
+    fence_before();
+    __syncthreads();
+    fence_after();
+    if (tid == 0) {
+        // copies still in flight after a wait gave up: wait for them, bounded
+        const int issued = s_issued;
+        for (int s = 0; s < kStages && s < issued; ++s) {
+            const int last = s + ((issued - 1 - s) / kStages) * kStages;
+            wait(&full[s], (last / kStages) & 1);
+        }
+        if (!ok) atomicOr(&b.status[w], kStatusTimeout);
+    }
+    __syncthreads();
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" :: "r"(tmem), "r"(kTmemCols));
+}
+
+struct CorrectSmem {
+    size_t z, r, st, total;
+};
+__host__ __device__ inline CorrectSmem correct_layout(int ldz) {
+    auto al = [](size_t x) { return (x + 15) / 16 * 16; };
+    CorrectSmem s{};
+    s.z = 0;
+    s.r = al((size_t)kRT * ldz * 4);
+    s.st = s.r + al((size_t)kRT * ldz * 4);
+    s.total = s.st + (size_t)2 * kKC * kCB * 4;
+    return s;
+}
+
+// V += R G for one 32-row tile, its convergence test, and its rows out to W
+// when it has converged or the passes are spent (last != 0).
+__global__ void __launch_bounds__(kTT) oz_correct_kernel(DevModel m, DevBatch b, OzView v, int last, int track_drift) {
+    const int w = blockIdx.x, spin = blockIdx.y, tt = blockIdx.z, ws = 2 * w + spin;
+    const int N = m.n_sites;
+    const int n = spin == 0 ? m.n_up : m.n_dn;
+    const int n_oth = N - n;
+    const int b0 = tt * kRT;
+    if (!v.active[ws] || b0 >= n_oth || v.done[(size_t)ws * v.tiles + tt]) return;
+    const int rows = min(kRT, n_oth - b0);
+    const int ldz = ld_tile(n), ldw = spin == 0 ? m.ld_up : m.ld_dn;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nt = blockDim.x, nw = nt / 32;
+    extern __shared__ __align__(16) unsigned char smem[];
+    const CorrectSmem L = correct_layout(ldz);
+    float *Z = reinterpret_cast<float *>(smem + L.z);
+    float *Rt = reinterpret_cast<float *>(smem + L.r);
+    float *St = reinterpret_cast<float *>(smem + L.st);
+    __shared__ double red[33];
+    __shared__ int s_fin;
+    const float *G = reinterpret_cast<const float *>(b.solve_scratch + ((size_t)w * 2 + spin) * b.solve_block) +
+                     (size_t)n * n;
+    float *Vw = v.V + ((size_t)ws * v.rows_v + b0) * v.ldz;
+    const float *Rw = v.R + ((size_t)ws * v.rows_v + b0) * v.ldz;
+    for (int e = tid; e < kRT * ldz; e += nt) {
+        const int r = e / ldz, c = e - r * ldz;
+        const bool ok = r < rows && c < n;
+        Z[e] = ok ? Vw[(size_t)r * v.ldz + c] : 0.f;
+        Rt[e] = ok ? Rw[(size_t)r * v.ldz + c] : 0.f;
+    }
+    const float d = tile_gemm(G, n, Rt, Z, ldz, rows, 1, St, red);   // V += R G (synchronises first)
+    if (tid == 0) {
+        const size_t k = (size_t)ws * v.tiles + tt;
+        const float dprev = v.dprev[k];
+        const float est = d < dprev ? d * d / dprev : INFINITY;   // a correction that grows: diverging
+        v.dprev[k] = d;
+        v.est[k] = est;
+        const int fin = !(est > 1e-6f) || last;
+        s_fin = fin;
+        if (fin) {
+            v.done[k] = 1;
+            if (!(est <= 1e-5f)) atomicOr(&b.status[w], kStatusRefine);
+        }
+    }
+    __syncthreads();
+    if (!s_fin) {
+        for (int e = tid; e < rows * n; e += nt) {
+            const int r = e / n, c = e - r * n;
+            Vw[(size_t)r * v.ldz + c] = Z[(size_t)r * ldz + c];
+        }
+        return;
+    }
+    // the tile's rows out, in label order: X[:, perm[i]] = V[:, i]
+    const bool cpt = b.compact != 0;
+    float *Wout = cpt ? b.G32 + (size_t)w * b.g_block + (spin == 0 ? 0 : (size_t)m.n_dn * m.ld_up)
+                      : b.W32 + (size_t)w * N * (m.ld_up + m.ld_dn) + (spin == 0 ? 0 : (size_t)N * m.ld_up);
+    const int *perm = v.perm + (size_t)ws * v.n_max;
+    const short *site_oth = v.site_oth + (size_t)ws * v.oth_max;
+    float dmax = 0.f;
+    for (int r = warp; r < rows; r += nw) {
+        float *wr = Wout + (size_t)(cpt ? b0 + r : site_oth[b0 + r]) * ldw;
+        for (int i = lane; i < n; i += 32) {
+            const float nv = Z[(size_t)r * ldz + i];
+            const int p = perm[i];
+            if (track_drift) dmax = fmaxf(dmax, fabsf(wr[p] - nv) / (1.f + fabsf(nv)));
+            wr[p] = nv;
+        }
+        if (!cpt)
+            for (int c = n + lane; c < ldw; c += 32) wr[c] = 0.f;
+    }
+    if (track_drift) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) dmax = fmaxf(dmax, __shfl_xor_sync(0xffffffffu, dmax, o));
+        if (lane == 0 && dmax > 0.f) atomic_max_nonneg(&b.drift[w], dmax);
+    }
+}
+
+using EncodeTiled = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                 const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                 CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiled encode_fn() {
+    static EncodeTiled fn = nullptr;
+    if (!fn) {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q{};
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<EncodeTiled>(p);
+    }
+    return fn;
+}
+
+// planes of [groups = kp/8][rows][8] bf16 per (walker-spin, plane); box =
+// all planes of one stage (kKS / 8 groups) and `box_rows` rows
+cudaError_t encode_planes(void *map, void *base, int rows, int kp, int planes, int ws_count, int box_rows) {
+    EncodeTiled fn = encode_fn();
+    if (!fn) return cudaErrorNotSupported;
+    const cuuint64_t dims[5] = {8, (cuuint64_t)rows, (cuuint64_t)(kp / 8), (cuuint64_t)planes, (cuuint64_t)ws_count};
+    const cuuint64_t strides[4] = {16, (cuuint64_t)rows * 16, (cuuint64_t)(kp / 8) * rows * 16,
+                                   (cuuint64_t)planes * (kp / 8) * rows * 16};
+    const cuuint32_t box[5] = {8, (cuuint32_t)box_rows, (cuuint32_t)(oz::kKS / 8), (cuuint32_t)planes, 1};
+    const cuuint32_t estr[5] = {1, 1, 1, 1, 1};
+    const CUresult r = fn(reinterpret_cast<CUtensorMap *>(map), CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 5, base, dims,
+                          strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                          CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
+}
+
+size_t align256(size_t x) { return (x + 255) / 256 * 256; }
+
+struct OzDims {
+    int n_max, oth_max, ldz, kp, rows_v, rows_m, tiles;
+};
+OzDims oz_dims(const DevModel &m) {
+    OzDims d;
+    d.n_max = std::max(m.n_up, m.n_dn);
+    d.oth_max = m.n_sites - std::min(m.n_up, m.n_dn);
+    d.ldz = (d.n_max + 3) & ~3;
+    d.kp = (d.n_max + oz::kKS - 1) / oz::kKS * oz::kKS;
+    d.rows_v = (d.oth_max + oz::kBM - 1) / oz::kBM * oz::kBM;
+    d.rows_m = (d.n_max + oz::kBN - 1) / oz::kBN * oz::kBN;
+    d.tiles = (d.oth_max + kRT - 1) / kRT;
+    return d;
+}
+
+// byte offsets of the per-walker-spin buffers inside one allocation
+struct OzOffsets {
+    size_t V, R, vd, mt, vexp, perm, srow, site_oth, est, dprev, done, active, total;
+};
+OzOffsets oz_offsets(const OzDims &d, int n_walkers) {
+    const size_t S = (size_t)2 * n_walkers;
+    OzOffsets o{};
+    size_t p = 0;
+    auto take = [&](size_t bytes) {
+        const size_t at = p;
+        p = align256(p + bytes);
+        return at;
+    };
+    o.V = take(S * d.rows_v * d.ldz * 4);
+    o.R = take(S * d.rows_v * d.ldz * 4);
+    o.vd = take(S * kOzVDigits * (size_t)d.kp * d.rows_v * 2);
+    o.mt = take(S * kOzUDigits * (size_t)d.kp * d.rows_m * 2);
+    o.vexp = take(S * d.rows_v * 4);
+    o.perm = take(S * d.n_max * 4);
+    o.srow = take(S * d.n_max * 4);
+    o.site_oth = take(S * d.oth_max * 2);
+    o.est = take(S * d.tiles * 4);
+    o.dprev = take(S * d.tiles * 4);
+    o.done = take(S * d.tiles * 4);
+    o.active = take(S * 4);
+    o.total = p;
+    return o;
+}
+
+}  // namespace
+
+size_t oz_scratch_bytes(const DevModel &m, int n_walkers) { return oz_offsets(oz_dims(m), n_walkers).total; }
+
+bool oz_supported(const DevModel &m, int optin) {
+    const OzDims d = oz_dims(m);
+    if (!m.U32_up_hi || d.n_max >= 1024 || 2 * d.n_max > 65535) return false;   // the exact-accumulation bound
+    const size_t need = std::max({refresh_tile_smem(m), (size_t)oz::kSmem, correct_layout(d.ldz).total});
+    return need + 1024 <= (size_t)optin;
+}
+
+void oz_digits_host(const double *U, int N, int n, uint16_t *ud, int *fexp) {
+    for (int j = 0; j < n; ++j) {
+        double cm = 0.0;
+        for (int s = 0; s < N; ++s) cm = std::max(cm, std::fabs(U[(size_t)s * n + j]));
+        int e = 0;
+        if (cm > 0.0) std::frexp(cm, &e);   // cm < 2^e
+        fexp[j] = e;
+        for (int s = 0; s < N; ++s) {
+            double y = std::ldexp(U[(size_t)s * n + j], 6 - e);   // |y| < 64
+            for (int t = 0; t < kOzUDigits; ++t) {
+                const double dg = std::nearbyint(y);              // |dg| <= 64
+                const float f = (float)dg;
+                uint32_t bits;
+                std::memcpy(&bits, &f, 4);
+                ud[((size_t)t * N + s) * n + j] = (uint16_t)(bits >> 16);   // exact in bf16
+                y = (y - dg) * 128.0;                              // exact; |y| <= 64
+            }
+        }
+    }
+}
+
+cudaError_t oz_setup(const DevModel &m, int n_walkers, void *scratch, OzRefresh &oz) {
+    const OzDims d = oz_dims(m);
+    const OzOffsets o = oz_offsets(d, n_walkers);
+    unsigned char *base = static_cast<unsigned char *>(scratch);
+    oz.n_max = d.n_max; oz.oth_max = d.oth_max; oz.ldz = d.ldz; oz.kp = d.kp;
+    oz.rows_v = d.rows_v; oz.rows_m = d.rows_m; oz.tiles = d.tiles;
+    oz.V = reinterpret_cast<float *>(base + o.V);
+    oz.R = reinterpret_cast<float *>(base + o.R);
+    oz.vd = reinterpret_cast<uint16_t *>(base + o.vd);
+    oz.mt = reinterpret_cast<uint16_t *>(base + o.mt);
+    oz.vexp = reinterpret_cast<int *>(base + o.vexp);
+    oz.perm = reinterpret_cast<int *>(base + o.perm);
+    oz.srow = reinterpret_cast<int *>(base + o.srow);
+    oz.site_oth = reinterpret_cast<short *>(base + o.site_oth);
+    oz.est = reinterpret_cast<float *>(base + o.est);
+    oz.dprev = reinterpret_cast<float *>(base + o.dprev);
+    oz.done = reinterpret_cast<int *>(base + o.done);
+    oz.active = reinterpret_cast<int *>(base + o.active);
+    cudaError_t e = encode_planes(oz.tmap_v, oz.vd, d.rows_v, d.kp, kOzVDigits, 2 * n_walkers, oz::kBM);
+    if (e == cudaSuccess) e = encode_planes(oz.tmap_m, oz.mt, d.rows_m, d.kp, kOzUDigits, 2 * n_walkers, oz::kBN);
+    return e;
+}
+
+cudaError_t launch_refresh_oz(const DevModel &m, const DevBatch &b, const OzRefresh &oz, int only_due,
+                              int track_drift, cudaStream_t stream) {
+    if (!m.U32_up_hi || !b.solve_scratch || !oz.V) return cudaErrorInvalidValue;
+    const OzView v = view_of(oz);
+    const int W = b.n_walkers;
+    const size_t sm_prep = refresh_tile_smem(m);
+    cudaError_t e = cudaFuncSetAttribute(oz_prep_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_prep);
+    if (e != cudaSuccess) return e;
+    oz_prep_kernel<<<dim3(W, 2), kTT, sm_prep, stream>>>(m, b, v, only_due, track_drift);
+    oz_gather_kernel<<<dim3(W, 2, kOzUDigits), 256, 0, stream>>>(m, v);
+    const size_t sm_corr = correct_layout(oz.ldz).total;
+    if ((e = cudaFuncSetAttribute(oz_correct_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_corr)))
+        return e;
+    if ((e = cudaFuncSetAttribute(oz_residual_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, oz::kSmem)))
+        return e;
+    CUtensorMap tmv, tmm;
+    std::memcpy(&tmv, oz.tmap_v, sizeof tmv);
+    std::memcpy(&tmm, oz.tmap_m, sizeof tmm);
+    const dim3 rgrid(oz.rows_v / oz::kBM, oz.rows_m / oz::kBN, 2 * W);
+    for (int pass = 0; pass < kMaxPasses; ++pass) {
+        oz_slice_kernel<<<dim3(W, 2, oz.tiles), 256, 0, stream>>>(m, v);
+        oz_residual_kernel<<<rgrid, 128, oz::kSmem, stream>>>(m, b, v, tmv, tmm);
+        oz_correct_kernel<<<dim3(W, 2, oz.tiles), kTT, sm_corr, stream>>>(m, b, v, pass == kMaxPasses - 1,
+                                                                          track_drift);
+    }
+    return cudaGetLastError();
+}
+
+}  // namespace kvmc

@@ -196,8 +196,10 @@ class Engine:
     def set_refresh32(self, mode=True):
         """Periodic refresh by FP32 iterative refinement (FP64 fallback per
         walker): True / 1 = one thread per row, 2 or "tiled" = tiles of 32 rows
-        per CTA (faster from about 200 orbitals per spin), False / 0 = FP64."""
-        value = 2 if mode in (2, "tiled") else int(bool(mode))
+        per CTA (faster from about 200 orbitals per spin), 3 or "tc" = tiled
+        with the refinement's residual on the tensor cores (exact bf16 digit
+        products), False / 0 = FP64."""
+        value = 2 if mode in (2, "tiled") else 3 if mode in (3, "tc") else int(bool(mode))
         self._check(self._lib.kvmc_set_tuning(self.h, 4, value))
 
     def set_cluster(self, ctas: int):

@@ -635,12 +635,14 @@ def test_tensor_core_flush_refused_off_its_path(kv):
     eng.close()
 
 
-@pytest.mark.parametrize("mode", [1, 2])
+@pytest.mark.parametrize("mode", [1, 2, 3])
 @pytest.mark.parametrize("N,placement", [(96, "hbm"), (216, "hbm"), (216, "chip"), (384, "hbm"), (864, "hbm")])
 def test_fp32_refinement_refresh(kv, N, placement, mode):
-    """The periodic refresh by FP32 iterative refinement, one thread per row (1)
-    or in tiles of 32 rows (2): W right after it within 5e-6 of the FP64
-    rebuild (relative to max(1, |W|)), and chains that follow the oracle."""
+    """The periodic refresh by FP32 iterative refinement, one thread per row (1),
+    in tiles of 32 rows (2), or tiled with the residual on the tensor cores (3):
+    W right after it within 5e-6 of the FP64 rebuild (relative to max(1, |W|)),
+    and chains that follow the oracle.  The tiled forms converge on their own:
+    at most a quarter of their refreshes are redone in FP64."""
     walkers, seed, R = (8, 61, 64) if N < 864 else (4, 61, 32)
     ham = ham_for(kv, N)
     eng = kv.Engine(ham, walkers, precision="mixed", seed=seed, refresh_interval=R, w_placement=placement)
@@ -650,6 +652,8 @@ def test_fp32_refinement_refresh(kv, N, placement, mode):
     ku0, kd0, _ = eng.get_state()
     st = eng.advance(2 * R)             # ends right after a refresh of every walker
     assert st["refreshes"] >= 2 * walkers and st["bad_walkers"] == 0
+    if mode >= 2:
+        assert 4 * st["fp64_redos"] <= st["refreshes"], st
     ku1, kd1, ct = eng.get_state()
     Wu, Wd = eng.get_w()
     for w in range(walkers):
@@ -665,8 +669,9 @@ def test_fp32_refinement_refresh(kv, N, placement, mode):
     eng.close()
 
 
+@pytest.mark.parametrize("mode", ["tiled", "tc"])
 @pytest.mark.parametrize("n1,n2,n_up", [(10, 5, 75), (10, 5, 77), (6, 3, 30), (4, 2, 12)])
-def test_tiled_refresh_ragged_sizes(kv, n1, n2, n_up):
+def test_tiled_refresh_ragged_sizes(kv, n1, n2, n_up, mode):
     """The tiled FP32 refresh where neither spin's orbital count nor the other
     spin's row count is a multiple of 4 or 32 (N = 150 with 75 + 75 and
     77 + 73 orbitals, N = 54 with 30 + 24, N = 24): W after a refresh of every
@@ -678,7 +683,7 @@ def test_tiled_refresh_ragged_sizes(kv, n1, n2, n_up):
     ham = kv.Hamiltonian(n_up, N - n_up, Uu, Ud, H, kv.get_nn(H))
     walkers, seed, R = 6, 17, 48
     eng = kv.Engine(ham, walkers, precision="mixed", seed=seed, refresh_interval=R, w_placement="hbm")
-    eng.set_refresh32("tiled")
+    eng.set_refresh32(mode)
     eng.set_drift_tolerance(1e9)
     eng.init()
     ku0, kd0, _ = eng.get_state()
