@@ -65,6 +65,7 @@ def args_():
     p.add_argument("--skip-grad", action="store_true")
     p.add_argument("--skip-uneven", action="store_true")
     p.add_argument("--skip-large", action="store_true")
+    p.add_argument("--large-walkers", type=int, default=512, help="walkers of the N=864 leg")
     p.add_argument("--skip-field", action="store_true")
     p.add_argument("--skip-batched", action="store_true")
     p.add_argument("--skip-plugin", action="store_true")
@@ -520,8 +521,10 @@ def large_run(kv, seed, device, walkers=512, moves=128, steps=2):
     """The large lattice: 12x12 doubled cells (N=864, 432 orbitals per spin),
     512 walkers, W (2 x 864 x 432 FP32 = 2.99 MB per walker, 1.53 GB in all)
     in HBM with rank-16 delayed updates, a refresh every 128 accepted moves
-    by the tiled FP32 refinement (FP64 for the walkers it hands back); the
-    same with the FP64 refresh; and the plain FP64 form on the same walkers."""
+    by the FP32 refinement with its residual on the tensor cores (FP64 for
+    the walkers it hands back); the same with the tiled FP32 refinement on
+    the CUDA cores and with the FP64 refresh; and the plain FP64 form on the
+    same walkers."""
     from kagomevmc import autotune
 
     ham = kv.Hamiltonian.build(432, 432, kv.DoubleKagome(1.0, 24, 12, (True, True), (False, True)))
@@ -546,7 +549,8 @@ def large_run(kv, seed, device, walkers=512, moves=128, steps=2):
         eng.close()
         return acc, ms, k0, k1, redos
 
-    acc, ms, k0, k1, redos = run(2)
+    acc, ms, k0, k1, redos = run(3)
+    acc2, ms2, _, k1_2, redos2 = run(2)
     acc64, ms64, _, k1_64, _ = run(0)
     w_bytes = 2 * 864 * 432 * 4
     flush_bytes = 2 * w_bytes / 16 * acc          # W read + written once per 16 accepted moves
@@ -559,18 +563,21 @@ def large_run(kv, seed, device, walkers=512, moves=128, steps=2):
     pacc = pst["accepted"]
     pe.close()
     return {"workload": f"kagome VMC, 12x12 doubled cells (N=864), {walkers} walkers, W in HBM, delayed k=16, "
-                        f"tiled FP32 refinement refresh every 128 accepted moves, {steps} x {moves} accepted moves "
-                        f"per walker",
+                        f"FP32 refinement refresh every 128 accepted moves with its residual on the tensor cores "
+                        f"(exact bf16 digit products), {steps} x {moves} accepted moves per walker",
             "value": acc / (ms * 1e-3), "unit": UNIT, "ms": ms, "sweep_ms": k0, "refresh_ms": k1,
             "refreshes_redone_fp64": redos,
             "sweep_only_moves_per_s": acc / (k0 * 1e-3) if k0 else None,
             "flush_hbm_gbs_in_sweep": flush_bytes / (k0 * 1e-3) / 1e9 if k0 else None,
+            "tiled_fp32_refresh": {"value": acc2 / (ms2 * 1e-3), "unit": UNIT, "refresh_ms": k1_2,
+                                   "refreshes_redone_fp64": redos2},
             "fp64_refresh": {"value": acc64 / (ms64 * 1e-3), "unit": UNIT, "refresh_ms": k1_64},
             "plain_fp64": {"value": pacc / (pms * 1e-3), "unit": UNIT, "moves_per_walker": 128,
                            "walker_refreshes": pst["refreshes"]},
             "note": "refresh-bound. One walker refresh (both spins): FP64 LU and solves 2*((2/3)n^3 + 2(N-n)n^2) "
-                    "= 0.43 GFLOP; the tiled FP32 form runs about 3.2 G FP32 operations (LU, inverse, V = B G, "
-                    "then per refinement pass a compensated residual of 6 operations per product and a GEMM)"}
+                    "= 0.43 GFLOP; the FP32 forms run the LU, G = M^-1 and V = B G, then per refinement pass the "
+                    "residual B - V M (tensor cores: 22 bf16 MMAs per k-step of 16 into seven exact weight classes; "
+                    "tiled: 6 FP32 operations per product) and V += R G"}
 
 
 def gpu_arm(a):
@@ -675,7 +682,7 @@ def gpu_arm(a):
     gate = None if a.skip_gate else energy_gate(ham, kv, a.gate_walkers, gate_calls, a.moves, choice, a.seed + 1)
     adjoint = None if a.skip_grad else adjoint_run(kv, 4, local)
     uneven = None if a.skip_uneven else uneven_run(kv, a.seed, local)
-    large = None if a.skip_large else large_run(kv, a.seed, local)
+    large = None if a.skip_large else large_run(kv, a.seed, local, walkers=a.large_walkers)
     field = None if a.skip_field else field_run(kv, a.seed, local)
     batched = None if a.skip_batched else batched_run(kv, a.seed, local)
     plugin = None if a.skip_plugin else plugin_run(kv, a.seed, local, walkers=a.walkers)

@@ -8,11 +8,15 @@
 // passes of V += (B - V M) G -- split into batched kernels so that the
 // residual B - V M, where the refinement needs more than FP32, runs as a
 // tensor-core GEMM over every walker and spin at once:
-//   oz_prep_kernel      one CTA per (walker, spin): site tables, the FP32 LU,
-//                       G and V = B G as in the tiled refresh; V, the pivot
-//                       order and the site tables to HBM; unit rows of W.
+//   oz_prep_kernel      one CTA per (walker, spin): site tables and the FP32
+//                       LU as in the tiled refresh; the pivot order and the
+//                       site tables to HBM; unit rows of W.
+//   oz_inverse_kernel   G = M^{-1}, one CTA per 32 identity rows.
 //   oz_gather_kernel    the digit planes of M^T for this configuration.
-//   per pass (at most 4):
+//   oz_correct_kernel   first pass: V = B G per 32-row tile.
+//   per pass (at most kOzPasses = 12; a pass only works on the tiles still
+//   refining, so a slowly contracting tile gets more passes than the tiled
+//   refresh's 4 before its walker is handed to the FP64 refresh):
 //   oz_slice_kernel     V's rows split into four digit planes.
 //   oz_residual_kernel  R = B - V M from the digit planes (tcgen05, TMA).
 //   oz_correct_kernel   V += R G per 32-row tile on the CUDA cores, the
@@ -63,6 +67,7 @@ constexpr int kStageBytes = kABytes + kBBytes;
 constexpr int kSmem = kStages * kStageBytes + 1024;   // + alignment slack
 constexpr uint32_t kTmemCols = 512;                   // kClasses * kBN = 448, rounded to a power of two
 constexpr uint32_t kWaitLimit = 1u << 22;
+constexpr int kOzPasses = 12;
 // Operand tiles in shared memory: plane p, k-group g (8 k), row r at byte
 // ((p * (kKS / 8) + g) * rows + r) * 16: every 8 rows x 16 bytes is one
 // core matrix of the no-swizzle K-major layout, adjacent along the rows 128
@@ -171,7 +176,8 @@ OzView view_of(const OzRefresh &o) {
     return v;
 }
 
-// Steps 1 and 2 of the tiled refresh, then V = B G per 32-row tile into HBM.
+// Step 1 of the tiled refresh (site tables, LU of tilde_U in HBM), its
+// results to HBM for the batched kernels, and the unit rows of W.
 __global__ void __launch_bounds__(kTT) oz_prep_kernel(DevModel m, DevBatch b, OzView v, int only_due, int track_drift) {
     const int w = blockIdx.x, spin = blockIdx.y, ws = 2 * w + spin;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nt = blockDim.x, nw = nt / 32;
@@ -184,7 +190,6 @@ __global__ void __launch_bounds__(kTT) oz_prep_kernel(DevModel m, DevBatch b, Oz
     const int n = spin == 0 ? m.n_up : m.n_dn;
     const int n_oth = N - n;
     const int ldw = spin == 0 ? m.ld_up : m.ld_dn;
-    const float *Uh = spin == 0 ? m.U32_up_hi : m.U32_dn_hi;
     const bool cpt = b.compact != 0;
     float *Wout = cpt ? b.G32 + (size_t)w * b.g_block + (spin == 0 ? 0 : (size_t)m.n_dn * m.ld_up)
                       : b.W32 + (size_t)w * N * (m.ld_up + m.ld_dn) + (spin == 0 ? 0 : (size_t)N * m.ld_up);
@@ -193,7 +198,6 @@ __global__ void __launch_bounds__(kTT) oz_prep_kernel(DevModel m, DevBatch b, Oz
     extern __shared__ __align__(16) unsigned char smem[];
     const TileSmem L = tile_smem_layout(n, n_oth);
     float *Z = reinterpret_cast<float *>(smem + L.z);
-    float *Rt = reinterpret_cast<float *>(smem + L.r);
     float *Pn = reinterpret_cast<float *>(smem + L.pn);
     float *Ut = reinterpret_cast<float *>(smem + L.ut);
     float *St = reinterpret_cast<float *>(smem + L.st);
@@ -204,12 +208,10 @@ __global__ void __launch_bounds__(kTT) oz_prep_kernel(DevModel m, DevBatch b, Oz
     short *site_oth = reinterpret_cast<short *>(smem + L.site_oth);
     __shared__ double red[33];
 
-    if (!tile_factor(m, b, w, spin, A, Z, Pn, Ut, St, invd, perm, srow, site_of, site_oth, red)) {
+    if (!tile_factor(m, b, w, spin, A, Z, Pn, Ut, St, invd, perm, srow, site_of, site_oth, red, false)) {
         if (tid == 0) v.active[ws] = 0;
         return;
     }
-    const int ldz = ld_tile(n);   // the tile functions' stride; V and R in HBM use v.ldz >= ldz
-    const float *G = A + (size_t)n * n;
     for (int i = tid; i < n; i += nt) {
         v.perm[(size_t)ws * v.n_max + i] = perm[i];
         v.srow[(size_t)ws * v.n_max + i] = srow[i];
@@ -219,23 +221,6 @@ __global__ void __launch_bounds__(kTT) oz_prep_kernel(DevModel m, DevBatch b, Oz
         v.est[(size_t)ws * v.tiles + t] = 1.f;
         v.dprev[(size_t)ws * v.tiles + t] = 1.f;
         v.done[(size_t)ws * v.tiles + t] = t * kRT < n_oth ? 0 : 1;
-    }
-    for (int e = tid; e < kRT * (ldz - n); e += nt) {
-        const int r = e / (ldz - n), c = n + e % (ldz - n);
-        Rt[(size_t)r * ldz + c] = 0.f;
-    }
-    float *Vw = v.V + (size_t)ws * v.rows_v * v.ldz;
-    for (int b0 = 0; b0 < n_oth; b0 += kRT) {
-        const int rows = min(kRT, n_oth - b0);
-        __syncthreads();
-        for (int cb = 0; cb < n; cb += 32)
-            stage_rows32(Rt + cb, ldz, kRT, min(32, n - cb), min(32, n - cb), [&](int r) -> const float * {
-                return r < rows ? Uh + (size_t)site_oth[b0 + r] * n + cb : nullptr;
-            });
-        tile_gemm(G, n, Rt, Z, ldz, rows, 0, St, red);
-        __syncthreads();
-        for (int r = warp; r < rows; r += nw)
-            for (int c = lane; c < n; c += 32) Vw[(size_t)(b0 + r) * v.ldz + c] = Z[(size_t)r * ldz + c];
     }
     // unit rows at the sites holding this spin (site-indexed W only)
     float dmax = 0.f;
@@ -255,6 +240,50 @@ __global__ void __launch_bounds__(kTT) oz_prep_kernel(DevModel m, DevBatch b, Oz
         if (lane == 0 && dmax > 0.f) atomic_max_nonneg(&b.drift[w], dmax);
     }
     if (tid == 0) v.active[ws] = 1;
+}
+
+// G = M^{-1} (row-major n x n after the LU in the walker-spin's scratch),
+// rows t0 .. t0 + 31 from the identity rows, as in the tiled refresh.
+struct InverseSmem {
+    size_t z, st, invd, perm, total;
+};
+__host__ __device__ inline InverseSmem inverse_layout(int n) {
+    auto al = [](size_t x) { return (x + 15) / 16 * 16; };
+    InverseSmem s{};
+    s.z = 0;
+    s.st = al((size_t)kRT * ld_tile(n) * 4);
+    s.invd = s.st + al((size_t)round4(n) * kLdc * 4);
+    s.perm = s.invd + al((size_t)n * 4);
+    s.total = s.perm + al((size_t)n * 4);
+    return s;
+}
+
+__global__ void __launch_bounds__(kTT) oz_inverse_kernel(DevModel m, DevBatch b, OzView v) {
+    const int w = blockIdx.x, spin = blockIdx.y, ws = 2 * w + spin;
+    const int n = spin == 0 ? m.n_up : m.n_dn;
+    const int t0 = blockIdx.z * kRT;
+    if (!v.active[ws] || t0 >= n) return;
+    const int rows = min(kRT, n - t0), ldz = ld_tile(n);
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nt = blockDim.x, nw = nt / 32;
+    extern __shared__ __align__(16) unsigned char smem[];
+    const InverseSmem L = inverse_layout(n);
+    float *Z = reinterpret_cast<float *>(smem + L.z);
+    float *St = reinterpret_cast<float *>(smem + L.st);
+    float *invd = reinterpret_cast<float *>(smem + L.invd);
+    int *perm = reinterpret_cast<int *>(smem + L.perm);
+    float *A = reinterpret_cast<float *>(b.solve_scratch + ((size_t)w * 2 + spin) * b.solve_block);
+    for (int i = tid; i < n; i += nt) perm[i] = v.perm[(size_t)ws * v.n_max + i];
+    __syncthreads();
+    for (int i = tid; i < n; i += nt) invd[i] = 1.f / A[(size_t)perm[i] * n + i];
+    for (int e = tid; e < kRT * ldz; e += nt) {
+        const int r = e / ldz, c = e - r * ldz;
+        Z[e] = (r < rows && c == t0 + r) ? 1.f : 0.f;
+    }
+    __syncthreads();
+    tile_solve(A, perm, n, invd, Z, ldz, rows, St, t0);
+    float *G = A + (size_t)n * n;
+    for (int r = warp; r < rows; r += nw)
+        for (int c = lane; c < n; c += 32) G[(size_t)(t0 + r) * n + c] = Z[(size_t)r * ldz + c];
 }
 
 // M^T's digit planes: plane t, k-group g, row j holds digit t of
@@ -510,8 +539,12 @@ __host__ __device__ inline CorrectSmem correct_layout(int ldz) {
 }
 
 // V += R G for one 32-row tile, its convergence test, and its rows out to W
-// when it has converged or the passes are spent (last != 0).
-__global__ void __launch_bounds__(kTT) oz_correct_kernel(DevModel m, DevBatch b, OzView v, int last, int track_drift) {
+// when it has converged or the passes are spent (last != 0).  The first pass
+// (first != 0) forms V = B G from V = 0 and R = B (U's high parts), the
+// tiled refresh's starting point: its relative correction is 1, so it never
+// ends a tile.
+__global__ void __launch_bounds__(kTT) oz_correct_kernel(DevModel m, DevBatch b, OzView v, int first, int last,
+                                                         int track_drift) {
     const int w = blockIdx.x, spin = blockIdx.y, tt = blockIdx.z, ws = 2 * w + spin;
     const int N = m.n_sites;
     const int n = spin == 0 ? m.n_up : m.n_dn;
@@ -532,11 +565,13 @@ __global__ void __launch_bounds__(kTT) oz_correct_kernel(DevModel m, DevBatch b,
                      (size_t)n * n;
     float *Vw = v.V + ((size_t)ws * v.rows_v + b0) * v.ldz;
     const float *Rw = v.R + ((size_t)ws * v.rows_v + b0) * v.ldz;
+    const float *Uh = spin == 0 ? m.U32_up_hi : m.U32_dn_hi;
+    const short *so = v.site_oth + (size_t)ws * v.oth_max + b0;
     for (int e = tid; e < kRT * ldz; e += nt) {
         const int r = e / ldz, c = e - r * ldz;
         const bool ok = r < rows && c < n;
-        Z[e] = ok ? Vw[(size_t)r * v.ldz + c] : 0.f;
-        Rt[e] = ok ? Rw[(size_t)r * v.ldz + c] : 0.f;
+        Z[e] = ok && !first ? Vw[(size_t)r * v.ldz + c] : 0.f;
+        Rt[e] = !ok ? 0.f : first ? Uh[(size_t)so[r] * n + c] : Rw[(size_t)r * v.ldz + c];
     }
     const float d = tile_gemm(G, n, Rt, Z, ldz, rows, 1, St, red);   // V += R G (synchronises first)
     if (tid == 0) {
@@ -545,7 +580,7 @@ __global__ void __launch_bounds__(kTT) oz_correct_kernel(DevModel m, DevBatch b,
         const float est = d < dprev ? d * d / dprev : INFINITY;   // a correction that grows: diverging
         v.dprev[k] = d;
         v.est[k] = est;
-        const int fin = !(est > 1e-6f) || last;
+        const int fin = !first && (!(est > 1e-6f) || last);
         s_fin = fin;
         if (fin) {
             v.done[k] = 1;
@@ -671,7 +706,8 @@ size_t oz_scratch_bytes(const DevModel &m, int n_walkers) { return oz_offsets(oz
 bool oz_supported(const DevModel &m, int optin) {
     const OzDims d = oz_dims(m);
     if (!m.U32_up_hi || d.n_max >= 1024 || 2 * d.n_max > 65535) return false;   // the exact-accumulation bound
-    const size_t need = std::max({refresh_tile_smem(m), (size_t)oz::kSmem, correct_layout(d.ldz).total});
+    const size_t need = std::max({refresh_tile_smem(m), (size_t)oz::kSmem, correct_layout(d.ldz).total,
+                                  inverse_layout(d.n_max).total});
     return need + 1024 <= (size_t)optin;
 }
 
@@ -728,6 +764,10 @@ cudaError_t launch_refresh_oz(const DevModel &m, const DevBatch &b, const OzRefr
     cudaError_t e = cudaFuncSetAttribute(oz_prep_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_prep);
     if (e != cudaSuccess) return e;
     oz_prep_kernel<<<dim3(W, 2), kTT, sm_prep, stream>>>(m, b, v, only_due, track_drift);
+    const size_t sm_inv = inverse_layout(oz.n_max).total;
+    if ((e = cudaFuncSetAttribute(oz_inverse_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_inv)))
+        return e;
+    oz_inverse_kernel<<<dim3(W, 2, (oz.n_max + kRT - 1) / kRT), kTT, sm_inv, stream>>>(m, b, v);
     oz_gather_kernel<<<dim3(W, 2, kOzUDigits), 256, 0, stream>>>(m, v);
     const size_t sm_corr = correct_layout(oz.ldz).total;
     if ((e = cudaFuncSetAttribute(oz_correct_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_corr)))
@@ -738,10 +778,11 @@ cudaError_t launch_refresh_oz(const DevModel &m, const DevBatch &b, const OzRefr
     std::memcpy(&tmv, oz.tmap_v, sizeof tmv);
     std::memcpy(&tmm, oz.tmap_m, sizeof tmm);
     const dim3 rgrid(oz.rows_v / oz::kBM, oz.rows_m / oz::kBN, 2 * W);
-    for (int pass = 0; pass < kMaxPasses; ++pass) {
+    oz_correct_kernel<<<dim3(W, 2, oz.tiles), kTT, sm_corr, stream>>>(m, b, v, 1, 0, track_drift);
+    for (int pass = 1; pass <= oz::kOzPasses; ++pass) {
         oz_slice_kernel<<<dim3(W, 2, oz.tiles), 256, 0, stream>>>(m, v);
         oz_residual_kernel<<<rgrid, 128, oz::kSmem, stream>>>(m, b, v, tmv, tmm);
-        oz_correct_kernel<<<dim3(W, 2, oz.tiles), kTT, sm_corr, stream>>>(m, b, v, pass == kMaxPasses - 1,
+        oz_correct_kernel<<<dim3(W, 2, oz.tiles), kTT, sm_corr, stream>>>(m, b, v, 0, pass == oz::kOzPasses,
                                                                           track_drift);
     }
     return cudaGetLastError();

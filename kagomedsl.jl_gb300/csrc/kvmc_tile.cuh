@@ -543,13 +543,13 @@ __device__ __forceinline__ void tile_residual(const float *Uh, const float *Ul, 
 // spins' labels (site_of, site_oth), tilde_U's FP32 LU in A (blocked in HBM,
 // rows never moved: row i of the factors is A[perm[i]]), srow[i] =
 // site_of[perm[i]], log|det tilde_U| and log(min|pivot| / max|pivot|) into
-// b.logdet, and G = M^{-1} (n x n, row-major) at A + n*n, built in the tile
-// Z with St as its block-column buffer.  Returns false, with kStatusRefine
-// set on the walker, for an incomplete configuration or an exactly zero
-// pivot (every thread sees the same answer).
+// b.logdet, and (with_inverse) G = M^{-1} (n x n, row-major) at A + n*n,
+// built in the tile Z with St as its block-column buffer.  Returns false,
+// with kStatusRefine set on the walker, for an incomplete configuration or
+// an exactly zero pivot (every thread sees the same answer).
 __device__ bool tile_factor(const DevModel &m, const DevBatch &b, int w, int spin, float *A, float *Z, float *Pn,
                             float *Ut, float *St, float *invd, int *perm, int *srow, short *site_of,
-                            short *site_oth, double *red) {
+                            short *site_oth, double *red, bool with_inverse = true) {
     const int N = m.n_sites;
     const int n = spin == 0 ? m.n_up : m.n_dn;
     const int n_oth = N - n;
@@ -608,6 +608,7 @@ __device__ bool tile_factor(const DevModel &m, const DevBatch &b, int w, int spi
             b.logdet[4 * w + 2 + spin] = log(dmin / dmaxp);
         }
     }
+    if (!with_inverse) return true;
     const int ldz = ld_tile(n);
     // G = M^{-1}, 32 identity rows at a time (pad columns n .. ldz stay zero)
     float *G = A + (size_t)n * n;
