@@ -173,7 +173,8 @@ int upload_kappa(kvmc_handle *h, const int32_t *ku, const int32_t *kd) {
 
 // The FP32 refresh by iterative refinement: one thread per row (1) or tiled (2)
 cudaError_t refresh32_launch(kvmc_handle *h, int only_due, int track_drift) {
-    if (h->refresh32 == 3) return kvmc::launch_refresh_oz(h->dm, h->db, h->oz, only_due, track_drift, h->stream);
+    if (h->refresh32 == 3)
+        return kvmc::launch_refresh_oz(h->dm, h->db, h->oz, only_due, track_drift, h->device, h->stream);
     return h->refresh32 == 2 ? kvmc::launch_refresh_tile(h->dm, h->db, only_due, track_drift, h->stream)
                              : kvmc::launch_refresh32(h->dm, h->db, only_due, track_drift, h->stream);
 }

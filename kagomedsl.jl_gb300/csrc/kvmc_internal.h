@@ -168,6 +168,11 @@ struct OzRefresh {
     short *site_oth;             // [W*2][oth_max]
     float *est, *dprev;          // [W*2][tiles] refinement state per tile
     int *done, *active;          // [W*2][tiles], [W*2]
+    int n_ws;                    // walker-spins: 2 W
+    int groups;                  // 128-row groups of the residual per (walker, spin): rows_v / 128
+    int *tile_list, *grp_list;   // [2][W*2*tiles], [2][W*2*groups]: work of a pass (ping-pong)
+    int *counts;                 // [4]: tiles and groups in list 0, tiles and groups in list 1
+    int *grp_flag;               // [W*2*groups]: the group is in the next pass's list
     alignas(64) unsigned char tmap_v[128], tmap_m[128];   // CUtensorMap of vd and mt
 };
 size_t oz_scratch_bytes(const DevModel &m, int n_walkers);
@@ -179,7 +184,7 @@ void oz_digits_host(const double *U, int N, int n, uint16_t *ud, int *fexp);
 // the caller) and encodes the tensor maps; ud / fexp must be set already.
 cudaError_t oz_setup(const DevModel &m, int n_walkers, void *scratch, OzRefresh &oz);
 cudaError_t launch_refresh_oz(const DevModel &m, const DevBatch &b, const OzRefresh &oz, int only_due,
-                              int track_drift, cudaStream_t stream);
+                              int track_drift, int device, cudaStream_t stream);
 
 // One warp per walker with W's non-trivial rows indexed by labels (kvmc_warp.cu).
 size_t warp_cta_smem(const DevModel &m);

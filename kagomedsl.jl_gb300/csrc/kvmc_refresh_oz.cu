@@ -155,7 +155,8 @@ __device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
 
 // Device view of the per-walker buffers (kvmc_internal.h: OzRefresh).
 struct OzView {
-    int n_max, oth_max, ldz, kp, rows_v, rows_m, tiles;
+    int n_max, oth_max, ldz, kp, rows_v, rows_m, tiles, n_ws, groups;
+    int *tile_list, *grp_list, *counts, *grp_flag;
     const uint16_t *ud0, *ud1;
     const int *fexp0, *fexp1;
     float *V, *R;
@@ -169,7 +170,8 @@ struct OzView {
 OzView view_of(const OzRefresh &o) {
     OzView v;
     v.n_max = o.n_max; v.oth_max = o.oth_max; v.ldz = o.ldz; v.kp = o.kp;
-    v.rows_v = o.rows_v; v.rows_m = o.rows_m; v.tiles = o.tiles;
+    v.rows_v = o.rows_v; v.rows_m = o.rows_m; v.tiles = o.tiles; v.n_ws = o.n_ws; v.groups = o.groups;
+    v.tile_list = o.tile_list; v.grp_list = o.grp_list; v.counts = o.counts; v.grp_flag = o.grp_flag;
     v.ud0 = o.ud[0]; v.ud1 = o.ud[1]; v.fexp0 = o.fexp[0]; v.fexp1 = o.fexp[1];
     v.V = o.V; v.R = o.R; v.vd = o.vd; v.mt = o.mt; v.vexp = o.vexp; v.perm = o.perm; v.srow = o.srow;
     v.site_oth = o.site_oth; v.est = o.est; v.dprev = o.dprev; v.done = o.done; v.active = o.active;
@@ -217,6 +219,7 @@ __global__ void __launch_bounds__(kTT) oz_prep_kernel(DevModel m, DevBatch b, Oz
         v.srow[(size_t)ws * v.n_max + i] = srow[i];
     }
     for (int i = tid; i < n_oth; i += nt) v.site_oth[(size_t)ws * v.oth_max + i] = site_oth[i];
+    for (int g = tid; g < v.groups; g += nt) v.grp_flag[(size_t)ws * v.groups + g] = 0;
     for (int t = tid; t < v.tiles; t += nt) {
         v.est[(size_t)ws * v.tiles + t] = 1.f;
         v.dprev[(size_t)ws * v.tiles + t] = 1.f;
@@ -316,92 +319,97 @@ __global__ void __launch_bounds__(256) oz_gather_kernel(DevModel m, OzView v) {
     }
 }
 
-// V's digit planes for the 32-row tiles still refining: row i is scaled by
-// 2^-e_i (2^e_i above its largest entry), then split into kOzVDigits digits.
-__global__ void __launch_bounds__(256) oz_slice_kernel(DevModel m, OzView v) {
-    const int w = blockIdx.x, spin = blockIdx.y, tt = blockIdx.z, ws = 2 * w + spin;
-    const int n = spin == 0 ? m.n_up : m.n_dn;
-    const int n_oth = m.n_sites - n;
-    const int b0 = tt * kRT;
-    if (!v.active[ws] || b0 >= n_oth || v.done[(size_t)ws * v.tiles + tt]) return;
-    const int rows = min(kRT, n_oth - b0);
+// V's digit planes for the 32-row tiles of the pass's list: row i is scaled
+// by 2^-e_i (2^e_i above its largest entry), then split into kOzVDigits
+// digits.  One CTA per listed tile, in a grid-stride loop over the list.
+__global__ void __launch_bounds__(256) oz_slice_kernel(DevModel m, OzView v, int cur) {
+    const int count = v.counts[2 * cur];
+    const int *list = v.tile_list + (size_t)cur * v.n_ws * v.tiles;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     __shared__ int s_e[kRT];
-    const float *Vw = v.V + ((size_t)ws * v.rows_v + b0) * v.ldz;
-    for (int r = warp; r < kRT; r += 8) {
-        float mx = 0.f;
-        if (r < rows)
-            for (int c = lane; c < n; c += 32) mx = fmaxf(mx, fabsf(Vw[(size_t)r * v.ldz + c]));
+    for (int it = blockIdx.x; it < count; it += gridDim.x) {
+        const int item = list[it], ws = item / v.tiles, tt = item - ws * v.tiles, spin = ws & 1;
+        const int n = spin == 0 ? m.n_up : m.n_dn;
+        const int n_oth = m.n_sites - n;
+        const int b0 = tt * kRT;
+        const int rows = min(kRT, n_oth - b0);
+        const float *Vw = v.V + ((size_t)ws * v.rows_v + b0) * v.ldz;
+        for (int r = warp; r < kRT; r += 8) {
+            float mx = 0.f;
+            if (r < rows)
+                for (int c = lane; c < n; c += 32) mx = fmaxf(mx, fabsf(Vw[(size_t)r * v.ldz + c]));
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-        if (lane == 0) {
-            int e = 0;
-            if (mx > 0.f && mx < INFINITY) frexpf(mx, &e);   // mx < 2^e
-            s_e[r] = e;
-            if (r < rows) v.vexp[(size_t)ws * v.rows_v + b0 + r] = e;
+            for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+            if (lane == 0) {
+                int e = 0;
+                if (mx > 0.f && mx < INFINITY) frexpf(mx, &e);   // mx < 2^e
+                s_e[r] = e;
+                if (r < rows) v.vexp[(size_t)ws * v.rows_v + b0 + r] = e;
+            }
         }
-    }
-    __syncthreads();
-    const int groups = (n + 7) / 8;
-    const size_t plane = (size_t)(v.kp / 8) * v.rows_v * 8;
-    uint16_t *dst = v.vd + (size_t)ws * kOzVDigits * plane;
-    for (int e = tid; e < groups * kRT; e += blockDim.x) {
-        const int r = e & (kRT - 1), g = e / kRT;
-        if (r >= rows) continue;
-        const float sc = oz::pow2(6 - s_e[r]);
-        float y[8];
-#pragma unroll
-        for (int q = 0; q < 8; ++q) {
-            const int k = 8 * g + q;
-            y[q] = k < n ? Vw[(size_t)r * v.ldz + k] * sc : 0.f;   // |y| < 64, exact
-        }
-#pragma unroll
-        for (int s = 0; s < kOzVDigits; ++s) {
-            uint32_t h[8];
+        __syncthreads();
+        const int groups = (n + 7) / 8;
+        const size_t plane = (size_t)(v.kp / 8) * v.rows_v * 8;
+        uint16_t *dst = v.vd + (size_t)ws * kOzVDigits * plane;
+        for (int e = tid; e < groups * kRT; e += blockDim.x) {
+            const int r = e & (kRT - 1), g = e / kRT;
+            if (r >= rows) continue;
+            const float sc = oz::pow2(6 - s_e[r]);
+            float y[8];
 #pragma unroll
             for (int q = 0; q < 8; ++q) {
-                const float d = rintf(y[q]);                   // |d| <= 64
-                h[q] = __float_as_uint(d) >> 16;               // exact in bf16
-                y[q] = (y[q] - d) * 128.f;                     // exact; |y| <= 64
+                const int k = 8 * g + q;
+                y[q] = k < n ? Vw[(size_t)r * v.ldz + k] * sc : 0.f;   // |y| < 64, exact
             }
-            uint4 pk;
-            pk.x = h[0] | (h[1] << 16);
-            pk.y = h[2] | (h[3] << 16);
-            pk.z = h[4] | (h[5] << 16);
-            pk.w = h[6] | (h[7] << 16);
-            *reinterpret_cast<uint4 *>(dst + s * plane + ((size_t)g * v.rows_v + b0 + r) * 8) = pk;
+#pragma unroll
+            for (int s = 0; s < kOzVDigits; ++s) {
+                uint32_t h[8];
+#pragma unroll
+                for (int q = 0; q < 8; ++q) {
+                    const float d = rintf(y[q]);                   // |d| <= 64
+                    h[q] = __float_as_uint(d) >> 16;               // exact in bf16
+                    y[q] = (y[q] - d) * 128.f;                     // exact; |y| <= 64
+                }
+                uint4 pk;
+                pk.x = h[0] | (h[1] << 16);
+                pk.y = h[2] | (h[3] << 16);
+                pk.z = h[4] | (h[5] << 16);
+                pk.w = h[6] | (h[7] << 16);
+                *reinterpret_cast<uint4 *>(dst + s * plane + ((size_t)g * v.rows_v + b0 + r) * 8) = pk;
+            }
         }
+        __syncthreads();
     }
 }
 
-// R = B - V M for one 128 x 64 tile of one (walker, spin).  Warp 0's first
-// lane loads the digit planes stage by stage with TMA, warp 1's first lane
-// issues the 22 MMAs of each k-step into the seven class accumulators, and
-// all four warps then read their 32 rows of the classes from tensor memory,
-// combine them and subtract them from B.  Every wait is bounded; one that
-// gives up marks the walker kStatusTimeout and the tile is left unwritten.
-__global__ void __launch_bounds__(128, 1)
-oz_residual_kernel(DevModel m, DevBatch b, OzView v, const __grid_constant__ CUtensorMap tmv,
+// R = B - V M.  Persistent: one CTA per SM walks the units of the pass --
+// (walker-spin, 128-row group, 64-column tile) for every group in the
+// list -- in steps of the grid.  Warp 4's first lane loads the digit planes
+// stage by stage with TMA, up to three stages ahead and across units; warp
+// 5's first lane issues the 22 MMAs of each k-step into the seven class
+// accumulators, and before a unit's first MMA waits until warps 0-3 have
+// read the previous unit's classes out of tensor memory; warps 0-3 (TMEM
+// lanes 0-127, the group's rows) combine the classes and subtract them from
+// B, whose entries they fetch ahead.  Every wait is bounded; one that gives
+// up stops the CTA, whose units' walkers are then marked kStatusTimeout.
+constexpr int kResThreads = 192;
+
+__global__ void __launch_bounds__(kResThreads, 1)
+oz_residual_kernel(DevModel m, DevBatch b, OzView v, int cur, const __grid_constant__ CUtensorMap tmv,
                    const __grid_constant__ CUtensorMap tmm) {
     using namespace oz;
-    const int ws = blockIdx.z, w = ws >> 1, spin = ws & 1;
-    if (!v.active[ws]) return;
-    const int n = spin == 0 ? m.n_up : m.n_dn;
-    const int n_oth = m.n_sites - n;
-    const int r0 = blockIdx.x * kBM, c0 = blockIdx.y * kBN;
-    if (r0 >= n_oth || c0 >= n) return;
-    bool any = false;
-    for (int q = 0; q < kBM / kRT; ++q) {
-        const int tt = r0 / kRT + q;
-        if (tt * kRT < n_oth && !v.done[(size_t)ws * v.tiles + tt]) any = true;
-    }
-    if (!any) return;
+    const int ngrp = v.counts[2 * cur + 1];
+    const int ctiles = v.rows_m / kBN;
+    const int units = ngrp * ctiles;
+    if ((int)blockIdx.x >= units) return;
+    const int *glist = v.grp_list + (size_t)cur * v.n_ws * v.groups;
 
     extern __shared__ unsigned char smem_raw[];
     unsigned char *sm = reinterpret_cast<unsigned char *>(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-    __shared__ __align__(8) uint64_t full[kStages], empty[kStages], done_bar;
+    __shared__ __align__(8) uint64_t full[kStages], empty[kStages], done_bar, tfree_bar;
     __shared__ uint32_t tmem_slot;
-    __shared__ int s_fail, s_issued;
+    __shared__ volatile int s_fail;
+    __shared__ int s_issued;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     if (tid == 0) {
         for (int s = 0; s < kStages; ++s) {
@@ -409,6 +417,7 @@ oz_residual_kernel(DevModel m, DevBatch b, OzView v, const __grid_constant__ CUt
             bar_init(&empty[s], 1);
         }
         bar_init(&done_bar, 1);
+        bar_init(&tfree_bar, 4);   // one arrival per epilogue warp
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         s_fail = 0;
         s_issued = 0;
@@ -422,90 +431,159 @@ oz_residual_kernel(DevModel m, DevBatch b, OzView v, const __grid_constant__ CUt
     __syncthreads();
     fence_after();
     const uint32_t tmem = tmem_slot;
-    const int nch = (n + kKS - 1) / kKS;
+    // unit u -> (walker-spin, first row, first column, orbitals, other rows); false: nothing to do
+    auto unit = [&](int u, int &item, int &ws, int &r0, int &c0, int &n, int &n_oth) {
+        const int gi = u / ctiles, ct = u - gi * ctiles;
+        item = glist[gi];
+        ws = item / v.groups;
+        r0 = (item - ws * v.groups) * kBM;
+        c0 = ct * kBN;
+        n = (ws & 1) == 0 ? m.n_up : m.n_dn;
+        n_oth = m.n_sites - n;
+        return c0 < n && r0 < n_oth;
+    };
 
-    if (warp == 0) {
+    if (warp == 4) {
         if (lane == 0) {
-            int ch = 0;
-            for (; ch < nch; ++ch) {
-                const int s = ch % kStages;
-                if (ch >= kStages && !wait(&empty[s], ((ch / kStages) - 1) & 1)) {
+            int gch = 0;
+            bool stop = false;
+            for (int u = blockIdx.x; u < units && !stop && !s_fail; u += gridDim.x) {
+                int item, ws, r0, c0, n, n_oth;
+                if (!unit(u, item, ws, r0, c0, n, n_oth)) continue;
+                if (c0 == 0) v.grp_flag[item] = 0;   // the next pass's correction may list the group again
+                const int nch = (n + kKS - 1) / kKS;
+                for (int ch = 0; ch < nch; ++ch, ++gch) {
+                    const int s = gch % kStages;
+                    if (gch >= kStages && !wait(&empty[s], ((gch / kStages) - 1) & 1)) {
+                        s_fail = 1;
+                        stop = true;
+                        break;
+                    }
+                    expect_tx(&full[s], kStageBytes);
+                    unsigned char *st = sm + (size_t)s * kStageBytes;
+                    tma_load5(st, &tmv, 0, r0, ch * (kKS / 8), 0, ws, &full[s]);
+                    tma_load5(st + kABytes, &tmm, 0, c0, ch * (kKS / 8), 0, ws, &full[s]);
+                }
+            }
+            s_issued = gch;
+        }
+        __syncwarp();
+    } else if (warp == 5) {
+        if (lane == 0) {
+            constexpr uint32_t idesc = idesc_bf16(kBM, kBN);
+            int gch = 0, k = 0;
+            for (int u = blockIdx.x; u < units && !s_fail; u += gridDim.x) {
+                int item, ws, r0, c0, n, n_oth;
+                if (!unit(u, item, ws, r0, c0, n, n_oth)) continue;
+                if (k > 0 && !wait(&tfree_bar, (k - 1) & 1)) {
                     s_fail = 1;
                     break;
                 }
-                expect_tx(&full[s], kStageBytes);
-                unsigned char *st = sm + (size_t)s * kStageBytes;
-                tma_load5(st, &tmv, 0, r0, ch * (kKS / 8), 0, ws, &full[s]);
-                tma_load5(st + kABytes, &tmm, 0, c0, ch * (kKS / 8), 0, ws, &full[s]);
-            }
-            s_issued = ch;
-        }
-        __syncwarp();
-    } else if (warp == 1) {
-        if (lane == 0) {
-            constexpr uint32_t idesc = idesc_bf16(kBM, kBN);
-            bool ok = true;
-            for (int ch = 0; ch < nch; ++ch) {
-                const int s = ch % kStages;
-                if (!wait(&full[s], (ch / kStages) & 1)) {
-                    ok = false;
-                    break;
-                }
                 fence_after();
-                const uint32_t a0 = smem_u32(sm + (size_t)s * kStageBytes), b0 = a0 + kABytes;
+                const int nch = (n + kKS - 1) / kKS;
+                bool ok = true;
+                for (int ch = 0; ch < nch; ++ch, ++gch) {
+                    const int s = gch % kStages;
+                    if (!wait(&full[s], (gch / kStages) & 1)) {
+                        ok = false;
+                        break;
+                    }
+                    fence_after();
+                    const uint32_t a0 = smem_u32(sm + (size_t)s * kStageBytes), b0 = a0 + kABytes;
 #pragma unroll
-                for (int q = 0; q < kKS / 16; ++q) {
+                    for (int q = 0; q < kKS / 16; ++q) {
 #pragma unroll
-                    for (int c = 0; c < kClasses; ++c) {
+                        for (int c = 0; c < kClasses; ++c) {
 #pragma unroll
-                        for (int sa = 0; sa < kOzVDigits; ++sa) {
-                            const int tb = c - sa;
-                            if (tb < 0 || tb >= kOzUDigits) continue;
-                            const uint64_t ad = sdesc(a0 + sa * (kBM * kKS * 2) + q * 2 * kLboA, kLboA, kSbo);
-                            const uint64_t bd = sdesc(b0 + tb * (kBN * kKS * 2) + q * 2 * kLboB, kLboB, kSbo);
-                            mma(tmem + (uint32_t)(c * kBN), ad, bd, idesc, (ch > 0 || q > 0 || sa > 0) ? 1u : 0u);
+                            for (int sa = 0; sa < kOzVDigits; ++sa) {
+                                const int tb = c - sa;
+                                if (tb < 0 || tb >= kOzUDigits) continue;
+                                const uint64_t ad = sdesc(a0 + sa * (kBM * kKS * 2) + q * 2 * kLboA, kLboA, kSbo);
+                                const uint64_t bd = sdesc(b0 + tb * (kBN * kKS * 2) + q * 2 * kLboB, kLboB, kSbo);
+                                mma(tmem + (uint32_t)(c * kBN), ad, bd, idesc, (ch > 0 || q > 0 || sa > 0) ? 1u : 0u);
+                            }
                         }
                     }
+                    commit(&empty[s]);   // the stage is free once these MMAs have read it
                 }
-                commit(&empty[s]);   // the stage is free once these MMAs have read it
+                commit(&done_bar);       // always, so that the epilogue's wait ends
+                ++k;
+                if (!ok) {
+                    s_fail = 1;
+                    break;
+                }
             }
-            if (!ok) s_fail = 1;
-            commit(&done_bar);       // arrives once every MMA issued above has completed
         }
         __syncwarp();
-    }
-    __syncthreads();
-    const bool ok = wait(&done_bar, 0) && !s_fail;
-    fence_after();
-
-    // epilogue: row i of the tile is TMEM lane i; warp g reads lanes 32 g ..
-    const int i = r0 + 32 * warp + lane;
-    const bool row_ok = ok && i < n_oth && !v.done[(size_t)ws * v.tiles + i / kRT];
-    const int *fexp = spin == 0 ? v.fexp0 : v.fexp1;
-    const float *Uh = spin == 0 ? m.U32_up_hi : m.U32_dn_hi;
-    const float *Ul = spin == 0 ? m.U32_up_lo : m.U32_dn_lo;
-    const int site = row_ok ? v.site_oth[(size_t)ws * v.oth_max + i] : 0;
-    const float sc_i = row_ok ? pow2(v.vexp[(size_t)ws * v.rows_v + i] - 12) : 0.f;
-    const float *bh = Uh + (size_t)site * n, *bl = Ul + (size_t)site * n;
-    float *Rrow = v.R + ((size_t)ws * v.rows_v + (row_ok ? i : 0)) * v.ldz;
-    const uint32_t tl = tmem + ((uint32_t)(32 * warp) << 16);
-    for (int cc = 0; cc < kBN; cc += 8) {
-        float d[kClasses][8];
+    } else {
+        // epilogue: warp g reads TMEM lanes 32 g .. 32 g + 31, rows r0 + 32 g + lane
+        const uint32_t tl = tmem + ((uint32_t)(32 * warp) << 16);
+        int k = 0;
+        for (int u = blockIdx.x; u < units; u += gridDim.x) {
+            int item, ws, r0, c0, n, n_oth;
+            if (!unit(u, item, ws, r0, c0, n, n_oth)) continue;
+            const int spin = ws & 1;
+            const int i = r0 + 32 * warp + lane;
+            const bool row_ok = i < n_oth;
+            const int *fexp = spin == 0 ? v.fexp0 : v.fexp1;
+            const float *Uh = spin == 0 ? m.U32_up_hi : m.U32_dn_hi;
+            const float *Ul = spin == 0 ? m.U32_up_lo : m.U32_dn_lo;
+            const int site = row_ok ? v.site_oth[(size_t)ws * v.oth_max + i] : 0;
+            const float sc_i = row_ok ? pow2(v.vexp[(size_t)ws * v.rows_v + i] - 12) : 0.f;
+            const float *bh = Uh + (size_t)site * n, *bl = Ul + (size_t)site * n;
+            float *Rrow = v.R + ((size_t)ws * v.rows_v + (row_ok ? i : 0)) * v.ldz;
+            float ph[8], pl[8];   // B's next eight entries, fetched ahead
 #pragma unroll
-        for (int c = 0; c < kClasses; ++c) ld8(tl + (uint32_t)(c * kBN + cc), d[c]);
-        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-        if (!row_ok) continue;
+            for (int q = 0; q < 8; ++q) {
+                const bool ok = row_ok && c0 + q < n;
+                ph[q] = ok ? bh[c0 + q] : 0.f;
+                pl[q] = ok ? bl[c0 + q] : 0.f;
+            }
+            if (!wait(&done_bar, k & 1)) {
+                s_fail = 1;
+                break;
+            }
+            fence_after();
+            const bool good = !s_fail;
+            for (int cc = 0; cc < kBN; cc += 8) {
+                float d[kClasses][8];
 #pragma unroll
-        for (int q = 0; q < 8; ++q) {
-            const int j = c0 + cc + q;
-            if (j >= n) break;
-            float h1, e1, h2, e2;
-            two_sum(d[0][q], d[1][q] * 0x1p-7f, h1, e1);
-            two_sum(h1, d[2][q] * 0x1p-14f, h2, e2);
-            const float t = fmaf(d[6][q], 0x1p-42f, fmaf(d[5][q], 0x1p-35f, fmaf(d[4][q], 0x1p-28f, d[3][q] * 0x1p-21f)));
-            const float lo = (e1 + e2) + t;
-            const float s = sc_i * pow2(fexp[j]);
-            Rrow[j] = ((bh[j] - h2 * s) - lo * s) + bl[j];
+                for (int c = 0; c < kClasses; ++c) ld8(tl + (uint32_t)(c * kBN + cc), d[c]);
+                asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+                float ch_[8], cl_[8];
+#pragma unroll
+                for (int q = 0; q < 8; ++q) {
+                    ch_[q] = ph[q];
+                    cl_[q] = pl[q];
+                }
+                if (cc + 8 < kBN) {
+#pragma unroll
+                    for (int q = 0; q < 8; ++q) {
+                        const int j = c0 + cc + 8 + q;
+                        const bool ok = row_ok && j < n;
+                        ph[q] = ok ? bh[j] : 0.f;
+                        pl[q] = ok ? bl[j] : 0.f;
+                    }
+                }
+                if (!(row_ok && good)) continue;
+#pragma unroll
+                for (int q = 0; q < 8; ++q) {
+                    const int j = c0 + cc + q;
+                    if (j >= n) break;
+                    float h1, e1, h2, e2;
+                    two_sum(d[0][q], d[1][q] * 0x1p-7f, h1, e1);
+                    two_sum(h1, d[2][q] * 0x1p-14f, h2, e2);
+                    const float t =
+                        fmaf(d[6][q], 0x1p-42f, fmaf(d[5][q], 0x1p-35f, fmaf(d[4][q], 0x1p-28f, d[3][q] * 0x1p-21f)));
+                    const float lo = (e1 + e2) + t;
+                    const float s = sc_i * pow2(fexp[j]);
+                    Rrow[j] = ((ch_[q] - h2 * s) - lo * s) + cl_[q];
+                }
+            }
+            fence_before();
+            __syncwarp();
+            if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" :: "r"(smem_u32(&tfree_bar)) : "memory");
+            ++k;
         }
     }
 
@@ -519,11 +597,17 @@ oz_residual_kernel(DevModel m, DevBatch b, OzView v, const __grid_constant__ CUt
             const int last = s + ((issued - 1 - s) / kStages) * kStages;
             wait(&full[s], (last / kStages) & 1);
         }
-        if (!ok) atomicOr(&b.status[w], kStatusTimeout);
+        if (s_fail)
+            for (int u = blockIdx.x; u < units; u += gridDim.x) {
+                int item, ws, r0, c0, n, n_oth;
+                unit(u, item, ws, r0, c0, n, n_oth);
+                atomicOr(&b.status[ws >> 1], kStatusTimeout);
+            }
     }
     __syncthreads();
     if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" :: "r"(tmem), "r"(kTmemCols));
 }
+
 
 struct CorrectSmem {
     size_t z, r, st, total;
@@ -539,13 +623,15 @@ __host__ __device__ inline CorrectSmem correct_layout(int ldz) {
 }
 
 // V += R G for one 32-row tile, its convergence test, and its rows out to W
-// when it has converged or the passes are spent (last != 0).  The first pass
-// (first != 0) forms V = B G from V = 0 and R = B (U's high parts), the
-// tiled refresh's starting point: its relative correction is 1, so it never
-// ends a tile.
-__global__ void __launch_bounds__(kTT) oz_correct_kernel(DevModel m, DevBatch b, OzView v, int first, int last,
-                                                         int track_drift) {
-    const int w = blockIdx.x, spin = blockIdx.y, tt = blockIdx.z, ws = 2 * w + spin;
+// when it has converged or the passes are spent (last != 0); a tile still
+// refining goes on the next pass's list (nxt), and its 128-row group on the
+// next group list unless it is there already.  The first pass (first != 0)
+// forms V = B G from V = 0 and R = B (U's high parts), the tiled refresh's
+// starting point: its relative correction is 1, so it never ends a tile.
+__device__ __forceinline__ void correct_tile(const DevModel &m, const DevBatch &b, const OzView &v, int ws, int tt,
+                                             int first, int last, int nxt, int track_drift, unsigned char *smem,
+                                             double *red, int *s_fin) {
+    const int w = ws >> 1, spin = ws & 1;
     const int N = m.n_sites;
     const int n = spin == 0 ? m.n_up : m.n_dn;
     const int n_oth = N - n;
@@ -554,13 +640,10 @@ __global__ void __launch_bounds__(kTT) oz_correct_kernel(DevModel m, DevBatch b,
     const int rows = min(kRT, n_oth - b0);
     const int ldz = ld_tile(n), ldw = spin == 0 ? m.ld_up : m.ld_dn;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nt = blockDim.x, nw = nt / 32;
-    extern __shared__ __align__(16) unsigned char smem[];
     const CorrectSmem L = correct_layout(ldz);
     float *Z = reinterpret_cast<float *>(smem + L.z);
     float *Rt = reinterpret_cast<float *>(smem + L.r);
     float *St = reinterpret_cast<float *>(smem + L.st);
-    __shared__ double red[33];
-    __shared__ int s_fin;
     const float *G = reinterpret_cast<const float *>(b.solve_scratch + ((size_t)w * 2 + spin) * b.solve_block) +
                      (size_t)n * n;
     float *Vw = v.V + ((size_t)ws * v.rows_v + b0) * v.ldz;
@@ -575,20 +658,25 @@ __global__ void __launch_bounds__(kTT) oz_correct_kernel(DevModel m, DevBatch b,
     }
     const float d = tile_gemm(G, n, Rt, Z, ldz, rows, 1, St, red);   // V += R G (synchronises first)
     if (tid == 0) {
-        const size_t k = (size_t)ws * v.tiles + tt;
-        const float dprev = v.dprev[k];
+        const int item = ws * v.tiles + tt;
+        const float dprev = v.dprev[item];
         const float est = d < dprev ? d * d / dprev : INFINITY;   // a correction that grows: diverging
-        v.dprev[k] = d;
-        v.est[k] = est;
+        v.dprev[item] = d;
+        v.est[item] = est;
         const int fin = !first && (!(est > 1e-6f) || last);
-        s_fin = fin;
+        *s_fin = fin;
         if (fin) {
-            v.done[k] = 1;
+            v.done[item] = 1;
             if (!(est <= 1e-5f)) atomicOr(&b.status[w], kStatusRefine);
+        } else {
+            v.tile_list[(size_t)nxt * v.n_ws * v.tiles + atomicAdd(&v.counts[2 * nxt], 1)] = item;
+            const int g = ws * v.groups + b0 / oz::kBM;
+            if (atomicExch(&v.grp_flag[g], 1) == 0)
+                v.grp_list[(size_t)nxt * v.n_ws * v.groups + atomicAdd(&v.counts[2 * nxt + 1], 1)] = g;
         }
     }
     __syncthreads();
-    if (!s_fin) {
+    if (!*s_fin) {
         for (int e = tid; e < rows * n; e += nt) {
             const int r = e / n, c = e - r * n;
             Vw[(size_t)r * v.ldz + c] = Z[(size_t)r * ldz + c];
@@ -619,6 +707,28 @@ __global__ void __launch_bounds__(kTT) oz_correct_kernel(DevModel m, DevBatch b,
         if (lane == 0 && dmax > 0.f) atomic_max_nonneg(&b.drift[w], dmax);
     }
 }
+
+// first != 0: one CTA per (walker, spin, tile), every tile; else a
+// grid-stride loop over the tiles of list `cur`.
+__global__ void __launch_bounds__(kTT) oz_correct_kernel(DevModel m, DevBatch b, OzView v, int first, int last,
+                                                         int cur, int track_drift) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ double red[33];
+    __shared__ int s_fin;
+    const int nxt = cur ^ 1;
+    if (first) {
+        correct_tile(m, b, v, 2 * blockIdx.x + blockIdx.y, blockIdx.z, 1, 0, nxt, track_drift, smem, red, &s_fin);
+        return;
+    }
+    const int count = v.counts[2 * cur];
+    const int *list = v.tile_list + (size_t)cur * v.n_ws * v.tiles;
+    for (int it = blockIdx.x; it < count; it += gridDim.x) {
+        const int item = list[it], ws = item / v.tiles;
+        correct_tile(m, b, v, ws, item - ws * v.tiles, 0, last, nxt, track_drift, smem, red, &s_fin);
+        __syncthreads();
+    }
+}
+
 
 using EncodeTiled = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
                                  const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
@@ -672,7 +782,8 @@ OzDims oz_dims(const DevModel &m) {
 
 // byte offsets of the per-walker-spin buffers inside one allocation
 struct OzOffsets {
-    size_t V, R, vd, mt, vexp, perm, srow, site_oth, est, dprev, done, active, total;
+    size_t V, R, vd, mt, vexp, perm, srow, site_oth, est, dprev, done, active, tile_list, grp_list, counts, grp_flag,
+        total;
 };
 OzOffsets oz_offsets(const OzDims &d, int n_walkers) {
     const size_t S = (size_t)2 * n_walkers;
@@ -695,6 +806,10 @@ OzOffsets oz_offsets(const OzDims &d, int n_walkers) {
     o.dprev = take(S * d.tiles * 4);
     o.done = take(S * d.tiles * 4);
     o.active = take(S * 4);
+    o.tile_list = take(2 * S * d.tiles * 4);
+    o.grp_list = take(2 * S * (d.rows_v / oz::kBM) * 4);
+    o.counts = take(4 * 4);
+    o.grp_flag = take(S * (d.rows_v / oz::kBM) * 4);
     o.total = p;
     return o;
 }
@@ -750,13 +865,19 @@ cudaError_t oz_setup(const DevModel &m, int n_walkers, void *scratch, OzRefresh 
     oz.dprev = reinterpret_cast<float *>(base + o.dprev);
     oz.done = reinterpret_cast<int *>(base + o.done);
     oz.active = reinterpret_cast<int *>(base + o.active);
+    oz.n_ws = 2 * n_walkers;
+    oz.groups = d.rows_v / oz::kBM;
+    oz.tile_list = reinterpret_cast<int *>(base + o.tile_list);
+    oz.grp_list = reinterpret_cast<int *>(base + o.grp_list);
+    oz.counts = reinterpret_cast<int *>(base + o.counts);
+    oz.grp_flag = reinterpret_cast<int *>(base + o.grp_flag);
     cudaError_t e = encode_planes(oz.tmap_v, oz.vd, d.rows_v, d.kp, kOzVDigits, 2 * n_walkers, oz::kBM);
     if (e == cudaSuccess) e = encode_planes(oz.tmap_m, oz.mt, d.rows_m, d.kp, kOzUDigits, 2 * n_walkers, oz::kBN);
     return e;
 }
 
 cudaError_t launch_refresh_oz(const DevModel &m, const DevBatch &b, const OzRefresh &oz, int only_due,
-                              int track_drift, cudaStream_t stream) {
+                              int track_drift, int device, cudaStream_t stream) {
     if (!m.U32_up_hi || !b.solve_scratch || !oz.V) return cudaErrorInvalidValue;
     const OzView v = view_of(oz);
     const int W = b.n_walkers;
@@ -777,13 +898,18 @@ cudaError_t launch_refresh_oz(const DevModel &m, const DevBatch &b, const OzRefr
     CUtensorMap tmv, tmm;
     std::memcpy(&tmv, oz.tmap_v, sizeof tmv);
     std::memcpy(&tmm, oz.tmap_m, sizeof tmm);
-    const dim3 rgrid(oz.rows_v / oz::kBM, oz.rows_m / oz::kBN, 2 * W);
-    oz_correct_kernel<<<dim3(W, 2, oz.tiles), kTT, sm_corr, stream>>>(m, b, v, 1, 0, track_drift);
+    int sms = 0;
+    if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device))) return e;
+    // the first correction lists every tile still refining in list 1; pass p
+    // works on list p & 1 and fills the other, whose counters are cleared first
+    if ((e = cudaMemsetAsync(oz.counts, 0, 4 * sizeof(int), stream))) return e;
+    oz_correct_kernel<<<dim3(W, 2, oz.tiles), kTT, sm_corr, stream>>>(m, b, v, 1, 0, 0, track_drift);
     for (int pass = 1; pass <= oz::kOzPasses; ++pass) {
-        oz_slice_kernel<<<dim3(W, 2, oz.tiles), 256, 0, stream>>>(m, v);
-        oz_residual_kernel<<<rgrid, 128, oz::kSmem, stream>>>(m, b, v, tmv, tmm);
-        oz_correct_kernel<<<dim3(W, 2, oz.tiles), kTT, sm_corr, stream>>>(m, b, v, 0, pass == oz::kOzPasses,
-                                                                          track_drift);
+        const int cur = pass & 1, nxt = cur ^ 1;
+        oz_slice_kernel<<<4 * sms, 256, 0, stream>>>(m, v, cur);
+        oz_residual_kernel<<<sms, kResThreads, oz::kSmem, stream>>>(m, b, v, cur, tmv, tmm);
+        if ((e = cudaMemsetAsync(oz.counts + 2 * nxt, 0, 2 * sizeof(int), stream))) return e;
+        oz_correct_kernel<<<sms, kTT, sm_corr, stream>>>(m, b, v, 0, pass == oz::kOzPasses, cur, track_drift);
     }
     return cudaGetLastError();
 }
