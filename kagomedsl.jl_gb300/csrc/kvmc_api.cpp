@@ -838,14 +838,15 @@ extern "C" int kvmc_create(const kvmc_model_desc *model, const kvmc_batch_desc *
     // the mixed real form on GB300: one thread per row below 96 orbitals per spin
     // (measured at 27 and 48), in tiles of 32 rows from 96 on (measured at 108,
     // 192 and 432: 1.4x, 3.5x and 2.1x the FP64 refresh) while its tiles fit in
-    // shared memory, and from 288 on with its residual on the tensor cores
-    // (measured at 432: 166 against 237 ms for two refreshes of 512 walkers; at
-    // 108 and 192 the tiled form is as fast or faster), else the FP64 refresh
+    // shared memory, and from 192 on with its residual and correction products
+    // on the tensor cores (measured at 432: 142 against 236 ms for two
+    // refreshes of 512 walkers; at 192: 8.8 against 9.7 ms; at 108 as fast as
+    // the tiled form), else the FP64 refresh
     if (h->mixed && !h->cplx) {
         const int nmax = std::max(nu, nd);
         if (nmax < 96) h->refresh32 = kvmc::refresh32_supported(m) ? 1 : 0;
         else h->refresh32 = kvmc::refresh_tile_smem(m) + 1024 <= (size_t)optin ? 2 : 0;
-        if (nmax >= 288 && kvmc::oz_supported(m, optin)) {
+        if (nmax >= 192 && kvmc::oz_supported(m, optin)) {
             if (int rc2 = oz_prepare(h)) return bail(rc2);
             h->refresh32 = 3;
         }

@@ -160,9 +160,13 @@ struct OzRefresh {
     int tiles;                   // 32-row tiles of X per (walker, spin): ceil(oth_max / 32)
     const uint16_t *ud[2];       // per spin: U's digits, [kOzUDigits][N][n] bf16 bits, row-major by site
     const int *fexp[2];          // per spin: column scale exponents, [n]
-    float *V, *R;                // [W*2][rows_v][ldz]
+    float *V;                    // [W*2][rows_v][ldz]
     uint16_t *vd;                // [W*2][kOzVDigits][kp/8][rows_v][8] bf16 bits
     uint16_t *mt;                // [W*2][kOzUDigits][kp/8][rows_m][8] bf16 bits: M^T's digits
+    int cn, rows_g;              // columns of V per correction tile; rows of the G^T planes (multiple of cn)
+    uint16_t *rd;                // [W*2][3][kp/8][rows_v][8] bf16 bits: R = r0 + r1 + r2
+    uint16_t *gd;                // [W*2][3][kp/8][rows_g][8] bf16 bits: G^T = g0 + g1 + g2
+    float *dmax, *vmax;          // [W*2][rows_v]: per row, max |R G| and max |V| of the pass
     int *vexp;                   // [W*2][rows_v] row scale exponents of V
     int *perm, *srow;            // [W*2][n_max] pivot order and the site of M's row i
     short *site_oth;             // [W*2][oth_max]
@@ -174,6 +178,7 @@ struct OzRefresh {
     int *counts;                 // [4]: tiles and groups in list 0, tiles and groups in list 1
     int *grp_flag;               // [W*2*groups]: the group is in the next pass's list
     alignas(64) unsigned char tmap_v[128], tmap_m[128];   // CUtensorMap of vd and mt
+    alignas(64) unsigned char tmap_r[128], tmap_g[128];   // CUtensorMap of rd and gd
 };
 size_t oz_scratch_bytes(const DevModel &m, int n_walkers);
 bool oz_supported(const DevModel &m, int optin);

@@ -1,28 +1,31 @@
-// The periodic refresh of the mixed real form with the residual of its
-// iterative refinement on the tensor cores (kvmc.h: KVMC_TUNE_REFRESH32 = 3).
+// The periodic refresh of the mixed real form with the GEMM-shaped work of
+// its iterative refinement on the tensor cores (kvmc.h: KVMC_TUNE_REFRESH32 = 3).
 //
 // Reference counterpart: reevaluateW! with tilde_U (KagomeDSL.jl
 // src/MonteCarlo.jl:55-115): W = U tilde_U^{-1}.  The algorithm is the tiled
 // FP32 refinement of kvmc_refresh_tile.cu -- X tilde_U = B for the n_oth rows
 // at the other spin's sites, V = B G with G = M^{-1} (M = P tilde_U), then
-// passes of V += (B - V M) G -- split into batched kernels so that the
-// residual B - V M, where the refinement needs more than FP32, runs as a
-// tensor-core GEMM over every walker and spin at once:
+// passes of V += (B - V M) G -- split into batched kernels over every walker
+// and spin at once, with both products per pass as tensor-core GEMMs:
 //   oz_prep_kernel      one CTA per (walker, spin): site tables and the FP32
 //                       LU as in the tiled refresh; the pivot order and the
 //                       site tables to HBM; unit rows of W.
-//   oz_inverse_kernel   G = M^{-1}, one CTA per 32 identity rows.
+//   oz_inverse_kernel   G = M^{-1}, one CTA per 32 identity rows; G^T as
+//                       three bf16 planes.
 //   oz_gather_kernel    the digit planes of M^T for this configuration.
-//   oz_correct_kernel   first pass: V = B G per 32-row tile.
-//   per pass (at most kOzPasses = 12; a pass only works on the tiles still
-//   refining, so a slowly contracting tile gets more passes than the tiled
-//   refresh's 4 before its walker is handed to the FP64 refresh):
+//   oz_bplanes_kernel   the first pass's R = B as three bf16 planes.
+//   oz_corr_kernel      V += R G (the first pass: V = B G), tcgen05 + TMA.
+//   oz_check_kernel     per 32-row tile: the convergence test of the tiled
+//                       refresh, and the tile's rows out to W once it has
+//                       converged or the passes are spent; the tiles still
+//                       refining make the next pass's work lists.
+//   then per pass (at most kOzPasses = 12; a pass works only on the tiles
+//   still refining, so a slowly contracting tile gets more passes than the
+//   tiled refresh's 4 before its walker is handed to the FP64 refresh):
 //   oz_slice_kernel     V's rows split into four digit planes.
-//   oz_residual_kernel  R = B - V M from the digit planes (tcgen05, TMA).
-//   oz_correct_kernel   V += R G per 32-row tile on the CUDA cores, the
-//                       tile's convergence test (as in the tiled refresh),
-//                       and the tile's rows out to W once it has converged
-//                       or the passes are spent.
+//   oz_residual_kernel  R = B - V M from the digit planes (tcgen05 + TMA),
+//                       written as R's three bf16 planes.
+//   oz_corr_kernel, oz_check_kernel as above.
 //
 // Error-free products (the splitting of Ozaki, Ogita, Oishi and Rump,
 // "Error-free transformations of matrix multiplication by using fast
@@ -145,6 +148,28 @@ __device__ __forceinline__ float pow2(int e) {
     return (e >= -126 && e <= 127) ? __int_as_float((e + 127) << 23) : ldexpf(1.f, e);
 }
 
+// x = x0 + x1 + x2 with every part a bf16 (rounded to nearest in turn; each
+// difference is exact in FP32, and three parts hold all 24 bits)
+__device__ __forceinline__ void split3(float x, uint32_t &h0, uint32_t &h1, uint32_t &h2) {
+    const __nv_bfloat16 a = __float2bfloat16_rn(x);
+    const float r1 = x - __bfloat162float(a);
+    const __nv_bfloat16 c = __float2bfloat16_rn(r1);
+    const float r2 = r1 - __bfloat162float(c);
+    const __nv_bfloat16 e = __float2bfloat16_rn(r2);
+    h0 = __bfloat16_as_ushort(a);
+    h1 = __bfloat16_as_ushort(c);
+    h2 = __bfloat16_as_ushort(e);
+}
+
+__device__ __forceinline__ uint4 pack8(const uint32_t (&h)[8]) {
+    uint4 pk;
+    pk.x = h[0] | (h[1] << 16);
+    pk.y = h[2] | (h[3] << 16);
+    pk.z = h[4] | (h[5] << 16);
+    pk.w = h[6] | (h[7] << 16);
+    return pk;
+}
+
 __device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
     s = a + b;
     const float bb = s - a;
@@ -159,8 +184,10 @@ struct OzView {
     int *tile_list, *grp_list, *counts, *grp_flag;
     const uint16_t *ud0, *ud1;
     const int *fexp0, *fexp1;
-    float *V, *R;
-    uint16_t *vd, *mt;
+    float *V;
+    uint16_t *vd, *mt, *rd, *gd;
+    int cn, rows_g;
+    float *dmax, *vmax;
     int *vexp, *perm, *srow;
     short *site_oth;
     float *est, *dprev;
@@ -173,7 +200,8 @@ OzView view_of(const OzRefresh &o) {
     v.rows_v = o.rows_v; v.rows_m = o.rows_m; v.tiles = o.tiles; v.n_ws = o.n_ws; v.groups = o.groups;
     v.tile_list = o.tile_list; v.grp_list = o.grp_list; v.counts = o.counts; v.grp_flag = o.grp_flag;
     v.ud0 = o.ud[0]; v.ud1 = o.ud[1]; v.fexp0 = o.fexp[0]; v.fexp1 = o.fexp[1];
-    v.V = o.V; v.R = o.R; v.vd = o.vd; v.mt = o.mt; v.vexp = o.vexp; v.perm = o.perm; v.srow = o.srow;
+    v.V = o.V; v.rd = o.rd; v.gd = o.gd; v.cn = o.cn; v.rows_g = o.rows_g; v.dmax = o.dmax; v.vmax = o.vmax;
+    v.vd = o.vd; v.mt = o.mt; v.vexp = o.vexp; v.perm = o.perm; v.srow = o.srow;
     v.site_oth = o.site_oth; v.est = o.est; v.dprev = o.dprev; v.done = o.done; v.active = o.active;
     return v;
 }
@@ -220,6 +248,10 @@ __global__ void __launch_bounds__(kTT) oz_prep_kernel(DevModel m, DevBatch b, Oz
     }
     for (int i = tid; i < n_oth; i += nt) v.site_oth[(size_t)ws * v.oth_max + i] = site_oth[i];
     for (int g = tid; g < v.groups; g += nt) v.grp_flag[(size_t)ws * v.groups + g] = 0;
+    for (int r = tid; r < v.rows_v; r += nt) {
+        v.dmax[(size_t)ws * v.rows_v + r] = 0.f;
+        v.vmax[(size_t)ws * v.rows_v + r] = 0.f;
+    }
     for (int t = tid; t < v.tiles; t += nt) {
         v.est[(size_t)ws * v.tiles + t] = 1.f;
         v.dprev[(size_t)ws * v.tiles + t] = 1.f;
@@ -284,9 +316,54 @@ __global__ void __launch_bounds__(kTT) oz_inverse_kernel(DevModel m, DevBatch b,
     }
     __syncthreads();
     tile_solve(A, perm, n, invd, Z, ldz, rows, St, t0);
-    float *G = A + (size_t)n * n;
-    for (int r = warp; r < rows; r += nw)
-        for (int c = lane; c < n; c += 32) G[(size_t)(t0 + r) * n + c] = Z[(size_t)r * ldz + c];
+    // G^T's three bf16 planes for the correction GEMM: plane p, k-group g,
+    // row j holds part p of G[8 g + q][j], q = 0..7 (k = G's row)
+    const size_t gplane = (size_t)(v.kp / 8) * v.rows_g * 8;
+    uint16_t *gdst = v.gd + (size_t)ws * 3 * gplane;
+    const int ng = (rows + 7) / 8;
+    for (int e = tid; e < ng * n; e += nt) {
+        const int gl = e / n, j = e - gl * n;
+        uint32_t h[3][8];
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+            const int r = 8 * gl + q;
+            oz::split3(r < rows ? Z[(size_t)r * ldz + j] : 0.f, h[0][q], h[1][q], h[2][q]);
+        }
+        const size_t at = ((size_t)(t0 / 8 + gl) * v.rows_g + j) * 8;
+#pragma unroll
+        for (int p = 0; p < 3; ++p) *reinterpret_cast<uint4 *>(gdst + p * gplane + at) = oz::pack8(h[p]);
+    }
+    (void)warp; (void)lane; (void)nw;
+}
+
+// The first pass's R = B (U's high parts at the other spin's sites) as the
+// three bf16 planes the correction GEMM reads: one CTA per 32-row tile.
+__global__ void __launch_bounds__(256) oz_bplanes_kernel(DevModel m, OzView v) {
+    const int w = blockIdx.x, spin = blockIdx.y, tt = blockIdx.z, ws = 2 * w + spin;
+    const int n = spin == 0 ? m.n_up : m.n_dn;
+    const int n_oth = m.n_sites - n;
+    const int b0 = tt * kRT;
+    if (!v.active[ws] || b0 >= n_oth) return;
+    const int rows = min(kRT, n_oth - b0);
+    const float *Uh = spin == 0 ? m.U32_up_hi : m.U32_dn_hi;
+    const short *so = v.site_oth + (size_t)ws * v.oth_max + b0;
+    const size_t rplane = (size_t)(v.kp / 8) * v.rows_v * 8;
+    uint16_t *dst = v.rd + (size_t)ws * 3 * rplane;
+    const int groups = (n + 7) / 8;
+    for (int e = threadIdx.x; e < groups * kRT; e += blockDim.x) {
+        const int r = e & (kRT - 1), g = e / kRT;
+        if (r >= rows) continue;
+        const float *src = Uh + (size_t)so[r] * n;
+        uint32_t h[3][8];
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+            const int k = 8 * g + q;
+            oz::split3(k < n ? src[k] : 0.f, h[0][q], h[1][q], h[2][q]);
+        }
+        const size_t at = ((size_t)g * v.rows_v + b0 + r) * 8;
+#pragma unroll
+        for (int p = 0; p < 3; ++p) *reinterpret_cast<uint4 *>(dst + p * rplane + at) = oz::pack8(h[p]);
+    }
 }
 
 // M^T's digit planes: plane t, k-group g, row j holds digit t of
@@ -531,7 +608,8 @@ oz_residual_kernel(DevModel m, DevBatch b, OzView v, int cur, const __grid_const
             const int site = row_ok ? v.site_oth[(size_t)ws * v.oth_max + i] : 0;
             const float sc_i = row_ok ? pow2(v.vexp[(size_t)ws * v.rows_v + i] - 12) : 0.f;
             const float *bh = Uh + (size_t)site * n, *bl = Ul + (size_t)site * n;
-            float *Rrow = v.R + ((size_t)ws * v.rows_v + (row_ok ? i : 0)) * v.ldz;
+            const size_t rplane = (size_t)(v.kp / 8) * v.rows_v * 8;
+            uint16_t *rdst = v.rd + (size_t)ws * 3 * rplane + (size_t)(row_ok ? i : 0) * 8;
             float ph[8], pl[8];   // B's next eight entries, fetched ahead
 #pragma unroll
             for (int q = 0; q < 8; ++q) {
@@ -565,20 +643,28 @@ oz_residual_kernel(DevModel m, DevBatch b, OzView v, int cur, const __grid_const
                         pl[q] = ok ? bl[j] : 0.f;
                     }
                 }
-                if (!(row_ok && good)) continue;
+                if (!(row_ok && good) || c0 + cc >= n) continue;
+                // R's entries c0 + cc .. + 7 (zero from n on) as the correction's k-group (c0 + cc) / 8
+                uint32_t h[3][8];
 #pragma unroll
                 for (int q = 0; q < 8; ++q) {
                     const int j = c0 + cc + q;
-                    if (j >= n) break;
-                    float h1, e1, h2, e2;
-                    two_sum(d[0][q], d[1][q] * 0x1p-7f, h1, e1);
-                    two_sum(h1, d[2][q] * 0x1p-14f, h2, e2);
-                    const float t =
-                        fmaf(d[6][q], 0x1p-42f, fmaf(d[5][q], 0x1p-35f, fmaf(d[4][q], 0x1p-28f, d[3][q] * 0x1p-21f)));
-                    const float lo = (e1 + e2) + t;
-                    const float s = sc_i * pow2(fexp[j]);
-                    Rrow[j] = ((ch_[q] - h2 * s) - lo * s) + cl_[q];
+                    float r = 0.f;
+                    if (j < n) {
+                        float h1, e1, h2, e2;
+                        two_sum(d[0][q], d[1][q] * 0x1p-7f, h1, e1);
+                        two_sum(h1, d[2][q] * 0x1p-14f, h2, e2);
+                        const float t = fmaf(d[6][q], 0x1p-42f,
+                                             fmaf(d[5][q], 0x1p-35f, fmaf(d[4][q], 0x1p-28f, d[3][q] * 0x1p-21f)));
+                        const float lo = (e1 + e2) + t;
+                        const float s = sc_i * pow2(fexp[j]);
+                        r = ((ch_[q] - h2 * s) - lo * s) + cl_[q];
+                    }
+                    split3(r, h[0][q], h[1][q], h[2][q]);
                 }
+                const size_t at = (size_t)((c0 + cc) / 8) * v.rows_v * 8;
+#pragma unroll
+                for (int p = 0; p < 3; ++p) *reinterpret_cast<uint4 *>(rdst + p * rplane + at) = pack8(h[p]);
             }
             fence_before();
             __syncwarp();
@@ -609,91 +695,270 @@ oz_residual_kernel(DevModel m, DevBatch b, OzView v, int cur, const __grid_const
 }
 
 
-struct CorrectSmem {
-    size_t z, r, st, total;
-};
-__host__ __device__ inline CorrectSmem correct_layout(int ldz) {
-    auto al = [](size_t x) { return (x + 15) / 16 * 16; };
-    CorrectSmem s{};
-    s.z = 0;
-    s.r = al((size_t)kRT * ldz * 4);
-    s.st = s.r + al((size_t)kRT * ldz * 4);
-    s.total = s.st + (size_t)2 * kKC * kCB * 4;
-    return s;
+// V += R G on the tensor cores.  R and G^T are three bf16 planes each
+// (x = x0 + x1 + x2 exactly); the six products with a + b <= 2 accumulate in
+// one FP32 accumulator, the three left out weigh 2^-24 of the product or
+// less, so the correction has FP32 accuracy, which the refinement needs (its
+// contraction factor grows by the correction's relative error times
+// cond(tilde_U)).  Persistent like the residual: units (walker-spin, 128-row
+// group, cn-column tile) of the pass's group list -- every group on the
+// first pass -- with the accumulator double-buffered in tensor memory, so the
+// MMAs of one unit run while warps 0-3 add the previous one into V and keep
+// each row's largest |R G| and |V| for the convergence test.
+constexpr int kCorrStages = 3;
+constexpr int kCorrABytes = 3 * oz::kBM * oz::kKS * 2;
+__host__ __device__ inline int corr_stage_bytes(int cn) { return kCorrABytes + 3 * cn * oz::kKS * 2; }
+__host__ __device__ inline int corr_smem(int cn) { return kCorrStages * corr_stage_bytes(cn) + 1024; }
+
+__global__ void __launch_bounds__(kResThreads, 1)
+oz_corr_kernel(DevModel m, DevBatch b, OzView v, int first, int cur, const __grid_constant__ CUtensorMap tmr,
+               const __grid_constant__ CUtensorMap tmg) {
+    using namespace oz;
+    const int cn = v.cn;
+    const int ctiles = v.rows_g / cn;
+    const int ngrp = first ? v.n_ws * v.groups : v.counts[2 * cur + 1];
+    const int units = ngrp * ctiles;
+    if ((int)blockIdx.x >= units) return;
+    const int *glist = v.grp_list + (size_t)cur * v.n_ws * v.groups;
+    const int stage_bytes = corr_stage_bytes(cn);
+    const uint32_t lbo_b = (uint32_t)cn * 16;
+
+    extern __shared__ unsigned char smem_raw[];
+    unsigned char *sm = reinterpret_cast<unsigned char *>(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    __shared__ __align__(8) uint64_t full[kCorrStages], empty[kCorrStages], done_bar[2], tfree_bar[2];
+    __shared__ uint32_t tmem_slot;
+    __shared__ volatile int s_fail;
+    __shared__ int s_issued;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    if (tid == 0) {
+        for (int s = 0; s < kCorrStages; ++s) {
+            bar_init(&full[s], 1);
+            bar_init(&empty[s], 1);
+        }
+        for (int q = 0; q < 2; ++q) {
+            bar_init(&done_bar[q], 1);
+            bar_init(&tfree_bar[q], 4);
+        }
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        s_fail = 0;
+        s_issued = 0;
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
+                     :: "r"(smem_u32(&tmem_slot)), "r"(kTmemCols));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    fence_before();
+    __syncthreads();
+    fence_after();
+    const uint32_t tmem = tmem_slot;
+    auto unit = [&](int u, int &ws, int &r0, int &c0, int &n, int &n_oth) {
+        const int gi = u / ctiles, ct = u - gi * ctiles;
+        const int item = first ? gi : glist[gi];
+        ws = item / v.groups;
+        r0 = (item - ws * v.groups) * kBM;
+        c0 = ct * cn;
+        n = (ws & 1) == 0 ? m.n_up : m.n_dn;
+        n_oth = m.n_sites - n;
+        return (!first || v.active[ws]) && c0 < n && r0 < n_oth;
+    };
+
+    if (warp == 4) {
+        if (lane == 0) {
+            int gch = 0;
+            bool stop = false;
+            for (int u = blockIdx.x; u < units && !stop && !s_fail; u += gridDim.x) {
+                int ws, r0, c0, n, n_oth;
+                if (!unit(u, ws, r0, c0, n, n_oth)) continue;
+                const int nch = (n + kKS - 1) / kKS;
+                for (int ch = 0; ch < nch; ++ch, ++gch) {
+                    const int s = gch % kCorrStages;
+                    if (gch >= kCorrStages && !wait(&empty[s], ((gch / kCorrStages) - 1) & 1)) {
+                        s_fail = 1;
+                        stop = true;
+                        break;
+                    }
+                    expect_tx(&full[s], (uint32_t)stage_bytes);
+                    unsigned char *st = sm + (size_t)s * stage_bytes;
+                    tma_load5(st, &tmr, 0, r0, ch * (kKS / 8), 0, ws, &full[s]);
+                    tma_load5(st + kCorrABytes, &tmg, 0, c0, ch * (kKS / 8), 0, ws, &full[s]);
+                }
+            }
+            s_issued = gch;
+        }
+        __syncwarp();
+    } else if (warp == 5) {
+        if (lane == 0) {
+            const uint32_t idesc = idesc_bf16(kBM, cn);
+            int gch = 0, k = 0;
+            for (int u = blockIdx.x; u < units && !s_fail; u += gridDim.x) {
+                int ws, r0, c0, n, n_oth;
+                if (!unit(u, ws, r0, c0, n, n_oth)) continue;
+                const int bf = k & 1, use = k >> 1;
+                if (use > 0 && !wait(&tfree_bar[bf], (use - 1) & 1)) {
+                    s_fail = 1;
+                    break;
+                }
+                fence_after();
+                const uint32_t acc_addr = tmem + (uint32_t)(bf * 256);
+                const int nch = (n + kKS - 1) / kKS;
+                bool ok = true;
+                for (int ch = 0; ch < nch; ++ch, ++gch) {
+                    const int s = gch % kCorrStages;
+                    if (!wait(&full[s], (gch / kCorrStages) & 1)) {
+                        ok = false;
+                        break;
+                    }
+                    fence_after();
+                    const uint32_t a0 = smem_u32(sm + (size_t)s * stage_bytes), b0 = a0 + kCorrABytes;
+#pragma unroll
+                    for (int q = 0; q < kKS / 16; ++q) {
+#pragma unroll
+                        for (int pr = 0; pr < 6; ++pr) {
+                            const int pa = pr < 3 ? (pr == 2 ? 1 : 0) : (pr == 5 ? 2 : pr == 4 ? 1 : 0);
+                            const int pb = pr < 3 ? (pr == 1 ? 1 : 0) : (pr == 3 ? 2 : pr == 4 ? 1 : 0);
+                            const uint64_t ad = sdesc(a0 + pa * (kBM * kKS * 2) + q * 2 * kLboA, kLboA, kSbo);
+                            const uint64_t bd = sdesc(b0 + pb * (cn * kKS * 2) + q * 2 * lbo_b, lbo_b, kSbo);
+                            mma(acc_addr, ad, bd, idesc, (ch > 0 || q > 0 || pr > 0) ? 1u : 0u);
+                        }
+                    }
+                    commit(&empty[s]);
+                }
+                commit(&done_bar[bf]);
+                ++k;
+                if (!ok) {
+                    s_fail = 1;
+                    break;
+                }
+            }
+        }
+        __syncwarp();
+    } else {
+        int k = 0;
+        for (int u = blockIdx.x; u < units; u += gridDim.x) {
+            int ws, r0, c0, n, n_oth;
+            if (!unit(u, ws, r0, c0, n, n_oth)) continue;
+            const int bf = k & 1, use = k >> 1;
+            const int i = r0 + 32 * warp + lane;
+            const bool row_ok = i < n_oth && !v.done[(size_t)ws * v.tiles + i / kRT];
+            float *Vrow = v.V + ((size_t)ws * v.rows_v + (row_ok ? i : 0)) * v.ldz;
+            if (!wait(&done_bar[bf], use & 1)) {
+                s_fail = 1;
+                break;
+            }
+            fence_after();
+            const bool good = row_ok && !s_fail;
+            const uint32_t tl = tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)(bf * 256);
+            float dm = 0.f, vm = 0.f;
+            for (int cc = 0; cc < cn; cc += 16) {
+                float d0[8], d1[8];
+                ld8(tl + (uint32_t)cc, d0);
+                ld8(tl + (uint32_t)(cc + 8), d1);
+                asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+                if (!good) continue;
+#pragma unroll
+                for (int q = 0; q < 16; ++q) {
+                    const int j = c0 + cc + q;
+                    if (j >= n) break;
+                    const float dv = q < 8 ? d0[q] : d1[q - 8];
+                    const float nv = (first ? 0.f : Vrow[j]) + dv;
+                    Vrow[j] = nv;
+                    dm = fmaxf(dm, isfinite(nv) ? fabsf(dv) : INFINITY);
+                    vm = fmaxf(vm, fabsf(nv));
+                }
+            }
+            if (good) {
+                atomic_max_nonneg(&v.dmax[(size_t)ws * v.rows_v + i], dm);
+                atomic_max_nonneg(&v.vmax[(size_t)ws * v.rows_v + i], vm);
+            }
+            fence_before();
+            __syncwarp();
+            if (lane == 0)
+                asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" :: "r"(smem_u32(&tfree_bar[bf])) : "memory");
+            ++k;
+        }
+    }
+
+    fence_before();
+    __syncthreads();
+    fence_after();
+    if (tid == 0) {
+        const int issued = s_issued;
+        for (int s = 0; s < kCorrStages && s < issued; ++s) {
+            const int last = s + ((issued - 1 - s) / kCorrStages) * kCorrStages;
+            wait(&full[s], (last / kCorrStages) & 1);
+        }
+        if (s_fail)
+            for (int u = blockIdx.x; u < units; u += gridDim.x) {
+                int ws, r0, c0, n, n_oth;
+                unit(u, ws, r0, c0, n, n_oth);
+                atomicOr(&b.status[ws >> 1], kStatusTimeout);
+            }
+    }
+    __syncthreads();
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" :: "r"(tmem), "r"(kTmemCols));
 }
 
-// V += R G for one 32-row tile, its convergence test, and its rows out to W
-// when it has converged or the passes are spent (last != 0); a tile still
-// refining goes on the next pass's list (nxt), and its 128-row group on the
-// next group list unless it is there already.  The first pass (first != 0)
-// forms V = B G from V = 0 and R = B (U's high parts), the tiled refresh's
-// starting point: its relative correction is 1, so it never ends a tile.
-__device__ __forceinline__ void correct_tile(const DevModel &m, const DevBatch &b, const OzView &v, int ws, int tt,
-                                             int first, int last, int nxt, int track_drift, unsigned char *smem,
-                                             double *red, int *s_fin) {
-    const int w = ws >> 1, spin = ws & 1;
+// The convergence test of one 32-row tile after a correction (as in the
+// tiled refresh: d = the largest |R G| relative to its row's largest |V|,
+// est = d^2 / d_prev), and its rows out to W when it has converged or the
+// passes are spent; a tile still refining goes on the next pass's list
+// (nxt), and its 128-row group on the next group list unless it is there
+// already.  The first pass's d is 1, so it ends no tile.
+__device__ __forceinline__ void check_tile(const DevModel &m, const DevBatch &b, const OzView &v, int item, int first,
+                                           int last, int nxt, int track_drift, int *s_fin) {
+    const int ws = item / v.tiles, tt = item - ws * v.tiles, w = ws >> 1, spin = ws & 1;
     const int N = m.n_sites;
     const int n = spin == 0 ? m.n_up : m.n_dn;
     const int n_oth = N - n;
     const int b0 = tt * kRT;
-    if (!v.active[ws] || b0 >= n_oth || v.done[(size_t)ws * v.tiles + tt]) return;
+    if (!v.active[ws] || b0 >= n_oth || v.done[item]) return;
     const int rows = min(kRT, n_oth - b0);
-    const int ldz = ld_tile(n), ldw = spin == 0 ? m.ld_up : m.ld_dn;
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nt = blockDim.x, nw = nt / 32;
-    const CorrectSmem L = correct_layout(ldz);
-    float *Z = reinterpret_cast<float *>(smem + L.z);
-    float *Rt = reinterpret_cast<float *>(smem + L.r);
-    float *St = reinterpret_cast<float *>(smem + L.st);
-    const float *G = reinterpret_cast<const float *>(b.solve_scratch + ((size_t)w * 2 + spin) * b.solve_block) +
-                     (size_t)n * n;
-    float *Vw = v.V + ((size_t)ws * v.rows_v + b0) * v.ldz;
-    const float *Rw = v.R + ((size_t)ws * v.rows_v + b0) * v.ldz;
-    const float *Uh = spin == 0 ? m.U32_up_hi : m.U32_dn_hi;
-    const short *so = v.site_oth + (size_t)ws * v.oth_max + b0;
-    for (int e = tid; e < kRT * ldz; e += nt) {
-        const int r = e / ldz, c = e - r * ldz;
-        const bool ok = r < rows && c < n;
-        Z[e] = ok && !first ? Vw[(size_t)r * v.ldz + c] : 0.f;
-        Rt[e] = !ok ? 0.f : first ? Uh[(size_t)so[r] * n + c] : Rw[(size_t)r * v.ldz + c];
-    }
-    const float d = tile_gemm(G, n, Rt, Z, ldz, rows, 1, St, red);   // V += R G (synchronises first)
-    if (tid == 0) {
-        const int item = ws * v.tiles + tt;
-        const float dprev = v.dprev[item];
-        const float est = d < dprev ? d * d / dprev : INFINITY;   // a correction that grows: diverging
-        v.dprev[item] = d;
-        v.est[item] = est;
-        const int fin = !first && (!(est > 1e-6f) || last);
-        *s_fin = fin;
-        if (fin) {
-            v.done[item] = 1;
-            if (!(est <= 1e-5f)) atomicOr(&b.status[w], kStatusRefine);
-        } else {
-            v.tile_list[(size_t)nxt * v.n_ws * v.tiles + atomicAdd(&v.counts[2 * nxt], 1)] = item;
-            const int g = ws * v.groups + b0 / oz::kBM;
-            if (atomicExch(&v.grp_flag[g], 1) == 0)
-                v.grp_list[(size_t)nxt * v.n_ws * v.groups + atomicAdd(&v.counts[2 * nxt + 1], 1)] = g;
+    const int ldw = spin == 0 ? m.ld_up : m.ld_dn;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = blockDim.x / 32;
+    if (warp == 0) {
+        float q = 0.f;
+        if (lane < rows) {
+            const size_t r = (size_t)ws * v.rows_v + b0 + lane;
+            const float qi = v.dmax[r] / fmaxf(v.vmax[r], 1e-30f);
+            q = isnan(qi) ? INFINITY : qi;
+            v.dmax[r] = 0.f;
+            v.vmax[r] = 0.f;
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) q = fmaxf(q, __shfl_xor_sync(0xffffffffu, q, o));
+        if (lane == 0) {
+            const float d = q, dprev = v.dprev[item];
+            const float est = d < dprev ? d * d / dprev : INFINITY;   // a correction that grows: diverging
+            v.dprev[item] = d;
+            v.est[item] = est;
+            const int fin = !first && (!(est > 1e-6f) || last);
+            *s_fin = fin;
+            if (fin) {
+                v.done[item] = 1;
+                if (!(est <= 1e-5f)) atomicOr(&b.status[w], kStatusRefine);
+            } else {
+                v.tile_list[(size_t)nxt * v.n_ws * v.tiles + atomicAdd(&v.counts[2 * nxt], 1)] = item;
+                const int g = ws * v.groups + b0 / oz::kBM;
+                if (atomicExch(&v.grp_flag[g], 1) == 0)
+                    v.grp_list[(size_t)nxt * v.n_ws * v.groups + atomicAdd(&v.counts[2 * nxt + 1], 1)] = g;
+            }
         }
     }
     __syncthreads();
-    if (!*s_fin) {
-        for (int e = tid; e < rows * n; e += nt) {
-            const int r = e / n, c = e - r * n;
-            Vw[(size_t)r * v.ldz + c] = Z[(size_t)r * ldz + c];
-        }
-        return;
-    }
+    if (!*s_fin) return;
     // the tile's rows out, in label order: X[:, perm[i]] = V[:, i]
     const bool cpt = b.compact != 0;
     float *Wout = cpt ? b.G32 + (size_t)w * b.g_block + (spin == 0 ? 0 : (size_t)m.n_dn * m.ld_up)
                       : b.W32 + (size_t)w * N * (m.ld_up + m.ld_dn) + (spin == 0 ? 0 : (size_t)N * m.ld_up);
     const int *perm = v.perm + (size_t)ws * v.n_max;
     const short *site_oth = v.site_oth + (size_t)ws * v.oth_max;
+    const float *Vw = v.V + ((size_t)ws * v.rows_v + b0) * v.ldz;
     float dmax = 0.f;
     for (int r = warp; r < rows; r += nw) {
         float *wr = Wout + (size_t)(cpt ? b0 + r : site_oth[b0 + r]) * ldw;
         for (int i = lane; i < n; i += 32) {
-            const float nv = Z[(size_t)r * ldz + i];
+            const float nv = Vw[(size_t)r * v.ldz + i];
             const int p = perm[i];
             if (track_drift) dmax = fmaxf(dmax, fabsf(wr[p] - nv) / (1.f + fabsf(nv)));
             wr[p] = nv;
@@ -708,27 +973,19 @@ __device__ __forceinline__ void correct_tile(const DevModel &m, const DevBatch &
     }
 }
 
-// first != 0: one CTA per (walker, spin, tile), every tile; else a
-// grid-stride loop over the tiles of list `cur`.
-__global__ void __launch_bounds__(kTT) oz_correct_kernel(DevModel m, DevBatch b, OzView v, int first, int last,
-                                                         int cur, int track_drift) {
-    extern __shared__ __align__(16) unsigned char smem[];
-    __shared__ double red[33];
+// first != 0: every tile of every walker-spin; else the tiles of list `cur`;
+// a grid-stride loop either way.
+__global__ void __launch_bounds__(256) oz_check_kernel(DevModel m, DevBatch b, OzView v, int first, int last,
+                                                       int cur, int track_drift) {
     __shared__ int s_fin;
     const int nxt = cur ^ 1;
-    if (first) {
-        correct_tile(m, b, v, 2 * blockIdx.x + blockIdx.y, blockIdx.z, 1, 0, nxt, track_drift, smem, red, &s_fin);
-        return;
-    }
-    const int count = v.counts[2 * cur];
+    const int count = first ? v.n_ws * v.tiles : v.counts[2 * cur];
     const int *list = v.tile_list + (size_t)cur * v.n_ws * v.tiles;
     for (int it = blockIdx.x; it < count; it += gridDim.x) {
-        const int item = list[it], ws = item / v.tiles;
-        correct_tile(m, b, v, ws, item - ws * v.tiles, 0, last, nxt, track_drift, smem, red, &s_fin);
+        check_tile(m, b, v, first ? it : list[it], first, last, nxt, track_drift, &s_fin);
         __syncthreads();
     }
 }
-
 
 using EncodeTiled = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
                                  const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
@@ -766,7 +1023,7 @@ cudaError_t encode_planes(void *map, void *base, int rows, int kp, int planes, i
 size_t align256(size_t x) { return (x + 255) / 256 * 256; }
 
 struct OzDims {
-    int n_max, oth_max, ldz, kp, rows_v, rows_m, tiles;
+    int n_max, oth_max, ldz, kp, rows_v, rows_m, tiles, cn, rows_g;
 };
 OzDims oz_dims(const DevModel &m) {
     OzDims d;
@@ -777,12 +1034,16 @@ OzDims oz_dims(const DevModel &m) {
     d.rows_v = (d.oth_max + oz::kBM - 1) / oz::kBM * oz::kBM;
     d.rows_m = (d.n_max + oz::kBN - 1) / oz::kBN * oz::kBN;
     d.tiles = (d.oth_max + kRT - 1) / kRT;
+    // the correction's column tiles: as few as fit 256 TMEM columns, equal widths, multiples of 16
+    const int nt = (d.n_max + 255) / 256;
+    d.cn = ((d.n_max + nt - 1) / nt + 15) / 16 * 16;
+    d.rows_g = nt * d.cn;
     return d;
 }
 
 // byte offsets of the per-walker-spin buffers inside one allocation
 struct OzOffsets {
-    size_t V, R, vd, mt, vexp, perm, srow, site_oth, est, dprev, done, active, tile_list, grp_list, counts, grp_flag,
+    size_t V, rd, gd, dmax, vmax, vd, mt, vexp, perm, srow, site_oth, est, dprev, done, active, tile_list, grp_list, counts, grp_flag,
         total;
 };
 OzOffsets oz_offsets(const OzDims &d, int n_walkers) {
@@ -795,7 +1056,10 @@ OzOffsets oz_offsets(const OzDims &d, int n_walkers) {
         return at;
     };
     o.V = take(S * d.rows_v * d.ldz * 4);
-    o.R = take(S * d.rows_v * d.ldz * 4);
+    o.rd = take(S * 3 * (size_t)d.kp * d.rows_v * 2);
+    o.gd = take(S * 3 * (size_t)d.kp * d.rows_g * 2);
+    o.dmax = take(S * d.rows_v * 4);
+    o.vmax = take(S * d.rows_v * 4);
     o.vd = take(S * kOzVDigits * (size_t)d.kp * d.rows_v * 2);
     o.mt = take(S * kOzUDigits * (size_t)d.kp * d.rows_m * 2);
     o.vexp = take(S * d.rows_v * 4);
@@ -821,7 +1085,7 @@ size_t oz_scratch_bytes(const DevModel &m, int n_walkers) { return oz_offsets(oz
 bool oz_supported(const DevModel &m, int optin) {
     const OzDims d = oz_dims(m);
     if (!m.U32_up_hi || d.n_max >= 1024 || 2 * d.n_max > 65535) return false;   // the exact-accumulation bound
-    const size_t need = std::max({refresh_tile_smem(m), (size_t)oz::kSmem, correct_layout(d.ldz).total,
+    const size_t need = std::max({refresh_tile_smem(m), (size_t)oz::kSmem, (size_t)corr_smem(d.cn),
                                   inverse_layout(d.n_max).total});
     return need + 1024 <= (size_t)optin;
 }
@@ -854,7 +1118,12 @@ cudaError_t oz_setup(const DevModel &m, int n_walkers, void *scratch, OzRefresh 
     oz.n_max = d.n_max; oz.oth_max = d.oth_max; oz.ldz = d.ldz; oz.kp = d.kp;
     oz.rows_v = d.rows_v; oz.rows_m = d.rows_m; oz.tiles = d.tiles;
     oz.V = reinterpret_cast<float *>(base + o.V);
-    oz.R = reinterpret_cast<float *>(base + o.R);
+    oz.rd = reinterpret_cast<uint16_t *>(base + o.rd);
+    oz.gd = reinterpret_cast<uint16_t *>(base + o.gd);
+    oz.dmax = reinterpret_cast<float *>(base + o.dmax);
+    oz.vmax = reinterpret_cast<float *>(base + o.vmax);
+    oz.cn = d.cn;
+    oz.rows_g = d.rows_g;
     oz.vd = reinterpret_cast<uint16_t *>(base + o.vd);
     oz.mt = reinterpret_cast<uint16_t *>(base + o.mt);
     oz.vexp = reinterpret_cast<int *>(base + o.vexp);
@@ -873,6 +1142,8 @@ cudaError_t oz_setup(const DevModel &m, int n_walkers, void *scratch, OzRefresh 
     oz.grp_flag = reinterpret_cast<int *>(base + o.grp_flag);
     cudaError_t e = encode_planes(oz.tmap_v, oz.vd, d.rows_v, d.kp, kOzVDigits, 2 * n_walkers, oz::kBM);
     if (e == cudaSuccess) e = encode_planes(oz.tmap_m, oz.mt, d.rows_m, d.kp, kOzUDigits, 2 * n_walkers, oz::kBN);
+    if (e == cudaSuccess) e = encode_planes(oz.tmap_r, oz.rd, d.rows_v, d.kp, 3, 2 * n_walkers, oz::kBM);
+    if (e == cudaSuccess) e = encode_planes(oz.tmap_g, oz.gd, d.rows_g, d.kp, 3, 2 * n_walkers, d.cn);
     return e;
 }
 
@@ -890,26 +1161,30 @@ cudaError_t launch_refresh_oz(const DevModel &m, const DevBatch &b, const OzRefr
         return e;
     oz_inverse_kernel<<<dim3(W, 2, (oz.n_max + kRT - 1) / kRT), kTT, sm_inv, stream>>>(m, b, v);
     oz_gather_kernel<<<dim3(W, 2, kOzUDigits), 256, 0, stream>>>(m, v);
-    const size_t sm_corr = correct_layout(oz.ldz).total;
-    if ((e = cudaFuncSetAttribute(oz_correct_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_corr)))
-        return e;
+    oz_bplanes_kernel<<<dim3(W, 2, oz.tiles), 256, 0, stream>>>(m, v);
     if ((e = cudaFuncSetAttribute(oz_residual_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, oz::kSmem)))
         return e;
-    CUtensorMap tmv, tmm;
+    const int sm_corr = corr_smem(oz.cn);
+    if ((e = cudaFuncSetAttribute(oz_corr_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, sm_corr))) return e;
+    CUtensorMap tmv, tmm, tmr, tmg;
     std::memcpy(&tmv, oz.tmap_v, sizeof tmv);
     std::memcpy(&tmm, oz.tmap_m, sizeof tmm);
+    std::memcpy(&tmr, oz.tmap_r, sizeof tmr);
+    std::memcpy(&tmg, oz.tmap_g, sizeof tmg);
     int sms = 0;
     if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device))) return e;
-    // the first correction lists every tile still refining in list 1; pass p
-    // works on list p & 1 and fills the other, whose counters are cleared first
+    // the first pass (V = B G) lists every tile still refining in list 1; pass
+    // p works on list p & 1 and fills the other, whose counters are cleared first
     if ((e = cudaMemsetAsync(oz.counts, 0, 4 * sizeof(int), stream))) return e;
-    oz_correct_kernel<<<dim3(W, 2, oz.tiles), kTT, sm_corr, stream>>>(m, b, v, 1, 0, 0, track_drift);
+    oz_corr_kernel<<<sms, kResThreads, sm_corr, stream>>>(m, b, v, 1, 0, tmr, tmg);
+    oz_check_kernel<<<4 * sms, 256, 0, stream>>>(m, b, v, 1, 0, 0, track_drift);
     for (int pass = 1; pass <= oz::kOzPasses; ++pass) {
         const int cur = pass & 1, nxt = cur ^ 1;
         oz_slice_kernel<<<4 * sms, 256, 0, stream>>>(m, v, cur);
         oz_residual_kernel<<<sms, kResThreads, oz::kSmem, stream>>>(m, b, v, cur, tmv, tmm);
+        oz_corr_kernel<<<sms, kResThreads, sm_corr, stream>>>(m, b, v, 0, cur, tmr, tmg);
         if ((e = cudaMemsetAsync(oz.counts + 2 * nxt, 0, 2 * sizeof(int), stream))) return e;
-        oz_correct_kernel<<<sms, kTT, sm_corr, stream>>>(m, b, v, 0, pass == oz::kOzPasses, cur, track_drift);
+        oz_check_kernel<<<4 * sms, 256, 0, stream>>>(m, b, v, 0, pass == oz::kOzPasses, cur, track_drift);
     }
     return cudaGetLastError();
 }
