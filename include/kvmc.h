@@ -298,13 +298,19 @@ KVMC_API int kvmc_kernel_time(kvmc_handle *h, int32_t kind, double *total_ms, in
  *   with exact products and compensated sums), walkers that do not converge
  *   falling back to the FP64 refresh; 2 = the same refinement with the
  *   solves and the residual in tiles of 32 rows, one CTA per walker and
- *   spin (the faster form from about 200 orbitals per spin); 0 = FP64 LU
- *   and solves.  It also
+ *   spin; 3 = the same refinement batched over all walkers with both
+ *   products of each pass on the tensor cores -- the residual B - V M from
+ *   exact bf16 digit products (V and U split on fixed-point grids, integer
+ *   sums in FP32 tensor memory), the correction V += R G from three bf16
+ *   parts of each factor -- with up to 12 passes; the handle then holds
+ *   about 90 * n^2 bytes more per walker (16 MB at 432 orbitals per spin;
+ *   fewer than 1024 orbitals per spin);
+ *   0 = FP64 LU and solves.  It also
  *   rebuilds W in kvmc_set_state and kvmc_init with given configurations
  *   (log|det| then from the FP32 factors); seeded starts and kvmc_refresh
  *   always use FP64.  The default for the mixed real form is 1 below 96
- *   orbitals per spin and 2 from 96 on (while the tiles fit in shared
- *   memory, up to about 540 orbitals); 0 for the other forms.
+ *   orbitals per spin, 2 from 96 on (while the tiles fit in shared memory)
+ *   and 3 from 192 on; 0 for the other forms.
  *   KVMC_TUNE_WARP_WALKERS: 0 = one CTA per walker (the kernels above);
  *   1..14 = one warp per walker, this many walkers per CTA (mixed real form
  *   with delay_k 4..16).  Each warp keeps only W's non-trivial rows -- the
