@@ -169,6 +169,7 @@ struct OzRefresh {
     float *dmax, *vmax;          // [W*2][rows_v]: per row, max |R G| and max |V| of the pass
     int *vexp;                   // [W*2][rows_v] row scale exponents of V
     int *perm, *srow;            // [W*2][n_max] pivot order and the site of M's row i
+    float *invd;                 // [W*2][n_max] 1 / diag of the LU's upper factor, in pivot order
     short *site_oth;             // [W*2][oth_max]
     float *est, *dprev;          // [W*2][tiles] refinement state per tile
     int *done, *active;          // [W*2][tiles], [W*2]

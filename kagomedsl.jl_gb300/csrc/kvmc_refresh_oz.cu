@@ -189,6 +189,7 @@ struct OzView {
     int cn, rows_g;
     float *dmax, *vmax;
     int *vexp, *perm, *srow;
+    float *invd;
     short *site_oth;
     float *est, *dprev;
     int *done, *active;
@@ -201,9 +202,29 @@ OzView view_of(const OzRefresh &o) {
     v.tile_list = o.tile_list; v.grp_list = o.grp_list; v.counts = o.counts; v.grp_flag = o.grp_flag;
     v.ud0 = o.ud[0]; v.ud1 = o.ud[1]; v.fexp0 = o.fexp[0]; v.fexp1 = o.fexp[1];
     v.V = o.V; v.rd = o.rd; v.gd = o.gd; v.cn = o.cn; v.rows_g = o.rows_g; v.dmax = o.dmax; v.vmax = o.vmax;
-    v.vd = o.vd; v.mt = o.mt; v.vexp = o.vexp; v.perm = o.perm; v.srow = o.srow;
+    v.vd = o.vd; v.mt = o.mt; v.vexp = o.vexp; v.perm = o.perm; v.srow = o.srow; v.invd = o.invd;
     v.site_oth = o.site_oth; v.est = o.est; v.dprev = o.dprev; v.done = o.done; v.active = o.active;
     return v;
+}
+
+// Shared memory of the LU step: the 32-column panel, the staged block of
+// U12, the pivot order and the site tables (70 KB at n = 432, so that two
+// CTAs share an SM).
+struct PrepSmem {
+    size_t pn, ut, invd, perm, srow, site_of, site_oth, total;
+};
+__host__ __device__ inline PrepSmem prep_layout(int n, int n_oth) {
+    auto al = [](size_t x) { return (x + 15) / 16 * 16; };
+    PrepSmem s{};
+    s.pn = 0;
+    s.ut = al((size_t)n * kLdc * 4);
+    s.invd = s.ut + (size_t)kPB * 64 * 4;
+    s.perm = al(s.invd + (size_t)n * 4);
+    s.srow = al(s.perm + (size_t)n * 4);
+    s.site_of = al(s.srow + (size_t)n * 4);
+    s.site_oth = al(s.site_of + (size_t)n * 2);
+    s.total = al(s.site_oth + (size_t)n_oth * 2);
+    return s;
 }
 
 // Step 1 of the tiled refresh (site tables, LU of tilde_U in HBM), its
@@ -226,11 +247,9 @@ __global__ void __launch_bounds__(kTT) oz_prep_kernel(DevModel m, DevBatch b, Oz
     float *A = reinterpret_cast<float *>(b.solve_scratch + ((size_t)w * 2 + spin) * b.solve_block);
 
     extern __shared__ __align__(16) unsigned char smem[];
-    const TileSmem L = tile_smem_layout(n, n_oth);
-    float *Z = reinterpret_cast<float *>(smem + L.z);
+    const PrepSmem L = prep_layout(n, n_oth);
     float *Pn = reinterpret_cast<float *>(smem + L.pn);
     float *Ut = reinterpret_cast<float *>(smem + L.ut);
-    float *St = reinterpret_cast<float *>(smem + L.st);
     float *invd = reinterpret_cast<float *>(smem + L.invd);
     int *perm = reinterpret_cast<int *>(smem + L.perm);
     int *srow = reinterpret_cast<int *>(smem + L.srow);
@@ -238,11 +257,12 @@ __global__ void __launch_bounds__(kTT) oz_prep_kernel(DevModel m, DevBatch b, Oz
     short *site_oth = reinterpret_cast<short *>(smem + L.site_oth);
     __shared__ double red[33];
 
-    if (!tile_factor(m, b, w, spin, A, Z, Pn, Ut, St, invd, perm, srow, site_of, site_oth, red, false)) {
+    if (!tile_factor(m, b, w, spin, A, nullptr, Pn, Ut, nullptr, invd, perm, srow, site_of, site_oth, red, false)) {
         if (tid == 0) v.active[ws] = 0;
         return;
     }
     for (int i = tid; i < n; i += nt) {
+        v.invd[(size_t)ws * v.n_max + i] = invd[i];
         v.perm[(size_t)ws * v.n_max + i] = perm[i];
         v.srow[(size_t)ws * v.n_max + i] = srow[i];
     }
@@ -279,17 +299,18 @@ __global__ void __launch_bounds__(kTT) oz_prep_kernel(DevModel m, DevBatch b, Oz
 
 // G = M^{-1} (row-major n x n after the LU in the walker-spin's scratch),
 // rows t0 .. t0 + 31 from the identity rows, as in the tiled refresh.
+// Shared memory of the inverse: the tile of identity rows and the staged
+// block column of the factors (112 KB at n = 432: two CTAs per SM); the
+// pivot order and 1 / diag(Uf) are read from HBM.
 struct InverseSmem {
-    size_t z, st, invd, perm, total;
+    size_t z, st, total;
 };
 __host__ __device__ inline InverseSmem inverse_layout(int n) {
     auto al = [](size_t x) { return (x + 15) / 16 * 16; };
     InverseSmem s{};
     s.z = 0;
     s.st = al((size_t)kRT * ld_tile(n) * 4);
-    s.invd = s.st + al((size_t)round4(n) * kLdc * 4);
-    s.perm = s.invd + al((size_t)n * 4);
-    s.total = s.perm + al((size_t)n * 4);
+    s.total = s.st + al((size_t)round4(n) * kLdc * 4);
     return s;
 }
 
@@ -304,12 +325,9 @@ __global__ void __launch_bounds__(kTT) oz_inverse_kernel(DevModel m, DevBatch b,
     const InverseSmem L = inverse_layout(n);
     float *Z = reinterpret_cast<float *>(smem + L.z);
     float *St = reinterpret_cast<float *>(smem + L.st);
-    float *invd = reinterpret_cast<float *>(smem + L.invd);
-    int *perm = reinterpret_cast<int *>(smem + L.perm);
+    const int *perm = v.perm + (size_t)ws * v.n_max;
+    const float *invd = v.invd + (size_t)ws * v.n_max;
     float *A = reinterpret_cast<float *>(b.solve_scratch + ((size_t)w * 2 + spin) * b.solve_block);
-    for (int i = tid; i < n; i += nt) perm[i] = v.perm[(size_t)ws * v.n_max + i];
-    __syncthreads();
-    for (int i = tid; i < n; i += nt) invd[i] = 1.f / A[(size_t)perm[i] * n + i];
     for (int e = tid; e < kRT * ldz; e += nt) {
         const int r = e / ldz, c = e - r * ldz;
         Z[e] = (r < rows && c == t0 + r) ? 1.f : 0.f;
@@ -1043,7 +1061,7 @@ OzDims oz_dims(const DevModel &m) {
 
 // byte offsets of the per-walker-spin buffers inside one allocation
 struct OzOffsets {
-    size_t V, rd, gd, dmax, vmax, vd, mt, vexp, perm, srow, site_oth, est, dprev, done, active, tile_list, grp_list, counts, grp_flag,
+    size_t V, rd, gd, dmax, vmax, invd, vd, mt, vexp, perm, srow, site_oth, est, dprev, done, active, tile_list, grp_list, counts, grp_flag,
         total;
 };
 OzOffsets oz_offsets(const OzDims &d, int n_walkers) {
@@ -1059,6 +1077,7 @@ OzOffsets oz_offsets(const OzDims &d, int n_walkers) {
     o.rd = take(S * 3 * (size_t)d.kp * d.rows_v * 2);
     o.gd = take(S * 3 * (size_t)d.kp * d.rows_g * 2);
     o.dmax = take(S * d.rows_v * 4);
+    o.invd = take(S * d.n_max * 4);
     o.vmax = take(S * d.rows_v * 4);
     o.vd = take(S * kOzVDigits * (size_t)d.kp * d.rows_v * 2);
     o.mt = take(S * kOzUDigits * (size_t)d.kp * d.rows_m * 2);
@@ -1085,7 +1104,7 @@ size_t oz_scratch_bytes(const DevModel &m, int n_walkers) { return oz_offsets(oz
 bool oz_supported(const DevModel &m, int optin) {
     const OzDims d = oz_dims(m);
     if (!m.U32_up_hi || d.n_max >= 1024 || 2 * d.n_max > 65535) return false;   // the exact-accumulation bound
-    const size_t need = std::max({refresh_tile_smem(m), (size_t)oz::kSmem, (size_t)corr_smem(d.cn),
+    const size_t need = std::max({prep_layout(d.n_max, d.oth_max).total, (size_t)oz::kSmem, (size_t)corr_smem(d.cn),
                                   inverse_layout(d.n_max).total});
     return need + 1024 <= (size_t)optin;
 }
@@ -1121,6 +1140,7 @@ cudaError_t oz_setup(const DevModel &m, int n_walkers, void *scratch, OzRefresh 
     oz.rd = reinterpret_cast<uint16_t *>(base + o.rd);
     oz.gd = reinterpret_cast<uint16_t *>(base + o.gd);
     oz.dmax = reinterpret_cast<float *>(base + o.dmax);
+    oz.invd = reinterpret_cast<float *>(base + o.invd);
     oz.vmax = reinterpret_cast<float *>(base + o.vmax);
     oz.cn = d.cn;
     oz.rows_g = d.rows_g;
@@ -1152,7 +1172,7 @@ cudaError_t launch_refresh_oz(const DevModel &m, const DevBatch &b, const OzRefr
     if (!m.U32_up_hi || !b.solve_scratch || !oz.V) return cudaErrorInvalidValue;
     const OzView v = view_of(oz);
     const int W = b.n_walkers;
-    const size_t sm_prep = refresh_tile_smem(m);
+    const size_t sm_prep = std::max(prep_layout(m.n_up, m.n_dn).total, prep_layout(m.n_dn, m.n_up).total);
     cudaError_t e = cudaFuncSetAttribute(oz_prep_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_prep);
     if (e != cudaSuccess) return e;
     oz_prep_kernel<<<dim3(W, 2), kTT, sm_prep, stream>>>(m, b, v, only_due, track_drift);
