@@ -53,6 +53,8 @@ def args_():
     p.add_argument("--threads", type=int, default=None, help="threads per walker with W in HBM")
     p.add_argument("--warp", type=int, default=None, help="walkers per CTA with one warp per walker (0: one CTA each)")
     p.add_argument("--guard", default=None, help="accuracy guard hi,lo of the one-warp sweep (0,0: off)")
+    p.add_argument("--refresh32", type=int, default=None,
+                   help="the periodic refresh's form: 0 FP64, 1 one thread per row, 2 tiled, 3 tensor cores")
     p.add_argument("--seed", type=int, default=2024)
     p.add_argument("--skip-plain", action="store_true")
     p.add_argument("--skip-cpu", action="store_true")
@@ -250,6 +252,8 @@ def mixed_choice(kv, ham, a):
         ch.warp = a.warp
     if a.guard is not None:
         ch.guard_hi, ch.guard_lo = (int(x) for x in a.guard.split(","))
+    if a.refresh32 is not None:
+        ch.refresh32 = a.refresh32
     ch.trials = []
     return ch
 

@@ -19,7 +19,7 @@
 //                       refresh, and the tile's rows out to W once it has
 //                       converged or the passes are spent; the tiles still
 //                       refining make the next pass's work lists.
-//   then per pass (at most kOzPasses = 12; a pass works only on the tiles
+//   then per pass (at most kOzPasses = 24; a pass works only on the tiles
 //   still refining, so a slowly contracting tile gets more passes than the
 //   tiled refresh's 4 before its walker is handed to the FP64 refresh):
 //   oz_slice_kernel     V's rows split into four digit planes.
@@ -70,7 +70,7 @@ constexpr int kStageBytes = kABytes + kBBytes;
 constexpr int kSmem = kStages * kStageBytes + 1024;   // + alignment slack
 constexpr uint32_t kTmemCols = 512;                   // kClasses * kBN = 448, rounded to a power of two
 constexpr uint32_t kWaitLimit = 1u << 22;
-constexpr int kOzPasses = 12;
+constexpr int kOzPasses = 24;
 // Operand tiles in shared memory: plane p, k-group g (8 k), row r at byte
 // ((p * (kKS / 8) + g) * rows + r) * 16: every 8 rows x 16 bytes is one
 // core matrix of the no-swizzle K-major layout, adjacent along the rows 128

@@ -56,6 +56,7 @@ class Choice:
     warp: int = 0            # > 0: one warp per walker, this many walkers per CTA
     guard_hi: int = 0
     guard_lo: int = 0
+    refresh32: int = -1      # the periodic refresh's form (KVMC_TUNE_REFRESH32); -1: the library's default
 
     def engine_kwargs(self) -> dict:
         return dict(precision="mixed", delay_k=self.delay_k, refresh_interval=self.refresh_interval,
@@ -96,6 +97,8 @@ def make_engine(ham, walkers, choice: Choice, **kw):
     from .montecarlo import Engine
 
     eng = Engine(ham, walkers, **choice.engine_kwargs(), **kw)
+    if choice.refresh32 >= 0:
+        eng.set_refresh32(choice.refresh32)
     if choice.warp > 0:
         eng.set_warp_walkers(choice.warp)
         eng.set_accuracy_guard(choice.guard_hi, choice.guard_lo)

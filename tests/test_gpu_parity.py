@@ -669,6 +669,43 @@ def test_fp32_refinement_refresh(kv, N, placement, mode):
     eng.close()
 
 
+def test_tensor_core_refresh_ragged_large(kv):
+    """The refresh on the tensor cores at N = 576 with 290 + 286 orbitals:
+    partial 64-column tiles in the residual, two 160-column tiles in the
+    correction, 128-row groups cut at 286 and 290 rows, and unequal spins.
+    W right after a refresh of every walker against the oracle's FP64
+    reevaluateW (5e-6 relative to max(1, |W|)), the chains against the
+    oracle, and no more than a quarter of the refreshes redone in FP64."""
+    lat = kv.DoubleKagome(1.0, 16, 12, (True, True), (False, True))
+    H = kv.Hmat(lat)
+    N = H.shape[0]
+    assert N == 576
+    Uu, Ud = kv.orbitals(H, 290, N - 290)
+    ham = kv.Hamiltonian(290, N - 290, Uu, Ud, H, kv.get_nn(H))
+    walkers, seed, R = 4, 23, 48
+    eng = kv.Engine(ham, walkers, precision="mixed", seed=seed, refresh_interval=R, w_placement="hbm")
+    eng.set_refresh32("tc")
+    eng.set_drift_tolerance(1e9)
+    eng.init()
+    ku0, kd0, _ = eng.get_state()
+    st = eng.advance(2 * R)
+    assert st["refreshes"] >= 2 * walkers and st["bad_walkers"] == 0
+    assert 4 * st["fp64_redos"] <= st["refreshes"], st
+    ku1, kd1, ct = eng.get_state()
+    Wu, Wd = eng.get_w()
+    for w in range(walkers):
+        assert close(Wu[w], o.reevaluateW(Uu, ku1[w]), 5e-6), w
+        assert close(Wd[w], o.reevaluateW(Ud, kd1[w]), 5e-6), w
+    m = oracle_c.OracleModel(Uu, Ud, ham.nn)
+    match = 0
+    for w in range(walkers):
+        ch = m.new_chain(ku0[w], kd0[w])
+        ch.run(seed, w, int(ct[w]), N - 290, N - 290, 0)
+        match += int(np.array_equal(ch.ku, ku1[w]) and np.array_equal(ch.kd, kd1[w]))
+    assert match >= walkers - 1
+    eng.close()
+
+
 @pytest.mark.parametrize("mode", ["tiled", "tc"])
 @pytest.mark.parametrize("n1,n2,n_up", [(10, 5, 75), (10, 5, 77), (6, 3, 30), (4, 2, 12)])
 def test_tiled_refresh_ragged_sizes(kv, n1, n2, n_up, mode):
