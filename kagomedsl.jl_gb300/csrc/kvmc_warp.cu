@@ -113,6 +113,56 @@ __device__ __forceinline__ float column_write(const CSpin<K> &S, int s, int l, i
     return mx;
 }
 
+// column_write for both spins of a move at once: each round issues four
+// loads per lane for each spin before any arithmetic, so the two spins'
+// L2 round trips overlap (the entries and their arithmetic are those of
+// column_write).
+template <int K>
+__device__ __forceinline__ float column_write2(const CSpin<K> &A, int sa, int la, float ipa, const CSpin<K> &B,
+                                               int sb, int lb, float ipb, int m, int lane) {
+    const int ta = A.n_oth + A.n_own, tb = B.n_oth + B.n_own;
+    const int tot = ta > tb ? ta : tb;
+    float mx = 0.f;
+    for (int base = 0; base < tot; base += 128) {
+        float wa[4], wb[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const int e = base + 32 * q + lane;
+            wa[q] = 0.f;
+            if (e < A.n_oth) wa[q] = A.G[(size_t)e * A.ldg + la];
+            else if (e < ta) wa[q] = A.G[(size_t)sa * A.ldg + (e - A.n_oth)];
+            wb[q] = 0.f;
+            if (e < B.n_oth) wb[q] = B.G[(size_t)e * B.ldg + lb];
+            else if (e < tb) wb[q] = B.G[(size_t)sb * B.ldg + (e - B.n_oth)];
+        }
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const int e = base + 32 * q + lane;
+            if (e < A.n_oth) {
+                const float v = wa[q] - A.pq(e, la);
+                mx = fmaxf(mx, fabsf(v));
+                if (e != sa) A.P[(size_t)e * K + m] = v * ipa;
+            } else if (e < ta) {
+                const int c = e - A.n_oth;
+                const float v = wa[q] - A.pq(sa, c);
+                mx = fmaxf(mx, fabsf(v));
+                if (c != la) A.Q[(size_t)c * K + m] = v;
+            }
+            if (e < B.n_oth) {
+                const float v = wb[q] - B.pq(e, lb);
+                mx = fmaxf(mx, fabsf(v));
+                if (e != sb) B.P[(size_t)e * K + m] = v * ipb;
+            } else if (e < tb) {
+                const int c = e - B.n_oth;
+                const float v = wb[q] - B.pq(sb, c);
+                mx = fmaxf(mx, fabsf(v));
+                if (c != lb) B.Q[(size_t)c * K + m] = v;
+            }
+        }
+    }
+    return mx;
+}
+
 // G -= P Q^T.  Lane = a group of four columns (Q of those columns held in
 // registers); rows streamed four at a time, all four loads in flight
 // before the arithmetic.
@@ -351,8 +401,7 @@ sweep_warp_kernel(DevModel m, DevBatch b, SweepParams p, int *active_count, size
         t += f + 1;
         // factor columns mm of both spins (from the configuration before the move)
         const float ipu = 1.f / pu, ipd = 1.f / pd;
-        float mx = column_write<K>(SU, bl, a, mm, ipu, lane);
-        mx = fmaxf(mx, column_write<K>(SD, a, bl, mm, ipd, lane));
+        float mx = column_write2<K>(SU, bl, a, ipu, SD, a, bl, ipd, mm, lane);
         // Z_mu change from the up-neighbour counts (configuration before the move)
         const int bu = nbr_off[Ku], du = nbr_off[Ku + 1] - bu;
         const int bd0 = nbr_off[Kd], dd = nbr_off[Kd + 1] - bd0;
