@@ -74,51 +74,17 @@ struct CSpin {
     __device__ __forceinline__ float eff(int r, int c) const { return G[(size_t)r * ldg + c] - pq(r, c); }
 };
 
-// The factor columns of an accepted move for one spin.  s = the other
-// spin's label whose row is replaced, l = the own label that moves (up:
-// s = b, l = a; down: s = a, l = b):
+// The factor columns of an accepted move, for both spins at once.  For a
+// spin, s = the other spin's label whose row is replaced, l = the own label
+// that moves (up: s = b, l = a; down: s = a, l = b):
 //   P[r][m] = (G_eff[r][l] + [r == s]) / piv,   Q[c][m] = G_eff[s][c] - [c == l]
 // The two entries that read P[s][m] / Q[l][m] themselves (r == s, c == l)
 // are written by the caller after a __syncwarp, so that every dot here sees
-// column m still zero.  Four loads per lane are issued before the
-// arithmetic.  Returns the largest |G_eff| entry the lane read.
+// column m still zero.  Each round issues four loads per lane for each spin
+// before any arithmetic, so the two spins' L2 round trips overlap.  Returns
+// the largest |G_eff| entry the lane read.
 template <int K>
-__device__ __forceinline__ float column_write(const CSpin<K> &S, int s, int l, int m, float ipiv, int lane) {
-    const int tot = S.n_oth + S.n_own;
-    float mx = 0.f;
-    for (int base = 0; base < tot; base += 128) {
-        float wv[4];
-#pragma unroll
-        for (int q = 0; q < 4; ++q) {
-            const int e = base + 32 * q + lane;
-            wv[q] = 0.f;
-            if (e < S.n_oth) wv[q] = S.G[(size_t)e * S.ldg + l];
-            else if (e < tot) wv[q] = S.G[(size_t)s * S.ldg + (e - S.n_oth)];
-        }
-#pragma unroll
-        for (int q = 0; q < 4; ++q) {
-            const int e = base + 32 * q + lane;
-            if (e < S.n_oth) {
-                const float v = wv[q] - S.pq(e, l);
-                mx = fmaxf(mx, fabsf(v));
-                if (e != s) S.P[(size_t)e * K + m] = v * ipiv;
-            } else if (e < tot) {
-                const int c = e - S.n_oth;
-                const float v = wv[q] - S.pq(s, c);
-                mx = fmaxf(mx, fabsf(v));
-                if (c != l) S.Q[(size_t)c * K + m] = v;
-            }
-        }
-    }
-    return mx;
-}
-
-// column_write for both spins of a move at once: each round issues four
-// loads per lane for each spin before any arithmetic, so the two spins'
-// L2 round trips overlap (the entries and their arithmetic are those of
-// column_write).
-template <int K>
-__device__ __forceinline__ float column_write2(const CSpin<K> &A, int sa, int la, float ipa, const CSpin<K> &B,
+__device__ __forceinline__ float column_write(const CSpin<K> &A, int sa, int la, float ipa, const CSpin<K> &B,
                                                int sb, int lb, float ipb, int m, int lane) {
     const int ta = A.n_oth + A.n_own, tb = B.n_oth + B.n_own;
     const int tot = ta > tb ? ta : tb;
@@ -401,7 +367,7 @@ sweep_warp_kernel(DevModel m, DevBatch b, SweepParams p, int *active_count, size
         t += f + 1;
         // factor columns mm of both spins (from the configuration before the move)
         const float ipu = 1.f / pu, ipd = 1.f / pd;
-        float mx = column_write2<K>(SU, bl, a, ipu, SD, a, bl, ipd, mm, lane);
+        float mx = column_write<K>(SU, bl, a, ipu, SD, a, bl, ipd, mm, lane);
         // Z_mu change from the up-neighbour counts (configuration before the move)
         const int bu = nbr_off[Ku], du = nbr_off[Ku + 1] - bu;
         const int bd0 = nbr_off[Kd], dd = nbr_off[Kd + 1] - bd0;
