@@ -130,9 +130,9 @@ __device__ __forceinline__ float column_write(const CSpin<K> &A, int sa, int la,
 }
 
 // G -= P Q^T.  Lane = a group of four columns (Q of those columns held in
-// registers); rows streamed four at a time, all four loads in flight
+// registers); rows streamed kRows at a time, all their loads in flight
 // before the arithmetic.
-template <int K>
+template <int K, int kRows>
 __device__ void warp_flush(const CSpin<K> &S, int lane) {
     const int q4 = S.ldg >> 2;
     for (int c4 = lane; c4 < q4; c4 += 32) {
@@ -146,7 +146,6 @@ __device__ void warp_flush(const CSpin<K> &S, int lane) {
                 q[j][4 * k] = v.x; q[j][4 * k + 1] = v.y; q[j][4 * k + 2] = v.z; q[j][4 * k + 3] = v.w;
             }
         }
-        constexpr int kRows = 4;
         for (int r0 = 0; r0 < S.n_oth; r0 += kRows) {
             float4 g[kRows];
 #pragma unroll
@@ -220,9 +219,9 @@ size_t warp_compact_block(const DevModel &m) {
 // sub-partition then holds four of the walkers' warps.
 constexpr int kWarpMaxWalkers = 14;
 
-template <int K>
-__global__ void __maxnreg__(128)
-sweep_warp_kernel(DevModel m, DevBatch b, SweepParams p, int *active_count, size_t cta_bytes, size_t walker_bytes) {
+template <int K, int kRows>
+__device__ __forceinline__ void sweep_warp_body(const DevModel &m, const DevBatch &b, const SweepParams &p,
+                                                int *active_count, size_t cta_bytes, size_t walker_bytes) {
     extern __shared__ __align__(16) unsigned char smem[];
     const int N = m.n_sites, nb = m.n_bonds;
     const int lane = threadIdx.x & 31, wl = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
@@ -301,17 +300,39 @@ sweep_warp_kernel(DevModel m, DevBatch b, SweepParams p, int *active_count, size
 
     while (true) {
         if (t == next_meas) {
-            // local energy (getOL): SzSz over the bonds, -1/2 ratio per antiparallel bond
+            // local energy (getOL): SzSz over the bonds, -1/2 ratio per antiparallel bond;
+            // four bonds per lane at a time, their G entries loaded before the sums
             __syncwarp();
             float el = 0.f;
-            for (int e = lane; e < nb; e += 32) {
-                const short2 bd = bonds[e];
-                const int li = lab[bd.x], lj = lab[bd.y];
-                if ((li > 0) == (lj > 0)) {
-                    el += 0.25f;
-                } else {
-                    const int a = (li > 0 ? li : lj) - 1, bl = (li > 0 ? -lj : -li) - 1;
-                    el = fmaf(-0.5f * SU.eff(bl, a), SD.eff(a, bl), el - 0.25f);
+            for (int e0 = lane; e0 < nb; e0 += 128) {
+                float gu[4], gd[4];
+                int ai[4], bi4[4], kind[4];
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    const int e = e0 + 32 * q;
+                    kind[q] = -1;
+                    gu[q] = gd[q] = 0.f;
+                    ai[q] = bi4[q] = 0;
+                    if (e < nb) {
+                        const short2 bd = bonds[e];
+                        const int li = lab[bd.x], lj = lab[bd.y];
+                        if ((li > 0) == (lj > 0)) {
+                            kind[q] = 0;
+                        } else {
+                            kind[q] = 1;
+                            ai[q] = (li > 0 ? li : lj) - 1;
+                            bi4[q] = (li > 0 ? -lj : -li) - 1;
+                            gu[q] = SU.G[(size_t)bi4[q] * SU.ldg + ai[q]];
+                            gd[q] = SD.G[(size_t)ai[q] * SD.ldg + bi4[q]];
+                        }
+                    }
+                }
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    if (kind[q] == 0)
+                        el += 0.25f;
+                    else if (kind[q] == 1)
+                        el = fmaf(-0.5f * (gu[q] - SU.pq(bi4[q], ai[q])), gd[q] - SD.pq(ai[q], bi4[q]), el - 0.25f);
                 }
             }
 #pragma unroll
@@ -400,8 +421,8 @@ sweep_warp_kernel(DevModel m, DevBatch b, SweepParams p, int *active_count, size
         }
         __syncwarp();
         if (mm == K) {
-            warp_flush<K>(SU, lane);
-            warp_flush<K>(SD, lane);
+            warp_flush<K, kRows>(SU, lane);
+            warp_flush<K, kRows>(SD, lane);
             __syncwarp();
             zero_factors<K>(SU, lane);
             zero_factors<K>(SD, lane);
@@ -410,8 +431,8 @@ sweep_warp_kernel(DevModel m, DevBatch b, SweepParams p, int *active_count, size
         }
     }
     if (mm > 0) {
-        warp_flush<K>(SU, lane);
-        warp_flush<K>(SD, lane);
+        warp_flush<K, kRows>(SU, lane);
+        warp_flush<K, kRows>(SD, lane);
     }
     __syncwarp();
     for (int s = lane; s < N; s += 32) {
@@ -430,6 +451,24 @@ sweep_warp_kernel(DevModel m, DevBatch b, SweepParams p, int *active_count, size
         b.n_meas[w] += n_meas;
         if (t < tend_all && acc < acc_left && !bad_walker) atomicAdd(active_count, 1);
     }
+}
+
+// Up to 14 walkers per CTA: 128 registers per thread, so that four warps
+// fit on each SM sub-partition; the flush streams four rows at a time.
+template <int K>
+__global__ void __maxnreg__(128)
+sweep_warp_kernel(DevModel m, DevBatch b, SweepParams p, int *active_count, size_t cta_bytes, size_t walker_bytes) {
+    sweep_warp_body<K, 4>(m, b, p, active_count, cta_bytes, walker_bytes);
+}
+
+// Up to 8 walkers per CTA (the shipped settings use 4 to 7): the registers
+// of 256 threads' worth, so the flush keeps eight rows in flight.
+constexpr int kWarpWideWalkers = 8;
+template <int K>
+__global__ void __launch_bounds__(32 * kWarpWideWalkers, 1)
+sweep_warp_wide_kernel(DevModel m, DevBatch b, SweepParams p, int *active_count, size_t cta_bytes,
+                       size_t walker_bytes) {
+    sweep_warp_body<K, 4>(m, b, p, active_count, cta_bytes, walker_bytes);
 }
 
 // Site-indexed W -> the label-indexed blocks (and back), one warp per walker.
@@ -540,9 +579,16 @@ static cudaError_t launch_warp_t(const DevModel &m, const DevBatch &b, const Swe
     const int wpb = p.warp_walkers;
     const size_t cta = warp_cta_smem(m), per = warp_walker_smem(m, K);
     const size_t sm = cta + (size_t)wpb * per;
+    const int grid = (b.n_walkers + wpb - 1) / wpb;
+    if (K >= 8 && wpb <= kWarpWideWalkers) {
+        cudaError_t e =
+            cudaFuncSetAttribute(sweep_warp_wide_kernel<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        if (e != cudaSuccess) return e;
+        sweep_warp_wide_kernel<K><<<grid, 32 * wpb, sm, stream>>>(m, b, p, active, cta, per);
+        return cudaGetLastError();
+    }
     cudaError_t e = cudaFuncSetAttribute(sweep_warp_kernel<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     if (e != cudaSuccess) return e;
-    const int grid = (b.n_walkers + wpb - 1) / wpb;
     sweep_warp_kernel<K><<<grid, 32 * wpb, sm, stream>>>(m, b, p, active, cta, per);
     return cudaGetLastError();
 }
