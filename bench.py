@@ -699,7 +699,7 @@ def gpu_arm(a):
     kern = {
         "sweep_mixed": {"ms": sweep_ms, "launches": sweep_n, "flop": tot["accepted"] * f_move,
                         "unit_work": "2*N^2 FP32 flop per accepted move (both spins' rank-1 update of N x n W)",
-                        **({"kernel": "sweep_warp_kernel (one warp per walker)",
+                        **({"kernel": "sweep_warp_kernel or sweep_warp_wide_kernel (one warp per walker)",
                             "executed_flop_per_move": N_SITES * N_SITES,
                             "executed_note": "the label-indexed blocks hold W's non-trivial rows only: "
                                              "2 spins x 2 flop x n_up x n_down = N^2 per accepted move"}
