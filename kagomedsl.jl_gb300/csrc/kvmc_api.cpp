@@ -793,6 +793,9 @@ extern "C" int kvmc_create(const kvmc_model_desc *model, const kvmc_batch_desc *
     if ((rc = h->alloc(&b.solve_scratch, b.solve_block * 2 * (size_t)Wk))) return bail(rc);
     b.lu_block = 0;
     b.lu_scratch = nullptr;
+    b.lu_invd = nullptr;
+    b.lu_perm = nullptr;
+    b.lu_aux_n = 0;
     b.G32 = nullptr;
     b.g_block = 0;
     b.cond_max = nullptr;
@@ -802,6 +805,12 @@ extern "C" int kvmc_create(const kvmc_model_desc *model, const kvmc_batch_desc *
         const size_t nmax = (size_t)std::max(nu, nd);
         b.lu_block = nmax * nmax;
         if ((rc = h->alloc(&b.lu_scratch, b.lu_block * 2 * (size_t)Wk))) return bail(rc);
+        // the FP64 refresh's row solves run as a separate launch over many CTAs
+        b.lu_aux_n = (int)nmax;
+        if ((rc = h->alloc(&b.lu_invd, nmax * 2 * (size_t)Wk)) ||
+            (rc = h->alloc(&b.lu_perm, (nmax + 1) * 2 * (size_t)Wk)))
+            return bail(rc);
+        cudaMemset(b.lu_perm, 0, (nmax + 1) * 2 * (size_t)Wk * sizeof(int));
     } else if (h->cplx && kvmc::complex_refresh_needs_large(m)) {
         // complex tilde_U factorised in HBM: n x n complex = 2 n^2 doubles per walker-spin
         const size_t nmax = (size_t)std::max(nu, nd);

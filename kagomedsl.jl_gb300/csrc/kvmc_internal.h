@@ -59,6 +59,12 @@ struct DevBatch {
     size_t solve_block;    // doubles per (walker, spin)
     double *lu_scratch;    // more than 160 orbitals: tilde_U factorised in HBM, [W][2][lu_block]
     size_t lu_block;       // doubles per (walker, spin), 0 when unused
+    // real orbitals beyond 160: the FP64 LU's 1/diag [W][2][lu_aux_n] and pivot
+    // order [W][2][lu_aux_n + 1] (the last entry: 1 when the LU succeeded), read
+    // by the row solves that run in a separate launch; null when unused
+    double *lu_invd;
+    int *lu_perm;
+    int lu_aux_n;
     // one-warp-per-walker sweep (kvmc_warp.cu): W's non-trivial rows indexed by
     // the other spin's label, [W][g_block] (null until that sweep is enabled)
     float *G32;

@@ -360,6 +360,10 @@ refresh_large_kernel(DevModel m, DevBatch b, int only_due, int track_drift) {
     constexpr bool kF32 = sizeof(LT) == 4;
     const int w = blockIdx.x;
     const int spin = blockIdx.y;
+    // FP64: the row solves run in refresh_large_rows_kernel when lu_perm is set;
+    // this launch marks the walker-spin's LU as not (yet) done
+    int *lu_flag = (!kF32 && b.lu_perm) ? b.lu_perm + ((size_t)w * 2 + spin) * (b.lu_aux_n + 1) + b.lu_aux_n : nullptr;
+    if (lu_flag && threadIdx.x == 0) *lu_flag = 0;
     if (only_due == 1 && b.since[w] >= 0) return;
     if (only_due == 2 && !(b.status[w] & kStatusRefine)) return;
     if (spin == 0 && threadIdx.x == 0) atomicAdd(b.refresh_count + (only_due == 2 ? 1 : 0), 1ull);
@@ -603,6 +607,17 @@ refresh_large_kernel(DevModel m, DevBatch b, int only_due, int track_drift) {
             for (int o = 16; o > 0; o >>= 1) dmax = fmaxf(dmax, __shfl_xor_sync(0xffffffffu, dmax, o));
             if (lane == 0 && dmax > 0.f) atomic_max_nonneg(&b.drift[w], dmax);
         }
+    } else if (lu_flag) {
+        // the factors' 1/diag and pivot order for the row solves' launch
+        double *gi = b.lu_invd + ((size_t)w * 2 + spin) * b.lu_aux_n;
+        int *gp = b.lu_perm + ((size_t)w * 2 + spin) * (b.lu_aux_n + 1);
+        for (int i = tid; i < n; i += nt) {
+            gi[i] = (double)invd[i];
+            gp[i] = perm[i];
+        }
+        if (tid == 0) *lu_flag = 1;
+        (void)nrows;
+        (void)Y;
     } else {
         for (int r0 = 0; r0 < nrows; r0 += blockDim.x) {
             const int cnt = min((int)blockDim.x, nrows - r0);
@@ -610,6 +625,50 @@ refresh_large_kernel(DevModel m, DevBatch b, int only_due, int track_drift) {
                                      track_drift != 0, krow);
         }
     }
+}
+
+// The row solves of the FP64 refresh beyond kSmemLuMaxN orbitals, after
+// refresh_large_kernel has factorised tilde_U: CTA z of (walker, spin)
+// solves the rows z * kRowsThreads .. of the sites not holding the spin, one
+// thread per row (solve_rows_blocked), so the N - n rows of one walker-spin
+// spread over many SMs' FP64 pipes instead of one.
+constexpr int kRowsThreads = 64;
+
+template <typename OutT>
+__global__ void __launch_bounds__(kRowsThreads) refresh_large_rows_kernel(DevModel m, DevBatch b, int track_drift) {
+    const int w = blockIdx.x, spin = blockIdx.y;
+    const size_t ws = (size_t)w * 2 + spin;
+    const int *gp = b.lu_perm + ws * (b.lu_aux_n + 1);
+    if (gp[b.lu_aux_n] != 1) return;
+    const int N = m.n_sites;
+    const int n = spin == 0 ? m.n_up : m.n_dn;
+    const int r0 = blockIdx.z * kRowsThreads;
+    if (r0 >= N - n) return;
+    const int ldw = spin == 0 ? m.ld_up : m.ld_dn;
+    const double *U = spin == 0 ? m.U_up : m.U_dn;
+    const short *kappa = (spin == 0 ? b.kappa_up : b.kappa_dn) + (size_t)w * N;
+    const size_t wblock = (size_t)N * (m.ld_up + m.ld_dn);
+    const bool cpt = sizeof(OutT) == 4 && b.compact;
+    OutT *W = cpt ? (OutT *)(b.G32 + (size_t)w * b.g_block + (spin == 0 ? 0 : (size_t)m.n_dn * m.ld_up))
+                  : (sizeof(OutT) == 8 ? (OutT *)b.W64 : (OutT *)b.W32) + (size_t)w * wblock +
+                        (spin == 0 ? 0 : (size_t)N * m.ld_up);
+    const short *krow = cpt ? (spin == 0 ? b.kappa_dn : b.kappa_up) + (size_t)w * N : nullptr;
+    const double *A = b.lu_scratch + ws * b.lu_block;
+    double *Y = b.solve_scratch + ws * b.solve_block;
+    extern __shared__ __align__(16) unsigned char smem[];
+    double *invd = reinterpret_cast<double *>(smem);
+    int *perm = reinterpret_cast<int *>(invd + n);
+    short *rows = reinterpret_cast<short *>(perm + n);
+    const double *gi = b.lu_invd + ws * b.lu_aux_n;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        invd[i] = gi[i];
+        perm[i] = gp[i];
+    }
+    const int nrows = collect_empty_rows(kappa, N, rows);   // synchronises the block
+    const int cnt = min(kRowsThreads, nrows - r0);
+    if (cnt <= 0) return;
+    solve_rows_blocked<OutT>(A, n, invd, perm, U, n, rows + r0, cnt, Y + (size_t)r0 * n, W, ldw, &b.drift[w],
+                             track_drift != 0, krow);
 }
 
 size_t refresh_large_smem(const DevModel &m, size_t lt_bytes) {
@@ -2196,16 +2255,22 @@ cudaError_t launch_refresh(const DevModel &m, const DevBatch &b, bool fp32_out, 
     const dim3 grid(b.n_walkers, 2);
     if (refresh_needs_large(m)) {
         const size_t sm = refresh_large_smem(m);
+        const int nmax = m.n_up > m.n_dn ? m.n_up : m.n_dn;
+        const int omax = m.n_sites - (m.n_up < m.n_dn ? m.n_up : m.n_dn);
+        const dim3 rgrid(b.n_walkers, 2, (omax + kRowsThreads - 1) / kRowsThreads);
+        const size_t rsm = (size_t)nmax * (8 + 4) + (size_t)m.n_sites * 2 + 16;
         if (fp32_out) {
             cudaError_t e = cudaFuncSetAttribute(refresh_large_kernel<double, float>,
                                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
             if (e != cudaSuccess) return e;
             refresh_large_kernel<double, float><<<grid, kRefreshThreads, sm, stream>>>(m, b, only_due, track_drift);
+            if (b.lu_perm) refresh_large_rows_kernel<float><<<rgrid, kRowsThreads, rsm, stream>>>(m, b, track_drift);
         } else {
             cudaError_t e = cudaFuncSetAttribute(refresh_large_kernel<double, double>,
                                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
             if (e != cudaSuccess) return e;
             refresh_large_kernel<double, double><<<grid, kRefreshThreads, sm, stream>>>(m, b, only_due, track_drift);
+            if (b.lu_perm) refresh_large_rows_kernel<double><<<rgrid, kRowsThreads, rsm, stream>>>(m, b, track_drift);
         }
         return cudaGetLastError();
     }
