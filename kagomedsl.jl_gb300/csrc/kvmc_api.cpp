@@ -233,7 +233,7 @@ cudaError_t sweep_launch(kvmc_handle *h, const kvmc::SweepParams &p) {
 // Rebuilds every walker's W.  allow32: with the FP32 refinement refresh
 // enabled, use it (FP64 for the walkers it flags); otherwise FP64 throughout.
 int full_refresh(kvmc_handle *h, bool track_drift, bool allow32 = true) {
-    h->db.compact = 0;  // outside a sweep call W32 is the state
+    h->db.compact = 0;  // W32 is rebuilt for every walker
     KV_TRY(h->cuda(cudaMemsetAsync(h->db.drift, 0, sizeof(float) * h->n_walkers, h->stream), "memset"));
     if (allow32 && h->refresh32 && !h->cplx) {
         KV_TRY(h->cuda(refresh32_launch(h, 0, track_drift ? 1 : 0), "refresh launch"));
@@ -925,6 +925,7 @@ extern "C" int kvmc_reset_stats(kvmc_handle *h) {
 extern "C" int kvmc_init(kvmc_handle *h, const int32_t *kappa_up, const int32_t *kappa_down, int32_t *attempts) {
     if (!h) return fail_global(KVMC_ERR_ARGUMENT, "null handle");
     KV_TRY(set_device(h));
+    h->db.compact = 0;   // every walker's W32 is rebuilt below
     const int Wk = h->n_walkers;
     KV_TRY(h->cuda(cudaMemsetAsync(h->db.t, 0, Wk * 8, h->stream), "memset"));
     KV_TRY(h->cuda(cudaMemsetAsync(h->db.status, 0, Wk * 4, h->stream), "memset"));
@@ -1164,11 +1165,13 @@ int sweep_end(kvmc_handle *h, kvmc_sweep_stats *stats, SweepCall &c) {
 
 bool warp_mode(const kvmc_handle *h) { return h->mixed && !h->cplx && h->warp_walkers > 0; }
 
-// One-warp mode: the sweep and the refreshes of a call work on the
-// label-indexed blocks; W32 is converted to them at the start of the call
-// and back at its end (the refreshes write the blocks while db.compact is set).
+// One-warp mode: the sweep and the refreshes work on the label-indexed
+// blocks (the refreshes write the blocks while db.compact is set).  The first
+// sweep call converts W32 to them; they then stay the state from call to call,
+// and W32 is brought back (compact_end, w_current) only by the calls that read
+// or write the site-indexed W.
 int compact_begin(kvmc_handle *h) {
-    if (!warp_mode(h)) return KVMC_OK;
+    if (!warp_mode(h) || h->db.compact) return KVMC_OK;
     KV_TRY(h->cuda(kvmc::launch_warp_convert(h->dm, h->db, true, h->stream), "to label-indexed W"));
     h->db.compact = 1;
     return KVMC_OK;
@@ -1178,6 +1181,14 @@ int compact_end(kvmc_handle *h) {
     if (!h->db.compact) return KVMC_OK;
     h->db.compact = 0;
     return h->cuda(kvmc::launch_warp_convert(h->dm, h->db, false, h->stream), "to site-indexed W");
+}
+
+// W32 current for a call that reads or writes it (and waits for the
+// conversion, since some of those calls copy on the legacy stream)
+int w_current(kvmc_handle *h) {
+    if (!h->db.compact) return KVMC_OK;
+    KV_TRY(compact_end(h));
+    return h->cuda(cudaStreamSynchronize(h->stream), "to site-indexed W");
 }
 
 // Runs (sweep, refresh) pairs until every walker has reached its target.
@@ -1219,9 +1230,7 @@ int run_sweep(kvmc_handle *h, int64_t proposals_per_walker, int64_t moves_per_wa
     } else {
         rc = run_pairs(h, p, c);
     }
-    const int rc2 = compact_end(h);
     if (rc != KVMC_OK) return rc;
-    KV_TRY(rc2);
     return sweep_end(h, stats, c);
 }
 
@@ -1429,6 +1438,7 @@ extern "C" int kvmc_group_last_error(const kvmc_group *g, char *buf, size_t len)
 extern "C" int kvmc_measure(kvmc_handle *h, double *local_energy) {
     if (!h || !local_energy) return fail_global(KVMC_ERR_ARGUMENT, "null argument");
     KV_TRY(set_device(h));
+    KV_TRY(w_current(h));
     KV_TRY(h->cuda(h->cplx ? kvmc::launch_measure_c(h->dm, h->db, h->mixed, h->stream)
                            : kvmc::launch_measure(h->dm, h->db, h->mixed, h->stream), "measure launch"));
     KV_TRY(h->cuda(cudaMemcpyAsync(local_energy, h->db.energy_out, sizeof(double) * h->n_walkers,
@@ -1439,6 +1449,7 @@ extern "C" int kvmc_measure(kvmc_handle *h, double *local_energy) {
 extern "C" int kvmc_eval_ratios(kvmc_handle *h, int32_t n_moves, const int32_t *moves, double *ratios) {
     if (!h || !moves || !ratios || n_moves <= 0) return fail_global(KVMC_ERR_ARGUMENT, "bad argument");
     KV_TRY(set_device(h));
+    KV_TRY(w_current(h));
     const size_t cnt = (size_t)h->n_walkers * n_moves;
     for (size_t k = 0; k < cnt; ++k) {
         const int32_t *mv = moves + 4 * k;
@@ -1462,6 +1473,7 @@ extern "C" int kvmc_eval_ratios(kvmc_handle *h, int32_t n_moves, const int32_t *
 extern "C" int kvmc_apply_moves(kvmc_handle *h, const int32_t *moves) {
     if (!h || !moves) return fail_global(KVMC_ERR_ARGUMENT, "bad argument");
     KV_TRY(set_device(h));
+    KV_TRY(w_current(h));
     for (int w = 0; w < h->n_walkers; ++w) {
         const int32_t *mv = moves + 5 * (size_t)w;
         if (mv[0] == 0) continue;
@@ -1482,6 +1494,7 @@ extern "C" int kvmc_apply_moves(kvmc_handle *h, const int32_t *moves) {
 extern "C" int kvmc_refresh(kvmc_handle *h) {
     if (!h) return fail_global(KVMC_ERR_ARGUMENT, "null handle");
     KV_TRY(set_device(h));
+    KV_TRY(w_current(h));
     KV_TRY(h->cuda(cudaMemsetAsync(h->db.status, 0, h->n_walkers * 4, h->stream), "memset"));
     KV_TRY(full_refresh(h, h->mixed, false));   // kvmc_refresh: the FP64 rebuild
     return check_status(h, nullptr);
@@ -1518,6 +1531,7 @@ extern "C" int kvmc_set_state(kvmc_handle *h, const int32_t *kappa_up, const int
 extern "C" int kvmc_get_w(kvmc_handle *h, double *W_up, double *W_down) {
     if (!h) return fail_global(KVMC_ERR_ARGUMENT, "null handle");
     KV_TRY(set_device(h));
+    KV_TRY(w_current(h));
     const int N = h->n_sites;
     const size_t cw = h->cplx ? 2 : 1;  // doubles per entry
     const size_t wblock = (size_t)N * (h->ld_up + h->ld_dn) * cw;
@@ -1547,6 +1561,8 @@ extern "C" int kvmc_get_w(kvmc_handle *h, double *W_up, double *W_down) {
 
 extern "C" int kvmc_set_tuning(kvmc_handle *h, int32_t key, int32_t value) {
     if (!h) return fail_global(KVMC_ERR_ARGUMENT, "null handle");
+    KV_TRY(set_device(h));
+    KV_TRY(w_current(h));   // a new launch shape may read W32
     if (key == KVMC_TUNE_STREAM_THREADS) {
         if (value != 128 && value != 256) return h->fail(KVMC_ERR_ARGUMENT, "stream threads must be 128 or 256");
         // the flush gives each thread four columns of one row group
@@ -1771,6 +1787,7 @@ extern "C" int kvmc_measure_grad(kvmc_handle *h, double *local_energy, double *l
     if (!h) return fail_global(KVMC_ERR_ARGUMENT, "null handle");
     if (h->n_params == 0) return h->fail(KVMC_ERR_ARGUMENT, "kvmc_set_log_derivatives has not been called");
     KV_TRY(set_device(h));
+    KV_TRY(w_current(h));
     kvmc::GradModel g{};
     g.n_params = h->n_params;
     g.MT = h->d_MT;

@@ -25,8 +25,10 @@
 // configuration live in shared memory (about 15 KB per walker at N = 216,
 // K = 8), so a CTA holds up to 14 walkers, one per warp.  Each warp runs its
 // own serial chain; the SM's other warps fill its latency.  G lives in
-// HBM/L2; a sweep call converts the handle's site-indexed W into G at its
-// start and back at its end, and the refreshes in between write G.  The G blocks of the walkers in flight should
+// HBM/L2; the first sweep call converts the handle's site-indexed W into G,
+// which then stays the state from call to call (the refreshes write G), and
+// the calls that read or write the site-indexed W convert it back.  The G
+// blocks of the walkers in flight should
 // fit in L2 (7 walkers per SM at N = 216: 99 MB): with more walkers in
 // flight the flushes stream from HBM and each chain slows down more than
 // the extra walkers gain.
@@ -474,8 +476,8 @@ sweep_warp_wide_kernel(DevModel m, DevBatch b, SweepParams p, int *active_count,
 }
 
 // Site-indexed W -> the label-indexed blocks (and back), one warp per walker.
-// A sweep call of a handle in one-warp mode converts at its start and end;
-// the sweep and the refreshes in between work on the blocks.
+// A handle in one-warp mode converts before its first sweep call, and back
+// only for a call that reads or writes the site-indexed W.
 __global__ void __launch_bounds__(128)
 warp_to_compact_kernel(DevModel m, DevBatch b) {
     const int lane = threadIdx.x & 31, w = blockIdx.x * 4 + (threadIdx.x >> 5);
