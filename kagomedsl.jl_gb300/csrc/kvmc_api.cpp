@@ -71,6 +71,8 @@ struct kvmc_handle {
     int *d_active = nullptr;
     int *d_attempt = nullptr;
     int *d_redo = nullptr;
+    double *d_stats = nullptr;  // two sets of kCallStats: a sweep call's start and end
+    double *h_stats = nullptr;  // pinned copy of d_stats
     void *d_scratch = nullptr;
     size_t scratch_bytes = 0;
 
@@ -246,6 +248,19 @@ int full_refresh(kvmc_handle *h, bool track_drift, bool allow32 = true) {
     if (h->db.cond_max)
         KV_TRY(h->cuda(cudaMemsetAsync(h->db.cond_max, 0, sizeof(float) * h->n_walkers, h->stream), "memset"));
     return h->cuda(cudaStreamSynchronize(h->stream), "refresh");
+}
+
+// The error for nb walkers with a status set, the first of them walker
+// `first` with status `code`.
+int status_error(kvmc_handle *h, int nb, int first, int code) {
+    if (nb) {
+        if (code & kvmc::kStatusSingular)
+            return h->fail(KVMC_ERR_SINGULAR, "%d walker(s) have a singular tilde_U (first: walker %d)", nb, first);
+        if (code & kvmc::kStatusTimeout)
+            return h->fail(KVMC_ERR_CUDA, "%d walker(s): a tensor-core wait timed out (first: walker %d)", nb, first);
+        return h->fail(KVMC_ERR_NUMERIC, "%d walker(s) produced a non-finite ratio (first: walker %d)", nb, first);
+    }
+    return KVMC_OK;
 }
 
 int check_status(kvmc_handle *h, int *bad) {
@@ -607,6 +622,7 @@ extern "C" int kvmc_destroy(kvmc_handle *h) {
     if (h->d_MT) cudaFree(h->d_MT);
     if (h->d_gsums) cudaFree(h->d_gsums);
     if (h->d_gout) cudaFree(h->d_gout);
+    if (h->h_stats) cudaFreeHost(h->h_stats);
     for (auto &e : h->ev_pool) cudaEventDestroy(e);
     for (auto &e : h->region)
         if (e) cudaEventDestroy(e);
@@ -787,7 +803,11 @@ extern "C" int kvmc_create(const kvmc_model_desc *model, const kvmc_batch_desc *
         (rc = h->alloc(&b.accepted, Wk)) || (rc = h->alloc(&b.proposals, Wk)) || (rc = h->alloc(&b.status, Wk)) ||
         (rc = h->alloc(&b.logdet, 4 * (size_t)Wk)) || (rc = h->alloc(&b.drift, Wk)) ||
         (rc = h->alloc(&b.energy_out, Wk)) || (rc = h->alloc(&b.refresh_count, 2)) || (rc = h->alloc(&h->d_active, 1)) ||
-        (rc = h->alloc(&h->d_attempt, Wk)) || (rc = h->alloc(&h->d_redo, Wk)))
+        (rc = h->alloc(&h->d_attempt, Wk)) || (rc = h->alloc(&h->d_redo, Wk)) ||
+        (rc = h->alloc(&h->d_stats, 2 * kvmc::kCallStats)))
+        return bail(rc);
+    if ((rc = h->cuda(cudaMallocHost(reinterpret_cast<void **>(&h->h_stats), 2 * kvmc::kCallStats * sizeof(double)),
+                      "cudaMallocHost")))
         return bail(rc);
     b.solve_block = kvmc::refresh_scratch_block(m) * cw;
     if ((rc = h->alloc(&b.solve_scratch, b.solve_block * 2 * (size_t)Wk))) return bail(rc);
@@ -1046,23 +1066,6 @@ int collect_timing(kvmc_handle *h) {
     return KVMC_OK;
 }
 
-struct Snapshot {
-    std::vector<double> se, se2;
-    std::vector<long long> nm, acc, prop;
-};
-
-int snapshot(kvmc_handle *h, Snapshot &s) {
-    const size_t Wk = h->n_walkers;
-    s.se.resize(Wk); s.se2.resize(Wk); s.nm.resize(Wk); s.acc.resize(Wk); s.prop.resize(Wk);
-    auto &b = h->db;
-    KV_TRY(h->cuda(cudaMemcpyAsync(s.se.data(), b.sum_e, Wk * 8, cudaMemcpyDeviceToHost, h->stream), "stats"));
-    KV_TRY(h->cuda(cudaMemcpyAsync(s.se2.data(), b.sum_e2, Wk * 8, cudaMemcpyDeviceToHost, h->stream), "stats"));
-    KV_TRY(h->cuda(cudaMemcpyAsync(s.nm.data(), b.n_meas, Wk * 8, cudaMemcpyDeviceToHost, h->stream), "stats"));
-    KV_TRY(h->cuda(cudaMemcpyAsync(s.acc.data(), b.accepted, Wk * 8, cudaMemcpyDeviceToHost, h->stream), "stats"));
-    KV_TRY(h->cuda(cudaMemcpyAsync(s.prop.data(), b.proposals, Wk * 8, cudaMemcpyDeviceToHost, h->stream), "stats"));
-    return h->cuda(cudaStreamSynchronize(h->stream), "stats");
-}
-
 }  // namespace
 
 namespace {
@@ -1089,19 +1092,19 @@ kvmc::SweepParams sweep_params(const kvmc_handle *h) {
 
 // The accounting around one kvmc_sweep / kvmc_advance call.
 struct SweepCall {
-    Snapshot before;
-    unsigned long long ref0[2] = {0, 0};
     int launches = 1;
-    int64_t moves = 0;  // kvmc_advance: accepted moves asked of every walker
+    int64_t moves = 0;      // kvmc_advance: accepted moves asked of every walker
+    int64_t proposals = 0;  // kvmc_sweep: proposals asked of every walker
 };
 
+// The call's statistics come from two device reductions of the per-walker
+// counters (call_stats_kernel), at its start and at its end, read back in one
+// pinned copy at the end.
 int sweep_begin(kvmc_handle *h, int64_t proposals_per_walker, int64_t moves_per_walker, bool stats, SweepCall &c) {
     KV_TRY(set_device(h));
     c.moves = proposals_per_walker > 0 ? 0 : moves_per_walker;
-    if (stats) {
-        KV_TRY(snapshot(h, c.before));
-        KV_TRY(h->cuda(cudaMemcpy(c.ref0, h->db.refresh_count, 16, cudaMemcpyDeviceToHost), "refresh count"));
-    }
+    c.proposals = proposals_per_walker;
+    if (stats) KV_TRY(h->cuda(kvmc::launch_call_stats(h->db, h->d_stats, h->stream), "stats"));
     KV_TRY(h->cuda(kvmc::launch_set_tend(h->db, proposals_per_walker, moves_per_walker, h->stream), "set t_end"));
     return h->cuda(cudaMemsetAsync(h->db.drift, 0, sizeof(float) * h->n_walkers, h->stream), "memset");
 }
@@ -1123,43 +1126,31 @@ int enqueue_pairs(kvmc_handle *h, const kvmc::SweepParams &p, int pairs, bool ti
 }
 
 int sweep_end(kvmc_handle *h, kvmc_sweep_stats *stats, SweepCall &c) {
-    int bad = 0;
-    KV_TRY(check_status(h, &bad));
-    if (c.moves > 0) {
+    constexpr int K = kvmc::kCallStats;
+    KV_TRY(h->cuda(kvmc::launch_call_stats(h->db, h->d_stats + K, h->stream), "stats"));
+    KV_TRY(h->cuda(cudaMemcpyAsync(h->h_stats, h->d_stats, 2 * K * sizeof(double), cudaMemcpyDeviceToHost, h->stream),
+                   "stats"));
+    KV_TRY(h->cuda(cudaStreamSynchronize(h->stream), "stats"));
+    const double *b0 = h->h_stats, *a = h->h_stats + K;
+    const int bad = (int)a[5];
+    KV_TRY(status_error(h, bad, (int)a[6], (int)a[7]));
+    if (c.moves > 0 && a[9] > 0)
         // a walker that used its proposal allowance without making its moves
-        std::vector<long long> acc(h->n_walkers), want(h->n_walkers);
-        KV_TRY(h->cuda(cudaMemcpy(acc.data(), h->db.accepted, acc.size() * 8, cudaMemcpyDeviceToHost), "accepted"));
-        KV_TRY(h->cuda(cudaMemcpy(want.data(), h->db.acc_end, want.size() * 8, cudaMemcpyDeviceToHost), "acc_end"));
-        int short_n = 0, first = -1;
-        for (int w = 0; w < h->n_walkers; ++w)
-            if (acc[w] < want[w]) { ++short_n; if (first < 0) first = w; }
-        if (short_n)
-            return h->fail(KVMC_ERR_NUMERIC,
-                           "%d walker(s) made fewer than %lld accepted moves within %lld proposals per move "
-                           "(first: walker %d)", short_n, (long long)c.moves, kvmc::kAdvanceProposalsPerMove, first);
-    }
+        return h->fail(KVMC_ERR_NUMERIC,
+                       "%d walker(s) made fewer than %lld accepted moves within %lld proposals per move "
+                       "(first: walker %d)", (int)a[9], (long long)c.moves, kvmc::kAdvanceProposalsPerMove, (int)a[10]);
     if (!stats) return KVMC_OK;
     std::memset(stats, 0, sizeof *stats);
-    Snapshot after;
-    KV_TRY(snapshot(h, after));
-    for (int w = 0; w < h->n_walkers; ++w) {
-        stats->proposals += after.prop[w] - c.before.prop[w];
-        stats->accepted += after.acc[w] - c.before.acc[w];
-        stats->measurements += after.nm[w] - c.before.nm[w];
-        stats->sum_energy += after.se[w] - c.before.se[w];
-        stats->sum_energy2 += after.se2[w] - c.before.se2[w];
-    }
-    std::vector<float> dr(h->n_walkers);
-    KV_TRY(h->cuda(cudaMemcpy(dr.data(), h->db.drift, dr.size() * 4, cudaMemcpyDeviceToHost), "drift"));
-    double md = 0;
-    for (float d : dr) md = std::max(md, (double)d);
-    stats->max_drift = md;
+    stats->proposals = (int64_t)(a[4] - b0[4]);
+    stats->accepted = (int64_t)(a[3] - b0[3]);
+    stats->measurements = (int64_t)(a[2] - b0[2]);
+    stats->sum_energy = a[0] - b0[0];
+    stats->sum_energy2 = a[1] - b0[1];
+    stats->max_drift = a[8];
     stats->bad_walkers = bad;
     stats->launches = c.launches;
-    unsigned long long ref1[2] = {0, 0};
-    KV_TRY(h->cuda(cudaMemcpy(ref1, h->db.refresh_count, 16, cudaMemcpyDeviceToHost), "refresh count"));
-    stats->refreshes = (int64_t)(ref1[0] - c.ref0[0]);
-    stats->fp64_redos = (int64_t)(ref1[1] - c.ref0[1]);
+    stats->refreshes = (int64_t)(a[11] - b0[11]);
+    stats->fp64_redos = (int64_t)(a[12] - b0[12]);
     return KVMC_OK;
 }
 
@@ -1194,10 +1185,16 @@ int w_current(kvmc_handle *h) {
 // Runs (sweep, refresh) pairs until every walker has reached its target.
 int run_pairs(kvmc_handle *h, const kvmc::SweepParams &p, SweepCall &c) {
     // Between host checks the loop issues a group of (sweep, refresh) pairs.
+    // A call of a proposal count that one launch covers usually ends with its
+    // first pair (the walkers that stop for a refresh go on in the groups
+    // after it), so its first group is one pair.
     const int group = h->mixed ? 4 : 8;
-    for (int iter = 0;; iter += group) {
-        KV_TRY(enqueue_pairs(h, p, group, true));
-        c.launches += 2 * group;
+    const bool one_launch = c.moves == 0 && c.proposals <= kvmc::kLaunchProposals;
+    for (int iter = 0;;) {
+        const int g = (iter == 0 && one_launch) ? 1 : group;
+        KV_TRY(enqueue_pairs(h, p, g, true));
+        c.launches += 2 * g;
+        iter += g;
         int active = 0;
         KV_TRY(h->cuda(cudaMemcpyAsync(&active, h->d_active, sizeof(int), cudaMemcpyDeviceToHost, h->stream), "active"));
         KV_TRY(h->cuda(cudaStreamSynchronize(h->stream), "sweep"));

@@ -150,6 +150,10 @@ size_t refresh_tile_smem(const DevModel &m);
 cudaError_t launch_refresh_tile(const DevModel &m, const DevBatch &b, int only_due, int track_drift,
                                 cudaStream_t stream);
 cudaError_t launch_clear_status(const DevBatch &b, int bits, cudaStream_t stream);
+// The sums a sweep call reports, reduced on the device (kvmc_refresh32.cu):
+// kCallStats doubles at `out`, laid out as call_stats_kernel documents.
+constexpr int kCallStats = 16;
+cudaError_t launch_call_stats(const DevBatch &b, double *out, cudaStream_t stream);
 
 // The tiled refresh with its residual B - V M on the tensor cores
 // (kvmc_refresh_oz.cu, KVMC_TUNE_REFRESH32 = 3).  U is split once per model

@@ -222,6 +222,73 @@ __global__ void clear_status_bits_kernel(DevBatch b, int bits) {
     if (w < b.n_walkers) b.status[w] &= ~bits;
 }
 
+// The per-call statistics of a sweep call in one CTA, every sum in a fixed
+// order (thread t takes walkers t, t + 512, ...; then a fixed tree), so the
+// result does not depend on scheduling.  out: [0] sum of sum_e, [1] of
+// sum_e2, [2] of n_meas, [3] of accepted, [4] of proposals, [5] walkers with
+// a status bit set, [6] the first of them (-1: none), [7] its status, [8] the
+// largest drift, [9] walkers short of acc_end, [10] the first of them,
+// [11], [12] the two refresh counters.
+constexpr int kStatsThreads = 512;
+__global__ void __launch_bounds__(kStatsThreads) call_stats_kernel(DevBatch b, double *out) {
+    __shared__ double sd[kStatsThreads][2];
+    __shared__ long long sl[kStatsThreads][5];
+    __shared__ int sf[kStatsThreads][2];
+    __shared__ float sm[kStatsThreads];
+    const int t = threadIdx.x;
+    double e = 0.0, e2 = 0.0;
+    long long nm = 0, acc = 0, prop = 0, nbad = 0, nshort = 0;
+    int fbad = 0x7fffffff, fshort = 0x7fffffff;
+    float dr = 0.f;
+    for (int w = t; w < b.n_walkers; w += kStatsThreads) {
+        e += b.sum_e[w];
+        e2 += b.sum_e2[w];
+        nm += b.n_meas[w];
+        acc += b.accepted[w];
+        prop += b.proposals[w];
+        if (b.status[w]) { ++nbad; fbad = min(fbad, w); }
+        if (b.accepted[w] < b.acc_end[w]) { ++nshort; fshort = min(fshort, w); }
+        dr = fmaxf(dr, b.drift[w]);
+    }
+    sd[t][0] = e; sd[t][1] = e2;
+    sl[t][0] = nm; sl[t][1] = acc; sl[t][2] = prop; sl[t][3] = nbad; sl[t][4] = nshort;
+    sf[t][0] = fbad; sf[t][1] = fshort;
+    sm[t] = dr;
+    __syncthreads();
+    for (int h = kStatsThreads / 2; h > 0; h >>= 1) {
+        if (t < h) {
+            sd[t][0] += sd[t + h][0];
+            sd[t][1] += sd[t + h][1];
+            for (int q = 0; q < 5; ++q) sl[t][q] += sl[t + h][q];
+            sf[t][0] = min(sf[t][0], sf[t + h][0]);
+            sf[t][1] = min(sf[t][1], sf[t + h][1]);
+            sm[t] = fmaxf(sm[t], sm[t + h]);
+        }
+        __syncthreads();
+    }
+    if (t == 0) {
+        out[0] = sd[0][0];
+        out[1] = sd[0][1];
+        out[2] = (double)sl[0][0];
+        out[3] = (double)sl[0][1];
+        out[4] = (double)sl[0][2];
+        out[5] = (double)sl[0][3];
+        const int fb = sf[0][0] == 0x7fffffff ? -1 : sf[0][0];
+        out[6] = fb;
+        out[7] = fb >= 0 ? (double)b.status[fb] : 0.0;
+        out[8] = sm[0];
+        out[9] = (double)sl[0][4];
+        out[10] = sf[0][1] == 0x7fffffff ? -1.0 : (double)sf[0][1];
+        out[11] = (double)b.refresh_count[0];
+        out[12] = (double)b.refresh_count[1];
+    }
+}
+
+cudaError_t launch_call_stats(const DevBatch &b, double *out, cudaStream_t stream) {
+    call_stats_kernel<<<1, kStatsThreads, 0, stream>>>(b, out);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_clear_status(const DevBatch &b, int bits, cudaStream_t stream) {
     clear_status_bits_kernel<<<(b.n_walkers + 255) / 256, 256, 0, stream>>>(b, bits);
     return cudaGetLastError();
