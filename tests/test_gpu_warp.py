@@ -213,3 +213,45 @@ def test_headline_energy_gate_and_drift_bound(kv):
     d = (out["mixed"][0] - out["plain"][0]) / 216
     assert abs(d.mean()) + 2 * d.std(ddof=1) / np.sqrt(walkers) <= 1e-4, (d.mean(), d.std())
     assert out["mixed"][1] <= 1e-2, out["mixed"][1]
+
+
+def test_warp_blocks_stay_the_state_across_calls_and_w_reads(kv):
+    """One-warp mode keeps W's label-indexed blocks as the state from one
+    sweep call to the next and converts back only for a call that reads the
+    site-indexed W.  Two calls of 120 accepted moves per walker with kvmc_get_w
+    and kvmc_measure between them end in exactly the configurations, counts and
+    energy sums of one call of 240 from the same starts (120 is a multiple of
+    the delay depth 12, so both runs flush the same moves together; no refresh
+    due in either run, guard off), and the W read in between is the oracle's
+    to 1e-2 relative (the FP32 state 120 moves after its last rebuild)."""
+    ham = ham_for(kv, 216)
+    walkers, seed = 14, 41
+    runs = []
+    for split in (True, False):
+        eng = kv.Engine(ham, walkers, precision="mixed", seed=seed, refresh_interval=4096, delay_k=12,
+                        w_placement="hbm")
+        eng.set_warp_walkers(7)
+        eng.set_drift_tolerance(1e9)
+        eng.init()
+        if split:
+            eng.advance(120)
+            Wu, Wd = eng.get_w()
+            ku, kd, _ = eng.get_state()
+            for w in range(walkers):
+                # FP32 W after 120 moves without a refresh (guard off): a
+                # conversion fault would show as O(1) errors
+                assert close(Wu[w], o.reevaluateW(ham.U_up, ku[w]), 1e-2), w
+                assert close(Wd[w], o.reevaluateW(ham.U_down, kd[w]), 1e-2), w
+            e = eng.measure()
+            assert np.all(np.isfinite(e))
+            eng.advance(120)
+        else:
+            eng.advance(240)
+        ku, kd, ct = eng.get_state()
+        stats = eng.walker_stats()
+        runs.append((ku, kd, ct, stats))
+        eng.close()
+    (ka, kda, ca, sa), (kb, kdb, cb, sb) = runs
+    assert np.array_equal(ka, kb) and np.array_equal(kda, kdb) and np.array_equal(ca, cb)
+    assert np.array_equal(sa["accepted"], sb["accepted"])
+    assert np.array_equal(sa["sum_e"], sb["sum_e"])
