@@ -1780,8 +1780,8 @@ __device__ __forceinline__ float eff_after(const DelayedSpin<K> &S, int r, int c
 }
 
 template <int K, bool kStream, int kThreads, bool kTC>
-__global__ void __launch_bounds__(kThreads, 512 / kThreads)
-sweep_pipe_kernel(DevModel m, DevBatch b, SweepParams p, int *active_count, int thr_in_smem) {
+__device__ __forceinline__ void sweep_pipe_body(const DevModel &m, const DevBatch &b, const SweepParams &p,
+                                                int *active_count, int thr_in_smem) {
     const int w = blockIdx.x;
     const int N = m.n_sites;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -2111,6 +2111,22 @@ sweep_pipe_kernel(DevModel m, DevBatch b, SweepParams p, int *active_count, int 
     }
 }
 
+// Two register budgets for the same body: two (or four) CTAs of 256 (128)
+// threads per SM, 128 registers a thread; and, where shared memory already
+// limits the launch to one CTA per SM (W in HBM at N = 864, k = 16: 187 KB),
+// without the cap, so nothing spills (72 bytes spilled at k = 16 under it).
+template <int K, bool kStream, int kThreads, bool kTC>
+__global__ void __launch_bounds__(kThreads, 512 / kThreads)
+sweep_pipe_kernel(DevModel m, DevBatch b, SweepParams p, int *active_count, int thr_in_smem) {
+    sweep_pipe_body<K, kStream, kThreads, kTC>(m, b, p, active_count, thr_in_smem);
+}
+
+template <int K>
+__global__ void __launch_bounds__(256, 1)
+sweep_pipe_wide_kernel(DevModel m, DevBatch b, SweepParams p, int *active_count, int thr_in_smem) {
+    sweep_pipe_body<K, true, 256, false>(m, b, p, active_count, thr_in_smem);
+}
+
 size_t delayed_smem_bytes(const DevModel &m, int K, bool w_on_chip) {
     const size_t N = m.n_sites;
     size_t s = w_on_chip ? N * (m.ld_up + m.ld_dn) * 4 : 0;  // W
@@ -2322,6 +2338,21 @@ static cudaError_t launch_pipe_t(const DevModel &m, const DevBatch &b, const Swe
     cudaError_t e = cudaFuncSetAttribute(sweep_pipe_kernel<K, kStream, kThreads, kTC>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     if (e != cudaSuccess) return e;
+    if constexpr (kStream && kThreads == 256 && !kTC && K >= 12) {
+        // the uncapped form where it keeps as many CTAs per SM
+        e = cudaFuncSetAttribute(sweep_pipe_wide_kernel<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        if (e != cudaSuccess) return e;
+        int occ_wide = 0, occ = 0;
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_wide, sweep_pipe_wide_kernel<K>, kThreads, sm);
+        if (e == cudaSuccess)
+            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, sweep_pipe_kernel<K, kStream, kThreads, kTC>,
+                                                              kThreads, sm);
+        if (e != cudaSuccess) return e;
+        if (occ_wide >= occ && occ_wide > 0) {
+            sweep_pipe_wide_kernel<K><<<b.n_walkers, kThreads, sm, stream>>>(m, b, p, active, thr_in_smem);
+            return cudaGetLastError();
+        }
+    }
     sweep_pipe_kernel<K, kStream, kThreads, kTC><<<b.n_walkers, kThreads, sm, stream>>>(m, b, p, active, thr_in_smem);
     return cudaGetLastError();
 }
