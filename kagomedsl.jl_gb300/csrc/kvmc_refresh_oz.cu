@@ -208,8 +208,9 @@ OzView view_of(const OzRefresh &o) {
 }
 
 // Shared memory of the LU step: the 32-column panel, the staged block of
-// U12, the pivot order and the site tables (70 KB at n = 432, so that two
-// CTAs share an SM).
+// U12, the pivot order and the site tables (70 KB at n = 432, so that three
+// CTAs share an SM; the launch bound keeps their registers to a third of
+// the SM's too).
 struct PrepSmem {
     size_t pn, ut, invd, perm, srow, site_of, site_oth, total;
 };
@@ -229,7 +230,7 @@ __host__ __device__ inline PrepSmem prep_layout(int n, int n_oth) {
 
 // Step 1 of the tiled refresh (site tables, LU of tilde_U in HBM), its
 // results to HBM for the batched kernels, and the unit rows of W.
-__global__ void __launch_bounds__(kTT) oz_prep_kernel(DevModel m, DevBatch b, OzView v, int only_due, int track_drift) {
+__global__ void __launch_bounds__(kTT, 3) oz_prep_kernel(DevModel m, DevBatch b, OzView v, int only_due, int track_drift) {
     const int w = blockIdx.x, spin = blockIdx.y, ws = 2 * w + spin;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nt = blockDim.x, nw = nt / 32;
     if (only_due && b.since[w] >= 0) {
