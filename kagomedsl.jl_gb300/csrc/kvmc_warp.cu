@@ -586,6 +586,13 @@ static cudaError_t launch_warp_t(const DevModel &m, const DevBatch &b, const Swe
     const int grid = (b.n_walkers + wpb - 1) / wpb;
     cudaError_t e = cudaFuncSetAttribute(sweep_warp_kernel<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     if (e != cudaSuccess) return e;
+    // shared memory no larger than the launch needs, so that the rest of the
+    // SM's 256 KB stays L1, where the window's and the column writes' G loads hit
+    const int carve = (int)std::min<size_t>(100, (sm * 100 + 228 * 1024 - 1) / (228 * 1024));
+    if ((e = cudaFuncSetAttribute(sweep_warp_kernel<K>, cudaFuncAttributePreferredSharedMemoryCarveout, carve)))
+        return e;
+    if ((e = cudaFuncSetAttribute(sweep_warp_wide_kernel<K>, cudaFuncAttributePreferredSharedMemoryCarveout, carve)))
+        return e;
     if (K >= 8 && wpb <= kWarpWideWalkers) {
         // the register-rich kernel where it keeps as many CTAs per SM as the
         // capped one (shared memory already limits them: N = 216, 7 walkers
