@@ -181,7 +181,7 @@ struct OzRefresh {
     int *perm, *srow;            // [W*2][n_max] pivot order and the site of M's row i
     float *invd;                 // [W*2][n_max] 1 / diag of the LU's upper factor, in pivot order
     short *site_oth;             // [W*2][oth_max]
-    float *est, *dprev;          // [W*2][tiles] refinement state per tile
+    float *dprev;                // [W*2][tiles] the last relative correction per tile
     int *done, *active;          // [W*2][tiles], [W*2]
     int n_ws;                    // walker-spins: 2 W
     int groups;                  // 128-row groups of the residual per (walker, spin): rows_v / 128

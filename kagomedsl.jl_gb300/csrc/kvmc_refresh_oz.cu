@@ -191,7 +191,7 @@ struct OzView {
     int *vexp, *perm, *srow;
     float *invd;
     short *site_oth;
-    float *est, *dprev;
+    float *dprev;
     int *done, *active;
 };
 
@@ -203,7 +203,7 @@ OzView view_of(const OzRefresh &o) {
     v.ud0 = o.ud[0]; v.ud1 = o.ud[1]; v.fexp0 = o.fexp[0]; v.fexp1 = o.fexp[1];
     v.V = o.V; v.rd = o.rd; v.gd = o.gd; v.cn = o.cn; v.rows_g = o.rows_g; v.dmax = o.dmax; v.vmax = o.vmax;
     v.vd = o.vd; v.mt = o.mt; v.vexp = o.vexp; v.perm = o.perm; v.srow = o.srow; v.invd = o.invd;
-    v.site_oth = o.site_oth; v.est = o.est; v.dprev = o.dprev; v.done = o.done; v.active = o.active;
+    v.site_oth = o.site_oth; v.dprev = o.dprev; v.done = o.done; v.active = o.active;
     return v;
 }
 
@@ -274,7 +274,6 @@ __global__ void __launch_bounds__(kTT, 3) oz_prep_kernel(DevModel m, DevBatch b,
         v.vmax[(size_t)ws * v.rows_v + r] = 0.f;
     }
     for (int t = tid; t < v.tiles; t += nt) {
-        v.est[(size_t)ws * v.tiles + t] = 1.f;
         v.dprev[(size_t)ws * v.tiles + t] = 1.f;
         v.done[(size_t)ws * v.tiles + t] = t * kRT < n_oth ? 0 : 1;
     }
@@ -950,7 +949,6 @@ __device__ __forceinline__ void check_tile(const DevModel &m, const DevBatch &b,
             const float d = q, dprev = v.dprev[item];
             const float est = d < dprev ? d * d / dprev : INFINITY;   // a correction that grows: diverging
             v.dprev[item] = d;
-            v.est[item] = est;
             const int fin = !first && (!(est > 1e-6f) || last);
             *s_fin = fin;
             if (fin) {
@@ -1062,7 +1060,7 @@ OzDims oz_dims(const DevModel &m) {
 
 // byte offsets of the per-walker-spin buffers inside one allocation
 struct OzOffsets {
-    size_t V, rd, gd, dmax, vmax, invd, vd, mt, vexp, perm, srow, site_oth, est, dprev, done, active, tile_list, grp_list, counts, grp_flag,
+    size_t V, rd, gd, dmax, vmax, invd, vd, mt, vexp, perm, srow, site_oth, dprev, done, active, tile_list, grp_list, counts, grp_flag,
         total;
 };
 OzOffsets oz_offsets(const OzDims &d, int n_walkers) {
@@ -1086,7 +1084,6 @@ OzOffsets oz_offsets(const OzDims &d, int n_walkers) {
     o.perm = take(S * d.n_max * 4);
     o.srow = take(S * d.n_max * 4);
     o.site_oth = take(S * d.oth_max * 2);
-    o.est = take(S * d.tiles * 4);
     o.dprev = take(S * d.tiles * 4);
     o.done = take(S * d.tiles * 4);
     o.active = take(S * 4);
@@ -1151,7 +1148,6 @@ cudaError_t oz_setup(const DevModel &m, int n_walkers, void *scratch, OzRefresh 
     oz.perm = reinterpret_cast<int *>(base + o.perm);
     oz.srow = reinterpret_cast<int *>(base + o.srow);
     oz.site_oth = reinterpret_cast<short *>(base + o.site_oth);
-    oz.est = reinterpret_cast<float *>(base + o.est);
     oz.dprev = reinterpret_cast<float *>(base + o.dprev);
     oz.done = reinterpret_cast<int *>(base + o.done);
     oz.active = reinterpret_cast<int *>(base + o.active);
