@@ -586,13 +586,19 @@ static cudaError_t launch_warp_t(const DevModel &m, const DevBatch &b, const Swe
     const int grid = (b.n_walkers + wpb - 1) / wpb;
     cudaError_t e = cudaFuncSetAttribute(sweep_warp_kernel<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     if (e != cudaSuccess) return e;
-    // shared memory no larger than the launch needs, so that the rest of the
-    // SM's 256 KB stays L1, where the window's and the column writes' G loads hit
-    const int carve = (int)std::min<size_t>(100, (sm * 100 + 228 * 1024 - 1) / (228 * 1024));
-    if ((e = cudaFuncSetAttribute(sweep_warp_kernel<K>, cudaFuncAttributePreferredSharedMemoryCarveout, carve)))
-        return e;
-    if ((e = cudaFuncSetAttribute(sweep_warp_wide_kernel<K>, cudaFuncAttributePreferredSharedMemoryCarveout, carve)))
-        return e;
+    // shared memory no larger than the CTAs the launch can hold per SM need,
+    // so that the rest of the SM's 256 KB stays L1, where the window's and the
+    // column writes' G loads hit
+    auto carve_for = [&](auto kernel, size_t smem) -> cudaError_t {
+        cudaError_t r = cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+        int ctas = 0;
+        if (r == cudaSuccess) r = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ctas, kernel, 32 * wpb, smem);
+        if (r != cudaSuccess) return r;
+        const size_t need = (size_t)std::max(ctas, 1) * (smem + 1024);
+        const int carve = (int)std::min<size_t>(100, (need * 100 + 228 * 1024 - 1) / (228 * 1024));
+        return cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout, carve);
+    };
+    if ((e = carve_for(sweep_warp_kernel<K>, sm))) return e;
     if (K >= 8 && wpb <= kWarpWideWalkers) {
         // the register-rich kernel where it keeps as many CTAs per SM as the
         // capped one (shared memory already limits them: N = 216, 7 walkers
@@ -600,6 +606,7 @@ static cudaError_t launch_warp_t(const DevModel &m, const DevBatch &b, const Swe
         // (N = 96, 4 walkers per CTA)
         e = cudaFuncSetAttribute(sweep_warp_wide_kernel<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
         if (e != cudaSuccess) return e;
+        if ((e = carve_for(sweep_warp_wide_kernel<K>, sm))) return e;
         int occ_wide = 0, occ = 0;
         e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_wide, sweep_warp_wide_kernel<K>, 32 * wpb, sm);
         if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, sweep_warp_kernel<K>, 32 * wpb, sm);
