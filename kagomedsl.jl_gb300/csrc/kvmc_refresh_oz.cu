@@ -303,21 +303,27 @@ __global__ void __launch_bounds__(kTT, 3) oz_prep_kernel(DevModel m, DevBatch b,
 // block column of the factors (112 KB at n = 432: two CTAs per SM); the
 // pivot order and 1 / diag(Uf) are read from HBM.
 struct InverseSmem {
-    size_t z, st, total;
+    size_t z, st, perm, total;
 };
 __host__ __device__ inline InverseSmem inverse_layout(int n) {
     auto al = [](size_t x) { return (x + 15) / 16 * 16; };
     InverseSmem s{};
     s.z = 0;
     s.st = al((size_t)kRT * ld_tile(n) * 4);
-    s.total = s.st + al((size_t)round4(n) * kLdc * 4);
+    s.perm = s.st + al((size_t)round4(n) * kLdc * 4);
+    s.total = s.perm + al((size_t)n * 4);
     return s;
 }
 
+// One CTA per (walker-spin, 32 identity rows), the tiles of a walker-spin
+// adjacent in the one-dimensional grid (x = tile + tiles * (2 w + spin)), so
+// that the CTAs reading one walker-spin's factors run together and share
+// them in L2 (512 walkers at 432 orbitals hold 764 MB of factors).
 __global__ void __launch_bounds__(kTT) oz_inverse_kernel(DevModel m, DevBatch b, OzView v) {
-    const int w = blockIdx.x, spin = blockIdx.y, ws = 2 * w + spin;
+    const int tiles = (v.n_max + kRT - 1) / kRT;
+    const int ws = blockIdx.x / tiles, w = ws >> 1, spin = ws & 1;
     const int n = spin == 0 ? m.n_up : m.n_dn;
-    const int t0 = blockIdx.z * kRT;
+    const int t0 = (blockIdx.x - ws * tiles) * kRT;
     if (!v.active[ws] || t0 >= n) return;
     const int rows = min(kRT, n - t0), ldz = ld_tile(n);
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nt = blockDim.x, nw = nt / 32;
@@ -325,9 +331,10 @@ __global__ void __launch_bounds__(kTT) oz_inverse_kernel(DevModel m, DevBatch b,
     const InverseSmem L = inverse_layout(n);
     float *Z = reinterpret_cast<float *>(smem + L.z);
     float *St = reinterpret_cast<float *>(smem + L.st);
-    const int *perm = v.perm + (size_t)ws * v.n_max;
+    int *perm = reinterpret_cast<int *>(smem + L.perm);
     const float *invd = v.invd + (size_t)ws * v.n_max;
     float *A = reinterpret_cast<float *>(b.solve_scratch + ((size_t)w * 2 + spin) * b.solve_block);
+    for (int i = tid; i < n; i += nt) perm[i] = v.perm[(size_t)ws * v.n_max + i];
     for (int e = tid; e < kRT * ldz; e += nt) {
         const int r = e / ldz, c = e - r * ldz;
         Z[e] = (r < rows && c == t0 + r) ? 1.f : 0.f;
@@ -1176,7 +1183,7 @@ cudaError_t launch_refresh_oz(const DevModel &m, const DevBatch &b, const OzRefr
     const size_t sm_inv = inverse_layout(oz.n_max).total;
     if ((e = cudaFuncSetAttribute(oz_inverse_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_inv)))
         return e;
-    oz_inverse_kernel<<<dim3(W, 2, (oz.n_max + kRT - 1) / kRT), kTT, sm_inv, stream>>>(m, b, v);
+    oz_inverse_kernel<<<W * 2 * ((oz.n_max + kRT - 1) / kRT), kTT, sm_inv, stream>>>(m, b, v);
     oz_gather_kernel<<<dim3(W, 2, kOzUDigits), 256, 0, stream>>>(m, v);
     oz_bplanes_kernel<<<dim3(W, 2, oz.tiles), 256, 0, stream>>>(m, v);
     if ((e = cudaFuncSetAttribute(oz_residual_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, oz::kSmem)))

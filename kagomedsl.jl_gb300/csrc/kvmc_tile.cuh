@@ -59,6 +59,35 @@ __device__ __forceinline__ void stage_rows32(float *dst, int ld, int rows, int n
     }
 }
 
+// 4-byte asynchronous copy global -> shared; ok = false writes a zero.
+__device__ __forceinline__ void cp_async4(float *dst, const float *src, bool ok) {
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" ::"r"(d), "l"(src), "r"(ok ? 4 : 0) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
+
+// stage_rows32 with every element's copy in flight at once (cp.async, 4
+// bytes each, no registers held), for block columns read once per solve
+// from HBM or L2: the CTA waits one memory latency per block column, not
+// one per eight elements.  `any` is a valid global address for the copies
+// that write a zero.  Ends with the copies landed and the CTA synchronised.
+template <typename Src>
+__device__ __forceinline__ void stage_rows32_async(float *dst, int ld, int rows, int nc, int wc, Src src,
+                                                   const float *any) {
+    const int total = rows * 32;
+    for (int e = threadIdx.x; e < total; e += blockDim.x) {
+        const int k = e >> 5, c = e & 31;
+        if (c >= wc) continue;
+        const float *p = c < nc ? src(k) : nullptr;
+        cp_async4(dst + (size_t)k * ld + c, p ? p + c : any, p != nullptr);
+    }
+    cp_async_commit();
+    cp_async_wait<0>();
+    __syncthreads();
+}
+
 // Shared-memory layout (byte offsets, each a multiple of 16).
 struct TileSmem {
     size_t z, r, pn, ut, st, invd, perm, srow, site_of, site_oth, total;
@@ -224,23 +253,26 @@ __device__ __forceinline__ bool lu_blocked(float *A, int n, float *Pn, float *Ut
 // Z := Z (L Uf)^{-1} for the tile (rows x n, leading dimension ldz): forward
 // with Uf, backward with the unit lower L, in pivot order.  Warp g owns rows
 // g, g + kNW, ...; lane = column within the block.  Uc stages one
-// block column of the factors.  Columns n .. round4(n) of Z are zero, and
-// so are its columns left of j0 (a multiple of 32), which the forward
-// sweep then skips.
+// block column of the factors (the forward sweep from row j0 on).  Columns
+// n .. round4(n) of Z are zero, and so are its columns left of j0 (a
+// multiple of 32), which the forward sweep then skips.  The pivots'
+// reciprocals of a block travel in a register of its lane and reach the
+// serial part by shuffles.
 __device__ __forceinline__ void tile_solve(const float *A, const int *perm, int n, const float *invd, float *Z, int ldz,
                                            int rows, float *Uc, int j0) {
     const int lane = threadIdx.x & 31, g = threadIdx.x >> 5;
     const int n4 = round4(n);
     for (int jb = j0; jb < n; jb += kPB) {
         const int nb = min(kPB, n - jb);
-        const int kr = jb + nb;
+        const int kr = jb + nb - j0;
+        const float dl = lane < nb ? invd[jb + lane] : 0.f;
         __syncthreads();
-        stage_rows32(Uc, kLdc, kr, nb, 32, [&](int k) -> const float * { return A + (size_t)perm[k] * n + jb; });
-        __syncthreads();
+        stage_rows32_async(Uc, kLdc, kr, nb, 32,
+                           [&](int k) -> const float * { return A + (size_t)perm[j0 + k] * n + jb; }, A);
         float acc[kRW] = {};
         for (int k = j0; k < jb; k += 4) {
-            const float u0 = Uc[(k + 0) * kLdc + lane], u1 = Uc[(k + 1) * kLdc + lane];
-            const float u2 = Uc[(k + 2) * kLdc + lane], u3 = Uc[(k + 3) * kLdc + lane];
+            const float *u = Uc + (size_t)(k - j0) * kLdc + lane;
+            const float u0 = u[0], u1 = u[kLdc], u2 = u[2 * kLdc], u3 = u[3 * kLdc];
 #pragma unroll
             for (int a = 0; a < kRW; ++a) {
                 const float4 z = *reinterpret_cast<const float4 *>(Z + (size_t)(g + kNW * a) * ldz + k);
@@ -257,8 +289,8 @@ __device__ __forceinline__ void tile_solve(const float *A, const int *perm, int 
             x[a] = (r < rows && lane < nb) ? Z[(size_t)r * ldz + jb + lane] - acc[a] : 0.f;
         }
         for (int j = 0; j < nb; ++j) {
-            const float uj = Uc[(jb + j) * kLdc + lane];
-            const float dj = invd[jb + j];
+            const float uj = Uc[(jb - j0 + j) * kLdc + lane];
+            const float dj = __shfl_sync(0xffffffffu, dl, j);
 #pragma unroll
             for (int a = 0; a < kRW; ++a) {
                 const float xj = __shfl_sync(0xffffffffu, x[a], j) * dj;
@@ -276,10 +308,9 @@ __device__ __forceinline__ void tile_solve(const float *A, const int *perm, int 
         const int nb = min(kPB, n - jb);
         const int kr = n4 - jb;
         __syncthreads();
-        stage_rows32(Uc, kLdc, kr, nb, 32, [&](int k) -> const float * {
-            return jb + k < n ? A + (size_t)perm[jb + k] * n + jb : nullptr;
-        });
-        __syncthreads();
+        stage_rows32_async(
+            Uc, kLdc, kr, nb, 32,
+            [&](int k) -> const float * { return jb + k < n ? A + (size_t)perm[jb + k] * n + jb : nullptr; }, A);
         float acc[kRW] = {};
         for (int k = jb + kPB; k < n4; k += 4) {
             const float *u = Uc + (size_t)(k - jb) * kLdc + lane;
@@ -315,15 +346,6 @@ __device__ __forceinline__ void tile_solve(const float *A, const int *perm, int 
     }
     __syncthreads();
 }
-
-// 4-byte asynchronous copy global -> shared; ok = false writes a zero.
-__device__ __forceinline__ void cp_async4(float *dst, const float *src, bool ok) {
-    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" ::"r"(d), "l"(src), "r"(ok ? 4 : 0) : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
-template <int N>
-__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
 
 // Chunk (k0 .. k0 + kKC) x (c0 .. c0 + kCB) of a matrix whose row k is
 // row(k) (n columns), into buf (row stride kCB); zero outside n x n.
