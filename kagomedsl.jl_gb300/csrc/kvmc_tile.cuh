@@ -116,6 +116,76 @@ __host__ __device__ inline TileSmem tile_smem_layout(int n, int n_oth) {
     return s;
 }
 
+// The LU of one staged panel (rp rows of Pn, nb <= 32 columns) with its rows
+// in registers, one row per thread (rp <= kTT, blockDim.x == kTT): the pivot
+// choice of the shared-memory form in lu_blocked (the largest |entry|, the
+// first position among equals) and its operations in the same order, so the
+// factors are the same bit for bit; two barriers per column in place of
+// three, and the column update in registers.  A row stays with its thread;
+// `pos` follows its position through the swaps, and the rows go back to Pn
+// in pivot order at the end.  permp is the pivot order from the panel's
+// first row on.  Returns false on an exactly zero pivot (every thread sees
+// the same answer).
+__device__ __noinline__ bool panel_lu_regs(float *Pn, int rp, int nb, int *permp) {
+    __shared__ float s_val[kNW];
+    __shared__ int s_pos[kNW];
+    __shared__ float s_row[kPB];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const bool mine = tid < rp;
+    int pos = tid;
+    float v[kPB];
+#pragma unroll
+    for (int j = 0; j < kPB; ++j) v[j] = mine ? Pn[(size_t)tid * kLdc + j] : 0.f;
+#pragma unroll
+    for (int k = 0; k < kPB; ++k) {
+        if (k >= nb) break;
+        float best = -1.f;
+        int bi = rp;
+        if (mine && pos >= k) {
+            const float a = fabsf(v[k]);
+            if (a > best) { best = a; bi = pos; }
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const float ob = __shfl_xor_sync(0xffffffffu, best, o);
+            const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+            if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
+        }
+        if (lane == 0) { s_val[warp] = best; s_pos[warp] = bi; }
+        __syncthreads();
+        best = s_val[0];
+        bi = s_pos[0];
+#pragma unroll
+        for (int g = 1; g < kNW; ++g) {
+            const float ob = s_val[g];
+            const int oi = s_pos[g];
+            if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
+        }
+        if (!(best > 0.f)) return false;
+        if (mine && pos == bi) {
+#pragma unroll
+            for (int j = 0; j < kPB; ++j) s_row[j] = v[j];
+        }
+        if (mine) pos = pos == k ? bi : (pos == bi ? k : pos);
+        if (tid == 0 && bi != k) { const int t = permp[k]; permp[k] = permp[bi]; permp[bi] = t; }
+        __syncthreads();
+        if (mine && pos > k) {
+            const float dinv = 1.f / s_row[k];
+            const float l = v[k] * dinv;
+            v[k] = l;
+#pragma unroll
+            for (int j = k + 1; j < kPB; ++j)
+                if (j < nb) v[j] = fmaf(-l, s_row[j], v[j]);
+        }
+    }
+    if (mine) {
+#pragma unroll
+        for (int j = 0; j < kPB; ++j) Pn[(size_t)pos * kLdc + j] = v[j];
+    }
+    __syncthreads();
+    return true;
+}
+
 // P A = L Uf of A (n x n, row-major, lda = n, global memory) in FP32 with
 // partial pivoting (first maximal |pivot| wins).  Rows stay where they are:
 // row i of the factors is A[perm[i]].  Returns false on an exactly zero
@@ -131,6 +201,9 @@ __device__ __forceinline__ bool lu_blocked(float *A, int n, float *Pn, float *Ut
         const int rp = n - pb;
         stage_rows32(Pn, kLdc, rp, nb, 32, [&](int r) -> const float * { return A + (size_t)perm[pb + r] * n + pb; });
         __syncthreads();
+        if (rp <= kTT && nt == kTT) {
+            if (!panel_lu_regs(Pn, rp, nb, perm + pb)) return false;
+        } else
         for (int k = 0; k < nb; ++k) {
             if (warp == 0) {
                 float best = -1.f;
