@@ -73,6 +73,9 @@ struct kvmc_handle {
     int *d_redo = nullptr;
     double *d_stats = nullptr;  // two sets of kCallStats: a sweep call's start and end
     double *h_stats = nullptr;  // pinned copy of d_stats
+    int32_t *d_labels = nullptr;  // both spins' labels in the caller's 32-bit layout (2 x walkers x sites)
+    int *d_bad = nullptr;         // per walker: the device label check failed
+    int *h_bad = nullptr;         // pinned copy of d_bad
     void *d_scratch = nullptr;
     size_t scratch_bytes = 0;
 
@@ -142,9 +145,11 @@ int set_device(kvmc_handle *h) { return h->cuda(cudaSetDevice(h->device), "cudaS
 
 // kappa validation: every site holds exactly one spinon, labels are a
 // permutation of 1..n per spin (src/Hamiltonian.jl:548-564, src/MonteCarlo.jl:92-115).
-int validate_kappa(kvmc_handle *h, const int32_t *ku, const int32_t *kd, int walker) {
+// One walker's labels: in range, every site holding exactly one spin, no
+// label twice.  seen_u / seen_d (n_up + 1, n_dn + 1 entries) hold the last
+// walker that used each label, so one pair of tables serves all walkers.
+int validate_kappa(kvmc_handle *h, const int32_t *ku, const int32_t *kd, int walker, int *seen_u, int *seen_d) {
     const int N = h->n_sites;
-    std::vector<char> seen_u(h->n_up + 1, 0), seen_d(h->n_dn + 1, 0);
     for (int s = 0; s < N; ++s) {
         const int a = ku[s], b = kd[s];
         if (a < 0 || a > h->n_up || b < 0 || b > h->n_dn)
@@ -152,25 +157,44 @@ int validate_kappa(kvmc_handle *h, const int32_t *ku, const int32_t *kd, int wal
         if ((a != 0) == (b != 0))
             return h->fail(KVMC_ERR_ARGUMENT, "walker %d site %d is %s", walker, s, a != 0 ? "doubly occupied" : "unoccupied");
         if (a != 0) {
-            if (seen_u[a]) return h->fail(KVMC_ERR_ARGUMENT, "walker %d: up label %d repeated", walker, a);
-            seen_u[a] = 1;
+            if (seen_u[a] == walker) return h->fail(KVMC_ERR_ARGUMENT, "walker %d: up label %d repeated", walker, a);
+            seen_u[a] = walker;
         } else {
-            if (seen_d[b]) return h->fail(KVMC_ERR_ARGUMENT, "walker %d: down label %d repeated", walker, b);
-            seen_d[b] = 1;
+            if (seen_d[b] == walker) return h->fail(KVMC_ERR_ARGUMENT, "walker %d: down label %d repeated", walker, b);
+            seen_d[b] = walker;
         }
     }
     return KVMC_OK;
 }
 
+// Copies every walker's labels to the device, checks them there (one warp
+// per walker) and only then converts them into the walkers' 16-bit labels:
+// nothing of the walkers' state changes when a walker is invalid.  The
+// first invalid walker is checked again on the host, whose check names the
+// site and the label.  Beyond 48 KB of label bitmaps per CTA (more than
+// about 6000 orbitals per spin) the host checks every walker.
 int upload_kappa(kvmc_handle *h, const int32_t *ku, const int32_t *kd) {
-    const size_t tot = (size_t)h->n_walkers * h->n_sites;
-    for (int w = 0; w < h->n_walkers; ++w)
-        KV_TRY(validate_kappa(h, ku + (size_t)w * h->n_sites, kd + (size_t)w * h->n_sites, w));
-    std::vector<short> a(tot), b(tot);
-    for (size_t e = 0; e < tot; ++e) { a[e] = (short)ku[e]; b[e] = (short)kd[e]; }
-    KV_TRY(h->cuda(cudaMemcpyAsync(h->db.kappa_up, a.data(), tot * 2, cudaMemcpyHostToDevice, h->stream), "upload kappa"));
-    KV_TRY(h->cuda(cudaMemcpyAsync(h->db.kappa_dn, b.data(), tot * 2, cudaMemcpyHostToDevice, h->stream), "upload kappa"));
-    return h->cuda(cudaStreamSynchronize(h->stream), "upload kappa");
+    const int N = h->n_sites, Wk = h->n_walkers;
+    const size_t tot = (size_t)Wk * N;
+    int32_t *du = h->d_labels, *dd = h->d_labels + tot;
+    KV_TRY(h->cuda(cudaMemcpyAsync(du, ku, tot * 4, cudaMemcpyHostToDevice, h->stream), "upload kappa"));
+    KV_TRY(h->cuda(cudaMemcpyAsync(dd, kd, tot * 4, cudaMemcpyHostToDevice, h->stream), "upload kappa"));
+    std::vector<int> seen_u(h->n_up + 1, -1), seen_d(h->n_dn + 1, -1);
+    if (kvmc::labels_check_smem(h->n_up, h->n_dn) > 48 * 1024) {
+        for (int w = 0; w < Wk; ++w)
+            KV_TRY(validate_kappa(h, ku + (size_t)w * N, kd + (size_t)w * N, w, seen_u.data(), seen_d.data()));
+    } else {
+        KV_TRY(h->cuda(kvmc::launch_labels_check(du, dd, Wk, N, h->n_up, h->n_dn, h->d_bad, h->stream), "label check"));
+        KV_TRY(h->cuda(cudaMemcpyAsync(h->h_bad, h->d_bad, (size_t)Wk * sizeof(int), cudaMemcpyDeviceToHost, h->stream),
+                       "label check"));
+        KV_TRY(h->cuda(cudaStreamSynchronize(h->stream), "label check"));
+        for (int w = 0; w < Wk; ++w)
+            if (h->h_bad[w]) {
+                KV_TRY(validate_kappa(h, ku + (size_t)w * N, kd + (size_t)w * N, w, seen_u.data(), seen_d.data()));
+                return h->fail(KVMC_ERR_ARGUMENT, "walker %d: invalid labels", w);
+            }
+    }
+    return h->cuda(kvmc::launch_labels_convert(du, dd, h->db, N, 1, h->stream), "upload kappa");
 }
 
 // The FP32 refresh by iterative refinement: one thread per row (1) or tiled (2)
@@ -623,6 +647,7 @@ extern "C" int kvmc_destroy(kvmc_handle *h) {
     if (h->d_gsums) cudaFree(h->d_gsums);
     if (h->d_gout) cudaFree(h->d_gout);
     if (h->h_stats) cudaFreeHost(h->h_stats);
+    if (h->h_bad) cudaFreeHost(h->h_bad);
     for (auto &e : h->ev_pool) cudaEventDestroy(e);
     for (auto &e : h->region)
         if (e) cudaEventDestroy(e);
@@ -807,6 +832,11 @@ extern "C" int kvmc_create(const kvmc_model_desc *model, const kvmc_batch_desc *
         (rc = h->alloc(&h->d_stats, 2 * kvmc::kCallStats)))
         return bail(rc);
     if ((rc = h->cuda(cudaMallocHost(reinterpret_cast<void **>(&h->h_stats), 2 * kvmc::kCallStats * sizeof(double)),
+                      "cudaMallocHost")))
+        return bail(rc);
+    if ((rc = h->alloc(&h->d_labels, 2 * (size_t)Wk * m.n_sites)) || (rc = h->alloc(&h->d_bad, Wk)))
+        return bail(rc);
+    if ((rc = h->cuda(cudaMallocHost(reinterpret_cast<void **>(&h->h_bad), (size_t)Wk * sizeof(int)),
                       "cudaMallocHost")))
         return bail(rc);
     b.solve_block = kvmc::refresh_scratch_block(m) * cw;
@@ -1501,14 +1531,13 @@ extern "C" int kvmc_get_state(kvmc_handle *h, int32_t *kappa_up, int32_t *kappa_
     if (!h) return fail_global(KVMC_ERR_ARGUMENT, "null handle");
     KV_TRY(set_device(h));
     const size_t tot = (size_t)h->n_walkers * h->n_sites;
-    std::vector<short> a(tot), b(tot);
-    KV_TRY(h->cuda(cudaMemcpy(a.data(), h->db.kappa_up, tot * 2, cudaMemcpyDeviceToHost), "kappa"));
-    KV_TRY(h->cuda(cudaMemcpy(b.data(), h->db.kappa_dn, tot * 2, cudaMemcpyDeviceToHost), "kappa"));
-    if (kappa_up) for (size_t e = 0; e < tot; ++e) kappa_up[e] = a[e];
-    if (kappa_down) for (size_t e = 0; e < tot; ++e) kappa_down[e] = b[e];
+    int32_t *du = h->d_labels, *dd = h->d_labels + tot;
+    KV_TRY(h->cuda(kvmc::launch_labels_convert(du, dd, h->db, h->n_sites, 0, h->stream), "kappa"));
+    if (kappa_up) KV_TRY(h->cuda(cudaMemcpyAsync(kappa_up, du, tot * 4, cudaMemcpyDeviceToHost, h->stream), "kappa"));
+    if (kappa_down) KV_TRY(h->cuda(cudaMemcpyAsync(kappa_down, dd, tot * 4, cudaMemcpyDeviceToHost, h->stream), "kappa"));
     if (counters)
-        KV_TRY(h->cuda(cudaMemcpy(counters, h->db.t, h->n_walkers * 8, cudaMemcpyDeviceToHost), "counters"));
-    return KVMC_OK;
+        KV_TRY(h->cuda(cudaMemcpyAsync(counters, h->db.t, h->n_walkers * 8, cudaMemcpyDeviceToHost, h->stream), "counters"));
+    return h->cuda(cudaStreamSynchronize(h->stream), "kappa");
 }
 
 extern "C" int kvmc_set_state(kvmc_handle *h, const int32_t *kappa_up, const int32_t *kappa_down, const int64_t *counters) {

@@ -150,6 +150,16 @@ size_t refresh_tile_smem(const DevModel &m);
 cudaError_t launch_refresh_tile(const DevModel &m, const DevBatch &b, int only_due, int track_drift,
                                 cudaStream_t stream);
 cudaError_t launch_clear_status(const DevBatch &b, int bits, cudaStream_t stream);
+// Labels from and to the caller's 32-bit arrays (kvmc_refresh32.cu): the
+// checks of kvmc_set_state per walker into bad[] (one warp per walker,
+// labels_check_smem bytes of shared memory), and the conversion to or from
+// the walkers' 16-bit labels.
+constexpr int kLabelWarps = 8;
+size_t labels_check_smem(int n_up, int n_dn);
+cudaError_t launch_labels_check(const int32_t *ku, const int32_t *kd, int n_walkers, int N, int n_up, int n_dn,
+                                int *bad, cudaStream_t stream);
+cudaError_t launch_labels_convert(int32_t *ku, int32_t *kd, const DevBatch &b, int N, int to_short,
+                                  cudaStream_t stream);
 // The sums a sweep call reports, reduced on the device (kvmc_refresh32.cu):
 // kCallStats doubles at `out`, laid out as call_stats_kernel documents.
 constexpr int kCallStats = 16;

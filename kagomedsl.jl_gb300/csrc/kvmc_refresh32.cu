@@ -289,6 +289,72 @@ cudaError_t launch_call_stats(const DevBatch &b, double *out, cudaStream_t strea
     return cudaGetLastError();
 }
 
+// The label checks of kvmc_set_state and kvmc_init, one warp per walker:
+// every label in range, every site holding exactly one spin, no label twice
+// (one bitmap per spin in shared memory, `words` 32-bit words each).
+// bad[w] = 1 for a walker that fails any of them.
+__global__ void __launch_bounds__(32 * kLabelWarps) labels_check_kernel(const int32_t *ku, const int32_t *kd,
+                                                                        int n_walkers, int N, int n_up, int n_dn,
+                                                                        int words, int *bad) {
+    extern __shared__ unsigned seen[];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int w = blockIdx.x * kLabelWarps + warp;
+    if (w >= n_walkers) return;
+    unsigned *su = seen + (size_t)warp * 2 * words, *sd = su + words;
+    for (int i = lane; i < 2 * words; i += 32) su[i] = 0u;
+    __syncwarp();
+    const int32_t *u = ku + (size_t)w * N, *d = kd + (size_t)w * N;
+    bool ok = true;
+    for (int s = lane; s < N; s += 32) {
+        const int a = u[s], b = d[s];
+        if (a < 0 || a > n_up || b < 0 || b > n_dn || (a != 0) == (b != 0)) {
+            ok = false;
+            continue;
+        }
+        const int l = a != 0 ? a : b;
+        const unsigned bit = 1u << (l & 31);
+        if (atomicOr((a != 0 ? su : sd) + (l >> 5), bit) & bit) ok = false;
+    }
+    ok = __all_sync(0xffffffffu, ok);
+    if (lane == 0) bad[w] = ok ? 0 : 1;
+}
+
+// Both spins' labels between the caller's 32-bit layout and the walkers'
+// 16-bit labels (to_short: ku, kd -> a, b; otherwise a, b -> ku, kd).
+__global__ void labels_convert_kernel(int32_t *ku, int32_t *kd, short *a, short *b, size_t tot, int to_short) {
+    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < tot; e += (size_t)gridDim.x * blockDim.x) {
+        if (to_short) {
+            a[e] = (short)ku[e];
+            b[e] = (short)kd[e];
+        } else {
+            ku[e] = a[e];
+            kd[e] = b[e];
+        }
+    }
+}
+
+size_t labels_check_smem(int n_up, int n_dn) {
+    const int words = (n_up > n_dn ? n_up : n_dn) / 32 + 1;
+    return (size_t)kLabelWarps * 2 * words * sizeof(unsigned);
+}
+
+cudaError_t launch_labels_check(const int32_t *ku, const int32_t *kd, int n_walkers, int N, int n_up, int n_dn,
+                                int *bad, cudaStream_t stream) {
+    const int words = (n_up > n_dn ? n_up : n_dn) / 32 + 1;
+    labels_check_kernel<<<(n_walkers + kLabelWarps - 1) / kLabelWarps, 32 * kLabelWarps,
+                          labels_check_smem(n_up, n_dn), stream>>>(ku, kd, n_walkers, N, n_up, n_dn, words, bad);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_labels_convert(int32_t *ku, int32_t *kd, const DevBatch &b, int N, int to_short,
+                                  cudaStream_t stream) {
+    const size_t tot = (size_t)b.n_walkers * N;
+    const size_t blocks = (tot + 255) / 256;
+    labels_convert_kernel<<<(unsigned)(blocks < 4096 ? blocks : 4096), 256, 0, stream>>>(ku, kd, b.kappa_up, b.kappa_dn,
+                                                                                       tot, to_short);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_clear_status(const DevBatch &b, int bits, cudaStream_t stream) {
     clear_status_bits_kernel<<<(b.n_walkers + 255) / 256, 256, 0, stream>>>(b, bits);
     return cudaGetLastError();
