@@ -186,14 +186,66 @@ __device__ __noinline__ bool panel_lu_regs(float *Pn, int rp, int nb, int *permp
     return true;
 }
 
+// The LU of one staged panel in shared memory, for panels of any height:
+// one warp finds the pivot (the largest |entry|, the first position among
+// equals), the pivot row is swapped into place, and every thread updates
+// rows below it.  permp is the pivot order from the panel's first row on.
+// Returns false on an exactly zero pivot (every thread sees the same
+// answer).
+__device__ __forceinline__ bool panel_lu_smem(float *Pn, int rp, int nb, int *permp) {
+    __shared__ int s_piv;
+    __shared__ float s_pmax, s_dinv;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nt = blockDim.x;
+    for (int k = 0; k < nb; ++k) {
+        if (warp == 0) {
+            float best = -1.f;
+            int bi = rp;
+            for (int i = k + lane; i < rp; i += 32) {
+                const float v = fabsf(Pn[(size_t)i * kLdc + k]);
+                if (v > best) { best = v; bi = i; }
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                const float ob = __shfl_xor_sync(0xffffffffu, best, o);
+                const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+                if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
+            }
+            if (lane == 0) {
+                s_piv = bi;
+                s_pmax = best;
+                s_dinv = best > 0.f ? 1.f / Pn[(size_t)bi * kLdc + k] : 0.f;
+            }
+        }
+        __syncthreads();
+        if (!(s_pmax > 0.f)) return false;
+        const int p = s_piv;
+        if (p != k) {
+            for (int j = tid; j < kPB; j += nt) {
+                const float a = Pn[(size_t)k * kLdc + j];
+                Pn[(size_t)k * kLdc + j] = Pn[(size_t)p * kLdc + j];
+                Pn[(size_t)p * kLdc + j] = a;
+            }
+            if (tid == 0) { const int t = permp[k]; permp[k] = permp[p]; permp[p] = t; }
+        }
+        __syncthreads();
+        const float dinv = s_dinv;
+        for (int i = k + 1 + tid; i < rp; i += nt) {
+            const float l = Pn[(size_t)i * kLdc + k] * dinv;
+            Pn[(size_t)i * kLdc + k] = l;
+            for (int j = k + 1; j < nb; ++j)
+                Pn[(size_t)i * kLdc + j] = fmaf(-l, Pn[(size_t)k * kLdc + j], Pn[(size_t)i * kLdc + j]);
+        }
+        __syncthreads();
+    }
+    return true;
+}
+
 // P A = L Uf of A (n x n, row-major, lda = n, global memory) in FP32 with
 // partial pivoting (first maximal |pivot| wins).  Rows stay where they are:
 // row i of the factors is A[perm[i]].  Returns false on an exactly zero
 // pivot (every thread sees the same answer).
 __device__ __forceinline__ bool lu_blocked(float *A, int n, float *Pn, float *Ut, float *invd, int *perm) {
-    __shared__ int s_piv;
-    __shared__ float s_pmax, s_dinv;
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nt = blockDim.x;
+    const int tid = threadIdx.x, nt = blockDim.x;
     for (int i = tid; i < n; i += nt) perm[i] = i;
     __syncthreads();
     for (int pb = 0; pb < n; pb += kPB) {
@@ -201,50 +253,8 @@ __device__ __forceinline__ bool lu_blocked(float *A, int n, float *Pn, float *Ut
         const int rp = n - pb;
         stage_rows32(Pn, kLdc, rp, nb, 32, [&](int r) -> const float * { return A + (size_t)perm[pb + r] * n + pb; });
         __syncthreads();
-        if (rp <= kTT && nt == kTT) {
-            if (!panel_lu_regs(Pn, rp, nb, perm + pb)) return false;
-        } else
-        for (int k = 0; k < nb; ++k) {
-            if (warp == 0) {
-                float best = -1.f;
-                int bi = rp;
-                for (int i = k + lane; i < rp; i += 32) {
-                    const float v = fabsf(Pn[(size_t)i * kLdc + k]);
-                    if (v > best) { best = v; bi = i; }
-                }
-#pragma unroll
-                for (int o = 16; o > 0; o >>= 1) {
-                    const float ob = __shfl_xor_sync(0xffffffffu, best, o);
-                    const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
-                    if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
-                }
-                if (lane == 0) {
-                    s_piv = bi;
-                    s_pmax = best;
-                    s_dinv = best > 0.f ? 1.f / Pn[(size_t)bi * kLdc + k] : 0.f;
-                }
-            }
-            __syncthreads();
-            if (!(s_pmax > 0.f)) return false;
-            const int p = s_piv;
-            if (p != k) {
-                for (int j = tid; j < kPB; j += nt) {
-                    const float a = Pn[(size_t)k * kLdc + j];
-                    Pn[(size_t)k * kLdc + j] = Pn[(size_t)p * kLdc + j];
-                    Pn[(size_t)p * kLdc + j] = a;
-                }
-                if (tid == 0) { const int t = perm[pb + k]; perm[pb + k] = perm[pb + p]; perm[pb + p] = t; }
-            }
-            __syncthreads();
-            const float dinv = s_dinv;
-            for (int i = k + 1 + tid; i < rp; i += nt) {
-                const float l = Pn[(size_t)i * kLdc + k] * dinv;
-                Pn[(size_t)i * kLdc + k] = l;
-                for (int j = k + 1; j < nb; ++j)
-                    Pn[(size_t)i * kLdc + j] = fmaf(-l, Pn[(size_t)k * kLdc + j], Pn[(size_t)i * kLdc + j]);
-            }
-            __syncthreads();
-        }
+        const bool ok = rp <= kTT && nt == kTT ? panel_lu_regs(Pn, rp, nb, perm + pb) : panel_lu_smem(Pn, rp, nb, perm + pb);
+        if (!ok) return false;
         for (int e = tid; e < rp * kPB; e += nt) {
             const int r = e >> 5, c = e & 31;
             if (c < nb) A[(size_t)perm[pb + r] * n + pb + c] = Pn[(size_t)r * kLdc + c];
