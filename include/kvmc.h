@@ -244,7 +244,10 @@ KVMC_API int kvmc_refresh(kvmc_handle *h);
  * counter (the position in the Philox stream).  set_state rebuilds W.
  * Any pointer may be NULL to skip that field (set_state: counters NULL
  * keeps the current counters).  kvmc_set_state rebuilds W: in FP64, or for
- * the mixed real form with KVMC_TUNE_REFRESH32 by FP32 refinement. */
+ * the mixed real form with KVMC_TUNE_REFRESH32 by FP32 refinement.  A label
+ * out of range (KVMC_ERR_BOUNDS), a label used twice or a site empty or
+ * doubly occupied (KVMC_ERR_ARGUMENT) in any walker leaves every walker's
+ * state as it was; the error names the first such walker and site. */
 KVMC_API int kvmc_get_state(kvmc_handle *h, int32_t *kappa_up, int32_t *kappa_down,
                    int64_t *counters);
 KVMC_API int kvmc_set_state(kvmc_handle *h, const int32_t *kappa_up, const int32_t *kappa_down,
