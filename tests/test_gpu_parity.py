@@ -224,6 +224,37 @@ def test_invalid_and_singular_configurations(kv):
     eng.close()
 
 
+def test_set_state_rejects_a_bad_walker_and_keeps_every_state(kv):
+    """The labels of set_state are checked on the device: an invalid walker
+    among valid ones fails the call, the error names the first invalid
+    walker and its site, and no walker's configuration or counter changes,
+    not even one whose new labels were valid."""
+    ham = ham_for(kv, 96)
+    walkers = 9
+    eng = kv.Engine(ham, walkers)
+    eng.init()
+    eng.advance(16)
+    ku0, kd0, ct0 = eng.get_state()
+    ku, kd = ku0.copy(), kd0.copy()
+    a, b = int(np.argmax(ku[0] > 0)), int(np.argmax(kd[0] > 0))   # walker 0: a valid exchange
+    ku[0, a], kd[0, a], ku[0, b], kd[0, b] = 0, kd0[0, b], ku0[0, a], 0
+    s5 = int(np.argmax(ku[5] > 0))
+    kd[5, s5] = 1                                                   # walker 5: doubly occupied
+    ku[7, int(np.argmax(ku[7] > 0))] = 999                          # walker 7: label out of range
+    with pytest.raises(kv.ArgumentError, match=f"walker 5 site {s5} is doubly occupied"):
+        eng.set_state(ku, kd, ct0)
+    ku[5], kd[5] = ku0[5], kd0[5]
+    with pytest.raises(kv.BoundsError, match="walker 7 site"):
+        eng.set_state(ku, kd, ct0)
+    ku1, kd1, ct1 = eng.get_state()
+    assert np.array_equal(ku1, ku0) and np.array_equal(kd1, kd0) and np.array_equal(ct1, ct0)
+    ku[7] = ku0[7]
+    eng.set_state(ku, kd, ct0)                                      # only walker 0 changed
+    ku2, kd2, _ = eng.get_state()
+    assert np.array_equal(ku2, ku) and np.array_equal(kd2, kd)
+    eng.close()
+
+
 def test_carlo_callbacks_and_checkpoint(kv):
     params = dict(n1=4, n2=2, PBC=(True, True), antiPBC=(False, True), N_up=12, N_down=12, walkers=8,
                   precision="mixed", proposals_per_sweep=12, seed=3)
